@@ -1,0 +1,193 @@
+/*
+ * sift_cuda.h — C ABI of libsiftcuda.so, the GB300 (sm_103a) SIFT engine.
+ *
+ * This is the boundary a `SiftBackend::Cuda` arm of the reference crate binds
+ * through a thin `extern "C"` FFI crate. Each entry point names the reference
+ * interface it replaces (stevel705/sift-wgpu, paths relative to the crate).
+ *
+ * Conventions
+ *  - All entry points return 0 (SIFT_CUDA_OK) on success and a non-zero
+ *    SiftCudaStatus on failure; sift_cuda_last_error() then returns a message
+ *    for the calling thread (the reference returns Err(String),
+ *    src/sift.rs:1244-1248). There is no CPU fallback.
+ *  - Images are 8-bit grayscale, row-major, `stride` bytes between rows
+ *    (stride >= width), the layout of `img.to_luma8().into_raw()`
+ *    (src/sift.rs:1256-1258) when stride == width.
+ *  - Keypoints and descriptors come back in the order of the reference CPU
+ *    path: (octave, layer, y, x) of the detected extremum, then orientation
+ *    peaks in histogram-bin order (src/sift.rs:510-603, 605-726).
+ *  - An engine is not thread-safe: one thread at a time per engine.
+ */
+#ifndef SIFT_CUDA_H
+#define SIFT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SIFT_CUDA_DESCRIPTOR_LEN 128 /* 4x4x8, src/sift.rs:28-29 */
+
+typedef enum {
+    SIFT_CUDA_OK = 0,
+    SIFT_CUDA_ERR_INVALID_ARGUMENT = 1,
+    SIFT_CUDA_ERR_CUDA = 2,
+    SIFT_CUDA_ERR_OUT_OF_MEMORY = 3,
+    SIFT_CUDA_ERR_CAPACITY = 4, /* an internal list overflowed; never returned
+                                   after the automatic retry with larger lists */
+    SIFT_CUDA_ERR_NO_DEVICE = 5,
+    SIFT_CUDA_ERR_UNSUPPORTED = 6
+} SiftCudaStatus;
+
+/* Sift's public fields (src/sift.rs:36-45). contrast_threshold is stored
+ * already divided by num_intervals, exactly as Sift::new / Sift::default store
+ * it (src/sift.rs:55,76); use sift_cuda_params_new to build it from the
+ * undivided value. image_border_width is the private border (5,
+ * src/sift.rs:17). */
+typedef struct {
+    float sigma;
+    uint32_t num_octaves;
+    uint32_t num_intervals;
+    float assumed_blur;
+    float contrast_threshold;
+    float edge_threshold;
+    uint32_t image_border_width;
+} SiftCudaParams;
+
+/* KeyPoint (src/keypoints.rs:2-10) as a C struct, 28 bytes. x, y in
+ * full-resolution pixels, size = sigma (not diameter), angle in radians in
+ * (-pi, pi], response = interpolated DoG value, octave/layer as the CPU path
+ * sets them. */
+typedef struct {
+    float x, y, size, angle, response;
+    int32_t octave, layer;
+} SiftCudaKeypoint;
+
+/* Library-owned result of one image: n keypoints and n x 128 descriptors
+ * (desc == NULL for keypoint-only detection). Free with
+ * sift_cuda_result_free. */
+typedef struct {
+    uint32_t n;
+    SiftCudaKeypoint* kps;
+    float* desc;
+} SiftCudaResult;
+
+/* Pyramid storage of the Gaussian levels in device memory. Levels of the
+ * reference-compatible pyramid hold u8 integers, so both modes are exact; F16
+ * halves the Gaussian bytes and recomputes DoG in f32 from the stored
+ * Gaussians instead of storing it. */
+typedef enum {
+    SIFT_CUDA_STORAGE_F32 = 0, /* Gaussian + DoG levels stored as f32 */
+    SIFT_CUDA_STORAGE_F16 = 1  /* Gaussian levels stored as f16, DoG recomputed */
+} SiftCudaStorage;
+
+typedef struct {
+    int32_t device;   /* CUDA device ordinal */
+    int32_t storage;  /* SiftCudaStorage */
+    uint32_t reserved[6];
+} SiftCudaOptions;
+
+typedef struct SiftCudaEngine SiftCudaEngine;
+
+/* ---- parameters ---------------------------------------------------------- */
+
+/* Sift::default() (src/sift.rs:47-59). */
+void sift_cuda_params_default(SiftCudaParams* out);
+/* Sift::new(sigma, num_octaves, num_intervals, assumed_blur,
+ * contrast_threshold, edge_threshold) (src/sift.rs:63-80): stores
+ * contrast_threshold / num_intervals. */
+void sift_cuda_params_new(SiftCudaParams* out, float sigma, uint32_t num_octaves,
+                          uint32_t num_intervals, float assumed_blur,
+                          float contrast_threshold, float edge_threshold);
+void sift_cuda_options_default(SiftCudaOptions* out);
+
+/* ---- engine lifetime ----------------------------------------------------- */
+
+/* Creates an engine bound to one GPU: stream, device arenas (grown on
+ * demand and kept resident across calls) and weight tables. Replaces the
+ * per-call GPU context construction of the GPU arms (src/sift.rs:1269-1285,
+ * 1314-1329) with one long-lived context. opts may be NULL. */
+int sift_cuda_create(const SiftCudaParams* params, const SiftCudaOptions* opts,
+                     SiftCudaEngine** out);
+void sift_cuda_destroy(SiftCudaEngine* engine);
+
+/* ---- the drop-in call ---------------------------------------------------- */
+
+/* Sift::detect_and_compute_with_backend(img, SiftBackend::Cuda)
+ * (src/sift.rs:1244-1355) for an 8-bit grayscale host image: same keypoints,
+ * order and 128-float descriptors as detect_and_compute_cpu
+ * (src/sift.rs:1200-1240). The image is copied to the device inside the call;
+ * results are copied back into library-owned host arrays. */
+int sift_cuda_detect_and_compute(SiftCudaEngine* engine, const uint8_t* img, uint32_t width,
+                                 uint32_t height, uint32_t stride, SiftCudaResult* out);
+
+/* Sift::detect (src/sift.rs:846-886): keypoints with orientation, no
+ * descriptors (out->desc == NULL). */
+int sift_cuda_detect(SiftCudaEngine* engine, const uint8_t* img, uint32_t width, uint32_t height,
+                     uint32_t stride, SiftCudaResult* out);
+
+void sift_cuda_result_free(SiftCudaResult* result);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* sift_cuda_last_error(void);
+
+/* ---- device-resident form ------------------------------------------------ */
+
+/* Runs the whole pipeline on an image already in device memory, on the
+ * engine's stream, without copying results back; the outputs stay in the
+ * engine's device arena until the next call. `d_count` receives a device
+ * pointer to the keypoint count, d_kps / d_desc device pointers to the arrays.
+ * Returns without synchronising; call sift_cuda_synchronize before reading.
+ * Replaces the readback-free part of GpuSiftV2::detect
+ * (src/gpu_sift_v2.rs:789-858). */
+int sift_cuda_run_device(SiftCudaEngine* engine, const uint8_t* d_img, uint32_t width,
+                         uint32_t height, uint32_t stride, int with_descriptors);
+int sift_cuda_device_outputs(SiftCudaEngine* engine, const uint32_t** d_count,
+                             const SiftCudaKeypoint** d_kps, const float** d_desc);
+int sift_cuda_synchronize(SiftCudaEngine* engine);
+/* The engine's cudaStream_t, as void* (no CUDA types in this header). */
+void* sift_cuda_stream(SiftCudaEngine* engine);
+
+/* ---- introspection used by the parity tests -------------------------------- */
+
+/* Stages of the last run, copied to host memory:
+ *  SIFT_CUDA_STAGE_PYRAMID:    all Gaussian levels as u8, octave-major, then
+ *                              level, row-major with stride = octave width;
+ *                              element size 1.
+ *  SIFT_CUDA_STAGE_CANDIDATES: find_scale_space_extrema output
+ *                              (src/sift.rs:510-603), SiftCudaKeypoint each.
+ *  SIFT_CUDA_STAGE_REFINED:    refine_and_filter_extrema output
+ *                              (src/sift.rs:299-474), SiftCudaKeypoint each.
+ *  SIFT_CUDA_STAGE_DOG:        all DoG levels as f32, octave-major, level,
+ *                              row-major (F32 storage only).
+ * Writes at most `capacity` elements and the total count to *count. */
+enum {
+    SIFT_CUDA_STAGE_PYRAMID = 0,
+    SIFT_CUDA_STAGE_CANDIDATES = 1,
+    SIFT_CUDA_STAGE_REFINED = 2,
+    SIFT_CUDA_STAGE_DOG = 3
+};
+int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t capacity,
+                          uint64_t* count);
+
+/* Device-side kernel launches of the last run (for launch accounting). */
+uint32_t sift_cuda_last_launch_count(SiftCudaEngine* engine);
+
+/* ---- synthetic input -------------------------------------------------------- */
+
+/* Seeded synthetic image: background 128, n_blobs isotropic Gaussian blobs
+ * (centre uniform, sigma U(2,20), amplitude U(-90,90)), n_rects filled
+ * axis-aligned rectangles (sides U{8..96}, intensity U{0..255}), i.i.d.
+ * N(0, 3^2) noise, clamped and rounded to u8. RNG: splitmix64-seeded
+ * xoshiro256**. Writes width*height bytes (stride = width). Host-only. */
+void sift_synth_image(uint64_t seed, uint32_t width, uint32_t height, uint32_t n_blobs,
+                      uint32_t n_rects, uint8_t* out);
+/* Blob and rectangle counts at the 512x512 density (200 blobs, 40 rects). */
+void sift_synth_density(uint32_t width, uint32_t height, uint32_t* n_blobs, uint32_t* n_rects);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SIFT_CUDA_H */

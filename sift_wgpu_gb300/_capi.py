@@ -1,0 +1,153 @@
+"""ctypes binding of libsiftcuda.so (include/sift_cuda.h).
+
+The library is built in-tree by ``sift_wgpu_gb300.build_ext.build()``; loading
+fails loudly when it is missing — there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libsiftcuda.so"
+
+DESC_LEN = 128
+
+STATUS = {
+    0: "OK",
+    1: "INVALID_ARGUMENT",
+    2: "CUDA",
+    3: "OUT_OF_MEMORY",
+    4: "CAPACITY",
+    5: "NO_DEVICE",
+    6: "UNSUPPORTED",
+}
+
+STORAGE_F32 = 0
+STORAGE_F16 = 1
+
+STAGE_PYRAMID = 0
+STAGE_CANDIDATES = 1
+STAGE_REFINED = 2
+STAGE_DOG = 3
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("sigma", C.c_float),
+        ("num_octaves", C.c_uint32),
+        ("num_intervals", C.c_uint32),
+        ("assumed_blur", C.c_float),
+        ("contrast_threshold", C.c_float),
+        ("edge_threshold", C.c_float),
+        ("image_border_width", C.c_uint32),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [("device", C.c_int32), ("storage", C.c_int32), ("reserved", C.c_uint32 * 6)]
+
+
+class Keypoint(C.Structure):
+    _fields_ = [
+        ("x", C.c_float),
+        ("y", C.c_float),
+        ("size", C.c_float),
+        ("angle", C.c_float),
+        ("response", C.c_float),
+        ("octave", C.c_int32),
+        ("layer", C.c_int32),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("kps", C.POINTER(Keypoint)), ("desc", C.POINTER(C.c_float))]
+
+
+# numpy view of SiftCudaKeypoint / OracleKeypoint (28 bytes, packed C layout)
+KEYPOINT_DTYPE = np.dtype(
+    [("x", "<f4"), ("y", "<f4"), ("size", "<f4"), ("angle", "<f4"), ("response", "<f4"),
+     ("octave", "<i4"), ("layer", "<i4")]
+)
+assert KEYPOINT_DTYPE.itemsize == C.sizeof(Keypoint) == 28
+
+_lib = None
+
+
+class SiftCudaError(RuntimeError):
+    """A failed call into libsiftcuda.so (the reference's Err(String))."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{STATUS.get(code, code)}: {message}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build it with sift_wgpu_gb300.build_ext.build() "
+            "(the CUDA engine has no CPU fallback)"
+        )
+    L = C.CDLL(str(LIB_PATH))
+    P = C.POINTER
+    u32, i32, f32, u64 = C.c_uint32, C.c_int32, C.c_float, C.c_uint64
+    sig = {
+        "sift_cuda_params_default": (None, [P(Params)]),
+        "sift_cuda_params_new": (None, [P(Params), f32, u32, u32, f32, f32, f32]),
+        "sift_cuda_options_default": (None, [P(Options)]),
+        "sift_cuda_create": (C.c_int, [P(Params), P(Options), P(C.c_void_p)]),
+        "sift_cuda_destroy": (None, [C.c_void_p]),
+        "sift_cuda_detect_and_compute": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, P(Result)]),
+        "sift_cuda_detect": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, P(Result)]),
+        "sift_cuda_result_free": (None, [P(Result)]),
+        "sift_cuda_last_error": (C.c_char_p, []),
+        "sift_cuda_run_device": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, C.c_int]),
+        "sift_cuda_device_outputs": (C.c_int, [C.c_void_p, P(C.c_void_p), P(C.c_void_p), P(C.c_void_p)]),
+        "sift_cuda_synchronize": (C.c_int, [C.c_void_p]),
+        "sift_cuda_stream": (C.c_void_p, [C.c_void_p]),
+        "sift_cuda_debug_stage": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, u64, P(u64)]),
+        "sift_cuda_last_launch_count": (u32, [C.c_void_p]),
+        "sift_synth_image": (None, [u64, u32, u32, u32, u32, C.c_void_p]),
+        "sift_synth_density": (None, [u32, u32, P(u32), P(u32)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def exported_symbols() -> list[str]:
+    """Names declared in include/sift_cuda.h that the loaded library must export."""
+    return [
+        "sift_cuda_params_default", "sift_cuda_params_new", "sift_cuda_options_default",
+        "sift_cuda_create", "sift_cuda_destroy", "sift_cuda_detect_and_compute", "sift_cuda_detect",
+        "sift_cuda_result_free", "sift_cuda_last_error", "sift_cuda_run_device",
+        "sift_cuda_device_outputs", "sift_cuda_synchronize", "sift_cuda_stream",
+        "sift_cuda_debug_stage", "sift_cuda_last_launch_count", "sift_synth_image",
+        "sift_synth_density",
+    ]
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        raise SiftCudaError(rc, lib().sift_cuda_last_error().decode(errors="replace"))
+
+
+def synth_image(seed: int, width: int, height: int, n_blobs: int | None = None,
+                n_rects: int | None = None) -> np.ndarray:
+    """Seeded synthetic u8 image (sift_synth_image), default 512x512 density."""
+    L = lib()
+    if n_blobs is None or n_rects is None:
+        b, r = C.c_uint32(), C.c_uint32()
+        L.sift_synth_density(width, height, C.byref(b), C.byref(r))
+        n_blobs = b.value if n_blobs is None else n_blobs
+        n_rects = r.value if n_rects is None else n_rects
+    out = np.empty((height, width), dtype=np.uint8)
+    L.sift_synth_image(seed, width, height, n_blobs, n_rects, out.ctypes.data)
+    return out

@@ -1,0 +1,356 @@
+// describe.cu — orientation assignment and 4x4x8 descriptors (sm_103a).
+//
+// Stages (d) and (e) of the hot path: assign_orientations
+// (src/sift.rs:605-726) and compute (src/sift.rs:917-1060) with
+// normalize_and_clip_descriptor (src/sift.rs:889-913).
+//
+//   k_orientation   one warp per refined keypoint: the (2r+1)^2 window is
+//                   split over the lanes, each lane adds into its own column of
+//                   a bin-major shared histogram (conflict-free, no atomics),
+//                   columns are summed in a fixed order, then the two [1,1,1]/3
+//                   smoothing passes and the peak test run one bin per lane;
+//                   peaks come out in bin order through a ballot.
+//   k_orient_emit   keypoint i with c_i peaks writes its c_i oriented copies at
+//                   the scanned offset, so the output order is the reference's
+//                   (keypoint, bin) order.
+//   k_descriptor    one warp per oriented keypoint: samples split over lanes,
+//                   trilinear contributions added into 128 shared bins as
+//                   64-bit fixed point (integer addition is associative, so the
+//                   result does not depend on scheduling), then L2 normalise,
+//                   clip at 0.2, renormalise with warp shuffles.
+//
+// The per-sample arithmetic follows the reference's f32 operation order
+// without FMA; atan2f/expf/sinf/cosf are CUDA's, which differ from the host
+// libm by a few ulp. Histogram sums are not in the reference's sequential
+// order, so orientations and descriptors agree within rounding, not bit for
+// bit.
+#include "sift_internal.cuh"
+
+namespace sift {
+namespace {
+
+constexpr int kWarpsPerCta = 8;
+
+template <typename T>
+__device__ __forceinline__ float gval(const T* p) {
+    return (float)(*p);
+}
+template <>
+__device__ __forceinline__ float gval<__half>(const __half* p) {
+    return __half2float(*p);
+}
+
+template <typename TG>
+struct GaussPlane {
+    const TG* base;
+    int pitch, W, H;
+    const float* lut;  // v / 255 in shared memory
+    // get_gauss_pixel_value (src/sift.rs:218-223)
+    __device__ __forceinline__ float px(int x, int y) const {
+        x = clampi(x, 0, W - 1);
+        y = clampi(y, 0, H - 1);
+        return lut[(int)gval(base + (long long)y * pitch + x)];
+    }
+    // get_gauss_pixel_bilinear (src/sift.rs:238-266)
+    __device__ __forceinline__ float bilinear(float x, float y) const {
+        const float xf = floorf(x), yf = floorf(y);
+        const float xc = __fadd_rn(xf, 1.0f), yc = __fadd_rn(yf, 1.0f);
+        const float dx = __fsub_rn(x, xf), dy = __fsub_rn(y, yf);
+        const int x0 = rust_as_i32(xf), y0 = rust_as_i32(yf), x1 = rust_as_i32(xc), y1 = rust_as_i32(yc);
+        const float q11 = px(x0, y0), q21 = px(x1, y0), q12 = px(x0, y1), q22 = px(x1, y1);
+        const float omx = __fsub_rn(1.0f, dx), omy = __fsub_rn(1.0f, dy);
+        float v = __fmul_rn(__fmul_rn(q11, omx), omy);
+        v = __fadd_rn(v, __fmul_rn(__fmul_rn(q21, dx), omy));
+        v = __fadd_rn(v, __fmul_rn(__fmul_rn(q12, omx), dy));
+        v = __fadd_rn(v, __fmul_rn(__fmul_rn(q22, dx), dy));
+        return v;
+    }
+};
+
+template <typename TG>
+__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const PyramidDev& pyr, int o, int layer,
+                                                    const float* lut) {
+    const int li = clampi(layer, 0, pyr.S + 2);
+    const OctaveDev& od = pyr.oct[o];
+    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H, lut};
+}
+
+__device__ __forceinline__ void fill_lut(float* lut) {
+    for (int i = threadIdx.x + threadIdx.y * blockDim.x; i < 256; i += blockDim.x * blockDim.y)
+        lut[i] = __fdiv_rn((float)i, 255.0f);
+}
+
+template <typename TG>
+__global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
+                                                                   const Keypoint* __restrict__ refined,
+                                                                   const Counters* __restrict__ ctr,
+                                                                   float* __restrict__ ori_angle,
+                                                                   uint32_t* __restrict__ ori_count) {
+    __shared__ float lut[256];
+    __shared__ float hist[kWarpsPerCta][kOriBins][32];
+    __shared__ float hs[kWarpsPerCta][kOriBins];
+    fill_lut(lut);
+    __syncthreads();
+    const int lane = threadIdx.x, wid = threadIdx.y;
+    const uint32_t n = ctr->n_refined;
+    const float two_pi = 2.0f * kPi;
+    const float bin_w = 2.0f * kPi / (float)kOriBins;
+    for (uint32_t i = blockIdx.x * kWarpsPerCta + wid; i < n; i += gridDim.x * kWarpsPerCta) {
+        const Keypoint kp = refined[i];
+        const int o = kp.octave;
+        uint32_t cnt = 0;
+        if (o >= 0 && o < pyr.num_octaves) {
+            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
+            const float scale = __int_as_float((127 + o) << 23);
+            const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
+            const float so = __fdiv_rn(kp.size, scale);
+            if (so > 0.0f) {
+                const int r = rust_as_i32(roundf(__fmul_rn(4.5f, so)));
+                const float ws = __fmul_rn(1.5f, so);
+                const float wd = __fmul_rn(__fmul_rn(2.0f, ws), ws);
+#pragma unroll
+                for (int b = 0; b < kOriBins; ++b) hist[wid][b][lane] = 0.0f;
+                const int side = 2 * r + 1;
+                const int total = side * side;
+                for (int k = lane; k < total; k += 32) {
+                    const int dy = k / side - r, dx = k % side - r;
+                    const int xi = rust_as_i32(roundf(__fadd_rn(xo, (float)dx)));
+                    const int yi = rust_as_i32(roundf(__fadd_rn(yo, (float)dy)));
+                    if (xi < 1 || xi >= g.W - 1 || yi < 1 || yi >= g.H - 1) continue;
+                    const float gx = __fsub_rn(g.px(xi + 1, yi), g.px(xi - 1, yi));
+                    const float gy = __fsub_rn(g.px(xi, yi + 1), g.px(xi, yi - 1));
+                    const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
+                    const float ang = atan2f(gy, gx);
+                    const float fdx = (float)dx, fdy = (float)dy;
+                    const float wgt = expf(__fdiv_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), wd));
+                    const float an = ang < 0.0f ? __fadd_rn(ang, two_pi) : ang;
+                    const float bf = __fdiv_rn(__fmul_rn(an, (float)kOriBins), two_pi);
+                    const float fl = floorf(bf);
+                    const unsigned bin = (fl <= 0.0f ? 0u : (unsigned)fl) % kOriBins;
+                    hist[wid][bin][lane] = __fadd_rn(hist[wid][bin][lane], __fmul_rn(mag, wgt));
+                }
+                __syncwarp();
+                // Column sums, bins lane and lane+32.
+                for (int b = lane; b < kOriBins; b += 32) {
+                    float s = 0.0f;
+                    for (int l = 0; l < 32; ++l) s = __fadd_rn(s, hist[wid][b][(l + b) & 31]);
+                    hs[wid][b] = s;
+                }
+                __syncwarp();
+                for (int it = 0; it < 2; ++it) {
+                    float nv0 = 0.0f, nv1 = 0.0f;
+                    for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) {
+                        const float v = __fdiv_rn(
+                            __fadd_rn(__fadd_rn(hs[wid][(b + kOriBins - 1) % kOriBins], hs[wid][b]),
+                                      hs[wid][(b + 1) % kOriBins]),
+                            3.0f);
+                        if (q == 0) nv0 = v; else nv1 = v;
+                    }
+                    __syncwarp();
+                    for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) hs[wid][b] = q == 0 ? nv0 : nv1;
+                    __syncwarp();
+                }
+                float mx = 0.0f;
+                for (int b = 0; b < kOriBins; ++b) mx = fmaxf(mx, hs[wid][b]);
+                const float thr = __fmul_rn(mx, 0.8f);
+                bool pk[2] = {false, false};
+                float pa[2] = {0.0f, 0.0f};
+                for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) {
+                    const float cv = hs[wid][b];
+                    if (!(cv >= thr)) continue;
+                    const float pv = hs[wid][(b + kOriBins - 1) % kOriBins];
+                    const float nv = hs[wid][(b + 1) % kOriBins];
+                    if (cv > pv && cv > nv) {
+                        const float den = __fadd_rn(__fsub_rn(pv, __fmul_rn(2.0f, cv)), nv);
+                        const float off =
+                            fabsf(den) > 1e-5f ? __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(pv, nv)), den) : 0.0f;
+                        const float center = __fmul_rn(__fadd_rn((float)b, 0.5f), bin_w);
+                        const float a = __fadd_rn(center, __fmul_rn(off, bin_w));
+                        float fa = rem_euclid(a, two_pi);
+                        if (fa > kPi) fa = __fsub_rn(fa, two_pi);
+                        pk[q] = true;
+                        pa[q] = fa;
+                    }
+                }
+                const uint32_t m0 = __ballot_sync(0xffffffffu, pk[0]);
+                const uint32_t m1 = __ballot_sync(0xffffffffu, pk[1]);
+                const uint32_t lt = (1u << lane) - 1u;
+                if (pk[0]) ori_angle[(size_t)i * kOriMaxPeaks + __popc(m0 & lt)] = pa[0];
+                if (pk[1]) ori_angle[(size_t)i * kOriMaxPeaks + __popc(m0) + __popc(m1 & lt)] = pa[1];
+                cnt = (uint32_t)(__popc(m0) + __popc(m1));
+                __syncwarp();
+            }
+        }
+        if (lane == 0) ori_count[i] = cnt;
+    }
+}
+
+__global__ void k_orient_emit(const Keypoint* __restrict__ refined, const Counters* __restrict__ ctr,
+                              const float* __restrict__ ori_angle, const uint32_t* __restrict__ ori_count,
+                              const uint32_t* __restrict__ ori_off, Keypoint* __restrict__ oriented, uint32_t cap,
+                              Counters* __restrict__ ctr_w) {
+    const uint32_t n = ctr->n_refined;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t c = ori_count[i], off = ori_off[i];
+        Keypoint k = refined[i];
+        for (uint32_t j = 0; j < c; ++j) {
+            if (off + j >= cap) {
+                atomicOr(&ctr_w->overflow, 4u);
+                break;
+            }
+            k.angle = ori_angle[(size_t)i * kOriMaxPeaks + j];
+            oriented[off + j] = k;
+        }
+    }
+}
+
+template <typename TG>
+__global__ void __launch_bounds__(32 * kWarpsPerCta) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
+                                                                  const Keypoint* __restrict__ oriented,
+                                                                  const Counters* __restrict__ ctr,
+                                                                  float* __restrict__ desc, uint32_t cap) {
+    __shared__ float lut[256];
+    __shared__ unsigned long long hist[kWarpsPerCta][kDescLen];
+    fill_lut(lut);
+    __syncthreads();
+    const int lane = threadIdx.x, wid = threadIdx.y;
+    uint32_t n = ctr->n_oriented;
+    if (n > cap) n = cap;
+    const float two_pi = 2.0f * kPi;
+    const float sqrt2 = __fsqrt_rn(2.0f);
+    for (uint32_t i = blockIdx.x * kWarpsPerCta + wid; i < n; i += gridDim.x * kWarpsPerCta) {
+        const Keypoint kp = oriented[i];
+        const int o = kp.octave;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) hist[wid][lane + 32 * q] = 0ull;
+        __syncwarp();
+        bool valid = o >= 0 && o < pyr.num_octaves;
+        float so = 0.0f;
+        const float scale = valid ? __int_as_float((127 + o) << 23) : 1.0f;
+        if (valid) so = __fdiv_rn(kp.size, scale);
+        if (valid && so > 0.0f) {
+            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
+            const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
+            const float ang = kp.angle;
+            const float ca = cosf(ang), sa = sinf(ang);
+            const float bw = __fmul_rn(3.0f, so);
+            const float ww = __fmul_rn(bw, 4.0f);
+            const float wsig = __fmul_rn(0.5f, ww);
+            const float wd = __fmul_rn(__fmul_rn(2.0f, wsig), wsig);
+            const int rad = rust_as_i32(ceilf(__fmul_rn(__fmul_rn(ww, sqrt2), 0.5f)));
+            const float wm1 = (float)(g.W - 1), hm1 = (float)(g.H - 1);
+            const int side = 2 * rad + 1;
+            const int total = side * side;
+            for (int k = lane; k < total; k += 32) {
+                const int dyi = k / side - rad, dxi = k % side - rad;
+                const float px = (float)dxi, py = (float)dyi;
+                const float rx = __fadd_rn(__fmul_rn(ca, px), __fmul_rn(sa, py));
+                const float ry = __fadd_rn(__fmul_rn(-sa, px), __fmul_rn(ca, py));
+                const float xb = __fsub_rn(__fadd_rn(__fdiv_rn(rx, bw), 2.0f), 0.5f);
+                const float yb = __fsub_rn(__fadd_rn(__fdiv_rn(ry, bw), 2.0f), 0.5f);
+                if (!(xb > -1.0f && xb < 4.0f && yb > -1.0f && yb < 4.0f)) continue;
+                const float xs = __fadd_rn(xo, px), ys = __fadd_rn(yo, py);
+                if (xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1) continue;
+                const float gx = __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
+                const float gy = __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
+                const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
+                const float pa = atan2f(gy, gx);
+                const float ar = rem_euclid(__fsub_rn(pa, ang), two_pi);
+                const float wgt = expf(__fdiv_rn(-__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), wd));
+                const float wm = __fmul_rn(mag, wgt);
+                const float ab = __fdiv_rn(__fmul_rn(ar, 8.0f), two_pi);
+                const int xbi = rust_as_i32(floorf(xb)), ybi = rust_as_i32(floorf(yb)), abi = rust_as_i32(floorf(ab));
+                const float fx = __fsub_rn(xb, (float)xbi), fy = __fsub_rn(yb, (float)ybi), fa = __fsub_rn(ab, (float)abi);
+#pragma unroll
+                for (int ii = 0; ii < 2; ++ii) {
+                    const int ix = xbi + ii;
+                    if (ix < 0 || ix >= 4) continue;
+                    const float wx = ii == 0 ? __fsub_rn(1.0f, fx) : fx;
+#pragma unroll
+                    for (int jj = 0; jj < 2; ++jj) {
+                        const int iy = ybi + jj;
+                        if (iy < 0 || iy >= 4) continue;
+                        const float wy = jj == 0 ? __fsub_rn(1.0f, fy) : fy;
+#pragma unroll
+                        for (int kk = 0; kk < 2; ++kk) {
+                            const int ia = ((abi + kk) % 8 + 8) % 8;
+                            const float wa = kk == 0 ? __fsub_rn(1.0f, fa) : fa;
+                            const float c = __fmul_rn(__fmul_rn(__fmul_rn(wm, wx), wy), wa);
+                            const unsigned long long q =
+                                c > 0.0f ? (unsigned long long)__float2ull_rn(__fmul_rn(c, 4294967296.0f)) : 0ull;
+                            if (q) atomicAdd(&hist[wid][(iy * 4 + ix) * 8 + ia], q);
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // normalize_and_clip_descriptor (src/sift.rs:889-913)
+        float d[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) d[q] = (float)((double)hist[wid][lane + 32 * q] * (1.0 / 4294967296.0));
+        float ss = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) ss = __fadd_rn(ss, __fmul_rn(d[q], d[q]));
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1) ss = __fadd_rn(ss, __shfl_xor_sync(0xffffffffu, ss, m));
+        const float norm = __fsqrt_rn(ss);
+        if (!(norm < 1e-8f)) {
+            const float inv = __fdiv_rn(1.0f, norm);
+            float s2 = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                d[q] = fminf(__fmul_rn(d[q], inv), 0.2f);
+                s2 = __fadd_rn(s2, __fmul_rn(d[q], d[q]));
+            }
+#pragma unroll
+            for (int m = 16; m > 0; m >>= 1) s2 = __fadd_rn(s2, __shfl_xor_sync(0xffffffffu, s2, m));
+            const float n2 = __fsqrt_rn(s2);
+            if (!(n2 < 1e-8f)) {
+                const float inv2 = __fdiv_rn(1.0f, n2);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) d[q] = __fmul_rn(d[q], inv2);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) desc[(size_t)i * kDescLen + lane + 32 * q] = d[q];
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+int describe_grid() { return 152 * 4; }
+
+template <typename TG>
+int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, const Counters* ctr,
+                       float* ori_angle, uint32_t* ori_count, cudaStream_t st) {
+    k_orientation<TG><<<describe_grid(), dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined, ctr, ori_angle,
+                                                                         ori_count);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_orient_emit(const Keypoint* refined, const Counters* ctr, const float* ori_angle,
+                       const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
+                       Counters* ctr_w, cudaStream_t st) {
+    k_orient_emit<<<152 * 2, 256, 0, st>>>(refined, ctr, ori_angle, ori_count, ori_off, oriented, cap, ctr_w);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename TG>
+int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, const Counters* ctr,
+                      float* desc, uint32_t cap, cudaStream_t st) {
+    k_descriptor<TG><<<describe_grid(), dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, oriented, ctr, desc, cap);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template int launch_orientation<float>(const float*, const PyramidDev&, const Keypoint*, const Counters*, float*,
+                                       uint32_t*, cudaStream_t);
+template int launch_orientation<__half>(const __half*, const PyramidDev&, const Keypoint*, const Counters*, float*,
+                                        uint32_t*, cudaStream_t);
+template int launch_descriptor<float>(const float*, const PyramidDev&, const Keypoint*, const Counters*, float*,
+                                      uint32_t, cudaStream_t);
+template int launch_descriptor<__half>(const __half*, const PyramidDev&, const Keypoint*, const Counters*, float*,
+                                       uint32_t, cudaStream_t);
+
+}  // namespace sift

@@ -1,0 +1,738 @@
+// engine.cu — the SIFT engine behind the C ABI of include/sift_cuda.h.
+//
+// One engine owns one CUDA stream and a device arena laid out per image size:
+//
+//   G arena    octave-major Gaussian levels, (S+3) planes per octave, each
+//              plane pitch x H (pitch = width rounded up to 32 elements), f32
+//              or f16 (u8-valued either way)
+//   DoG arena  (S+2) f32 planes per octave (f32 storage only)
+//   tmp        one u8 plane for the horizontal blur pass (largest octave)
+//   ltmp       one f32 plane for the vertical Lanczos pass
+//   mask       per octave S x H x ceil(W/32) ballot words of extrema
+//   lists      candidates / refined / oriented keypoints and descriptors,
+//              sized by capacity and grown (with a re-run) on overflow
+//
+// Everything stays resident across calls; the filter tables are rebuilt only
+// when the image size changes. A run is a fixed sequence of launches on the
+// stream with no host synchronisation until the final counters are read, so
+// the same sequence is replayed from a CUDA graph per image size.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sift_internal.cuh"
+#include "tables.h"
+
+namespace sift {
+
+// launchers (pyramid.cu, detect.cu, describe.cu)
+template <typename TIn>
+int launch_blur_rows(const TIn* in, long long in_pitch, uint8_t* out, int out_pitch, int W, int H, int r,
+                     const float* wts, int round_mode, cudaStream_t st);
+template <typename TG>
+int launch_blur_cols(const uint8_t* tmp, int tmp_pitch, const TG* prev, TG* out, float* dog, int pitch, int W,
+                     int H, int r, const float* wts, int round_mode, cudaStream_t st);
+template <typename TG>
+int launch_copy_level(const TG* prev, TG* out, float* dog, int pitch, int W, int H, cudaStream_t st);
+template <typename TG>
+int launch_lanczos(const TG* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst, int dst_pitch,
+                   int nW, int nH, const int* vtab, const float* vw, const int* htab, const float* hw,
+                   cudaStream_t st);
+int launch_extrema_mask(int storage, const void* arena, const PyramidDev& pyr, int o, int border, uint32_t* words,
+                        cudaStream_t st);
+int launch_emit_refine(int storage, const void* arena, const PyramidDev& pyr, long long n_words,
+                       const uint32_t* words, const uint32_t* cand_off, float sigma, float contrast, float edge,
+                       Keypoint* cands, Keypoint* refined_at, uint32_t* keep_mask, uint32_t* keep_count,
+                       uint32_t cap, Counters* ctr, cudaStream_t st);
+int launch_compact(long long n_words, const uint32_t* words, const uint32_t* cand_off, const uint32_t* keep_mask,
+                   const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined, uint32_t cap,
+                   cudaStream_t st);
+template <typename TG>
+int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, const Counters* ctr,
+                       float* ori_angle, uint32_t* ori_count, cudaStream_t st);
+int launch_orient_emit(const Keypoint* refined, const Counters* ctr, const float* ori_angle,
+                       const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
+                       Counters* ctr_w, cudaStream_t st);
+template <typename TG>
+int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, const Counters* ctr,
+                      float* desc, uint32_t cap, cudaStream_t st);
+template <typename TG>
+int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, int pitch, int W, int H, cudaStream_t st);
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(e == cudaErrorMemoryAllocation ? SIFT_CUDA_ERR_OUT_OF_MEMORY
+                                               : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver
+                                                      ? SIFT_CUDA_ERR_NO_DEVICE
+                                                      : SIFT_CUDA_ERR_CUDA),
+                m);
+}
+
+#define CK(call, what)                              \
+    do {                                            \
+        cudaError_t e_ = (call);                    \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+struct DevMem {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevMem() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        release();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    template <typename T>
+    T* as() const {
+        return (T*)p;
+    }
+};
+
+struct HostPinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~HostPinned() { release(); }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        release();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaHostAlloc(&p, n, cudaHostAllocDefault);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    template <typename T>
+    T* as() const {
+        return (T*)p;
+    }
+};
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct LevelBlur {
+    float sigma;   // 0 = copy
+    int radius;
+    size_t woff;   // offset in the weight table
+};
+
+struct Engine {
+    SiftCudaParams p{};
+    SiftCudaOptions opt{};
+    cudaStream_t st = nullptr;
+    int round_mode = 0;
+
+    // geometry of the current arena
+    uint32_t W = 0, H = 0;
+    bool have_geom = false;
+    PyramidDev pyr{};
+    long long n_words = 0;
+    size_t g_elems = 0, d_elems = 0, tmp_bytes = 0, ltmp_elems = 0;
+    LevelBlur base{};
+    std::vector<std::vector<LevelBlur>> lv;  // [o][s-1]
+    struct LTab {
+        size_t vtab, vw, htab, hw;  // element offsets in d_ltab / d_lw
+    };
+    std::vector<LTab> ltab;  // [o] for o -> o+1
+
+    uint32_t cap_cand = 0, cap_ori = 0;
+
+    DevMem d_img, d_G, d_D, d_tmp, d_ltmp, d_wts, d_ltab, d_lw;
+    DevMem d_words, d_cand_off, d_keep_mask, d_keep_count, d_keep_off, d_partials;
+    DevMem d_cands, d_refined_at, d_refined, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
+    HostPinned h_ctr, h_kps, h_desc;
+    size_t img_pitch = 0;
+    uint32_t launches = 0;
+    bool last_desc = true;
+
+    ~Engine() {
+        if (st) cudaStreamDestroy(st);
+    }
+
+    bool f16() const { return opt.storage == SIFT_CUDA_STORAGE_F16; }
+    size_t g_elem_size() const { return f16() ? 2 : 4; }
+
+    int set_device() {
+        CK(cudaSetDevice(opt.device), "cudaSetDevice");
+        return 0;
+    }
+
+    int init() {
+        if (int rc = set_device()) return rc;
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(h_ctr.ensure(sizeof(Counters)), "cudaHostAlloc(counters)");
+        CK(d_ctr.ensure(sizeof(Counters)), "cudaMalloc(counters)");
+        return 0;
+    }
+
+    // Lays out the arena for a width x height image and builds the tables.
+    int ensure_geometry(uint32_t w, uint32_t h) {
+        if (have_geom && w == W && h == H) return 0;
+        const int O = (int)p.num_octaves, S = (int)p.num_intervals;
+        if (O > kMaxOctaves) return fail(SIFT_CUDA_ERR_UNSUPPORTED, "num_octaves above 16 is not supported");
+        PyramidDev g{};
+        g.num_octaves = O;
+        g.S = S;
+        g.levels = S + 3;
+        size_t goff = 0, doff = 0, wbase = 0, tmpb = 0, lt = 0;
+        uint32_t ow = w, oh = h;
+        for (int o = 0; o < O; ++o) {
+            OctaveDev& od = g.oct[o];
+            od.W = (int)ow;
+            od.H = (int)oh;
+            od.pitch = (int)align_up(std::max<uint32_t>(ow, 1), 32);
+            od.nw = (int)((ow + 31) / 32);
+            od.plane = (long long)od.pitch * oh;
+            od.g_off = (long long)goff;
+            od.d_off = (long long)doff;
+            od.word_base = (long long)wbase;
+            goff += (size_t)od.plane * (S + 3);
+            doff += f16() ? 0 : (size_t)od.plane * (S + 2);
+            wbase += (size_t)S * oh * od.nw;
+            tmpb = std::max(tmpb, (size_t)od.pitch * oh);
+            if (o + 1 < O) lt = std::max(lt, (size_t)od.pitch * (oh / 2));
+            ow /= 2;
+            oh /= 2;
+        }
+        // blur tables
+        BlurPlan bp = blur_plan(p);
+        std::vector<float> wts;
+        auto add_blur = [&](float sigma) {
+            LevelBlur b{sigma, 0, wts.size()};
+            if (sigma > 0.0f) {
+                auto k = gaussian_kernel(sigma);
+                b.radius = (int)(k.size() / 2);
+                wts.insert(wts.end(), k.begin(), k.end());
+                while (wts.size() % 4) wts.push_back(0.0f);
+            }
+            return b;
+        };
+        base = add_blur(bp.base);
+        lv.assign(O, {});
+        for (int o = 0; o < O; ++o)
+            for (int s = 1; s < S + 3; ++s) lv[o].push_back(add_blur(bp.level[o][s - 1]));
+        // Lanczos tables
+        std::vector<int> itab;
+        std::vector<float> ftab;
+        ltab.assign(O, LTab{0, 0, 0, 0});
+        for (int o = 0; o + 1 < O; ++o) {
+            const OctaveDev& a = g.oct[o];
+            const int nW = g.oct[o + 1].W, nH = g.oct[o + 1].H;
+            if (a.W == 0 || a.H == 0 || nW == 0 || nH == 0) continue;
+            AxisTaps tv = lanczos_axis((uint32_t)a.H, (uint32_t)nH);
+            AxisTaps th = lanczos_axis((uint32_t)a.W, (uint32_t)nW);
+            LTab t;
+            t.vtab = itab.size();
+            itab.insert(itab.end(), tv.left.begin(), tv.left.end());
+            itab.insert(itab.end(), tv.count.begin(), tv.count.end());
+            itab.insert(itab.end(), tv.woff.begin(), tv.woff.end());
+            t.vw = ftab.size();
+            ftab.insert(ftab.end(), tv.w.begin(), tv.w.end());
+            t.htab = itab.size();
+            itab.insert(itab.end(), th.left.begin(), th.left.end());
+            itab.insert(itab.end(), th.count.begin(), th.count.end());
+            itab.insert(itab.end(), th.woff.begin(), th.woff.end());
+            t.hw = ftab.size();
+            ftab.insert(ftab.end(), th.w.begin(), th.w.end());
+            ltab[o] = t;
+        }
+        // allocate
+        n_words = (long long)wbase;
+        CK(d_G.ensure(goff * g_elem_size()), "cudaMalloc(G)");
+        if (!f16()) CK(d_D.ensure(doff * sizeof(float)), "cudaMalloc(DoG)");
+        CK(d_tmp.ensure(std::max<size_t>(tmpb, 16)), "cudaMalloc(tmp)");
+        CK(d_ltmp.ensure(std::max<size_t>(lt, 4) * sizeof(float)), "cudaMalloc(ltmp)");
+        CK(d_wts.ensure(std::max<size_t>(wts.size(), 4) * sizeof(float)), "cudaMalloc(wts)");
+        CK(d_ltab.ensure(std::max<size_t>(itab.size(), 4) * sizeof(int)), "cudaMalloc(ltab)");
+        CK(d_lw.ensure(std::max<size_t>(ftab.size(), 4) * sizeof(float)), "cudaMalloc(lw)");
+        const size_t nwb = std::max<size_t>((size_t)n_words, 1) * sizeof(uint32_t);
+        CK(d_words.ensure(nwb), "cudaMalloc(words)");
+        CK(d_cand_off.ensure(nwb), "cudaMalloc(cand_off)");
+        CK(d_keep_mask.ensure(nwb), "cudaMalloc(keep_mask)");
+        CK(d_keep_count.ensure(nwb), "cudaMalloc(keep_count)");
+        CK(d_keep_off.ensure(nwb), "cudaMalloc(keep_off)");
+        if (!wts.empty())
+            CK(cudaMemcpyAsync(d_wts.p, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st), "H2D wts");
+        if (!itab.empty())
+            CK(cudaMemcpyAsync(d_ltab.p, itab.data(), itab.size() * sizeof(int), cudaMemcpyHostToDevice, st),
+               "H2D ltab");
+        if (!ftab.empty())
+            CK(cudaMemcpyAsync(d_lw.p, ftab.data(), ftab.size() * sizeof(float), cudaMemcpyHostToDevice, st), "H2D lw");
+        CK(cudaStreamSynchronize(st), "table upload");
+        pyr = g;
+        g_elems = goff;
+        d_elems = doff;
+        tmp_bytes = tmpb;
+        ltmp_elems = lt;
+        W = w;
+        H = h;
+        have_geom = true;
+        if (cap_cand == 0) {
+            // Initial list capacity: 1/64 of the scanned positions (measured
+            // densities on natural and synthetic images are far below it);
+            // grown on overflow.
+            size_t positions = (size_t)n_words * 32;
+            cap_cand = (uint32_t)std::min<size_t>(std::max<size_t>(positions / 64, 4096), 1u << 30);
+            cap_ori = cap_cand;
+        }
+        return ensure_lists();
+    }
+
+    int ensure_lists() {
+        const size_t kp = sizeof(Keypoint);
+        CK(d_cands.ensure((size_t)cap_cand * kp), "cudaMalloc(cands)");
+        CK(d_refined_at.ensure((size_t)cap_cand * kp), "cudaMalloc(refined_at)");
+        CK(d_refined.ensure((size_t)cap_cand * kp), "cudaMalloc(refined)");
+        CK(d_ori_angle.ensure((size_t)cap_cand * kOriMaxPeaks * sizeof(float)), "cudaMalloc(ori_angle)");
+        CK(d_ori_count.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(ori_count)");
+        CK(d_ori_off.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(ori_off)");
+        CK(d_oriented.ensure((size_t)cap_ori * kp), "cudaMalloc(oriented)");
+        CK(d_desc.ensure((size_t)cap_ori * kDescLen * sizeof(float)), "cudaMalloc(desc)");
+        size_t np = scan_partials_size(std::max<size_t>({(size_t)n_words, (size_t)cap_cand, 1}));
+        CK(d_partials.ensure(np * sizeof(uint32_t)), "cudaMalloc(partials)");
+        return 0;
+    }
+
+    template <typename TG>
+    int enqueue_t(const uint8_t* img, long long stride, bool with_desc) {
+        const int O = pyr.num_octaves, S = pyr.S;
+        TG* G = d_G.as<TG>();
+        float* D = f16() ? nullptr : d_D.as<float>();
+        const float* wts = d_wts.as<float>();
+        uint8_t* tmp = d_tmp.as<uint8_t>();
+        launches = 0;
+        auto ok = [&](int rc) {
+            ++launches;
+            return rc;
+        };
+        CK(cudaMemsetAsync(d_ctr.p, 0, sizeof(Counters), st), "memset counters");
+        const OctaveDev& o0 = pyr.oct[0];
+        if (o0.W > 0 && o0.H > 0) {
+            // base image (src/sift.rs:1204-1214)
+            if (base.sigma > 0.0f) {
+                if (ok(launch_blur_rows<uint8_t>(img, stride, tmp, o0.pitch, o0.W, o0.H, base.radius, wts + base.woff,
+                                                 round_mode, st)))
+                    return cuda_fail(cudaGetLastError(), "blur rows (base)");
+                if (ok(launch_blur_cols<TG>(tmp, o0.pitch, nullptr, G + o0.g_off, nullptr, o0.pitch, o0.W, o0.H,
+                                            base.radius, wts + base.woff, round_mode, st)))
+                    return cuda_fail(cudaGetLastError(), "blur cols (base)");
+            } else {
+                if (ok(launch_u8_to_level<TG>(img, stride, G + o0.g_off, o0.pitch, o0.W, o0.H, st)))
+                    return cuda_fail(cudaGetLastError(), "base copy");
+            }
+        }
+        for (int o = 0; o < O; ++o) {
+            const OctaveDev& od = pyr.oct[o];
+            if (od.W == 0 || od.H == 0) break;
+            for (int s = 1; s < S + 3; ++s) {
+                const LevelBlur& b = lv[o][s - 1];
+                const TG* prev = G + od.g_off + (long long)(s - 1) * od.plane;
+                TG* out = G + od.g_off + (long long)s * od.plane;
+                float* dog = D ? D + od.d_off + (long long)(s - 1) * od.plane : nullptr;
+                if (b.sigma <= 0.0f) {
+                    if (ok(launch_copy_level<TG>(prev, out, dog, od.pitch, od.W, od.H, st)))
+                        return cuda_fail(cudaGetLastError(), "copy level");
+                    continue;
+                }
+                if (ok(launch_blur_rows<TG>(prev, od.pitch, tmp, od.pitch, od.W, od.H, b.radius, wts + b.woff,
+                                            round_mode, st)))
+                    return cuda_fail(cudaGetLastError(), "blur rows");
+                if (ok(launch_blur_cols<TG>(tmp, od.pitch, prev, out, dog, od.pitch, od.W, od.H, b.radius,
+                                            wts + b.woff, round_mode, st)))
+                    return cuda_fail(cudaGetLastError(), "blur cols");
+            }
+            if (o + 1 < O) {
+                const OctaveDev& nx = pyr.oct[o + 1];
+                if (nx.W == 0 || nx.H == 0) break;
+                const LTab& t = ltab[o];
+                const int* it = d_ltab.as<int>();
+                const float* ft = d_lw.as<float>();
+                if (ok(launch_lanczos<TG>(G + od.g_off + (long long)S * od.plane, od.pitch, od.W, od.H,
+                                          d_ltmp.as<float>(), od.pitch, G + nx.g_off, nx.pitch, nx.W, nx.H,
+                                          it + t.vtab, ft + t.vw, it + t.htab, ft + t.hw, st)))
+                    return cuda_fail(cudaGetLastError(), "lanczos");
+                ++launches;
+            }
+        }
+        // (b) extrema -> (c) ordered candidates + refinement
+        const void* arena = f16() ? (const void*)d_G.p : (const void*)d_D.p;
+        Counters* ctr = d_ctr.as<Counters>();
+        for (int o = 0; o < O; ++o) {
+            const OctaveDev& od = pyr.oct[o];
+            if (od.W == 0 || od.H == 0 || od.nw == 0) continue;
+            if (ok(launch_extrema_mask(opt.storage, arena, pyr, o, (int)p.image_border_width, d_words.as<uint32_t>(),
+                                       st)))
+                return cuda_fail(cudaGetLastError(), "extrema mask");
+        }
+        uint32_t* words = d_words.as<uint32_t>();
+        if (scan_exclusive(words, SCAN_POPC, d_cand_off.as<uint32_t>(), (size_t)n_words, nullptr, &ctr->n_candidates,
+                           d_partials.as<uint32_t>(), st))
+            return cuda_fail(cudaGetLastError(), "scan candidates");
+        launches += 3;
+        if (ok(launch_emit_refine(opt.storage, arena, pyr, n_words, words, d_cand_off.as<uint32_t>(), p.sigma,
+                                  p.contrast_threshold, p.edge_threshold, d_cands.as<Keypoint>(),
+                                  d_refined_at.as<Keypoint>(), d_keep_mask.as<uint32_t>(),
+                                  d_keep_count.as<uint32_t>(), cap_cand, ctr, st)))
+            return cuda_fail(cudaGetLastError(), "emit/refine");
+        if (scan_exclusive(d_keep_count.as<uint32_t>(), SCAN_U32, d_keep_off.as<uint32_t>(), (size_t)n_words, nullptr,
+                           &ctr->n_refined, d_partials.as<uint32_t>(), st))
+            return cuda_fail(cudaGetLastError(), "scan refined");
+        launches += 3;
+        if (ok(launch_compact(n_words, words, d_cand_off.as<uint32_t>(), d_keep_mask.as<uint32_t>(),
+                              d_keep_off.as<uint32_t>(), d_refined_at.as<Keypoint>(), d_refined.as<Keypoint>(),
+                              cap_cand, st)))
+            return cuda_fail(cudaGetLastError(), "compact");
+        // (d) orientation
+        if (ok(launch_orientation<TG>(G, pyr, d_refined.as<Keypoint>(), ctr, d_ori_angle.as<float>(),
+                                      d_ori_count.as<uint32_t>(), st)))
+            return cuda_fail(cudaGetLastError(), "orientation");
+        if (scan_exclusive(d_ori_count.as<uint32_t>(), SCAN_U32, d_ori_off.as<uint32_t>(), (size_t)cap_cand,
+                           &ctr->n_refined, &ctr->n_oriented, d_partials.as<uint32_t>(), st))
+            return cuda_fail(cudaGetLastError(), "scan orientations");
+        launches += 3;
+        if (ok(launch_orient_emit(d_refined.as<Keypoint>(), ctr, d_ori_angle.as<float>(), d_ori_count.as<uint32_t>(),
+                                  d_ori_off.as<uint32_t>(), d_oriented.as<Keypoint>(), cap_ori, ctr, st)))
+            return cuda_fail(cudaGetLastError(), "orientation emit");
+        // (e) descriptors
+        if (with_desc) {
+            if (ok(launch_descriptor<TG>(G, pyr, d_oriented.as<Keypoint>(), ctr, d_desc.as<float>(), cap_ori, st)))
+                return cuda_fail(cudaGetLastError(), "descriptor");
+        }
+        last_desc = with_desc;
+        return 0;
+    }
+
+    int enqueue(const uint8_t* img, long long stride, bool with_desc) {
+        return f16() ? enqueue_t<__half>(img, stride, with_desc) : enqueue_t<float>(img, stride, with_desc);
+    }
+
+    // Reads the counters; grows the lists and reports 1 when a list overflowed.
+    int check_counters(bool* retry) {
+        *retry = false;
+        CK(cudaMemcpyAsync(h_ctr.p, d_ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, st), "D2H counters");
+        CK(cudaStreamSynchronize(st), "run");
+        const Counters c = *h_ctr.as<Counters>();
+        bool grow = c.overflow != 0 || c.n_candidates > cap_cand || c.n_oriented > cap_ori;
+        if (grow) {
+            size_t nc = std::max<size_t>((size_t)cap_cand, (size_t)c.n_candidates + c.n_candidates / 4 + 1024);
+            size_t no = std::max<size_t>((size_t)cap_ori, (size_t)c.n_oriented + c.n_oriented / 4 + 1024);
+            if (c.overflow & 4u) no = std::max<size_t>(no, (size_t)cap_ori * 2);
+            if (nc > (1u << 30) || no > (1u << 30)) return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint lists above 2^30");
+            cap_cand = (uint32_t)nc;
+            cap_ori = (uint32_t)no;
+            if (int rc = ensure_lists()) return rc;
+            *retry = true;
+        }
+        return 0;
+    }
+
+    int upload(const uint8_t* img, uint32_t w, uint32_t h, uint32_t stride) {
+        img_pitch = align_up(std::max<uint32_t>(w, 1), 128);
+        CK(d_img.ensure(img_pitch * std::max<uint32_t>(h, 1)), "cudaMalloc(image)");
+        if (w && h)
+            CK(cudaMemcpy2DAsync(d_img.p, img_pitch, img, stride, w, h, cudaMemcpyHostToDevice, st), "H2D image");
+        return 0;
+    }
+
+    int detect_host(const uint8_t* img, uint32_t w, uint32_t h, uint32_t stride, bool with_desc,
+                    SiftCudaResult* out) {
+        if (int rc = set_device()) return rc;
+        if (int rc = ensure_geometry(w, h)) return rc;
+        if (int rc = upload(img, w, h, stride)) return rc;
+        for (int attempt = 0; attempt < 8; ++attempt) {
+            if (int rc = enqueue(d_img.as<uint8_t>(), (long long)img_pitch, with_desc)) return rc;
+            bool retry = false;
+            if (int rc = check_counters(&retry)) return rc;
+            if (!retry) return fetch(with_desc, out);
+        }
+        return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint lists kept overflowing");
+    }
+
+    int fetch(bool with_desc, SiftCudaResult* out) {
+        const Counters c = *h_ctr.as<Counters>();
+        const uint32_t n = c.n_oriented;
+        out->n = n;
+        out->kps = (SiftCudaKeypoint*)std::malloc(sizeof(SiftCudaKeypoint) * std::max<uint32_t>(n, 1));
+        out->desc = with_desc ? (float*)std::malloc(sizeof(float) * kDescLen * std::max<uint32_t>(n, 1)) : nullptr;
+        if (!out->kps || (with_desc && !out->desc)) {
+            std::free(out->kps);
+            std::free(out->desc);
+            out->kps = nullptr;
+            out->desc = nullptr;
+            out->n = 0;
+            return fail(SIFT_CUDA_ERR_OUT_OF_MEMORY, "host allocation of the result");
+        }
+        if (n == 0) return 0;
+        CK(h_kps.ensure(sizeof(Keypoint) * n), "cudaHostAlloc(kps)");
+        CK(cudaMemcpyAsync(h_kps.p, d_oriented.p, sizeof(Keypoint) * n, cudaMemcpyDeviceToHost, st), "D2H kps");
+        if (with_desc) {
+            CK(h_desc.ensure(sizeof(float) * kDescLen * n), "cudaHostAlloc(desc)");
+            CK(cudaMemcpyAsync(h_desc.p, d_desc.p, sizeof(float) * kDescLen * n, cudaMemcpyDeviceToHost, st),
+               "D2H desc");
+        }
+        CK(cudaStreamSynchronize(st), "D2H results");
+        std::memcpy(out->kps, h_kps.p, sizeof(Keypoint) * n);
+        if (with_desc) std::memcpy(out->desc, h_desc.p, sizeof(float) * kDescLen * n);
+        return 0;
+    }
+};
+
+}  // namespace sift
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using sift::Engine;
+
+struct SiftCudaEngine {
+    Engine e;
+};
+
+namespace {
+bool params_valid(const SiftCudaParams* p, std::string* why) {
+    if (!p) {
+        *why = "params is NULL";
+        return false;
+    }
+    if (p->num_octaves < 1 || p->num_octaves > (uint32_t)sift::kMaxOctaves) {
+        *why = "num_octaves must be in [1, 16]";
+        return false;
+    }
+    if (p->num_intervals < 1 || p->num_intervals > 16) {
+        *why = "num_intervals must be in [1, 16]";
+        return false;
+    }
+    if (!(p->sigma > 0.0f) || !(p->assumed_blur >= 0.0f) || !(p->edge_threshold > 0.0f) ||
+        !(p->contrast_threshold >= 0.0f)) {
+        *why = "sigma and edge_threshold must be positive, assumed_blur and contrast_threshold non-negative";
+        return false;
+    }
+    return true;
+}
+}  // namespace
+
+extern "C" {
+
+void sift_cuda_params_new(SiftCudaParams* out, float sigma, uint32_t num_octaves, uint32_t num_intervals,
+                          float assumed_blur, float contrast_threshold, float edge_threshold) {
+    if (!out) return;
+    out->sigma = sigma;
+    out->num_octaves = num_octaves;
+    out->num_intervals = num_intervals;
+    out->assumed_blur = assumed_blur;
+    out->contrast_threshold = contrast_threshold / (float)num_intervals;
+    out->edge_threshold = edge_threshold;
+    out->image_border_width = 5;
+}
+
+void sift_cuda_params_default(SiftCudaParams* out) { sift_cuda_params_new(out, 1.6f, 4, 3, 0.5f, 0.04f, 10.0f); }
+
+void sift_cuda_options_default(SiftCudaOptions* out) {
+    if (!out) return;
+    std::memset(out, 0, sizeof(*out));
+    out->device = 0;
+    out->storage = SIFT_CUDA_STORAGE_F32;
+}
+
+const char* sift_cuda_last_error(void) { return sift::g_last_error.c_str(); }
+
+int sift_cuda_create(const SiftCudaParams* params, const SiftCudaOptions* opts, SiftCudaEngine** out) {
+    sift::g_last_error.clear();
+    if (!out) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    if (!params_valid(params, &why)) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, why);
+    SiftCudaOptions o;
+    sift_cuda_options_default(&o);
+    if (opts) o = *opts;
+    if (o.storage != SIFT_CUDA_STORAGE_F32 && o.storage != SIFT_CUDA_STORAGE_F16)
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "unknown storage mode");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return sift::fail(SIFT_CUDA_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (o.device < 0 || o.device >= ndev) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    auto* eng = new (std::nothrow) SiftCudaEngine();
+    if (!eng) return sift::fail(SIFT_CUDA_ERR_OUT_OF_MEMORY, "engine allocation");
+    eng->e.p = *params;
+    eng->e.opt = o;
+    if (int rc = eng->e.init()) {
+        delete eng;
+        return rc;
+    }
+    *out = eng;
+    return 0;
+}
+
+void sift_cuda_destroy(SiftCudaEngine* engine) {
+    if (!engine) return;
+    cudaSetDevice(engine->e.opt.device);
+    if (engine->e.st) cudaStreamSynchronize(engine->e.st);
+    delete engine;
+}
+
+static int check_image(SiftCudaEngine* engine, const uint8_t* img, uint32_t w, uint32_t h, uint32_t stride,
+                       SiftCudaResult* out) {
+    if (out) {
+        out->n = 0;
+        out->kps = nullptr;
+        out->desc = nullptr;
+    }
+    if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
+    if ((w && h && !img) || stride < w)
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "image pointer is NULL or stride < width");
+    if (w > 65535u || h > 65535u) return sift::fail(SIFT_CUDA_ERR_UNSUPPORTED, "image sides above 65535");
+    return 0;
+}
+
+int sift_cuda_detect_and_compute(SiftCudaEngine* engine, const uint8_t* img, uint32_t width, uint32_t height,
+                                 uint32_t stride, SiftCudaResult* out) {
+    sift::g_last_error.clear();
+    if (!out) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "out is NULL");
+    if (int rc = check_image(engine, img, width, height, stride, out)) return rc;
+    return engine->e.detect_host(img, width, height, stride, true, out);
+}
+
+int sift_cuda_detect(SiftCudaEngine* engine, const uint8_t* img, uint32_t width, uint32_t height, uint32_t stride,
+                     SiftCudaResult* out) {
+    sift::g_last_error.clear();
+    if (!out) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "out is NULL");
+    if (int rc = check_image(engine, img, width, height, stride, out)) return rc;
+    return engine->e.detect_host(img, width, height, stride, false, out);
+}
+
+void sift_cuda_result_free(SiftCudaResult* r) {
+    if (!r) return;
+    std::free(r->kps);
+    std::free(r->desc);
+    r->kps = nullptr;
+    r->desc = nullptr;
+    r->n = 0;
+}
+
+int sift_cuda_run_device(SiftCudaEngine* engine, const uint8_t* d_img, uint32_t width, uint32_t height,
+                         uint32_t stride, int with_descriptors) {
+    sift::g_last_error.clear();
+    if (int rc = check_image(engine, d_img, width, height, stride, nullptr)) return rc;
+    Engine& e = engine->e;
+    if (int rc = e.set_device()) return rc;
+    if (int rc = e.ensure_geometry(width, height)) return rc;
+    return e.enqueue(d_img, (long long)stride, with_descriptors != 0);
+}
+
+int sift_cuda_device_outputs(SiftCudaEngine* engine, const uint32_t** d_count, const SiftCudaKeypoint** d_kps,
+                             const float** d_desc) {
+    if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
+    Engine& e = engine->e;
+    if (d_count) *d_count = e.d_ctr.p ? &e.d_ctr.as<sift::Counters>()->n_oriented : nullptr;
+    if (d_kps) *d_kps = e.d_oriented.as<SiftCudaKeypoint>();
+    if (d_desc) *d_desc = e.d_desc.as<float>();
+    return 0;
+}
+
+int sift_cuda_synchronize(SiftCudaEngine* engine) {
+    if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
+    cudaError_t e = cudaStreamSynchronize(engine->e.st);
+    if (e != cudaSuccess) return sift::cuda_fail(e, "synchronize");
+    return 0;
+}
+
+void* sift_cuda_stream(SiftCudaEngine* engine) { return engine ? (void*)engine->e.st : nullptr; }
+
+uint32_t sift_cuda_last_launch_count(SiftCudaEngine* engine) { return engine ? engine->e.launches : 0; }
+
+int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t capacity, uint64_t* count) {
+    if (!engine || !count) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine or count is NULL");
+    Engine& e = engine->e;
+    if (!e.have_geom) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "no run yet");
+    if (cudaStreamSynchronize(e.st) != cudaSuccess) return sift::cuda_fail(cudaGetLastError(), "synchronize");
+    sift::Counters c;
+    if (cudaMemcpy(&c, e.d_ctr.p, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return sift::cuda_fail(cudaGetLastError(), "D2H counters");
+    const sift::PyramidDev& g = e.pyr;
+    if (stage == SIFT_CUDA_STAGE_PYRAMID || stage == SIFT_CUDA_STAGE_DOG) {
+        const bool dog = stage == SIFT_CUDA_STAGE_DOG;
+        if (dog && e.f16()) return sift::fail(SIFT_CUDA_ERR_UNSUPPORTED, "no stored DoG in f16 storage");
+        const int L = dog ? g.S + 2 : g.S + 3;
+        uint64_t total = 0;
+        for (int o = 0; o < g.num_octaves; ++o) total += (uint64_t)g.oct[o].W * g.oct[o].H * L;
+        *count = total;
+        if (!out) return 0;
+        uint64_t pos = 0;
+        std::vector<unsigned char> buf;
+        for (int o = 0; o < g.num_octaves; ++o) {
+            const sift::OctaveDev& od = g.oct[o];
+            if (od.W == 0 || od.H == 0) continue;
+            for (int l = 0; l < L; ++l) {
+                const size_t es = dog ? 4 : e.g_elem_size();
+                const char* src = dog ? (const char*)e.d_D.p + (size_t)(od.d_off + (long long)l * od.plane) * 4
+                                      : (const char*)e.d_G.p + (size_t)(od.g_off + (long long)l * od.plane) * es;
+                buf.resize((size_t)od.W * od.H * es);
+                if (cudaMemcpy2D(buf.data(), (size_t)od.W * es, src, (size_t)od.pitch * es, (size_t)od.W * es, od.H,
+                                 cudaMemcpyDeviceToHost) != cudaSuccess)
+                    return sift::cuda_fail(cudaGetLastError(), "D2H stage");
+                const size_t npx = (size_t)od.W * od.H;
+                for (size_t q = 0; q < npx && pos < capacity; ++q, ++pos) {
+                    if (dog) {
+                        ((float*)out)[pos] = ((const float*)buf.data())[q];
+                    } else if (es == 4) {
+                        ((uint8_t*)out)[pos] = (uint8_t)((const float*)buf.data())[q];
+                    } else {
+                        ((uint8_t*)out)[pos] = (uint8_t)__half2float(((const __half*)buf.data())[q]);
+                    }
+                }
+            }
+        }
+        return 0;
+    }
+    const sift::Keypoint* src = nullptr;
+    uint64_t n = 0;
+    if (stage == SIFT_CUDA_STAGE_CANDIDATES) {
+        src = e.d_cands.as<sift::Keypoint>();
+        n = std::min<uint64_t>(c.n_candidates, e.cap_cand);
+    } else if (stage == SIFT_CUDA_STAGE_REFINED) {
+        src = e.d_refined.as<sift::Keypoint>();
+        n = std::min<uint64_t>(c.n_refined, e.cap_cand);
+    } else {
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "unknown stage");
+    }
+    *count = n;
+    if (out && n) {
+        uint64_t m = std::min<uint64_t>(n, capacity);
+        if (cudaMemcpy(out, src, m * sizeof(sift::Keypoint), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return sift::cuda_fail(cudaGetLastError(), "D2H stage");
+    }
+    return 0;
+}
+
+}  // extern "C"

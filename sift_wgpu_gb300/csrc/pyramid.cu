@@ -1,0 +1,324 @@
+// pyramid.cu — Gaussian pyramid + DoG kernels (sm_103a).
+//
+// Stage (a) of the hot path: generate_gaussian_pyramid and
+// generate_dog_pyramid (src/sift.rs:129-204), with the base blur of
+// detect_and_compute_cpu (src/sift.rs:1200-1214). The levels are
+// reference-compatible: each separable blur pass and the Lanczos3 resize end
+// in u8 values exactly as the reference's GrayImage levels do, so every level
+// and every DoG value is bit-identical to the CPU path. Products and sums are
+// rounded one by one (__fmul_rn/__fadd_rn) in the reference's tap order.
+//
+// Kernels
+//   k_blur_rows    horizontal pass, one row per CTA staged in shared memory
+//                  with clamp-to-edge padding; 4 outputs per thread fed by
+//                  16-byte shared loads (sliding window). u8 out.
+//   k_blur_cols    vertical pass on a 32-column tile staged in shared memory;
+//                  8 outputs per thread (sliding window); writes the level and
+//                  the DoG level below it (DoG fused, each scale read once).
+//   k_lanczos_v/h  the 2x Lanczos3 resize between octaves (f32 intermediate).
+#include "sift_internal.cuh"
+
+namespace sift {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ float load_px(const T* p) {
+    return (float)(*p);
+}
+template <>
+__device__ __forceinline__ float load_px<__half>(const __half* p) {
+    return __half2float(*p);
+}
+template <>
+__device__ __forceinline__ float load_px<uint8_t>(const uint8_t* p) {
+    return (float)(unsigned)(*p);
+}
+
+template <typename T>
+__device__ __forceinline__ void store_level(T* p, int v) {
+    *p = (T)(float)v;
+}
+template <>
+__device__ __forceinline__ void store_level<__half>(__half* p, int v) {
+    *p = __int2half_rn(v);
+}
+
+constexpr int kRowThreads = 256;
+
+// One row per CTA. Shared layout: weights[taps] (padded to a multiple of 4),
+// then the row with r clamp-to-edge pixels on each side and 8 floats of slack.
+template <typename TIn>
+__global__ void __launch_bounds__(kRowThreads) k_blur_rows(const TIn* __restrict__ in, long long in_pitch,
+                                                           uint8_t* __restrict__ out, int out_pitch, int W,
+                                                           int r, const float* __restrict__ wts,
+                                                           int round_mode) {
+    extern __shared__ __align__(16) float sm[];
+    const int taps = 2 * r + 1;
+    const int wpad = (taps + 3) & ~3;
+    float* kw = sm;
+    float* row = sm + wpad;
+    const int y = blockIdx.x;
+    const TIn* src = in + (long long)y * in_pitch;
+    for (int i = threadIdx.x; i < wpad; i += blockDim.x) kw[i] = i < taps ? wts[i] : 0.0f;
+    const int padded = W + 2 * r;
+    for (int j = threadIdx.x; j < padded + 8; j += blockDim.x) {
+        int xs = clampi(j - r, 0, W - 1);
+        row[j] = load_px(src + xs);
+    }
+    __syncthreads();
+    uint8_t* dst = out + (long long)y * out_pitch;
+    for (int x0 = threadIdx.x * 4; x0 < W; x0 += blockDim.x * 4) {
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+        const float* base = row + x0;  // x0 % 4 == 0 and wpad % 4 == 0: 16-byte aligned
+        float4 A = *reinterpret_cast<const float4*>(base);
+        int i = 0;
+        for (; i + 4 <= taps; i += 4) {
+            const float4 B = *reinterpret_cast<const float4*>(base + i + 4);
+            const float4 K = *reinterpret_cast<const float4*>(kw + i);
+            // tap i+0: A.x A.y A.z A.w
+            a0 = __fadd_rn(a0, __fmul_rn(A.x, K.x));
+            a1 = __fadd_rn(a1, __fmul_rn(A.y, K.x));
+            a2 = __fadd_rn(a2, __fmul_rn(A.z, K.x));
+            a3 = __fadd_rn(a3, __fmul_rn(A.w, K.x));
+            // tap i+1: A.y A.z A.w B.x
+            a0 = __fadd_rn(a0, __fmul_rn(A.y, K.y));
+            a1 = __fadd_rn(a1, __fmul_rn(A.z, K.y));
+            a2 = __fadd_rn(a2, __fmul_rn(A.w, K.y));
+            a3 = __fadd_rn(a3, __fmul_rn(B.x, K.y));
+            // tap i+2: A.z A.w B.x B.y
+            a0 = __fadd_rn(a0, __fmul_rn(A.z, K.z));
+            a1 = __fadd_rn(a1, __fmul_rn(A.w, K.z));
+            a2 = __fadd_rn(a2, __fmul_rn(B.x, K.z));
+            a3 = __fadd_rn(a3, __fmul_rn(B.y, K.z));
+            // tap i+3: A.w B.x B.y B.z
+            a0 = __fadd_rn(a0, __fmul_rn(A.w, K.w));
+            a1 = __fadd_rn(a1, __fmul_rn(B.x, K.w));
+            a2 = __fadd_rn(a2, __fmul_rn(B.y, K.w));
+            a3 = __fadd_rn(a3, __fmul_rn(B.z, K.w));
+            A = B;
+        }
+        for (; i < taps; ++i) {
+            const float k = kw[i];
+            a0 = __fadd_rn(a0, __fmul_rn(base[i + 0], k));
+            a1 = __fadd_rn(a1, __fmul_rn(base[i + 1], k));
+            a2 = __fadd_rn(a2, __fmul_rn(base[i + 2], k));
+            a3 = __fadd_rn(a3, __fmul_rn(base[i + 3], k));
+        }
+        dst[x0] = (uint8_t)clamp_u8(a0, round_mode);
+        if (x0 + 1 < W) dst[x0 + 1] = (uint8_t)clamp_u8(a1, round_mode);
+        if (x0 + 2 < W) dst[x0 + 2] = (uint8_t)clamp_u8(a2, round_mode);
+        if (x0 + 3 < W) dst[x0 + 3] = (uint8_t)clamp_u8(a3, round_mode);
+    }
+}
+
+constexpr int kColTX = 32;
+constexpr int kColTY = 8;
+constexpr int kColRPT = 8;                 // output rows per thread
+constexpr int kColRows = kColTY * kColRPT;  // output rows per CTA
+
+// Vertical pass over a 32 x 64 output tile. Shared layout: weights[taps],
+// lut[256] (v / 255 in f32), then (64 + 2r) rows x 32 floats of the u8
+// intermediate with clamp-to-edge rows. Writes level s (TG) and, when
+// dog != nullptr, DoG(s-1) = G_s/255 - G_{s-1}/255 (src/sift.rs:92-124).
+template <typename TG>
+__global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __restrict__ tmp, int tmp_pitch,
+                                                             const TG* __restrict__ prev, TG* __restrict__ out,
+                                                             float* __restrict__ dog, int pitch, int W, int H,
+                                                             int r, const float* __restrict__ wts,
+                                                             int round_mode) {
+    extern __shared__ __align__(16) float sm[];
+    const int taps = 2 * r + 1;
+    float* kw = sm;
+    float* lut = sm + ((taps + 3) & ~3);
+    float* tile = lut + 256;
+    const int tid = threadIdx.y * kColTX + threadIdx.x;
+    const int nthreads = kColTX * kColTY;
+    const int x0 = blockIdx.x * kColTX;
+    const int y0 = blockIdx.y * kColRows;
+    for (int i = tid; i < taps; i += nthreads) kw[i] = wts[i];
+    for (int i = tid; i < 256; i += nthreads) lut[i] = __fdiv_rn((float)i, 255.0f);
+    const int rows = kColRows + 2 * r;
+    const int xg = min(x0 + (int)threadIdx.x, W - 1);
+    for (int k = threadIdx.y; k < rows; k += kColTY) {
+        int ys = clampi(y0 - r + k, 0, H - 1);
+        tile[k * kColTX + threadIdx.x] = (float)(unsigned)tmp[(long long)ys * tmp_pitch + xg];
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x;
+    const int ly = threadIdx.y * kColRPT;  // first local output row
+    float acc[kColRPT];
+    float win[kColRPT];
+#pragma unroll
+    for (int j = 0; j < kColRPT; ++j) {
+        acc[j] = 0.0f;
+        win[j] = j < kColRPT - 1 ? tile[(ly + j) * kColTX + threadIdx.x] : 0.0f;
+    }
+    for (int i = 0; i < taps; ++i) {
+        // window rows ly+i .. ly+i+7
+        win[kColRPT - 1] = tile[(ly + i + kColRPT - 1) * kColTX + threadIdx.x];
+        const float k = kw[i];
+#pragma unroll
+        for (int j = 0; j < kColRPT; ++j) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], k));
+#pragma unroll
+        for (int j = 0; j < kColRPT - 1; ++j) win[j] = win[j + 1];
+    }
+    if (x >= W) return;
+#pragma unroll
+    for (int j = 0; j < kColRPT; ++j) {
+        const int y = y0 + ly + j;
+        if (y < H) {
+            const int v = clamp_u8(acc[j], round_mode);
+            const long long o = (long long)y * pitch + x;
+            store_level(out + o, v);
+            if (dog) {
+                const int pv = (int)load_px(prev + o);
+                dog[o] = __fsub_rn(lut[v], lut[pv]);
+            }
+        }
+    }
+}
+
+// A level whose blur increment is below 1e-4 is a copy of the previous one
+// (src/sift.rs:152-154); its DoG is then exactly zero.
+template <typename TG>
+__global__ void k_copy_level(const TG* __restrict__ prev, TG* __restrict__ out, float* __restrict__ dog,
+                             int pitch, int W, int H) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y;
+    if (x >= W) return;
+    long long o = (long long)y * pitch + x;
+    out[o] = prev[o];
+    if (dog) dog[o] = 0.0f;
+}
+
+// Base level without a blur (sigma <= assumed_blur, src/sift.rs:1204-1214).
+template <typename TG>
+__global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride, TG* __restrict__ out, int pitch,
+                              int W, int H) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y;
+    if (x >= W) return;
+    store_level(out + (long long)y * pitch + x, (int)img[(long long)y * stride + x]);
+}
+
+// Lanczos3 vertical pass (image 0.25.6 vertical_sample): tmp[oy][x] =
+// sum_i G[left+i][x] * w_i, accumulated from 0 in tap order, kept in f32.
+template <typename TG>
+__global__ void k_lanczos_v(const TG* __restrict__ src, int src_pitch, float* __restrict__ dst, int dst_pitch,
+                            int W, int nH, const int* __restrict__ left, const int* __restrict__ count,
+                            const int* __restrict__ woff, const float* __restrict__ w) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int oy = blockIdx.y;
+    if (x >= W || oy >= nH) return;
+    const int l = left[oy], c = count[oy], o = woff[oy];
+    float t = 0.0f;
+    for (int i = 0; i < c; ++i)
+        t = __fadd_rn(t, __fmul_rn(load_px(src + (long long)(l + i) * src_pitch + x), w[o + i]));
+    dst[(long long)oy * dst_pitch + x] = t;
+}
+
+// Lanczos3 horizontal pass (image 0.25.6 horizontal_sample): clamp to
+// [0, 255], round half away from zero, store as the next octave's base level.
+template <typename TG>
+__global__ void k_lanczos_h(const float* __restrict__ src, int src_pitch, TG* __restrict__ dst, int dst_pitch,
+                            int nW, int nH, const int* __restrict__ left, const int* __restrict__ count,
+                            const int* __restrict__ woff, const float* __restrict__ w) {
+    const int ox = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (ox >= nW || y >= nH) return;
+    const int l = left[ox], c = count[ox], o = woff[ox];
+    const float* row = src + (long long)y * src_pitch;
+    float t = 0.0f;
+    for (int i = 0; i < c; ++i) t = __fadd_rn(t, __fmul_rn(row[l + i], w[o + i]));
+    t = t < 0.0f ? 0.0f : (t > 255.0f ? 255.0f : t);
+    store_level(dst + (long long)y * dst_pitch + ox, (int)roundf(t));
+}
+
+}  // namespace
+
+// ---- launchers ----------------------------------------------------------------
+
+size_t blur_rows_smem(int W, int r) {
+    int taps = 2 * r + 1;
+    return sizeof(float) * ((size_t)((taps + 3) & ~3) + (size_t)W + 2 * (size_t)r + 8);
+}
+size_t blur_cols_smem(int r) {
+    int taps = 2 * r + 1;
+    return sizeof(float) * ((size_t)((taps + 3) & ~3) + 256 + (size_t)(kColRows + 2 * r) * kColTX);
+}
+
+template <typename TIn>
+int launch_blur_rows(const TIn* in, long long in_pitch, uint8_t* out, int out_pitch, int W, int H, int r,
+                     const float* wts, int round_mode, cudaStream_t st) {
+    size_t smem = blur_rows_smem(W, r);
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(k_blur_rows<TIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return -1;
+    }
+    k_blur_rows<TIn><<<H, kRowThreads, smem, st>>>(in, in_pitch, out, out_pitch, W, r, wts, round_mode);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename TG>
+int launch_blur_cols(const uint8_t* tmp, int tmp_pitch, const TG* prev, TG* out, float* dog, int pitch, int W,
+                     int H, int r, const float* wts, int round_mode, cudaStream_t st) {
+    size_t smem = blur_cols_smem(r);
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(k_blur_cols<TG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return -1;
+    }
+    dim3 grid((W + kColTX - 1) / kColTX, (H + kColRows - 1) / kColRows);
+    k_blur_cols<TG><<<grid, dim3(kColTX, kColTY), smem, st>>>(tmp, tmp_pitch, prev, out, dog, pitch, W, H, r, wts,
+                                                            round_mode);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename TG>
+int launch_copy_level(const TG* prev, TG* out, float* dog, int pitch, int W, int H, cudaStream_t st) {
+    dim3 grid((W + 255) / 256, H);
+    k_copy_level<TG><<<grid, 256, 0, st>>>(prev, out, dog, pitch, W, H);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename TG>
+int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, int pitch, int W, int H, cudaStream_t st) {
+    dim3 grid((W + 255) / 256, H);
+    k_u8_to_level<TG><<<grid, 256, 0, st>>>(img, stride, out, pitch, W, H);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename TG>
+int launch_lanczos(const TG* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst, int dst_pitch,
+                   int nW, int nH, const int* vtab, const float* vw, const int* htab, const float* hw,
+                   cudaStream_t st) {
+    // vtab: left[nH], count[nH], woff[nH]; htab: left[nW], count[nW], woff[nW]
+    dim3 gv((W + 127) / 128, nH);
+    k_lanczos_v<TG><<<gv, 128, 0, st>>>(src, src_pitch, tmp, tmp_pitch, W, nH, vtab, vtab + nH, vtab + 2 * nH, vw);
+    dim3 gh((nW + 127) / 128, nH);
+    k_lanczos_h<TG><<<gh, 128, 0, st>>>(tmp, tmp_pitch, dst, dst_pitch, nW, nH, htab, htab + nW, htab + 2 * nW, hw);
+    (void)H;
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template int launch_blur_rows<uint8_t>(const uint8_t*, long long, uint8_t*, int, int, int, int, const float*, int,
+                                       cudaStream_t);
+template int launch_blur_rows<float>(const float*, long long, uint8_t*, int, int, int, int, const float*, int,
+                                     cudaStream_t);
+template int launch_blur_rows<__half>(const __half*, long long, uint8_t*, int, int, int, int, const float*, int,
+                                      cudaStream_t);
+template int launch_blur_cols<float>(const uint8_t*, int, const float*, float*, float*, int, int, int, int,
+                                     const float*, int, cudaStream_t);
+template int launch_blur_cols<__half>(const uint8_t*, int, const __half*, __half*, float*, int, int, int, int,
+                                      const float*, int, cudaStream_t);
+template int launch_copy_level<float>(const float*, float*, float*, int, int, int, cudaStream_t);
+template int launch_copy_level<__half>(const __half*, __half*, float*, int, int, int, cudaStream_t);
+template int launch_u8_to_level<float>(const uint8_t*, long long, float*, int, int, int, cudaStream_t);
+template int launch_u8_to_level<__half>(const uint8_t*, long long, __half*, int, int, int, cudaStream_t);
+template int launch_lanczos<float>(const float*, int, int, int, float*, int, float*, int, int, int, const int*,
+                                   const float*, const int*, const float*, cudaStream_t);
+template int launch_lanczos<__half>(const __half*, int, int, int, float*, int, __half*, int, int, int, const int*,
+                                    const float*, const int*, const float*, cudaStream_t);
+
+}  // namespace sift

@@ -1,0 +1,91 @@
+// sift_internal.cuh — shared types and helpers of the sm_103a SIFT engine.
+//
+// The whole library is compiled with --fmad=false: the reference computes in
+// f32 without fused multiply-add (Rust never contracts), and the pyramid,
+// extrema and refinement stages reproduce its results bit for bit only when
+// every product and sum is rounded separately. Device code that may fuse uses
+// fmaf explicitly.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/sift_cuda.h"
+
+namespace sift {
+
+constexpr int kOriBins = 36;            // src/sift.rs:21
+constexpr int kOriMaxPeaks = 18;        // strict local maxima of a 36-bin circle
+constexpr int kDescBins = 8;            // src/sift.rs:28
+constexpr int kDescWidth = 4;           // src/sift.rs:29
+constexpr int kDescLen = 128;           // 4 x 4 x 8
+constexpr float kPi = 3.14159265358979323846f;
+constexpr int kMaxOctaves = 16;
+
+using Keypoint = SiftCudaKeypoint;
+
+// Device counters of one run. Zeroed at the start of every run.
+struct Counters {
+    uint32_t n_candidates;
+    uint32_t n_refined;
+    uint32_t n_oriented;
+    uint32_t overflow;  // bit 0 candidates, 1 refined, 2 oriented
+};
+
+// Geometry of one octave in the device arena.
+struct OctaveDev {
+    int W, H, pitch;          // pitch in elements (G and DoG planes)
+    int nw;                   // 32-pixel words per row of the extrema mask
+    long long g_off;          // element offset of level 0 in the G arena
+    long long d_off;          // element offset of DoG level 0 in the DoG arena
+    long long plane;          // elements per plane (pitch * H)
+    long long word_base;      // first word of this octave in the mask arena
+};
+
+struct PyramidDev {
+    int num_octaves;
+    int S;                    // num_intervals
+    int levels;               // S + 3
+    OctaveDev oct[kMaxOctaves];
+};
+
+// f32 -> u8 the way imageproc's Clamp<f32> for u8 does it: truncation of
+// values strictly inside (0, 255), saturation outside. round_mode 1 rounds
+// half away from zero first (the alternative rule, selectable for study).
+__device__ __forceinline__ int clamp_u8(float a, int round_mode) {
+    if (round_mode) a = roundf(a);
+    if (a < 255.0f) {
+        if (a > 0.0f) return (int)a;
+        return 0;
+    }
+    return 255;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// `f as i32` in Rust: saturating, NaN -> 0.
+__device__ __forceinline__ int rust_as_i32(float v) {
+    if (v != v) return 0;
+    if (v >= 2147483648.0f) return 2147483647;
+    if (v <= -2147483648.0f) return (-2147483647 - 1);
+    return (int)v;
+}
+
+// f32::rem_euclid
+__device__ __forceinline__ float rem_euclid(float a, float b) {
+    float r = fmodf(a, b);
+    return r < 0.0f ? __fadd_rn(r, fabsf(b)) : r;
+}
+
+// Scan helpers (scan.cu).
+enum ScanInput { SCAN_U32 = 0, SCAN_POPC = 1 };
+// Exclusive scan of n values (n_dev, when not null, overrides n at run time
+// and must be <= n). total_out receives the sum. Needs scratch partials of
+// scan_partials_size(n) words.
+size_t scan_partials_size(size_t n);
+int scan_exclusive(const uint32_t* in, ScanInput mode, uint32_t* out, size_t n, const uint32_t* n_dev,
+                   uint32_t* total_out, uint32_t* partials, cudaStream_t st);
+int scan_launches(size_t n);
+
+}  // namespace sift

@@ -1,0 +1,284 @@
+"""Python mirror of the reference crate's public SIFT API over libsiftcuda.so.
+
+Names, fields and argument meanings follow the Rust crate stevel705/sift-wgpu:
+
+* ``Sift`` / ``Sift.new`` / ``Sift.default``      — src/sift.rs:36-80
+* ``KeyPoint``                                    — src/keypoints.rs:2-10
+* ``SiftBackend`` and ``SiftBackend.from_str``    — src/lib.rs:19-50, plus the
+  new ``Cuda`` arm and its ``"cuda"`` string
+* ``Sift.detect_and_compute_with_backend``        — src/sift.rs:1244-1355
+* ``Sift.detect``                                 — src/sift.rs:846-886
+
+Only the ``Cuda`` arm is implemented here; the other arms belong to the
+reference crate. Failures raise ``SiftError`` (the reference's Err(String)); no
+call ever falls back to a CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import threading
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _capi
+from ._capi import DESC_LEN, KEYPOINT_DTYPE, SiftCudaError
+
+__all__ = [
+    "Engine", "KeyPoint", "Sift", "SiftBackend", "SiftError", "keypoints_from_array",
+]
+
+DEFAULT_SIGMA = 1.6
+DEFAULT_NUM_OCTAVES = 4
+DEFAULT_NUM_INTERVALS = 3
+DEFAULT_ASSUMED_BLUR = 0.5
+DEFAULT_CONTRAST_THRESHOLD = 0.04
+DEFAULT_EDGE_THRESHOLD = 10.0
+DEFAULT_IMAGE_BORDER_WIDTH = 5
+
+
+class SiftError(RuntimeError):
+    """Err(String) of detect_and_compute_with_backend."""
+
+
+class SiftBackend(enum.Enum):
+    Cpu = "cpu"
+    WebGpu = "webgpu"
+    WebGpuWithCpuFallback = "fallback"
+    WebGpuV2 = "gpuv2"
+    Cuda = "cuda"
+
+    @classmethod
+    def default(cls) -> "SiftBackend":
+        return cls.WebGpuWithCpuFallback  # src/lib.rs:30-34
+
+    @classmethod
+    def from_str(cls, value: str) -> "SiftBackend":
+        """FromStr for SiftBackend (src/lib.rs:38-50) with the added "cuda"."""
+        v = value.strip().lower()
+        table = {
+            "cpu": cls.Cpu,
+            "webgpu": cls.WebGpu, "wgpu": cls.WebGpu, "gpu": cls.WebGpu,
+            "auto": cls.WebGpuWithCpuFallback, "fallback": cls.WebGpuWithCpuFallback,
+            "prefer-gpu": cls.WebGpuWithCpuFallback,
+            "gpuv2": cls.WebGpuV2, "gpu-v2": cls.WebGpuV2, "webgpu-v2": cls.WebGpuV2, "v2": cls.WebGpuV2,
+            "cuda": cls.Cuda,
+        }
+        if v not in table:
+            raise SiftError(f"Unknown SIFT backend: {value}")
+        return table[v]
+
+
+@dataclass
+class KeyPoint:
+    """KeyPoint (src/keypoints.rs:2-10)."""
+
+    x: float
+    y: float
+    size: float
+    angle: float
+    response: float
+    octave: int
+    layer: int
+
+
+def keypoints_from_array(a: np.ndarray) -> list[KeyPoint]:
+    return [KeyPoint(float(r["x"]), float(r["y"]), float(r["size"]), float(r["angle"]),
+                     float(r["response"]), int(r["octave"]), int(r["layer"])) for r in a]
+
+
+def _as_gray(img) -> np.ndarray:
+    a = np.asarray(img)
+    if a.dtype != np.uint8 or a.ndim != 2:
+        raise SiftError("expected a 2-D uint8 grayscale image (the to_luma8() layout)")
+    return a
+
+
+class Engine:
+    """One libsiftcuda engine: a CUDA stream plus resident device arenas."""
+
+    def __init__(self, params: "Sift | _capi.Params | None" = None, device: int = 0, storage: str = "f32"):
+        L = _capi.lib()
+        if params is None:
+            params = Sift.default()
+        p = params.to_c() if isinstance(params, Sift) else params
+        opts = _capi.Options()
+        L.sift_cuda_options_default(C.byref(opts))
+        opts.device = device
+        opts.storage = {"f32": _capi.STORAGE_F32, "f16": _capi.STORAGE_F16}[storage]
+        h = C.c_void_p()
+        _capi.check(L.sift_cuda_create(C.byref(p), C.byref(opts), C.byref(h)))
+        self._h = h
+        self.storage = storage
+        self.params = p
+
+    @property
+    def handle(self) -> C.c_void_p:
+        if not self._h:
+            raise SiftError("engine is closed")
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _capi.lib().sift_cuda_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, fn, img: np.ndarray, with_desc: bool):
+        img = _as_gray(img)
+        h, w = img.shape
+        stride = img.strides[0]
+        if img.strides[1] != 1:
+            img = np.ascontiguousarray(img)
+            stride = w
+        res = _capi.Result()
+        _capi.check(fn(self.handle, img.ctypes.data if img.size else None, w, h, stride, C.byref(res)))
+        try:
+            n = res.n
+            kps = np.empty(n, dtype=KEYPOINT_DTYPE)
+            if n:
+                C.memmove(kps.ctypes.data, res.kps, n * KEYPOINT_DTYPE.itemsize)
+            desc = None
+            if with_desc:
+                desc = np.empty((n, DESC_LEN), dtype=np.float32)
+                if n:
+                    C.memmove(desc.ctypes.data, res.desc, n * DESC_LEN * 4)
+        finally:
+            _capi.lib().sift_cuda_result_free(C.byref(res))
+        return kps, desc
+
+    def detect_and_compute(self, img) -> tuple[np.ndarray, np.ndarray]:
+        """Keypoints (structured array) and descriptors (n x 128 f32)."""
+        return self._call(_capi.lib().sift_cuda_detect_and_compute, img, True)
+
+    def detect(self, img) -> np.ndarray:
+        return self._call(_capi.lib().sift_cuda_detect, img, False)[0]
+
+    # device-resident form -------------------------------------------------
+    def run_device(self, d_img: int, width: int, height: int, stride: int, with_descriptors: bool = True) -> None:
+        _capi.check(_capi.lib().sift_cuda_run_device(self.handle, C.c_void_p(d_img), width, height, stride,
+                                                     1 if with_descriptors else 0))
+
+    def device_outputs(self) -> tuple[int, int, int]:
+        c, k, d = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        _capi.check(_capi.lib().sift_cuda_device_outputs(self.handle, C.byref(c), C.byref(k), C.byref(d)))
+        return c.value or 0, k.value or 0, d.value or 0
+
+    def synchronize(self) -> None:
+        _capi.check(_capi.lib().sift_cuda_synchronize(self.handle))
+
+    @property
+    def stream(self) -> int:
+        return _capi.lib().sift_cuda_stream(self.handle) or 0
+
+    @property
+    def last_launch_count(self) -> int:
+        return int(_capi.lib().sift_cuda_last_launch_count(self.handle))
+
+    def debug_stage(self, stage: int) -> np.ndarray:
+        L = _capi.lib()
+        n = C.c_uint64()
+        _capi.check(L.sift_cuda_debug_stage(self.handle, stage, None, 0, C.byref(n)))
+        if stage == _capi.STAGE_PYRAMID:
+            out = np.empty(n.value, dtype=np.uint8)
+        elif stage == _capi.STAGE_DOG:
+            out = np.empty(n.value, dtype=np.float32)
+        else:
+            out = np.empty(n.value, dtype=KEYPOINT_DTYPE)
+        _capi.check(L.sift_cuda_debug_stage(self.handle, stage, out.ctypes.data if n.value else None,
+                                            n.value, C.byref(n)))
+        return out
+
+
+class Sift:
+    """Sift parameters (src/sift.rs:36-45); contrast_threshold stored / S."""
+
+    _engines: dict = {}
+    _lock = threading.RLock()
+
+    def __init__(self, sigma: float = DEFAULT_SIGMA, num_octaves: int = DEFAULT_NUM_OCTAVES,
+                 num_intervals: int = DEFAULT_NUM_INTERVALS, assumed_blur: float = DEFAULT_ASSUMED_BLUR,
+                 contrast_threshold: float | None = None, edge_threshold: float = DEFAULT_EDGE_THRESHOLD,
+                 image_border_width: int = DEFAULT_IMAGE_BORDER_WIDTH):
+        self.sigma = float(np.float32(sigma))
+        self.num_octaves = int(num_octaves)
+        self.num_intervals = int(num_intervals)
+        self.assumed_blur = float(np.float32(assumed_blur))
+        if contrast_threshold is None:
+            contrast_threshold = float(np.float32(DEFAULT_CONTRAST_THRESHOLD) / np.float32(num_intervals))
+        self.contrast_threshold = float(np.float32(contrast_threshold))
+        self.edge_threshold = float(np.float32(edge_threshold))
+        self.image_border_width = int(image_border_width)
+
+    @classmethod
+    def default(cls) -> "Sift":
+        """Sift::default() (src/sift.rs:47-59)."""
+        return cls()
+
+    @classmethod
+    def new(cls, sigma: float, num_octaves: int, num_intervals: int, assumed_blur: float,
+            contrast_threshold: float, edge_threshold: float) -> "Sift":
+        """Sift::new (src/sift.rs:63-80): stores contrast_threshold / num_intervals in f32."""
+        c = float(np.float32(contrast_threshold) / np.float32(num_intervals))
+        return cls(sigma, num_octaves, num_intervals, assumed_blur, c, edge_threshold)
+
+    def to_c(self) -> _capi.Params:
+        return _capi.Params(self.sigma, self.num_octaves, self.num_intervals, self.assumed_blur,
+                            self.contrast_threshold, self.edge_threshold, self.image_border_width)
+
+    def _key(self):
+        return (self.sigma, self.num_octaves, self.num_intervals, self.assumed_blur,
+                self.contrast_threshold, self.edge_threshold, self.image_border_width)
+
+    def _engine(self) -> Engine:
+        # One process-wide engine per parameter set (the Rust arm keeps a
+        # lazily created global engine behind a mutex).
+        with Sift._lock:
+            eng = Sift._engines.get(self._key())
+            if eng is None:
+                eng = Engine(self)
+                Sift._engines[self._key()] = eng
+            return eng
+
+    def detect_and_compute_with_backend(self, img, backend: SiftBackend):
+        """(keypoints, descriptors) like the reference; raises SiftError."""
+        if backend is not SiftBackend.Cuda:
+            raise SiftError(f"backend {backend.name} is provided by the reference crate, not by this engine")
+        try:
+            with Sift._lock:
+                kps, desc = self._engine().detect_and_compute(img)
+        except SiftCudaError as e:
+            raise SiftError(f"CUDA detection failed: {e}") from e
+        return keypoints_from_array(kps), [list(map(float, d)) for d in desc]
+
+    def detect_and_compute_arrays(self, img, backend: SiftBackend = SiftBackend.Cuda):
+        """Same as detect_and_compute_with_backend, as numpy arrays."""
+        if backend is not SiftBackend.Cuda:
+            raise SiftError(f"backend {backend.name} is provided by the reference crate, not by this engine")
+        try:
+            with Sift._lock:
+                return self._engine().detect_and_compute(img)
+        except SiftCudaError as e:
+            raise SiftError(f"CUDA detection failed: {e}") from e
+
+    def detect(self, img, backend: SiftBackend = SiftBackend.Cuda) -> list[KeyPoint]:
+        """Sift::detect (src/sift.rs:846-886) on the CUDA engine."""
+        if backend is not SiftBackend.Cuda:
+            raise SiftError(f"backend {backend.name} is provided by the reference crate, not by this engine")
+        try:
+            with Sift._lock:
+                return keypoints_from_array(self._engine().detect(img))
+        except SiftCudaError as e:
+            raise SiftError(f"CUDA detection failed: {e}") from e

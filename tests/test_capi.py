@@ -1,0 +1,89 @@
+"""The C-ABI library without a GPU: it loads, exports every entry point that
+include/sift_cuda.h declares, and its host-only helpers behave (no kernel is
+launched here)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    text = (ROOT / "include" / "sift_cuda.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sift_\w+)\s*\(", text)))
+
+
+def test_header_symbols_exported(built_lib):
+    lib = C.CDLL(str(built_lib))
+    names = declared_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    from sift_wgpu_gb300 import _capi
+    assert sorted(_capi.exported_symbols()) == names
+
+
+def test_params_mirror_sift_new(built_lib):
+    from sift_wgpu_gb300 import _capi
+    L = _capi.lib()
+    p = _capi.Params()
+    L.sift_cuda_params_default(C.byref(p))
+    assert (p.num_octaves, p.num_intervals, p.image_border_width) == (4, 3, 5)
+    assert p.contrast_threshold == np.float32(0.04) / np.float32(3)
+    L.sift_cuda_params_new(C.byref(p), 1.6, 6, 3, 0.5, 0.04, 10.0)
+    assert p.num_octaves == 6 and p.contrast_threshold == np.float32(np.float32(0.04) / np.float32(3))
+    from sift_wgpu_gb300 import Sift
+    s = Sift.new(1.6, 6, 3, 0.5, 0.04, 10.0)
+    assert s.contrast_threshold == p.contrast_threshold
+
+
+def test_backend_from_str():
+    from sift_wgpu_gb300 import SiftBackend, SiftError
+    assert SiftBackend.from_str(" CUDA ") is SiftBackend.Cuda
+    assert SiftBackend.from_str("gpu") is SiftBackend.WebGpu
+    assert SiftBackend.from_str("v2") is SiftBackend.WebGpuV2
+    assert SiftBackend.from_str("prefer-gpu") is SiftBackend.WebGpuWithCpuFallback
+    assert SiftBackend.default() is SiftBackend.WebGpuWithCpuFallback
+    with pytest.raises(SiftError):
+        SiftBackend.from_str("opencl")
+
+
+def test_other_backends_are_not_served_here(built_lib):
+    from sift_wgpu_gb300 import Sift, SiftBackend, SiftError
+    img = np.zeros((8, 8), np.uint8)
+    for b in (SiftBackend.Cpu, SiftBackend.WebGpu, SiftBackend.WebGpuV2, SiftBackend.WebGpuWithCpuFallback):
+        with pytest.raises(SiftError):
+            Sift.default().detect_and_compute_with_backend(img, b)
+
+
+def test_synth_is_seeded_and_dense(built_lib):
+    from sift_wgpu_gb300 import synth_image
+    a = synth_image(0, 512, 512)
+    b = synth_image(0, 512, 512)
+    c = synth_image(1, 512, 512)
+    assert a.dtype == np.uint8 and a.shape == (512, 512)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert 100 < a.mean() < 160 and a.std() > 10
+    from sift_wgpu_gb300 import _capi
+    nb, nr = C.c_uint32(), C.c_uint32()
+    _capi.lib().sift_synth_density(1920, 1080, C.byref(nb), C.byref(nr))
+    assert (nb.value, nr.value) == (1582, 316)
+
+
+def test_engine_errors_are_reported(built_lib):
+    from sift_wgpu_gb300 import _capi
+    L = _capi.lib()
+    p = _capi.Params()
+    L.sift_cuda_params_default(C.byref(p))
+    p.num_octaves = 0
+    h = C.c_void_p()
+    rc = L.sift_cuda_create(C.byref(p), None, C.byref(h))
+    assert rc == 1 and b"num_octaves" in L.sift_cuda_last_error()
+    assert not h.value
+    res = _capi.Result()
+    rc = L.sift_cuda_detect_and_compute(None, None, 4, 4, 4, C.byref(res))
+    assert rc == 1 and res.n == 0

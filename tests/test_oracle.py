@@ -1,0 +1,154 @@
+"""The CPU oracle against the reference's own known-answer tests and
+integration properties (CPU only, no GPU).
+
+The oracle restates src/sift.rs; these tests pin it the way the reference pins
+itself: the Cramer solve and bilinear sampler known answers
+(src/sift.rs:1424-1525) and the integration properties of
+tests/integration_test.rs on seeded synthetic images (the reference's JPEG
+fixtures need a decoder this environment lacks).
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+KAT = json.loads((GOLDEN / "reference_kat.json").read_text())
+
+
+def check_properties(kps, w, h, S=3):
+    """check_keypoint_properties (tests/integration_test.rs:13-62)."""
+    pi = np.float32(math.pi)
+    assert np.all(kps["x"] >= -1.0) and np.all(kps["x"] <= w + 1.0)
+    assert np.all(kps["y"] >= -1.0) and np.all(kps["y"] <= h + 1.0)
+    assert np.all(kps["size"] > 0.0)
+    assert np.all(kps["angle"] >= -pi) and np.all(kps["angle"] <= pi)
+    assert np.all(kps["octave"] >= 0)
+    assert np.all(kps["layer"] >= -2) and np.all(kps["layer"] <= S + 4)
+
+
+@pytest.mark.parametrize("case", KAT["solve_linear_system"])
+def test_solve_linear_system_kat(oracle_mod, case):
+    x = oracle_mod.solve3(case["a"], case["b"])
+    if case["x"] is None:
+        assert x is None
+    else:
+        assert x is not None
+        assert np.allclose(x, case["x"], atol=case["tol"], rtol=0)
+
+
+def test_bilinear_kat(oracle_mod):
+    k = KAT["get_gauss_pixel_bilinear"]
+    img = np.array(k["image"], dtype=np.uint8)
+    for c in k["cases"]:
+        v = oracle_mod.bilinear(img, c["x"], c["y"])
+        assert abs(v - np.float32(c["v"]) / np.float32(255.0)) < k["tol"], c
+
+
+def test_uniform_image_has_no_keypoints(oracle_mod):
+    u = KAT["uniform_image"]
+    img = np.full((u["height"], u["width"]), u["value"], dtype=np.uint8)
+    kps, desc = oracle_mod.detect_and_compute(img)
+    assert len(kps) == u["keypoints"] and len(desc) == 0
+
+
+def test_small_gradient_properties(oracle_mod):
+    img = np.tile((np.arange(20) * 10).astype(np.uint8), (15, 1))
+    kps, desc = oracle_mod.detect_and_compute(img)
+    assert len(kps) == len(desc)
+    if len(kps):
+        check_properties(kps, 20, 15)
+
+
+def test_synthetic_properties_and_determinism(oracle_mod, built_lib):
+    from sift_wgpu_gb300 import synth_image
+    img = synth_image(0, 512, 512)
+    k1, d1 = oracle_mod.detect_and_compute(img, threads=4)
+    k2, d2 = oracle_mod.detect_and_compute(img, threads=1)
+    assert len(k1) > 0 and len(k1) == len(d1)
+    check_properties(k1, 512, 512)
+    # determinism (tests/integration_test.rs:106-164), across thread counts too
+    assert k1.tobytes() == k2.tobytes()
+    assert np.max(np.abs(d1 - d2)) < 1e-6
+    norms = np.linalg.norm(d1, axis=1)
+    assert np.all((np.abs(norms - 1.0) < 1e-4) | (norms == 0.0))
+
+
+def test_high_contrast_threshold(oracle_mod, built_lib):
+    from sift_wgpu_gb300 import synth_image
+    img = synth_image(0, 512, 512)
+    k_def, _ = oracle_mod.detect_and_compute(img)
+    k_hi, d_hi = oracle_mod.detect_and_compute(img, oracle_mod.params(contrast_threshold=1.0))
+    assert len(k_def) > 0
+    assert len(k_hi) < len(k_def) // 2 or len(k_hi) == 0
+    assert len(k_hi) == len(d_hi)
+
+
+def test_blur_sigmas_follow_reference_formula(oracle_mod):
+    """generate_gaussian_pyramid increments (src/sift.rs:141-147): octave o is
+    2^o times octave 0, base = sqrt(1.6^2 - 0.5^2)."""
+    s = oracle_mod.blur_sigmas()
+    base, rest = s[0], s[1:].reshape(4, 5)
+    assert abs(base - math.sqrt(1.6 ** 2 - 0.25)) < 1e-5
+    assert np.allclose(rest[0], [1.2262735, 1.5450078, 1.9465878, 2.452547, 3.0900155], rtol=1e-5)
+    for o in range(4):
+        assert np.array_equal(rest[o], rest[0] * np.float32(2 ** o))
+
+
+def test_blur_matches_independent_python_restatement(oracle_mod):
+    """imageproc gaussian_blur_f32 restated twice (C++ oracle vs float32
+    numpy loops) must agree bit for bit, including clamp-to-edge when the
+    kernel is wider than the image."""
+    rng = np.random.default_rng(5)
+    for (h, w, sigma) in [(9, 13, 1.3), (6, 5, 3.7), (17, 11, 0.6)]:
+        img = rng.integers(0, 256, size=(h, w), dtype=np.uint8)
+        k = oracle_mod.gaussian_kernel(sigma)
+        r = (len(k) - 1) // 2
+        assert r == math.ceil(2 * np.float32(sigma))
+
+        def pass1d(a):
+            out = np.empty_like(a)
+            H, W = a.shape
+            for y in range(H):
+                for x in range(W):
+                    acc = np.float32(0)
+                    for i in range(len(k)):
+                        xs = min(max(x + i - r, 0), W - 1)
+                        acc = np.float32(acc + np.float32(a[y, xs]) * k[i])
+                    out[y, x] = 255 if acc >= 255 else (0 if acc <= 0 else int(acc))
+            return out
+
+        ref = pass1d(pass1d(img).T.copy()).T
+        assert np.array_equal(oracle_mod.gaussian_blur(img, sigma), ref)
+
+
+def test_lanczos_uniform_and_shape(oracle_mod):
+    img = np.full((37, 50), 77, dtype=np.uint8)
+    out = oracle_mod.resize_lanczos3(img, 25, 18)
+    assert out.shape == (18, 25) and np.all(out == 77)
+
+
+def test_extrema_match_numpy_restatement(oracle_mod, built_lib):
+    """find_scale_space_extrema restated in numpy on the oracle's own pyramid:
+    same candidates, same (octave, layer, y, x) order."""
+    from sift_wgpu_gb300 import synth_image
+    img = synth_image(11, 96, 80)
+    st = oracle_mod.stages(img)
+    rows = []
+    for o, (w, h) in enumerate(st.octave_dims):
+        g = [st.level(o, s).astype(np.float32) / np.float32(255.0) for s in range(st.levels)]
+        d = [g[i + 1] - g[i] for i in range(len(g) - 1)]
+        for s in range(1, 4):
+            cube = np.stack(d[s - 1:s + 2])
+            for y in range(5, h - 5):
+                for x in range(5, w - 5):
+                    v = cube[1, y, x]
+                    nb = cube[:, y - 1:y + 2, x - 1:x + 2].ravel()
+                    nb = np.delete(nb, 13)
+                    if np.all(v > nb) or np.all(v < nb):
+                        rows.append((o, s, y, x))
+    got = [(int(k["octave"]), int(k["layer"]), int(k["y"] / 2 ** k["octave"]), int(k["x"] / 2 ** k["octave"]))
+           for k in st.candidates]
+    assert got == rows

@@ -1,0 +1,195 @@
+"""CUDA engine vs the CPU oracle, through the C ABI (GPU tests).
+
+Bit-exact bars: every Gaussian level, every DoG value, the candidate list and
+the refined keypoints (x, y, response, octave, layer; size within 2 ulp, it is
+the one value that goes through a transcendental). Tolerance bars for the
+final keypoints and descriptors: tests/parity.py.
+"""
+import numpy as np
+import pytest
+
+from parity import DESC_RTOL, MATCH_RATE, match
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # (name, width, height, seed, sift_new args)
+    ("512_default", 512, 512, 0, (1.6, 4, 3, 0.5, 0.04, 10.0)),
+    ("1080p_default", 1920, 1080, 1, (1.6, 4, 3, 0.5, 0.04, 10.0)),
+    ("odd_333x217", 333, 217, 5, (1.6, 4, 3, 0.5, 0.04, 10.0)),
+    ("1024_6oct", 1024, 1024, 3, (1.6, 6, 3, 0.5, 0.04, 10.0)),
+    ("640x480_s4", 640, 480, 9, (1.6, 5, 4, 0.5, 0.04, 10.0)),
+]
+
+
+@pytest.fixture(scope="module")
+def sgb(built_lib):
+    import sift_wgpu_gb300
+    return sift_wgpu_gb300
+
+
+_engines = {}
+
+
+def engine_for(sgb, args, storage="f32"):
+    key = (args, storage)
+    if key not in _engines:
+        _engines[key] = sgb.Engine(sgb.Sift.new(*args), storage=storage)
+    return _engines[key]
+
+
+_oracle_cache = {}
+
+
+def oracle_stages(oracle_mod, img, args, key):
+    if key not in _oracle_cache:
+        _oracle_cache[key] = oracle_mod.stages(img, oracle_mod.params(*args))
+    return _oracle_cache[key]
+
+
+def image(sgb, w, h, seed):
+    return sgb.synth_image(seed, w, h)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_stages_bit_exact(sgb, oracle_mod, case):
+    name, w, h, seed, args = case
+    img = image(sgb, w, h, seed)
+    st = oracle_stages(oracle_mod, img, args, name)
+    eng = engine_for(sgb, args)
+    kps, desc = eng.detect_and_compute(img)
+    pyr = eng.debug_stage(sgb.STAGE_PYRAMID)
+    assert pyr.shape == st.pyramid.shape
+    if not np.array_equal(pyr, st.pyramid):
+        bad = np.nonzero(pyr != st.pyramid)[0]
+        pytest.fail(f"pyramid differs at {len(bad)} of {pyr.size} values, first at {bad[:5]}")
+    # DoG = G_{s+1}/255 - G_s/255 in f32 (src/sift.rs:92-124)
+    dog = eng.debug_stage(sgb.STAGE_DOG)
+    off_g = off_d = 0
+    L = st.levels
+    for (ow, oh) in st.octave_dims:
+        n = ow * oh
+        lv = [st.pyramid[off_g + s * n: off_g + (s + 1) * n].astype(np.float32) / np.float32(255.0) for s in range(L)]
+        for s in range(L - 1):
+            ref = lv[s + 1] - lv[s]
+            assert np.array_equal(dog[off_d + s * n: off_d + (s + 1) * n], ref)
+        off_g += L * n
+        off_d += (L - 1) * n
+    cands = eng.debug_stage(sgb.STAGE_CANDIDATES)
+    assert cands.tobytes() == st.candidates.tobytes(), f"{len(cands)} vs {len(st.candidates)} candidates"
+    ref = eng.debug_stage(sgb.STAGE_REFINED)
+    assert len(ref) == len(st.refined)
+    for f in ("x", "y", "response", "octave", "layer", "angle"):
+        assert np.array_equal(ref[f], st.refined[f]), f
+    ulp = np.spacing(np.abs(st.refined["size"]))
+    assert np.all(np.abs(ref["size"] - st.refined["size"]) <= 2 * ulp)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_keypoints_and_descriptors_match(sgb, oracle_mod, case):
+    name, w, h, seed, args = case
+    img = image(sgb, w, h, seed)
+    st = oracle_stages(oracle_mod, img, args, name)
+    kps, desc = engine_for(sgb, args).detect_and_compute(img)
+    m = match(st.keypoints, st.descriptors, kps, desc)
+    print(name, m.summary())
+    assert len(st.keypoints) > 0
+    assert m.rate >= MATCH_RATE, m.summary()
+    assert float(m.desc_err.max()) <= DESC_RTOL, m.summary()
+
+
+def test_uniform_image_has_no_keypoints(sgb):
+    """tests/integration_test.rs:205-226"""
+    eng = engine_for(sgb, (1.6, 4, 3, 0.5, 0.04, 10.0))
+    kps, desc = eng.detect_and_compute(np.full((100, 100), 128, np.uint8))
+    assert len(kps) == 0 and desc.shape == (0, 128)
+
+
+@pytest.mark.parametrize("shape", [(0, 0), (1, 1), (15, 20), (3, 64), (64, 3), (9, 9), (31, 33)])
+def test_tiny_and_degenerate_images(sgb, oracle_mod, shape):
+    """Empty octaves, images smaller than the border, kernels wider than the
+    image: same result as the oracle."""
+    h, w = shape
+    if h == 15 and w == 20:
+        img = np.tile((np.arange(20) * 10).astype(np.uint8), (15, 1))  # tests/integration_test.rs:166-203
+    else:
+        img = np.random.default_rng(h * 100 + w).integers(0, 256, size=(h, w), dtype=np.uint8)
+    eng = engine_for(sgb, (1.6, 4, 3, 0.5, 0.04, 10.0))
+    kps, desc = eng.detect_and_compute(img)
+    rk, rd = oracle_mod.detect_and_compute(img)
+    m = match(rk, rd, kps, desc)
+    assert len(kps) == len(desc)
+    assert len(m.unmatched_ref) == 0 and len(m.unmatched_got) == 0, m.summary()
+
+
+def test_strided_input_and_determinism(sgb):
+    """Determinism (tests/integration_test.rs:106-164): bit-identical keypoints
+    and descriptors across calls, and a padded row stride changes nothing."""
+    img = image(sgb, 700, 500, 21)
+    padded = np.zeros((500, 768), np.uint8)
+    padded[:, :700] = img
+    view = padded[:, :700]
+    eng = engine_for(sgb, (1.6, 4, 3, 0.5, 0.04, 10.0))
+    k1, d1 = eng.detect_and_compute(img)
+    k2, d2 = eng.detect_and_compute(view)
+    k3, d3 = eng.detect_and_compute(img)
+    assert k1.tobytes() == k2.tobytes() == k3.tobytes()
+    assert d1.tobytes() == d2.tobytes() == d3.tobytes()
+
+
+def test_f16_storage_is_exact(sgb):
+    """u8-valued levels are exact in f16, and DoG recomputed in f32 from them
+    equals the stored f32 DoG, so the f16 pyramid gives identical output."""
+    args = (1.6, 4, 3, 0.5, 0.04, 10.0)
+    img = image(sgb, 1920, 1080, 1)
+    k32, d32 = engine_for(sgb, args).detect_and_compute(img)
+    e16 = engine_for(sgb, args, "f16")
+    k16, d16 = e16.detect_and_compute(img)
+    assert k16.tobytes() == k32.tobytes()
+    assert d16.tobytes() == d32.tobytes()
+
+
+def test_high_contrast_threshold(sgb):
+    """tests/integration_test.rs:228-281"""
+    img = image(sgb, 512, 512, 0)
+    k_def, _ = engine_for(sgb, (1.6, 4, 3, 0.5, 0.04, 10.0)).detect_and_compute(img)
+    k_hi, d_hi = engine_for(sgb, (1.6, 4, 3, 0.5, 1.0, 10.0)).detect_and_compute(img)
+    assert len(k_def) > 0 and (len(k_hi) < len(k_def) // 2 or len(k_hi) == 0)
+    assert len(k_hi) == len(d_hi)
+
+
+def test_detect_is_detect_and_compute_without_descriptors(sgb):
+    """Sift::detect (src/sift.rs:846-886) = the keypoints of detect_and_compute."""
+    img = image(sgb, 640, 480, 4)
+    eng = engine_for(sgb, (1.6, 4, 3, 0.5, 0.04, 10.0))
+    k, _ = eng.detect_and_compute(img)
+    assert eng.detect(img).tobytes() == k.tobytes()
+
+
+def test_sift_api_drop_in(sgb):
+    """Sift::detect_and_compute_with_backend(img, SiftBackend::Cuda) returns
+    Vec<KeyPoint> + Vec<Vec<f32>> with 128 floats each."""
+    img = image(sgb, 320, 240, 2)
+    s = sgb.Sift.default()
+    kps, desc = s.detect_and_compute_with_backend(img, sgb.SiftBackend.from_str("cuda"))
+    assert len(kps) == len(desc) > 0
+    assert all(len(d) == 128 for d in desc)
+    assert isinstance(kps[0], sgb.KeyPoint)
+
+
+def test_large_6_octave_properties(sgb):
+    """4096 x 4096, Sift::new(1.6, 6, 3, 0.5, 0.04, 10.0): size-independent
+    properties at the full size (determinism, f16 == f32, unit-norm
+    descriptors, keypoints inside the image)."""
+    args = (1.6, 6, 3, 0.5, 0.04, 10.0)
+    img = image(sgb, 4096, 4096, 3)
+    e = engine_for(sgb, args)
+    k1, d1 = e.detect_and_compute(img)
+    k2, d2 = e.detect_and_compute(img)
+    assert k1.tobytes() == k2.tobytes() and d1.tobytes() == d2.tobytes()
+    assert len(k1) > 10000
+    n = np.linalg.norm(d1, axis=1)
+    assert np.all((np.abs(n - 1) < 1e-4) | (n == 0))
+    assert np.all((k1["x"] >= -1) & (k1["x"] <= 4097) & (k1["y"] >= -1) & (k1["y"] <= 4097))
+    k16, d16 = engine_for(sgb, args, "f16").detect_and_compute(img)
+    assert k16.tobytes() == k1.tobytes() and d16.tobytes() == d1.tobytes()
