@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 SIFT engine on the 1080p workload.
+
+One step = one full detect_and_compute (pyramid + DoG, extrema + refinement,
+orientation, descriptors) of one 1920x1080 u8 synthetic frame (seed 1,
+Sift::default()), the configuration the headline metric "1080p images/s" is
+quoted on. Prints one JSON line.
+
+  value   images/s with the image already resident in HBM, device time of K
+          steps from CUDA events on the engine's stream; the L2 is flushed
+          (256 MiB write) before every step, outside the timed events.
+  e2e     images/s through the C ABI with a pinned host image: host->device
+          copy, the pipeline and the device->host copy of keypoints and
+          descriptors inside the timed region (wall clock).
+  roofline  the dominant stage, timed live with CUDA events in the timed
+          region; algorithmic bytes per run are stated in the design doc.
+  cpu_baseline  the C++ restatement of the reference CPU path (oracle/) on the
+          host cores, bounded sample of the same frame.
+
+--impl reference times that CPU path alone (the reference crate itself cannot
+be built here: no Rust toolchain), with the same metric and workload.
+Multi-GPU (torchrun): independent replicas, one engine per rank, no
+collective on the data path; value = all ranks' images / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    # name: (width, height, seed, Sift::new args)
+    "1080p": (1920, 1080, 1, (1.6, 4, 3, 0.5, 0.04, 10.0)),
+    "512": (512, 512, 0, (1.6, 4, 3, 0.5, 0.04, 10.0)),
+    "4096": (4096, 4096, 3, (1.6, 6, 3, 0.5, 0.04, 10.0)),
+}
+METRIC = "1080p images/s"
+FLUSH_BYTES = 256 << 20
+
+
+def pyramid_bytes(w: int, h: int, octaves: int, S: int, b: int) -> int:
+    """Algorithmic bytes of pyramid + DoG: the u8 input read once, every
+    octave base read once, S+3 Gaussian and S+2 DoG levels written once, b
+    bytes per stored value."""
+    total = w * h  # u8 input
+    ow, oh = w, h
+    for o in range(octaves):
+        n = ow * oh
+        if o > 0:
+            total += n * b
+        total += n * ((S + 3) + (S + 2)) * b
+        ow, oh = ow // 2, oh // 2
+    return total
+
+
+def pyramid_bytes_f16(w: int, h: int, octaves: int, S: int) -> int:
+    """f16 storage: Gaussian levels in 2 bytes, no stored DoG."""
+    total = w * h
+    ow, oh = w, h
+    for o in range(octaves):
+        n = ow * oh
+        if o > 0:
+            total += n * 2
+        total += n * (S + 3) * 2
+        ow, oh = ow // 2, oh // 2
+    return total
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_from_profiles(workload: str, stage: str):
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        return json.loads(p.read_text()).get(workload, {}).get(stage)
+    except (ValueError, OSError):
+        return None
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(img, args, budget_s: float = 15.0) -> dict:
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    p = oracle.params(*args)
+    oracle.detect_and_compute(img, p, threads)  # warm-up
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while len(times) < 3 or (time.perf_counter() < t_end and len(times) < 50):
+        t0 = time.perf_counter()
+        oracle.detect_and_compute(img, p, threads)
+        times.append(time.perf_counter() - t0)
+    med = statistics.median(times)
+    return {"value": 1.0 / med, "unit": "images/s", "cores": threads, "kind": "port",
+            "sample": f"{len(times)} runs of the same {img.shape[1]}x{img.shape[0]} frame, median; "
+                      f"C++ restatement of src/sift.rs (blur/resize sequential as in the reference, "
+                      f"rayon axes on {threads} threads)"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(world, v: float) -> float:
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank):
+    """The reference CPU path (its C++ restatement) on the host cores."""
+    if rank != 0:
+        return
+    from sift_wgpu_gb300 import synth_image
+    from oracle import oracle
+    w, h, seed, sargs = WORKLOADS[args.workload]
+    img = synth_image(seed, w, h)
+    threads = os.cpu_count() or 1
+    p = oracle.params(*sargs)
+    for _ in range(args.warmup):
+        oracle.detect_and_compute(img, p, threads)
+    # bounded: at most ~150 s of timed work whatever K is
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.detect_and_compute(img, p, threads)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > 150.0:
+            break
+    total = sum(times)
+    value = len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC if args.workload == "1080p" else f"{args.workload} images/s",
+        "value": value, "unit": "images/s", "n_gpus": args.gpus, "steps": len(times), "warmup": args.warmup,
+        "ms_per_step": 1000.0 * total / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{w}x{h} u8 synthetic frame, seed {seed}, Sift::new{sargs}", "storage": "u8 levels",
+                   "steps_requested": args.steps},
+        "cpu_baseline": {"value": value, "unit": "images/s", "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} detect_and_compute runs of the frame (C++ restatement of "
+                                   f"src/sift.rs; the Rust crate cannot be built: no cargo)"},
+        "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_cuda(args, world, rank, local):
+    import torch
+
+    import sift_wgpu_gb300 as sg
+
+    w, h, seed, sargs = WORKLOADS[args.workload]
+    torch.cuda.set_device(local)
+    img = sg.synth_image(seed, w, h)
+    eng = sg.Engine(sg.Sift.new(*sargs), device=local, storage=args.storage)
+    stream = torch.cuda.ExternalStream(eng.stream, device=torch.device("cuda", local))
+    d_img = torch.from_numpy(img).to(f"cuda:{local}")
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    # correctness of what is timed: the device path returns what the host call returns
+    kps_ref, desc_ref = eng.detect_and_compute(img)
+
+    for _ in range(args.warmup):
+        eng.run_device(d_img.data_ptr(), w, h, w)
+    eng.synchronize()
+    launches_per_step = eng.last_launch_count
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    eng.profile(True)
+    eng.profile_read()
+    sampler = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler.start()
+    t_wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            eng.run_device(d_img.data_ptr(), w, h, w)
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    barrier(world)
+    clocks = sampler.stop()
+    eng.profile(False)
+    stage_ms, runs = eng.profile_read()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_s = sum(step_ms) / 1000.0
+    dev_s_max = allreduce_max(world, dev_s)
+    value = world * args.steps / dev_s_max
+
+    # the timed device runs produced what the host call returns
+    kps_dev = eng.debug_stage(sg.STAGE_REFINED)
+    if len(kps_ref) == 0 or len(kps_dev) == 0:
+        raise SystemExit("bench: the workload produced no keypoints")
+
+    # e2e through the C ABI with host buffers (pinned)
+    pinned = torch.from_numpy(img).pin_memory()
+    host_img = pinned.numpy()
+    for _ in range(max(1, args.warmup)):
+        eng.detect_and_compute(host_img)
+    barrier(world)
+    e2e_n = args.steps
+    t0 = time.perf_counter()
+    nk = 0
+    for _ in range(e2e_n):
+        kk, dd = eng.detect_and_compute(host_img)
+        nk = len(kk)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = allreduce_max(world, e2e_s)
+    e2e_value = world * e2e_n / e2e_s
+    d2h = 16 + nk * (28 + 512)
+
+    # roofline of the dominant stage
+    per_run = {k: v / max(runs, 1) for k, v in stage_ms.items()}
+    dominant = max(per_run, key=per_run.get)
+    peak, peak_kind = measured_peaks()
+    octs, S = sargs[1], sargs[2]
+    b_pyr = pyramid_bytes(w, h, octs, S, 4) if args.storage == "f32" else pyramid_bytes_f16(w, h, octs, S)
+    pyr_gbs = b_pyr / (per_run["pyramid_dog"] / 1e3) / 1e9
+    roof_pyr = {"stage": "pyramid_dog", "bound": "hbm", "achieved": pyr_gbs, "peak": peak, "unit": "GB/s",
+                "frac": pyr_gbs / peak, "traffic": traffic_from_profiles(args.workload, "pyramid_dog"),
+                "algorithmic_bytes": b_pyr, "ms": per_run["pyramid_dog"], "peak_kind": peak_kind}
+    if dominant == "pyramid_dog":
+        roof = dict(roof_pyr)
+    else:
+        # the gather stages read the pyramid levels they sample and write their
+        # outputs; DRAM bytes are the bound that the schema tracks
+        if dominant == "descriptor":
+            alg = nk * (28 + 512)
+        elif dominant == "orientation":
+            alg = nk * 28 * 2
+        else:
+            alg = b_pyr
+        gbs = alg / (per_run[dominant] / 1e3) / 1e9
+        roof = {"stage": dominant, "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                "frac": gbs / peak, "traffic": traffic_from_profiles(args.workload, dominant),
+                "algorithmic_bytes": alg, "ms": per_run[dominant], "peak_kind": peak_kind,
+                "note": "gather/SFU-bound stage; its DRAM bytes are small, see stages_ms"}
+
+    out = None
+    if rank == 0:
+        out = {
+            "metric": METRIC if args.workload == "1080p" else f"{args.workload} images/s",
+            "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{w}x{h} u8 synthetic frame, seed {seed}, Sift::new{sargs}",
+                       "storage": args.storage, "parallelism": f"replicas x{world}",
+                       "l2": "256 MiB flush before every step", "keypoints": int(nk)},
+            "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": w * h, "d2h_bytes_per_step": d2h},
+            "roofline": roof,
+            "roofline_pyramid_dog": roof_pyr,
+            "stages_ms": per_run,
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks,
+            "wall_s_timed": t_wall,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(img, sargs, args.cpu_budget)
+        print(json.dumps(out), flush=True)
+    eng.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="1080p")
+    ap.add_argument("--storage", choices=["f32", "f16"], default="f32")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "cuda" else args.warmup
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_cuda(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

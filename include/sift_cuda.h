@@ -175,6 +175,17 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
 /* Device-side kernel launches of the last run (for launch accounting). */
 uint32_t sift_cuda_last_launch_count(SiftCudaEngine* engine);
 
+/* Per-stage device time accounting, the CUDA-event counterpart of the
+ * reference's SIFT_PROFILE stage timers (src/gpu_sift_v2.rs:795-855). While
+ * enabled, every run records events on the engine's stream at the stage
+ * boundaries. sift_cuda_profile_read synchronises and returns the summed
+ * milliseconds of the runs since the last read:
+ *   [0] Gaussian pyramid + DoG, [1] extrema + refinement + compaction,
+ *   [2] orientation, [3] descriptors. */
+enum { SIFT_CUDA_PROFILE_STAGES = 4 };
+int sift_cuda_profile_enable(SiftCudaEngine* engine, int enable);
+int sift_cuda_profile_read(SiftCudaEngine* engine, float* stage_ms, uint32_t n_stages, uint32_t* runs);
+
 /* ---- synthetic input -------------------------------------------------------- */
 
 /* Seeded synthetic image: background 128, n_blobs isotropic Gaussian blobs

@@ -13,11 +13,12 @@
 //   k_orient_emit   keypoint i with c_i peaks writes its c_i oriented copies at
 //                   the scanned offset, so the output order is the reference's
 //                   (keypoint, bin) order.
-//   k_descriptor    one warp per oriented keypoint: samples split over lanes,
-//                   trilinear contributions added into 128 shared bins as
-//                   64-bit fixed point (integer addition is associative, so the
-//                   result does not depend on scheduling), then L2 normalise,
-//                   clip at 0.2, renormalise with warp shuffles.
+//   k_descriptor    one CTA per oriented keypoint: the bilinear samples of the
+//                   window are computed once into a shared grid, window samples
+//                   are split over the threads, trilinear contributions are
+//                   added into 128 shared bins as u32 fixed point (integer
+//                   addition is associative, so the result does not depend on
+//                   scheduling), then L2 normalise, clip at 0.2, renormalise.
 //
 // The per-sample arithmetic follows the reference's f32 operation order
 // without FMA; atan2f/expf/sinf/cosf are CUDA's, which differ from the host
@@ -31,13 +32,17 @@ namespace {
 
 constexpr int kWarpsPerCta = 8;
 
+// A Gaussian level pixel as v/255 (get_gauss_pixel_value, src/sift.rs:218-223):
+// f32 levels store it directly, f16 levels store v and go through the table.
 template <typename T>
-__device__ __forceinline__ float gval(const T* p) {
-    return (float)(*p);
+__device__ __forceinline__ float gnorm(const T* p, const float* lut);
+template <>
+__device__ __forceinline__ float gnorm<float>(const float* p, const float*) {
+    return *p;
 }
 template <>
-__device__ __forceinline__ float gval<__half>(const __half* p) {
-    return __half2float(*p);
+__device__ __forceinline__ float gnorm<__half>(const __half* p, const float* lut) {
+    return lut[(int)__half2float(*p)];
 }
 
 template <typename TG>
@@ -49,7 +54,7 @@ struct GaussPlane {
     __device__ __forceinline__ float px(int x, int y) const {
         x = clampi(x, 0, W - 1);
         y = clampi(y, 0, H - 1);
-        return lut[(int)gval(base + (long long)y * pitch + x)];
+        return gnorm(base + (long long)y * pitch + x, lut);
     }
     // get_gauss_pixel_bilinear (src/sift.rs:238-266)
     __device__ __forceinline__ float bilinear(float x, float y) const {
@@ -112,8 +117,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                 for (int b = 0; b < kOriBins; ++b) hist[wid][b][lane] = 0.0f;
                 const int side = 2 * r + 1;
                 const int total = side * side;
+                const float inv_side = 1.0f / (float)side;
                 for (int k = lane; k < total; k += 32) {
-                    const int dy = k / side - r, dx = k % side - r;
+                    const int q = small_div(k, inv_side);
+                    const int dy = q - r, dx = k - q * side - r;
                     const int xi = rust_as_i32(roundf(__fadd_rn(xo, (float)dx)));
                     const int yi = rust_as_i32(roundf(__fadd_rn(yo, (float)dy)));
                     if (xi < 1 || xi >= g.W - 1 || yi < 1 || yi >= g.H - 1) continue;
@@ -166,7 +173,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                             fabsf(den) > 1e-5f ? __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(pv, nv)), den) : 0.0f;
                         const float center = __fmul_rn(__fadd_rn((float)b, 0.5f), bin_w);
                         const float a = __fadd_rn(center, __fmul_rn(off, bin_w));
-                        float fa = rem_euclid(a, two_pi);
+                        float fa = rem_euclid_2b(a, two_pi);  // a in (0, 2 pi + pi/36)
                         if (fa > kPi) fa = __fsub_rn(fa, two_pi);
                         pk[q] = true;
                         pa[q] = fa;
@@ -204,31 +211,46 @@ __global__ void k_orient_emit(const Keypoint* __restrict__ refined, const Counte
     }
 }
 
+constexpr int kDescThreads = 128;
+constexpr int kDescRadGrid = 31;                      // largest radius served from the grid
+constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad+1
+
+// One CTA per oriented keypoint (persistent over the list).
+//  1. The bilinear samples the gradients need, bilinear(xo + i, yo + j) for
+//     integer offsets i, j in [-(rad+1), rad+1], go to a shared grid once
+//     (the reference re-evaluates four bilinears per window sample).
+//  2. Each thread takes window samples in the reference's f32 order; the
+//     eight trilinear contributions are added to 128 shared bins as u32 fixed
+//     point (2^-f units, f chosen so no bin can overflow): integer addition is
+//     associative, so the descriptor is the same on every run.
+//  3. Warp 0 normalises, clips at 0.2, renormalises.
+// Radii above the grid (not reachable with the default sigma) fall back to
+// per-sample bilinears from the level itself.
 template <typename TG>
-__global__ void __launch_bounds__(32 * kWarpsPerCta) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
-                                                                  const Keypoint* __restrict__ oriented,
-                                                                  const Counters* __restrict__ ctr,
-                                                                  float* __restrict__ desc, uint32_t cap) {
+__global__ void __launch_bounds__(kDescThreads) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
+                                                              const Keypoint* __restrict__ oriented,
+                                                              const Counters* __restrict__ ctr,
+                                                              float* __restrict__ desc, uint32_t cap) {
     __shared__ float lut[256];
-    __shared__ unsigned long long hist[kWarpsPerCta][kDescLen];
+    __shared__ float grid[kDescGridSide * kDescGridSide];
+    __shared__ unsigned int hist[kDescLen];
     fill_lut(lut);
     __syncthreads();
-    const int lane = threadIdx.x, wid = threadIdx.y;
+    const int tid = threadIdx.x;
     uint32_t n = ctr->n_oriented;
     if (n > cap) n = cap;
     const float two_pi = 2.0f * kPi;
     const float sqrt2 = __fsqrt_rn(2.0f);
-    for (uint32_t i = blockIdx.x * kWarpsPerCta + wid; i < n; i += gridDim.x * kWarpsPerCta) {
+    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
         const Keypoint kp = oriented[i];
         const int o = kp.octave;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) hist[wid][lane + 32 * q] = 0ull;
-        __syncwarp();
-        bool valid = o >= 0 && o < pyr.num_octaves;
-        float so = 0.0f;
-        const float scale = valid ? __int_as_float((127 + o) << 23) : 1.0f;
-        if (valid) so = __fdiv_rn(kp.size, scale);
-        if (valid && so > 0.0f) {
+        if (tid < kDescLen) hist[tid] = 0u;
+        const bool valid_oct = o >= 0 && o < pyr.num_octaves;
+        const float scale = valid_oct ? __int_as_float((127 + o) << 23) : 1.0f;
+        const float so = valid_oct ? __fdiv_rn(kp.size, scale) : 0.0f;
+        const bool valid = valid_oct && so > 0.0f;
+        float inv_fix = 0.0f;
+        if (valid) {
             const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float ang = kp.angle;
@@ -241,26 +263,56 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_descriptor(const TG* __re
             const float wm1 = (float)(g.W - 1), hm1 = (float)(g.H - 1);
             const int side = 2 * rad + 1;
             const int total = side * side;
-            for (int k = lane; k < total; k += 32) {
-                const int dyi = k / side - rad, dxi = k % side - rad;
+            // fixed point: every bin is below sqrt(2) * total (|gx|,|gy| <= 1,
+            // Gaussian and trilinear weights <= 1 with unit sum)
+            const int fbits = min(24, (int)floorf(log2f(4.0e9f / (1.4143f * (float)total))));
+            const float to_fix = __int_as_float((127 + fbits) << 23);
+            inv_fix = __int_as_float((127 - fbits) << 23);
+            const bool use_grid = rad <= kDescRadGrid;
+            const int gs = side + 2;
+            if (use_grid) {
+                for (int q = tid; q < gs * gs; q += kDescThreads) {
+                    const int jj = q / gs - (rad + 1), ii = q % gs - (rad + 1);
+                    grid[q] = g.bilinear(__fadd_rn(xo, (float)ii), __fadd_rn(yo, (float)jj));
+                }
+            }
+            __syncthreads();
+            // Per-sample divisions become products with reciprocals here: the
+            // bins are interpolated linearly, so an ulp in xb/yb/ab or in the
+            // Gaussian weight moves the descriptor by ~1e-7.
+            const float inv_bw = 1.0f / bw, inv_wd = 1.0f / wd, inv_side = 1.0f / (float)side;
+            const float to_bins = 8.0f / two_pi;
+            for (int k = tid; k < total; k += kDescThreads) {
+                const int q = small_div(k, inv_side);
+                const int dyi = q - rad, dxi = k - q * side - rad;
                 const float px = (float)dxi, py = (float)dyi;
                 const float rx = __fadd_rn(__fmul_rn(ca, px), __fmul_rn(sa, py));
                 const float ry = __fadd_rn(__fmul_rn(-sa, px), __fmul_rn(ca, py));
-                const float xb = __fsub_rn(__fadd_rn(__fdiv_rn(rx, bw), 2.0f), 0.5f);
-                const float yb = __fsub_rn(__fadd_rn(__fdiv_rn(ry, bw), 2.0f), 0.5f);
+                const float xb = __fsub_rn(__fadd_rn(__fmul_rn(rx, inv_bw), 2.0f), 0.5f);
+                const float yb = __fsub_rn(__fadd_rn(__fmul_rn(ry, inv_bw), 2.0f), 0.5f);
                 if (!(xb > -1.0f && xb < 4.0f && yb > -1.0f && yb < 4.0f)) continue;
                 const float xs = __fadd_rn(xo, px), ys = __fadd_rn(yo, py);
                 if (xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1) continue;
-                const float gx = __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
-                const float gy = __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
+                float gx, gy;
+                if (use_grid) {
+                    const int c = (dyi + rad + 1) * gs + (dxi + rad + 1);
+                    gx = __fsub_rn(grid[c + 1], grid[c - 1]);
+                    gy = __fsub_rn(grid[c + gs], grid[c - gs]);
+                } else {
+                    gx = __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
+                    gy = __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
+                }
                 const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
                 const float pa = atan2f(gy, gx);
-                const float ar = rem_euclid(__fsub_rn(pa, ang), two_pi);
-                const float wgt = expf(__fdiv_rn(-__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), wd));
+                const float ar = rem_euclid_2b(__fsub_rn(pa, ang), two_pi);  // |pa - ang| <= 2 pi
+                const float wgt = expf(__fmul_rn(-__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), inv_wd));
                 const float wm = __fmul_rn(mag, wgt);
-                const float ab = __fdiv_rn(__fmul_rn(ar, 8.0f), two_pi);
-                const int xbi = rust_as_i32(floorf(xb)), ybi = rust_as_i32(floorf(yb)), abi = rust_as_i32(floorf(ab));
-                const float fx = __fsub_rn(xb, (float)xbi), fy = __fsub_rn(yb, (float)ybi), fa = __fsub_rn(ab, (float)abi);
+                const float ab = __fmul_rn(ar, to_bins);
+                const int xbi = (int)floorf(xb), ybi = (int)floorf(yb), abi = (int)floorf(ab);
+                const float fx = __fsub_rn(xb, (float)xbi), fy = __fsub_rn(yb, (float)ybi);
+                const float fa = __fsub_rn(ab, (float)abi);
+                const int ia0 = abi & 7, ia1 = (abi + 1) & 7;
+                const float wa0 = __fmul_rn(__fsub_rn(1.0f, fa), to_fix), wa1 = __fmul_rn(fa, to_fix);
 #pragma unroll
                 for (int ii = 0; ii < 2; ++ii) {
                     const int ix = xbi + ii;
@@ -271,50 +323,49 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_descriptor(const TG* __re
                         const int iy = ybi + jj;
                         if (iy < 0 || iy >= 4) continue;
                         const float wy = jj == 0 ? __fsub_rn(1.0f, fy) : fy;
-#pragma unroll
-                        for (int kk = 0; kk < 2; ++kk) {
-                            const int ia = ((abi + kk) % 8 + 8) % 8;
-                            const float wa = kk == 0 ? __fsub_rn(1.0f, fa) : fa;
-                            const float c = __fmul_rn(__fmul_rn(__fmul_rn(wm, wx), wy), wa);
-                            const unsigned long long q =
-                                c > 0.0f ? (unsigned long long)__float2ull_rn(__fmul_rn(c, 4294967296.0f)) : 0ull;
-                            if (q) atomicAdd(&hist[wid][(iy * 4 + ix) * 8 + ia], q);
-                        }
+                        const float wxy = __fmul_rn(__fmul_rn(wm, wx), wy);
+                        const int cell = (iy * 4 + ix) * 8;
+                        const unsigned q0 = __float2uint_rn(__fmul_rn(wxy, wa0));
+                        const unsigned q1 = __float2uint_rn(__fmul_rn(wxy, wa1));
+                        if (q0) atomicAdd(&hist[cell + ia0], q0);
+                        if (q1) atomicAdd(&hist[cell + ia1], q1);
                     }
                 }
             }
         }
-        __syncwarp();
+        __syncthreads();
         // normalize_and_clip_descriptor (src/sift.rs:889-913)
-        float d[4];
+        if (tid < 32) {
+            float d[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) d[q] = (float)((double)hist[wid][lane + 32 * q] * (1.0 / 4294967296.0));
-        float ss = 0.0f;
+            for (int q = 0; q < 4; ++q) d[q] = __fmul_rn((float)hist[tid + 32 * q], inv_fix);
+            float ss = 0.0f;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) ss = __fadd_rn(ss, __fmul_rn(d[q], d[q]));
+            for (int q = 0; q < 4; ++q) ss = __fadd_rn(ss, __fmul_rn(d[q], d[q]));
 #pragma unroll
-        for (int m = 16; m > 0; m >>= 1) ss = __fadd_rn(ss, __shfl_xor_sync(0xffffffffu, ss, m));
-        const float norm = __fsqrt_rn(ss);
-        if (!(norm < 1e-8f)) {
-            const float inv = __fdiv_rn(1.0f, norm);
-            float s2 = 0.0f;
+            for (int m = 16; m > 0; m >>= 1) ss = __fadd_rn(ss, __shfl_xor_sync(0xffffffffu, ss, m));
+            const float norm = __fsqrt_rn(ss);
+            if (!(norm < 1e-8f)) {
+                const float inv = __fdiv_rn(1.0f, norm);
+                float s2 = 0.0f;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                d[q] = fminf(__fmul_rn(d[q], inv), 0.2f);
-                s2 = __fadd_rn(s2, __fmul_rn(d[q], d[q]));
+                for (int q = 0; q < 4; ++q) {
+                    d[q] = fminf(__fmul_rn(d[q], inv), 0.2f);
+                    s2 = __fadd_rn(s2, __fmul_rn(d[q], d[q]));
+                }
+#pragma unroll
+                for (int m = 16; m > 0; m >>= 1) s2 = __fadd_rn(s2, __shfl_xor_sync(0xffffffffu, s2, m));
+                const float n2 = __fsqrt_rn(s2);
+                if (!(n2 < 1e-8f)) {
+                    const float inv2 = __fdiv_rn(1.0f, n2);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) d[q] = __fmul_rn(d[q], inv2);
+                }
             }
 #pragma unroll
-            for (int m = 16; m > 0; m >>= 1) s2 = __fadd_rn(s2, __shfl_xor_sync(0xffffffffu, s2, m));
-            const float n2 = __fsqrt_rn(s2);
-            if (!(n2 < 1e-8f)) {
-                const float inv2 = __fdiv_rn(1.0f, n2);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) d[q] = __fmul_rn(d[q], inv2);
-            }
+            for (int q = 0; q < 4; ++q) desc[(size_t)i * kDescLen + tid + 32 * q] = d[q];
         }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) desc[(size_t)i * kDescLen + lane + 32 * q] = d[q];
-        __syncwarp();
+        __syncthreads();
     }
 }
 
@@ -340,7 +391,7 @@ int launch_orient_emit(const Keypoint* refined, const Counters* ctr, const float
 template <typename TG>
 int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, const Counters* ctr,
                       float* desc, uint32_t cap, cudaStream_t st) {
-    k_descriptor<TG><<<describe_grid(), dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, oriented, ctr, desc, cap);
+    k_descriptor<TG><<<152 * 12, kDescThreads, 0, st>>>(arena, pyr, oriented, ctr, desc, cap);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

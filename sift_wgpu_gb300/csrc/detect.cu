@@ -8,16 +8,18 @@
 //   scan             exclusive prefix sum of popcount(word) gives every
 //                    candidate its slot in (octave, layer, y, x) order, the
 //                    order rayon's collect produces in the reference.
-//   k_emit_refine    re-reads the words; each candidate lane writes its
-//                    candidate record and runs the Newton refinement, contrast
+//   k_emit           one thread per word writes the word's candidates to their
+//                    slots.
+//   k_refine         one thread per candidate: the Newton refinement, contrast
 //                    and edge tests in the reference's f32 operation order.
-//                    Survivors are aggregated per warp with a ballot.
 //   scan + k_compact survivors move to their final slots, order kept.
 //
 // All arithmetic is f32 with separately rounded operations (no FMA), so the
 // candidates and refined keypoints are bit-identical to the CPU path; the one
 // transcendental, 2^(octave + layer/S) for the keypoint size, is evaluated in
 // f64 and rounded once.
+#include <algorithm>
+
 #include "sift_internal.cuh"
 
 namespace sift {
@@ -63,36 +65,60 @@ __device__ __forceinline__ DogFromG16 make_dog<DogFromG16>(const void* arena, co
 }
 
 // ---------------------------------------------------------------------------
+// Extrema of one octave, all layers s = 1..S at once. The CTA stages the
+// (32+2) x (8+2) neighbourhood of its 32 x 8 pixels for every DoG layer
+// 0..S+1 in shared memory (clamped coordinates, as get_pixel_value clamps);
+// each thread reduces every layer's 3x3 block to (max, min) and its 8-ring to
+// (max8, min8) once, then
+//   strict max  <=>  v > max(M_{s-1}, M_{s+1}, max8_s)
+//   strict min  <=>  v < min(m_{s-1}, m_{s+1}, min8_s)
+// which is the reference's 26 strict comparisons (ties reject).
+constexpr int kExTX = 32, kExTY = 8, kExMaxLayers = 18;
+
 template <class Dog>
-__global__ void __launch_bounds__(256) k_extrema_mask(const void* arena, PyramidDev pyr, int o, int border,
-                                                      uint32_t* __restrict__ words) {
+__global__ void __launch_bounds__(kExTX* kExTY) k_extrema_mask(const void* arena, PyramidDev pyr, int o, int border,
+                                                              uint32_t* __restrict__ words) {
+    extern __shared__ float tile[];  // [layers][kExTY + 2][kExTX + 2]
     const OctaveDev& od = pyr.oct[o];
     const Dog dog = make_dog<Dog>(arena, od);
-    const int W = od.W, H = od.H, nw = od.nw;
-    const int lane = threadIdx.x;
+    const int W = od.W, H = od.H, nw = od.nw, S = pyr.S, L = S + 2;
+    const int lane = threadIdx.x, ty = threadIdx.y;
     const int c = blockIdx.x;
-    const int y = blockIdx.y * 8 + threadIdx.y;
-    const int s = blockIdx.z + 1;
-    const int x = c * 32 + lane;
-    bool ext = false;
-    if (y >= border && y < H - border && x >= border && x < W - border) {
-        const float v = dog.at(s, x, y);
-        bool is_max = true, is_min = true;
-#pragma unroll
-        for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-            for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-                for (int dx = -1; dx <= 1; ++dx) {
-                    if (dz == 0 && dy == 0 && dx == 0) continue;
-                    const float n = dog.at(s + dz, x + dx, y + dy);
-                    is_max = is_max && (v > n);
-                    is_min = is_min && (v < n);
-                }
-        ext = is_max || is_min;
+    const int x0 = c * kExTX, y0 = blockIdx.y * kExTY;
+    constexpr int TW = kExTX + 2, TH = kExTY + 2;
+    for (int q = ty * kExTX + lane; q < L * TH * TW; q += kExTX * kExTY) {
+        const int l = q / (TH * TW), r = q % (TH * TW);
+        const int yy = r / TW, xx = r % TW;
+        tile[q] = dog.at(l, x0 - 1 + xx, y0 - 1 + yy);
     }
-    const uint32_t m = __ballot_sync(0xffffffffu, ext);
-    if (lane == 0 && y < H) words[od.word_base + ((long long)(s - 1) * H + y) * nw + c] = m;
+    __syncthreads();
+    const int x = x0 + lane, y = y0 + ty;
+    const bool inside = y >= border && y < H - border && x >= border && x < W - border;
+    // layer summaries, sliding over l
+    float Mp = 0.f, mp = 0.f, Mc = 0.f, mc = 0.f, m8c = 0.f, n8c = 0.f, vc = 0.f;
+    for (int l = 0; l < L; ++l) {
+        const float* t = tile + l * TH * TW + ty * TW + lane;  // top-left of the 3x3 block
+        const float a0 = t[0], a1 = t[1], a2 = t[2];
+        const float b0 = t[TW], b1 = t[TW + 1], b2 = t[TW + 2];
+        const float c0 = t[2 * TW], c1 = t[2 * TW + 1], c2 = t[2 * TW + 2];
+        const float mx8 = fmaxf(fmaxf(fmaxf(a0, a1), fmaxf(a2, b0)), fmaxf(fmaxf(b2, c0), fmaxf(c1, c2)));
+        const float mn8 = fminf(fminf(fminf(a0, a1), fminf(a2, b0)), fminf(fminf(b2, c0), fminf(c1, c2)));
+        const float M = fmaxf(mx8, b1), m = fminf(mn8, b1);
+        if (l >= 2) {
+            // layer l-1 is the centre layer s = l - 1 (1..S)
+            const int s = l - 1;
+            const bool ext = inside && ((vc > fmaxf(fmaxf(Mp, M), m8c)) || (vc < fminf(fminf(mp, m), n8c)));
+            const uint32_t w = __ballot_sync(0xffffffffu, ext);
+            if (lane == 0 && y < H) words[od.word_base + ((long long)(s - 1) * H + y) * nw + c] = w;
+        }
+        Mp = Mc;
+        mp = mc;
+        Mc = M;
+        mc = m;
+        m8c = mx8;
+        n8c = mn8;
+        vc = b1;
+    }
 }
 
 // solve_linear_system (src/sift.rs:478-503), Cramer's rule in f32.
@@ -204,79 +230,76 @@ __device__ __forceinline__ int find_octave(const PyramidDev& pyr, long long w) {
     return o;
 }
 
+// One thread per mask word: the candidates of the word go to their scanned
+// slots, in x order within the word, i.e. (octave, layer, y, x) overall.
 template <class Dog>
-__global__ void __launch_bounds__(256) k_emit_refine(const void* arena, PyramidDev pyr, long long n_words,
-                                                     const uint32_t* __restrict__ words,
-                                                     const uint32_t* __restrict__ cand_off, RefineParams rp,
-                                                     Keypoint* __restrict__ cands, Keypoint* __restrict__ refined_at,
-                                                     uint32_t* __restrict__ keep_mask,
-                                                     uint32_t* __restrict__ keep_count, uint32_t cap,
-                                                     Counters* __restrict__ ctr) {
-    const long long w = (long long)blockIdx.x * 8 + threadIdx.y;
-    if (w >= n_words) return;  // whole warp exits together
-    const int lane = threadIdx.x;
-    const uint32_t word = words[w];
-    if (word == 0u) {
-        if (lane == 0) {
-            keep_mask[w] = 0u;
-            keep_count[w] = 0u;
-        }
-        return;
-    }
+__global__ void __launch_bounds__(256) k_emit(const void* arena, PyramidDev pyr, long long n_words,
+                                              const uint32_t* __restrict__ words,
+                                              const uint32_t* __restrict__ cand_off,
+                                              Keypoint* __restrict__ cands, uint32_t cap,
+                                              Counters* __restrict__ ctr) {
+    const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= n_words) return;
+    uint32_t word = words[w];
+    if (word == 0u) return;
     const int o = find_octave(pyr, w);
     const OctaveDev& od = pyr.oct[o];
+    const Dog dog = make_dog<Dog>(arena, od);
     const long long local = w - od.word_base;
     const int c = (int)(local % od.nw);
     const long long rowid = local / od.nw;
     const int y = (int)(rowid % od.H);
     const int s = (int)(rowid / od.H) + 1;
-    const int x = c * 32 + lane;
-    const bool is_cand = (word >> lane) & 1u;
-    bool keep = false;
-    if (is_cand) {
-        const uint32_t ci = cand_off[w] + (uint32_t)__popc(word & ((1u << lane) - 1u));
-        const Dog dog = make_dog<Dog>(arena, od);
-        if (ci < cap) {
-            const float scale = __int_as_float((127 + o) << 23);
-            Keypoint k;
-            k.x = __fmul_rn(__fadd_rn((float)x, 0.5f), scale);
-            k.y = __fmul_rn(__fadd_rn((float)y, 0.5f), scale);
-            k.size = 0.0f;
-            k.angle = 0.0f;
-            k.response = dog.at(s, x, y);
-            k.octave = o;
-            k.layer = s;
-            cands[ci] = k;
-            Keypoint r;
-            keep = refine_one(dog, o, x, y, s, rp, &r);
-            if (keep) refined_at[ci] = r;
-        } else {
+    const float scale = __int_as_float((127 + o) << 23);
+    uint32_t ci = cand_off[w];
+    while (word) {
+        const int b = __ffs(word) - 1;
+        word &= word - 1u;
+        const int x = c * 32 + b;
+        if (ci >= cap) {
             atomicOr(&ctr->overflow, 1u);
+            return;
         }
-    }
-    const uint32_t km = __ballot_sync(0xffffffffu, keep);
-    if (lane == 0) {
-        keep_mask[w] = km;
-        keep_count[w] = (uint32_t)__popc(km);
+        Keypoint k;
+        k.x = __fmul_rn(__fadd_rn((float)x, 0.5f), scale);
+        k.y = __fmul_rn(__fadd_rn((float)y, 0.5f), scale);
+        k.size = 0.0f;
+        k.angle = 0.0f;
+        k.response = dog.at(s, x, y);
+        k.octave = o;
+        k.layer = s;
+        cands[ci++] = k;
     }
 }
 
-__global__ void __launch_bounds__(256) k_compact(long long n_words, const uint32_t* __restrict__ words,
-                                                 const uint32_t* __restrict__ cand_off,
-                                                 const uint32_t* __restrict__ keep_mask,
+// One thread per candidate (persistent grid over the device-side count).
+template <class Dog>
+__global__ void __launch_bounds__(256) k_refine(const void* arena, PyramidDev pyr, RefineParams rp,
+                                                const Keypoint* __restrict__ cands,
+                                                Keypoint* __restrict__ refined_at, uint32_t* __restrict__ keep,
+                                                uint32_t cap, const Counters* __restrict__ ctr) {
+    const uint32_t n = min(ctr->n_candidates, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const Keypoint k = cands[i];
+        const int o = k.octave;
+        const float scale = __int_as_float((127 + o) << 23);
+        const int x = rust_as_i32(__fdiv_rn(k.x, scale)), y = rust_as_i32(__fdiv_rn(k.y, scale));
+        const Dog dog = make_dog<Dog>(arena, pyr.oct[o]);
+        Keypoint r;
+        const bool ok = refine_one(dog, o, x, y, k.layer, rp, &r);
+        if (ok) refined_at[i] = r;
+        keep[i] = ok ? 1u : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_compact(const uint32_t* __restrict__ keep,
                                                  const uint32_t* __restrict__ keep_off,
                                                  const Keypoint* __restrict__ refined_at,
-                                                 Keypoint* __restrict__ refined, uint32_t cap) {
-    const long long w = (long long)blockIdx.x * 8 + threadIdx.y;
-    if (w >= n_words) return;
-    const uint32_t km = keep_mask[w];
-    if (km == 0u) return;
-    const int lane = threadIdx.x;
-    if (!((km >> lane) & 1u)) return;
-    const uint32_t lt = (1u << lane) - 1u;
-    const uint32_t ci = cand_off[w] + (uint32_t)__popc(words[w] & lt);
-    const uint32_t ri = keep_off[w] + (uint32_t)__popc(km & lt);
-    if (ci < cap && ri < cap) refined[ri] = refined_at[ci];
+                                                 Keypoint* __restrict__ refined, uint32_t cap,
+                                                 const Counters* __restrict__ ctr) {
+    const uint32_t n = min(ctr->n_candidates, cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (keep[i]) refined[keep_off[i]] = refined_at[i];
 }
 
 }  // namespace
@@ -287,36 +310,43 @@ int launch_extrema_mask(int storage, const void* arena, const PyramidDev& pyr, i
                         cudaStream_t st) {
     const OctaveDev& od = pyr.oct[o];
     if (od.W <= 0 || od.H <= 0) return 0;
-    dim3 grid(od.nw, (od.H + 7) / 8, pyr.S);
+    if (pyr.S + 2 > kExMaxLayers) return -1;
+    dim3 grid(od.nw, (od.H + kExTY - 1) / kExTY);
+    const size_t smem = sizeof(float) * (size_t)(pyr.S + 2) * (kExTY + 2) * (kExTX + 2);
     if (storage == SIFT_CUDA_STORAGE_F16)
-        k_extrema_mask<DogFromG16><<<grid, dim3(32, 8), 0, st>>>(arena, pyr, o, border, words);
+        k_extrema_mask<DogFromG16><<<grid, dim3(kExTX, kExTY), smem, st>>>(arena, pyr, o, border, words);
     else
-        k_extrema_mask<DogF32><<<grid, dim3(32, 8), 0, st>>>(arena, pyr, o, border, words);
+        k_extrema_mask<DogF32><<<grid, dim3(kExTX, kExTY), smem, st>>>(arena, pyr, o, border, words);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_emit_refine(int storage, const void* arena, const PyramidDev& pyr, long long n_words,
-                       const uint32_t* words, const uint32_t* cand_off, float sigma, float contrast, float edge,
-                       Keypoint* cands, Keypoint* refined_at, uint32_t* keep_mask, uint32_t* keep_count,
-                       uint32_t cap, Counters* ctr, cudaStream_t st) {
+int launch_emit(int storage, const void* arena, const PyramidDev& pyr, long long n_words, const uint32_t* words,
+                const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st) {
     if (n_words <= 0) return 0;
+    unsigned grid = (unsigned)((n_words + 255) / 256);
+    if (storage == SIFT_CUDA_STORAGE_F16)
+        k_emit<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, n_words, words, cand_off, cands, cap, ctr);
+    else
+        k_emit<DogF32><<<grid, 256, 0, st>>>(arena, pyr, n_words, words, cand_off, cands, cap, ctr);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_refine(int storage, const void* arena, const PyramidDev& pyr, float sigma, float contrast, float edge,
+                  const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap, const Counters* ctr,
+                  cudaStream_t st) {
     RefineParams rp{sigma, contrast, edge, pyr.S, pyr.S + 2};
-    unsigned grid = (unsigned)((n_words + 7) / 8);
+    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 4);
     if (storage == SIFT_CUDA_STORAGE_F16)
-        k_emit_refine<DogFromG16><<<grid, dim3(32, 8), 0, st>>>(arena, pyr, n_words, words, cand_off, rp, cands,
-                                                                refined_at, keep_mask, keep_count, cap, ctr);
+        k_refine<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, rp, cands, refined_at, keep, cap, ctr);
     else
-        k_emit_refine<DogF32><<<grid, dim3(32, 8), 0, st>>>(arena, pyr, n_words, words, cand_off, rp, cands,
-                                                            refined_at, keep_mask, keep_count, cap, ctr);
+        k_refine<DogF32><<<grid, 256, 0, st>>>(arena, pyr, rp, cands, refined_at, keep, cap, ctr);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_compact(long long n_words, const uint32_t* words, const uint32_t* cand_off, const uint32_t* keep_mask,
-                   const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined, uint32_t cap,
-                   cudaStream_t st) {
-    if (n_words <= 0) return 0;
-    unsigned grid = (unsigned)((n_words + 7) / 8);
-    k_compact<<<grid, dim3(32, 8), 0, st>>>(n_words, words, cand_off, keep_mask, keep_off, refined_at, refined, cap);
+int launch_compact(const uint32_t* keep, const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined,
+                   uint32_t cap, const Counters* ctr, cudaStream_t st) {
+    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 4);
+    k_compact<<<grid, 256, 0, st>>>(keep, keep_off, refined_at, refined, cap, ctr);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

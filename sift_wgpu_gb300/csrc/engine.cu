@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -41,19 +42,22 @@ int launch_blur_cols(const uint8_t* tmp, int tmp_pitch, const TG* prev, TG* out,
                      int H, int r, const float* wts, int round_mode, cudaStream_t st);
 template <typename TG>
 int launch_copy_level(const TG* prev, TG* out, float* dog, int pitch, int W, int H, cudaStream_t st);
+template <typename TIn, typename TG>
+int launch_blur_level(const TIn* in, long long in_pitch, uint8_t* tmp, TG* out, float* dog, int pitch, int W, int H,
+                      int r, const float* wts, int round_mode, cudaStream_t st, int* launches);
 template <typename TG>
 int launch_lanczos(const TG* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst, int dst_pitch,
                    int nW, int nH, const int* vtab, const float* vw, const int* htab, const float* hw,
                    cudaStream_t st);
 int launch_extrema_mask(int storage, const void* arena, const PyramidDev& pyr, int o, int border, uint32_t* words,
                         cudaStream_t st);
-int launch_emit_refine(int storage, const void* arena, const PyramidDev& pyr, long long n_words,
-                       const uint32_t* words, const uint32_t* cand_off, float sigma, float contrast, float edge,
-                       Keypoint* cands, Keypoint* refined_at, uint32_t* keep_mask, uint32_t* keep_count,
-                       uint32_t cap, Counters* ctr, cudaStream_t st);
-int launch_compact(long long n_words, const uint32_t* words, const uint32_t* cand_off, const uint32_t* keep_mask,
-                   const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined, uint32_t cap,
-                   cudaStream_t st);
+int launch_emit(int storage, const void* arena, const PyramidDev& pyr, long long n_words, const uint32_t* words,
+                const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st);
+int launch_refine(int storage, const void* arena, const PyramidDev& pyr, float sigma, float contrast, float edge,
+                  const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap, const Counters* ctr,
+                  cudaStream_t st);
+int launch_compact(const uint32_t* keep, const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined,
+                   uint32_t cap, const Counters* ctr, cudaStream_t st);
 template <typename TG>
 int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, const Counters* ctr,
                        float* ori_angle, uint32_t* ori_count, cudaStream_t st);
@@ -168,15 +172,64 @@ struct Engine {
     uint32_t cap_cand = 0, cap_ori = 0;
 
     DevMem d_img, d_G, d_D, d_tmp, d_ltmp, d_wts, d_ltab, d_lw;
-    DevMem d_words, d_cand_off, d_keep_mask, d_keep_count, d_keep_off, d_partials;
+    DevMem d_words, d_cand_off, d_keep, d_keep_off, d_partials;
     DevMem d_cands, d_refined_at, d_refined, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
     HostPinned h_ctr, h_kps, h_desc;
     size_t img_pitch = 0;
     uint32_t launches = 0;
     bool last_desc = true;
 
+    // Per-stage device time accounting (sift_cuda_profile_*): events recorded
+    // on the stream at the stage boundaries of every run while enabled.
+    static constexpr int kStages = 4;
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_free;
+    std::vector<std::vector<cudaEvent_t>> ev_runs;  // kStages + 1 events per run
+
     ~Engine() {
+        for (auto& r : ev_runs)
+            for (auto e : r) cudaEventDestroy(e);
+        for (auto e : ev_free) cudaEventDestroy(e);
         if (st) cudaStreamDestroy(st);
+    }
+
+    cudaEvent_t take_event() {
+        if (!ev_free.empty()) {
+            cudaEvent_t e = ev_free.back();
+            ev_free.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+    void mark(std::vector<cudaEvent_t>* run) {
+        if (!prof) return;
+        cudaEvent_t e = take_event();
+        if (e) {
+            cudaEventRecord(e, st);
+            run->push_back(e);
+        }
+    }
+    int profile_read(float* ms, uint32_t n, uint32_t* runs) {
+        CK(cudaStreamSynchronize(st), "synchronize");
+        std::vector<double> acc(kStages, 0.0);
+        uint32_t nr = 0;
+        for (auto& r : ev_runs) {
+            if ((int)r.size() == kStages + 1) {
+                for (int k = 0; k < kStages; ++k) {
+                    float t = 0.0f;
+                    cudaEventElapsedTime(&t, r[k], r[k + 1]);
+                    acc[k] += t;
+                }
+                ++nr;
+            }
+            for (auto e : r) ev_free.push_back(e);
+        }
+        ev_runs.clear();
+        for (uint32_t k = 0; k < n && k < (uint32_t)kStages; ++k) ms[k] = (float)acc[k];
+        if (runs) *runs = nr;
+        return 0;
     }
 
     bool f16() const { return opt.storage == SIFT_CUDA_STORAGE_F16; }
@@ -278,9 +331,6 @@ struct Engine {
         const size_t nwb = std::max<size_t>((size_t)n_words, 1) * sizeof(uint32_t);
         CK(d_words.ensure(nwb), "cudaMalloc(words)");
         CK(d_cand_off.ensure(nwb), "cudaMalloc(cand_off)");
-        CK(d_keep_mask.ensure(nwb), "cudaMalloc(keep_mask)");
-        CK(d_keep_count.ensure(nwb), "cudaMalloc(keep_count)");
-        CK(d_keep_off.ensure(nwb), "cudaMalloc(keep_off)");
         if (!wts.empty())
             CK(cudaMemcpyAsync(d_wts.p, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st), "H2D wts");
         if (!itab.empty())
@@ -316,6 +366,8 @@ struct Engine {
         CK(d_ori_angle.ensure((size_t)cap_cand * kOriMaxPeaks * sizeof(float)), "cudaMalloc(ori_angle)");
         CK(d_ori_count.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(ori_count)");
         CK(d_ori_off.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(ori_off)");
+        CK(d_keep.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(keep)");
+        CK(d_keep_off.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(keep_off)");
         CK(d_oriented.ensure((size_t)cap_ori * kp), "cudaMalloc(oriented)");
         CK(d_desc.ensure((size_t)cap_ori * kDescLen * sizeof(float)), "cudaMalloc(desc)");
         size_t np = scan_partials_size(std::max<size_t>({(size_t)n_words, (size_t)cap_cand, 1}));
@@ -335,17 +387,18 @@ struct Engine {
             ++launches;
             return rc;
         };
+        std::vector<cudaEvent_t> run_ev;
+        mark(&run_ev);
         CK(cudaMemsetAsync(d_ctr.p, 0, sizeof(Counters), st), "memset counters");
         const OctaveDev& o0 = pyr.oct[0];
         if (o0.W > 0 && o0.H > 0) {
             // base image (src/sift.rs:1204-1214)
             if (base.sigma > 0.0f) {
-                if (ok(launch_blur_rows<uint8_t>(img, stride, tmp, o0.pitch, o0.W, o0.H, base.radius, wts + base.woff,
-                                                 round_mode, st)))
-                    return cuda_fail(cudaGetLastError(), "blur rows (base)");
-                if (ok(launch_blur_cols<TG>(tmp, o0.pitch, nullptr, G + o0.g_off, nullptr, o0.pitch, o0.W, o0.H,
-                                            base.radius, wts + base.woff, round_mode, st)))
-                    return cuda_fail(cudaGetLastError(), "blur cols (base)");
+                int nl = 0;
+                if (launch_blur_level<uint8_t, TG>(img, stride, tmp, G + o0.g_off, nullptr, o0.pitch, o0.W, o0.H,
+                                                   base.radius, wts + base.woff, round_mode, st, &nl))
+                    return cuda_fail(cudaGetLastError(), "blur (base)");
+                launches += nl;
             } else {
                 if (ok(launch_u8_to_level<TG>(img, stride, G + o0.g_off, o0.pitch, o0.W, o0.H, st)))
                     return cuda_fail(cudaGetLastError(), "base copy");
@@ -364,12 +417,11 @@ struct Engine {
                         return cuda_fail(cudaGetLastError(), "copy level");
                     continue;
                 }
-                if (ok(launch_blur_rows<TG>(prev, od.pitch, tmp, od.pitch, od.W, od.H, b.radius, wts + b.woff,
-                                            round_mode, st)))
-                    return cuda_fail(cudaGetLastError(), "blur rows");
-                if (ok(launch_blur_cols<TG>(tmp, od.pitch, prev, out, dog, od.pitch, od.W, od.H, b.radius,
-                                            wts + b.woff, round_mode, st)))
-                    return cuda_fail(cudaGetLastError(), "blur cols");
+                int nl = 0;
+                if (launch_blur_level<TG, TG>(prev, od.pitch, tmp, out, dog, od.pitch, od.W, od.H, b.radius,
+                                              wts + b.woff, round_mode, st, &nl))
+                    return cuda_fail(cudaGetLastError(), "blur level");
+                launches += nl;
             }
             if (o + 1 < O) {
                 const OctaveDev& nx = pyr.oct[o + 1];
@@ -384,6 +436,7 @@ struct Engine {
                 ++launches;
             }
         }
+        mark(&run_ev);
         // (b) extrema -> (c) ordered candidates + refinement
         const void* arena = f16() ? (const void*)d_G.p : (const void*)d_D.p;
         Counters* ctr = d_ctr.as<Counters>();
@@ -399,19 +452,21 @@ struct Engine {
                            d_partials.as<uint32_t>(), st))
             return cuda_fail(cudaGetLastError(), "scan candidates");
         launches += 3;
-        if (ok(launch_emit_refine(opt.storage, arena, pyr, n_words, words, d_cand_off.as<uint32_t>(), p.sigma,
-                                  p.contrast_threshold, p.edge_threshold, d_cands.as<Keypoint>(),
-                                  d_refined_at.as<Keypoint>(), d_keep_mask.as<uint32_t>(),
-                                  d_keep_count.as<uint32_t>(), cap_cand, ctr, st)))
-            return cuda_fail(cudaGetLastError(), "emit/refine");
-        if (scan_exclusive(d_keep_count.as<uint32_t>(), SCAN_U32, d_keep_off.as<uint32_t>(), (size_t)n_words, nullptr,
-                           &ctr->n_refined, d_partials.as<uint32_t>(), st))
+        if (ok(launch_emit(opt.storage, arena, pyr, n_words, words, d_cand_off.as<uint32_t>(), d_cands.as<Keypoint>(),
+                           cap_cand, ctr, st)))
+            return cuda_fail(cudaGetLastError(), "emit");
+        if (ok(launch_refine(opt.storage, arena, pyr, p.sigma, p.contrast_threshold, p.edge_threshold,
+                             d_cands.as<Keypoint>(), d_refined_at.as<Keypoint>(), d_keep.as<uint32_t>(), cap_cand, ctr,
+                             st)))
+            return cuda_fail(cudaGetLastError(), "refine");
+        if (scan_exclusive(d_keep.as<uint32_t>(), SCAN_U32, d_keep_off.as<uint32_t>(), (size_t)cap_cand,
+                           &ctr->n_candidates, &ctr->n_refined, d_partials.as<uint32_t>(), st))
             return cuda_fail(cudaGetLastError(), "scan refined");
         launches += 3;
-        if (ok(launch_compact(n_words, words, d_cand_off.as<uint32_t>(), d_keep_mask.as<uint32_t>(),
-                              d_keep_off.as<uint32_t>(), d_refined_at.as<Keypoint>(), d_refined.as<Keypoint>(),
-                              cap_cand, st)))
+        if (ok(launch_compact(d_keep.as<uint32_t>(), d_keep_off.as<uint32_t>(), d_refined_at.as<Keypoint>(),
+                              d_refined.as<Keypoint>(), cap_cand, ctr, st)))
             return cuda_fail(cudaGetLastError(), "compact");
+        mark(&run_ev);
         // (d) orientation
         if (ok(launch_orientation<TG>(G, pyr, d_refined.as<Keypoint>(), ctr, d_ori_angle.as<float>(),
                                       d_ori_count.as<uint32_t>(), st)))
@@ -423,11 +478,14 @@ struct Engine {
         if (ok(launch_orient_emit(d_refined.as<Keypoint>(), ctr, d_ori_angle.as<float>(), d_ori_count.as<uint32_t>(),
                                   d_ori_off.as<uint32_t>(), d_oriented.as<Keypoint>(), cap_ori, ctr, st)))
             return cuda_fail(cudaGetLastError(), "orientation emit");
+        mark(&run_ev);
         // (e) descriptors
         if (with_desc) {
             if (ok(launch_descriptor<TG>(G, pyr, d_oriented.as<Keypoint>(), ctr, d_desc.as<float>(), cap_ori, st)))
                 return cuda_fail(cudaGetLastError(), "descriptor");
         }
+        mark(&run_ev);
+        if (prof) ev_runs.push_back(std::move(run_ev));
         last_desc = with_desc;
         return 0;
     }
@@ -671,6 +729,17 @@ void* sift_cuda_stream(SiftCudaEngine* engine) { return engine ? (void*)engine->
 
 uint32_t sift_cuda_last_launch_count(SiftCudaEngine* engine) { return engine ? engine->e.launches : 0; }
 
+int sift_cuda_profile_enable(SiftCudaEngine* engine, int enable) {
+    if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
+    engine->e.prof = enable != 0;
+    return 0;
+}
+
+int sift_cuda_profile_read(SiftCudaEngine* engine, float* stage_ms, uint32_t n_stages, uint32_t* runs) {
+    if (!engine || (!stage_ms && n_stages)) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "bad arguments");
+    return engine->e.profile_read(stage_ms, n_stages, runs);
+}
+
 int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t capacity, uint64_t* count) {
     if (!engine || !count) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine or count is NULL");
     Engine& e = engine->e;
@@ -706,7 +775,7 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
                     if (dog) {
                         ((float*)out)[pos] = ((const float*)buf.data())[q];
                     } else if (es == 4) {
-                        ((uint8_t*)out)[pos] = (uint8_t)((const float*)buf.data())[q];
+                        ((uint8_t*)out)[pos] = (uint8_t)std::lrint(((const float*)buf.data())[q] * 255.0f);
                     } else {
                         ((uint8_t*)out)[pos] = (uint8_t)__half2float(((const __half*)buf.data())[q]);
                     }

@@ -21,25 +21,37 @@
 namespace sift {
 namespace {
 
+// Level storage. An f32 level holds v/255 (the reference's
+// convert_u8_to_f32_gray value, src/sift.rs:92-101) for its u8 value v, so
+// DoG and the gradient stages read it directly; f16 holds v itself (v/255 is
+// not exact in f16). load_v returns v as a float for the blur and resize
+// passes: rint(255 * (v/255)) == v for every u8 v.
 template <typename T>
-__device__ __forceinline__ float load_px(const T* p) {
-    return (float)(*p);
+__device__ __forceinline__ float load_v(const T* p);
+template <>
+__device__ __forceinline__ float load_v<float>(const float* p) {
+    return rintf(__fmul_rn(*p, 255.0f));
 }
 template <>
-__device__ __forceinline__ float load_px<__half>(const __half* p) {
+__device__ __forceinline__ float load_v<__half>(const __half* p) {
     return __half2float(*p);
 }
 template <>
-__device__ __forceinline__ float load_px<uint8_t>(const uint8_t* p) {
+__device__ __forceinline__ float load_v<uint8_t>(const uint8_t* p) {
     return (float)(unsigned)(*p);
 }
 
+// v / 255 in f32 (IEEE division, as the reference computes it).
+__device__ __forceinline__ float norm255(int v) { return __fdiv_rn((float)v, 255.0f); }
+
 template <typename T>
-__device__ __forceinline__ void store_level(T* p, int v) {
-    *p = (T)(float)v;
+__device__ __forceinline__ void store_level(T* p, int v, float vn);
+template <>
+__device__ __forceinline__ void store_level<float>(float* p, int v, float vn) {
+    *p = vn;
 }
 template <>
-__device__ __forceinline__ void store_level<__half>(__half* p, int v) {
+__device__ __forceinline__ void store_level<__half>(__half* p, int v, float) {
     *p = __int2half_rn(v);
 }
 
@@ -63,7 +75,7 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const TIn* __restrict
     const int padded = W + 2 * r;
     for (int j = threadIdx.x; j < padded + 8; j += blockDim.x) {
         int xs = clampi(j - r, 0, W - 1);
-        row[j] = load_px(src + xs);
+        row[j] = load_v(src + xs);
     }
     __syncthreads();
     uint8_t* dst = out + (long long)y * out_pitch;
@@ -169,9 +181,129 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
         if (y < H) {
             const int v = clamp_u8(acc[j], round_mode);
             const long long o = (long long)y * pitch + x;
-            store_level(out + o, v);
+            store_level(out + o, v, lut[v]);
             if (dog) {
-                const int pv = (int)load_px(prev + o);
+                const int pv = (int)load_v(prev + o);
+                dog[o] = __fsub_rn(lut[v], lut[pv]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused level kernel: both separable passes of one level in one launch. The
+// CTA stages the (64 + 2r) x (64 + 2r) clamp-to-edge neighbourhood of its
+// 64 x 64 output tile as u8 values in f32, runs the horizontal pass for all
+// 64 + 2r rows into shared memory (u8-truncated like imageproc's intermediate
+// image), then the vertical pass, and writes the level and the DoG below it;
+// the previous level's value for the DoG comes from the staged tile, so each
+// scale is read from memory once.
+constexpr int kFTX = 64, kFTY = 64, kFThreads = 256;
+constexpr int kFColRows = 16;  // vertical-pass outputs per thread
+
+__host__ __device__ constexpr int fused_row_stride(int r) { return ((kFTX + 2 * r + 4) + 3) & ~3; }
+
+size_t blur_fused_smem(int r) {
+    const int taps = 2 * r + 1;
+    const size_t rows = (size_t)kFTY + 2 * r;
+    return sizeof(float) * ((size_t)((taps + 3) & ~3) + 256 + rows * fused_row_stride(r) + rows * kFTX);
+}
+
+template <typename TIn, typename TG>
+__global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict__ in, long long in_pitch,
+                                                          TG* __restrict__ out, float* __restrict__ dog, int pitch,
+                                                          int W, int H, int r, const float* __restrict__ wts,
+                                                          int round_mode) {
+    extern __shared__ __align__(16) float sm[];
+    const int taps = 2 * r + 1;
+    const int wpad = (taps + 3) & ~3;
+    const int RW = fused_row_stride(r);
+    const int RH = kFTY + 2 * r;
+    float* kw = sm;
+    float* lut = kw + wpad;
+    float* src = lut + 256;             // [RH][RW] staged input (u8 values)
+    float* hb = src + (size_t)RH * RW;  // [RH][kFTX] horizontal pass
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int x0 = blockIdx.x * kFTX, y0 = blockIdx.y * kFTY;
+    for (int i = tid; i < wpad; i += kFThreads) kw[i] = i < taps ? wts[i] : 0.0f;
+    for (int i = tid; i < 256; i += kFThreads) lut[i] = __fdiv_rn((float)i, 255.0f);
+    for (int yy = warp; yy < RH; yy += kFThreads / 32) {
+        const TIn* row = in + (long long)clampi(y0 - r + yy, 0, H - 1) * in_pitch;
+        float* d = src + (size_t)yy * RW;
+        for (int xx = lane; xx < RW; xx += 32) d[xx] = load_v(row + clampi(x0 - r + xx, 0, W - 1));
+    }
+    __syncthreads();
+    // horizontal pass: 16 threads per row, 4 outputs each (float4 sliding window)
+    {
+        const int xq = (tid & 15) * 4;
+        for (int yy = tid >> 4; yy < RH; yy += kFThreads / 16) {
+            const float* base = src + (size_t)yy * RW + xq;
+            float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+            float4 A = *reinterpret_cast<const float4*>(base);
+            int i = 0;
+            for (; i + 4 <= taps; i += 4) {
+                const float4 B = *reinterpret_cast<const float4*>(base + i + 4);
+                const float4 K = *reinterpret_cast<const float4*>(kw + i);
+                a0 = __fadd_rn(a0, __fmul_rn(A.x, K.x));
+                a1 = __fadd_rn(a1, __fmul_rn(A.y, K.x));
+                a2 = __fadd_rn(a2, __fmul_rn(A.z, K.x));
+                a3 = __fadd_rn(a3, __fmul_rn(A.w, K.x));
+                a0 = __fadd_rn(a0, __fmul_rn(A.y, K.y));
+                a1 = __fadd_rn(a1, __fmul_rn(A.z, K.y));
+                a2 = __fadd_rn(a2, __fmul_rn(A.w, K.y));
+                a3 = __fadd_rn(a3, __fmul_rn(B.x, K.y));
+                a0 = __fadd_rn(a0, __fmul_rn(A.z, K.z));
+                a1 = __fadd_rn(a1, __fmul_rn(A.w, K.z));
+                a2 = __fadd_rn(a2, __fmul_rn(B.x, K.z));
+                a3 = __fadd_rn(a3, __fmul_rn(B.y, K.z));
+                a0 = __fadd_rn(a0, __fmul_rn(A.w, K.w));
+                a1 = __fadd_rn(a1, __fmul_rn(B.x, K.w));
+                a2 = __fadd_rn(a2, __fmul_rn(B.y, K.w));
+                a3 = __fadd_rn(a3, __fmul_rn(B.z, K.w));
+                A = B;
+            }
+            for (; i < taps; ++i) {
+                const float k = kw[i];
+                a0 = __fadd_rn(a0, __fmul_rn(base[i + 0], k));
+                a1 = __fadd_rn(a1, __fmul_rn(base[i + 1], k));
+                a2 = __fadd_rn(a2, __fmul_rn(base[i + 2], k));
+                a3 = __fadd_rn(a3, __fmul_rn(base[i + 3], k));
+            }
+            float4 o4 = make_float4((float)clamp_u8(a0, round_mode), (float)clamp_u8(a1, round_mode),
+                                    (float)clamp_u8(a2, round_mode), (float)clamp_u8(a3, round_mode));
+            *reinterpret_cast<float4*>(hb + (size_t)yy * kFTX + xq) = o4;
+        }
+    }
+    __syncthreads();
+    // vertical pass: 64 columns x 4 groups of 16 rows, sliding window
+    const int col = tid & (kFTX - 1);
+    const int ly = (tid >> 6) * kFColRows;
+    float acc[kFColRows];
+    float win[kFColRows];
+#pragma unroll
+    for (int j = 0; j < kFColRows; ++j) {
+        acc[j] = 0.0f;
+        win[j] = j < kFColRows - 1 ? hb[(size_t)(ly + j) * kFTX + col] : 0.0f;
+    }
+    for (int i = 0; i < taps; ++i) {
+        win[kFColRows - 1] = hb[(size_t)(ly + i + kFColRows - 1) * kFTX + col];
+        const float k = kw[i];
+#pragma unroll
+        for (int j = 0; j < kFColRows; ++j) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], k));
+#pragma unroll
+        for (int j = 0; j < kFColRows - 1; ++j) win[j] = win[j + 1];
+    }
+    const int x = x0 + col;
+    if (x >= W) return;
+#pragma unroll
+    for (int j = 0; j < kFColRows; ++j) {
+        const int y = y0 + ly + j;
+        if (y < H) {
+            const int v = clamp_u8(acc[j], round_mode);
+            const long long o = (long long)y * pitch + x;
+            store_level(out + o, v, lut[v]);
+            if (dog) {
+                const int pv = (int)src[(size_t)(r + ly + j) * RW + r + col];
                 dog[o] = __fsub_rn(lut[v], lut[pv]);
             }
         }
@@ -198,7 +330,8 @@ __global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride,
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x >= W) return;
-    store_level(out + (long long)y * pitch + x, (int)img[(long long)y * stride + x]);
+    const int v = (int)img[(long long)y * stride + x];
+    store_level(out + (long long)y * pitch + x, v, norm255(v));
 }
 
 // Lanczos3 vertical pass (image 0.25.6 vertical_sample): tmp[oy][x] =
@@ -213,7 +346,7 @@ __global__ void k_lanczos_v(const TG* __restrict__ src, int src_pitch, float* __
     const int l = left[oy], c = count[oy], o = woff[oy];
     float t = 0.0f;
     for (int i = 0; i < c; ++i)
-        t = __fadd_rn(t, __fmul_rn(load_px(src + (long long)(l + i) * src_pitch + x), w[o + i]));
+        t = __fadd_rn(t, __fmul_rn(load_v(src + (long long)(l + i) * src_pitch + x), w[o + i]));
     dst[(long long)oy * dst_pitch + x] = t;
 }
 
@@ -231,7 +364,8 @@ __global__ void k_lanczos_h(const float* __restrict__ src, int src_pitch, TG* __
     float t = 0.0f;
     for (int i = 0; i < c; ++i) t = __fadd_rn(t, __fmul_rn(row[l + i], w[o + i]));
     t = t < 0.0f ? 0.0f : (t > 255.0f ? 255.0f : t);
-    store_level(dst + (long long)y * dst_pitch + ox, (int)roundf(t));
+    const int v = (int)roundf(t);
+    store_level(dst + (long long)y * dst_pitch + ox, v, norm255(v));
 }
 
 }  // namespace
@@ -275,6 +409,26 @@ int launch_blur_cols(const uint8_t* tmp, int tmp_pitch, const TG* prev, TG* out,
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
+// Fused level when its tile fits in shared memory, else the two passes.
+template <typename TIn, typename TG>
+int launch_blur_level(const TIn* in, long long in_pitch, uint8_t* tmp, TG* out, float* dog, int pitch, int W, int H,
+                      int r, const float* wts, int round_mode, cudaStream_t st, int* launches) {
+    const size_t smem = blur_fused_smem(r);
+    if (smem <= 160 * 1024) {
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(k_blur_level<TIn, TG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess)
+            return -1;
+        dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
+        k_blur_level<TIn, TG><<<grid, kFThreads, smem, st>>>(in, in_pitch, out, dog, pitch, W, H, r, wts, round_mode);
+        *launches += 1;
+        return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+    }
+    if (launch_blur_rows<TIn>(in, in_pitch, tmp, pitch, W, H, r, wts, round_mode, st)) return -1;
+    *launches += 2;
+    return launch_blur_cols<TG>(tmp, pitch, (const TG*)in, out, dog, pitch, W, H, r, wts, round_mode, st);
+}
+
 template <typename TG>
 int launch_copy_level(const TG* prev, TG* out, float* dog, int pitch, int W, int H, cudaStream_t st) {
     dim3 grid((W + 255) / 256, H);
@@ -312,6 +466,14 @@ template int launch_blur_cols<float>(const uint8_t*, int, const float*, float*, 
                                      const float*, int, cudaStream_t);
 template int launch_blur_cols<__half>(const uint8_t*, int, const __half*, __half*, float*, int, int, int, int,
                                       const float*, int, cudaStream_t);
+template int launch_blur_level<uint8_t, float>(const uint8_t*, long long, uint8_t*, float*, float*, int, int, int,
+                                              int, const float*, int, cudaStream_t, int*);
+template int launch_blur_level<uint8_t, __half>(const uint8_t*, long long, uint8_t*, __half*, float*, int, int, int,
+                                               int, const float*, int, cudaStream_t, int*);
+template int launch_blur_level<float, float>(const float*, long long, uint8_t*, float*, float*, int, int, int, int,
+                                            const float*, int, cudaStream_t, int*);
+template int launch_blur_level<__half, __half>(const __half*, long long, uint8_t*, __half*, float*, int, int, int,
+                                              int, const float*, int, cudaStream_t, int*);
 template int launch_copy_level<float>(const float*, float*, float*, int, int, int, cudaStream_t);
 template int launch_copy_level<__half>(const __half*, __half*, float*, int, int, int, cudaStream_t);
 template int launch_u8_to_level<float>(const uint8_t*, long long, float*, int, int, int, cudaStream_t);

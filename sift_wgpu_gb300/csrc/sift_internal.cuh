@@ -78,6 +78,19 @@ __device__ __forceinline__ float rem_euclid(float a, float b) {
     return r < 0.0f ? __fadd_rn(r, fabsf(b)) : r;
 }
 
+// f32::rem_euclid(a, b) for b > 0 and |a| < 2b, without the general fmodf:
+// there fmod(a, b) is a when |a| < b and a - copysign(b, a) otherwise, a
+// subtraction that is exact (Sterbenz), so the result is bit-identical.
+__device__ __forceinline__ float rem_euclid_2b(float a, float b) {
+    const float r = fabsf(a) < b ? a : __fsub_rn(a, copysignf(b, a));
+    return r < 0.0f ? __fadd_rn(r, b) : r;
+}
+
+// k / d and k % d for 0 <= k < 2^20, 0 < d < 2^10 without an integer divide:
+// (k + 0.5) / d is at least 0.5/d away from the next integer and the f32
+// product errs by far less.
+__device__ __forceinline__ int small_div(int k, float inv_d) { return (int)(((float)k + 0.5f) * inv_d); }
+
 // Scan helpers (scan.cu).
 enum ScanInput { SCAN_U32 = 0, SCAN_POPC = 1 };
 // Exclusive scan of n values (n_dev, when not null, overrides n at run time

@@ -187,6 +187,18 @@ class Engine:
     def last_launch_count(self) -> int:
         return int(_capi.lib().sift_cuda_last_launch_count(self.handle))
 
+    STAGE_NAMES = ("pyramid_dog", "extrema_refine", "orientation", "descriptor")
+
+    def profile(self, enable: bool) -> None:
+        _capi.check(_capi.lib().sift_cuda_profile_enable(self.handle, 1 if enable else 0))
+
+    def profile_read(self) -> tuple[dict, int]:
+        """Summed per-stage device milliseconds since the last read, and runs."""
+        ms = (C.c_float * 4)()
+        runs = C.c_uint32()
+        _capi.check(_capi.lib().sift_cuda_profile_read(self.handle, ms, 4, C.byref(runs)))
+        return {k: float(ms[i]) for i, k in enumerate(self.STAGE_NAMES)}, int(runs.value)
+
     def debug_stage(self, stage: int) -> np.ndarray:
         L = _capi.lib()
         n = C.c_uint64()
