@@ -9,9 +9,10 @@ quoted on. Prints one JSON line.
   value   images/s with the image already resident in HBM, device time of K
           steps from CUDA events on the engine's stream; the L2 is flushed
           (256 MiB write) before every step, outside the timed events.
-  e2e     images/s through the C ABI with a pinned host image: host->device
-          copy, the pipeline and the device->host copy of keypoints and
-          descriptors inside the timed region (wall clock).
+  e2e     images/s through the C ABI with a pinned host image
+          (sift_cuda_detect_and_compute_view): host->device copy, the pipeline
+          and the device->host copy of keypoints and descriptors into host
+          memory inside the timed region (wall clock).
   roofline  the dominant stage, timed live with CUDA events in the timed
           region; algorithmic bytes per run are stated in the design doc.
   cpu_baseline  the C++ restatement of the reference CPU path (oracle/) on the
@@ -253,8 +254,6 @@ def run_cuda(args, world, rank, local):
     launches_per_step = eng.last_launch_count
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    eng.profile(True)
-    eng.profile_read()
     sampler = ClockSampler(local)
     barrier(world)
     torch.cuda.synchronize()
@@ -270,12 +269,23 @@ def run_cuda(args, world, rank, local):
     t_wall = time.perf_counter() - t_wall0
     barrier(world)
     clocks = sampler.stop()
-    eng.profile(False)
-    stage_ms, runs = eng.profile_read()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     dev_s = sum(step_ms) / 1000.0
     dev_s_max = allreduce_max(world, dev_s)
     value = world * args.steps / dev_s_max
+
+    # Stage breakdown: a second timed region of the same K steps with per-stage
+    # CUDA events (in-order launches instead of the graph's two-stream DAG, so
+    # each stage has a start and an end).
+    eng.profile(True)
+    eng.profile_read()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            eng.run_device(d_img.data_ptr(), w, h, w)
+    torch.cuda.synchronize()
+    stage_ms, runs = eng.profile_read()
+    eng.profile(False)
 
     # the timed device runs produced what the host call returns
     kps_dev = eng.debug_stage(sg.STAGE_REFINED)
@@ -286,13 +296,13 @@ def run_cuda(args, world, rank, local):
     pinned = torch.from_numpy(img).pin_memory()
     host_img = pinned.numpy()
     for _ in range(max(1, args.warmup)):
-        eng.detect_and_compute(host_img)
+        eng.detect_and_compute_view(host_img)
     barrier(world)
     e2e_n = args.steps
     t0 = time.perf_counter()
     nk = 0
     for _ in range(e2e_n):
-        kk, dd = eng.detect_and_compute(host_img)
+        kk, dd = eng.detect_and_compute_view(host_img)
         nk = len(kk)
     e2e_s = time.perf_counter() - t0
     e2e_s = allreduce_max(world, e2e_s)

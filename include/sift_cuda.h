@@ -123,6 +123,14 @@ void sift_cuda_destroy(SiftCudaEngine* engine);
 int sift_cuda_detect_and_compute(SiftCudaEngine* engine, const uint8_t* img, uint32_t width,
                                  uint32_t height, uint32_t stride, SiftCudaResult* out);
 
+/* The same call with zero-copy results: out->kps and out->desc point into
+ * pinned host buffers owned by the engine, valid until the next call on the
+ * engine or sift_cuda_destroy; do not pass them to sift_cuda_result_free. The
+ * form an FFI wrapper uses when it copies into its own containers anyway (the
+ * Rust arm builds Vec<KeyPoint> / Vec<Vec<f32>>, src/sift.rs:1288-1291). */
+int sift_cuda_detect_and_compute_view(SiftCudaEngine* engine, const uint8_t* img, uint32_t width,
+                                      uint32_t height, uint32_t stride, SiftCudaResult* out);
+
 /* Sift::detect (src/sift.rs:846-886): keypoints with orientation, no
  * descriptors (out->desc == NULL). */
 int sift_cuda_detect(SiftCudaEngine* engine, const uint8_t* img, uint32_t width, uint32_t height,
@@ -162,12 +170,17 @@ void* sift_cuda_stream(SiftCudaEngine* engine);
  *                              (src/sift.rs:299-474), SiftCudaKeypoint each.
  *  SIFT_CUDA_STAGE_DOG:        all DoG levels as f32, octave-major, level,
  *                              row-major (F32 storage only).
+ *  SIFT_CUDA_STAGE_KEYPOINTS:  the final keypoints, SiftCudaKeypoint each.
+ *  SIFT_CUDA_STAGE_DESCRIPTORS: the final descriptors, 128 floats each
+ *                              (count = keypoints x 128).
  * Writes at most `capacity` elements and the total count to *count. */
 enum {
     SIFT_CUDA_STAGE_PYRAMID = 0,
     SIFT_CUDA_STAGE_CANDIDATES = 1,
     SIFT_CUDA_STAGE_REFINED = 2,
-    SIFT_CUDA_STAGE_DOG = 3
+    SIFT_CUDA_STAGE_DOG = 3,
+    SIFT_CUDA_STAGE_KEYPOINTS = 4,
+    SIFT_CUDA_STAGE_DESCRIPTORS = 5
 };
 int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t capacity,
                           uint64_t* count);

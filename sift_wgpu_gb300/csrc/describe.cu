@@ -56,6 +56,8 @@ struct GaussPlane {
         y = clampi(y, 0, H - 1);
         return gnorm(base + (long long)y * pitch + x, lut);
     }
+    // the same for coordinates already inside the level
+    __device__ __forceinline__ float px_in(int x, int y) const { return gnorm(base + y * pitch + x, lut); }
     // get_gauss_pixel_bilinear (src/sift.rs:238-266)
     __device__ __forceinline__ float bilinear(float x, float y) const {
         const float xf = floorf(x), yf = floorf(y);
@@ -118,14 +120,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                 const int side = 2 * r + 1;
                 const int total = side * side;
                 const float inv_side = 1.0f / (float)side;
+                // Branch-free: samples outside the level add +0.0, which leaves
+                // the bin bit-identical; their loads use clamped coordinates.
                 for (int k = lane; k < total; k += 32) {
                     const int q = small_div(k, inv_side);
                     const int dy = q - r, dx = k - q * side - r;
                     const int xi = rust_as_i32(roundf(__fadd_rn(xo, (float)dx)));
                     const int yi = rust_as_i32(roundf(__fadd_rn(yo, (float)dy)));
-                    if (xi < 1 || xi >= g.W - 1 || yi < 1 || yi >= g.H - 1) continue;
-                    const float gx = __fsub_rn(g.px(xi + 1, yi), g.px(xi - 1, yi));
-                    const float gy = __fsub_rn(g.px(xi, yi + 1), g.px(xi, yi - 1));
+                    const bool in = !(xi < 1 || xi >= g.W - 1 || yi < 1 || yi >= g.H - 1);
+                    const int xc = clampi(xi, 1, g.W - 2), yc = clampi(yi, 1, g.H - 2);
+                    const float gx = __fsub_rn(g.px_in(xc + 1, yc), g.px_in(xc - 1, yc));
+                    const float gy = __fsub_rn(g.px_in(xc, yc + 1), g.px_in(xc, yc - 1));
                     const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
                     const float ang = atan2f(gy, gx);
                     const float fdx = (float)dx, fdy = (float)dy;
@@ -134,7 +139,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                     const float bf = __fdiv_rn(__fmul_rn(an, (float)kOriBins), two_pi);
                     const float fl = floorf(bf);
                     const unsigned bin = (fl <= 0.0f ? 0u : (unsigned)fl) % kOriBins;
-                    hist[wid][bin][lane] = __fadd_rn(hist[wid][bin][lane], __fmul_rn(mag, wgt));
+                    const float v = in ? __fmul_rn(mag, wgt) : 0.0f;
+                    hist[wid][bin][lane] = __fadd_rn(hist[wid][bin][lane], v);
                 }
                 __syncwarp();
                 // Column sums, bins lane and lane+32.
@@ -227,13 +233,15 @@ constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad
 // Radii above the grid (not reachable with the default sigma) fall back to
 // per-sample bilinears from the level itself.
 template <typename TG>
-__global__ void __launch_bounds__(kDescThreads) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
+__global__ void __launch_bounds__(kDescThreads, 6) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
                                                               const Keypoint* __restrict__ oriented,
                                                               const Counters* __restrict__ ctr,
                                                               float* __restrict__ desc, uint32_t cap) {
     __shared__ float lut[256];
     __shared__ float grid[kDescGridSide * kDescGridSide];
+    __shared__ float patch[(kDescGridSide + 1) * (kDescGridSide + 1)];
     __shared__ unsigned int hist[kDescLen];
+    __shared__ float red_lo[kDescThreads / 32], red_hi[kDescThreads / 32];
     fill_lut(lut);
     __syncthreads();
     const int tid = threadIdx.x;
@@ -263,25 +271,71 @@ __global__ void __launch_bounds__(kDescThreads) k_descriptor(const TG* __restric
             const float wm1 = (float)(g.W - 1), hm1 = (float)(g.H - 1);
             const int side = 2 * rad + 1;
             const int total = side * side;
-            // fixed point: every bin is below sqrt(2) * total (|gx|,|gy| <= 1,
-            // Gaussian and trilinear weights <= 1 with unit sum)
-            const int fbits = min(24, (int)floorf(log2f(4.0e9f / (1.4143f * (float)total))));
-            const float to_fix = __int_as_float((127 + fbits) << 23);
-            inv_fix = __int_as_float((127 - fbits) << 23);
             const bool use_grid = rad <= kDescRadGrid;
             const int gs = side + 2;
+            float lo = 1.0f, hi = 0.0f;
             if (use_grid) {
-                for (int q = tid; q < gs * gs; q += kDescThreads) {
-                    const int jj = q / gs - (rad + 1), ii = q % gs - (rad + 1);
-                    grid[q] = g.bilinear(__fadd_rn(xo, (float)ii), __fadd_rn(yo, (float)jj));
+                // Stage the clamped patch of the level (get_gauss_pixel_value
+                // clamps), then bilinear samples at the window's integer
+                // offsets. All of them share the fraction of (xo, yo): the
+                // reference's sample positions xo + i differ from it only by
+                // the rounding of that sum.
+                const float xf = floorf(xo), yf = floorf(yo);
+                const float fdx = __fsub_rn(xo, xf), fdy = __fsub_rn(yo, yf);
+                const float omx = __fsub_rn(1.0f, fdx), omy = __fsub_rn(1.0f, fdy);
+                const int px0 = (int)xf - (rad + 1), py0 = (int)yf - (rad + 1);
+                const int ps = gs + 1;
+                for (int jj = tid >> 5; jj < ps; jj += kDescThreads / 32) {
+                    const int yy = clampi(py0 + jj, 0, g.H - 1);
+                    for (int ii = tid & 31; ii < ps; ii += 32) patch[jj * ps + ii] = g.px_in(clampi(px0 + ii, 0, g.W - 1), yy);
                 }
+                __syncthreads();
+                const float inv_gs = 1.0f / (float)gs;
+                for (int q = tid; q < gs * gs; q += kDescThreads) {
+                    const int qy = small_div(q, inv_gs);
+                    const int qx = q - qy * gs;
+                    const float* pp = patch + qy * ps + qx;
+                    const float q11 = pp[0], q21 = pp[1], q12 = pp[ps], q22 = pp[ps + 1];
+                    float b = __fmul_rn(__fmul_rn(q11, omx), omy);
+                    b = __fadd_rn(b, __fmul_rn(__fmul_rn(q21, fdx), omy));
+                    b = __fadd_rn(b, __fmul_rn(__fmul_rn(q12, omx), fdy));
+                    b = __fadd_rn(b, __fmul_rn(__fmul_rn(q22, fdx), fdy));
+                    grid[q] = b;
+                    lo = fminf(lo, b);
+                    hi = fmaxf(hi, b);
+                }
+            } else {
+                lo = 0.0f;
+                hi = 1.0f;
+            }
+            // Fixed point: |gx|, |gy| <= range of the sampled values, so every
+            // bin is below sqrt(2) * range * total (Gaussian and trilinear
+            // weights <= 1 with unit sum); the scale is the largest power of
+            // two that keeps that bound under 2^32.
+#pragma unroll
+            for (int m = 16; m > 0; m >>= 1) {
+                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, m));
+                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, m));
+            }
+            if ((tid & 31) == 0) {
+                red_lo[tid >> 5] = lo;
+                red_hi[tid >> 5] = hi;
             }
             __syncthreads();
+            lo = fminf(fminf(red_lo[0], red_lo[1]), fminf(red_lo[2], red_lo[3]));
+            hi = fmaxf(fmaxf(red_hi[0], red_hi[1]), fmaxf(red_hi[2], red_hi[3]));
+            const float range = fmaxf(hi - lo, 1.0f / 65536.0f);
+            const int fbits = max(0, min(40, (int)floorf(log2f(4.0e9f / (1.4143f * range * (float)total)))));
+            const float to_fix = __int_as_float((127 + fbits) << 23);
+            inv_fix = __int_as_float((127 - fbits) << 23);
             // Per-sample divisions become products with reciprocals here: the
             // bins are interpolated linearly, so an ulp in xb/yb/ab or in the
             // Gaussian weight moves the descriptor by ~1e-7.
             const float inv_bw = 1.0f / bw, inv_wd = 1.0f / wd, inv_side = 1.0f / (float)side;
             const float to_bins = 8.0f / two_pi;
+            // Branch-free sample loop: samples outside the rotated 4x4 window
+            // or the level carry weight 0 and their adds are predicated off,
+            // so the lanes of a warp never split.
             for (int k = tid; k < total; k += kDescThreads) {
                 const int q = small_div(k, inv_side);
                 const int dyi = q - rad, dxi = k - q * side - rad;
@@ -290,9 +344,9 @@ __global__ void __launch_bounds__(kDescThreads) k_descriptor(const TG* __restric
                 const float ry = __fadd_rn(__fmul_rn(-sa, px), __fmul_rn(ca, py));
                 const float xb = __fsub_rn(__fadd_rn(__fmul_rn(rx, inv_bw), 2.0f), 0.5f);
                 const float yb = __fsub_rn(__fadd_rn(__fmul_rn(ry, inv_bw), 2.0f), 0.5f);
-                if (!(xb > -1.0f && xb < 4.0f && yb > -1.0f && yb < 4.0f)) continue;
                 const float xs = __fadd_rn(xo, px), ys = __fadd_rn(yo, py);
-                if (xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1) continue;
+                const bool in = (xb > -1.0f && xb < 4.0f && yb > -1.0f && yb < 4.0f) &&
+                                !(xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1);
                 float gx, gy;
                 if (use_grid) {
                     const int c = (dyi + rad + 1) * gs + (dxi + rad + 1);
@@ -302,34 +356,34 @@ __global__ void __launch_bounds__(kDescThreads) k_descriptor(const TG* __restric
                     gx = __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
                     gy = __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
                 }
-                const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
-                const float pa = atan2f(gy, gx);
+                const float m2 = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
+                const float mag = m2 > 0.0f ? m2 * rsqrtf(m2) : 0.0f;
+                const float pa = atan2_poly(gy, gx);
                 const float ar = rem_euclid_2b(__fsub_rn(pa, ang), two_pi);  // |pa - ang| <= 2 pi
-                const float wgt = expf(__fmul_rn(-__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), inv_wd));
-                const float wm = __fmul_rn(mag, wgt);
+                const float wgt = __expf(__fmul_rn(-__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), inv_wd));
+                const float wm = in ? __fmul_rn(mag, wgt) : 0.0f;
                 const float ab = __fmul_rn(ar, to_bins);
-                const int xbi = (int)floorf(xb), ybi = (int)floorf(yb), abi = (int)floorf(ab);
-                const float fx = __fsub_rn(xb, (float)xbi), fy = __fsub_rn(yb, (float)ybi);
-                const float fa = __fsub_rn(ab, (float)abi);
+                const float xbf = floorf(xb), ybf = floorf(yb), abf = floorf(ab);
+                const int xbi = (int)xbf, ybi = (int)ybf, abi = (int)abf;
+                const float fx = __fsub_rn(xb, xbf), fy = __fsub_rn(yb, ybf), fa = __fsub_rn(ab, abf);
                 const int ia0 = abi & 7, ia1 = (abi + 1) & 7;
                 const float wa0 = __fmul_rn(__fsub_rn(1.0f, fa), to_fix), wa1 = __fmul_rn(fa, to_fix);
+                // cells (xbi + i, ybi + j), i, j in {0, 1}, inside 0..3
+                const float wx0 = xbi >= 0 && xbi <= 3 ? __fsub_rn(1.0f, fx) : 0.0f;
+                const float wx1 = xbi >= -1 && xbi <= 2 ? fx : 0.0f;
+                const float wy0 = ybi >= 0 && ybi <= 3 ? __fsub_rn(1.0f, fy) : 0.0f;
+                const float wy1 = ybi >= -1 && ybi <= 2 ? fy : 0.0f;
+                const int cx0 = clampi(xbi, 0, 3), cx1 = clampi(xbi + 1, 0, 3);
+                const int cy0 = clampi(ybi, 0, 3), cy1 = clampi(ybi + 1, 0, 3);
 #pragma unroll
-                for (int ii = 0; ii < 2; ++ii) {
-                    const int ix = xbi + ii;
-                    if (ix < 0 || ix >= 4) continue;
-                    const float wx = ii == 0 ? __fsub_rn(1.0f, fx) : fx;
-#pragma unroll
-                    for (int jj = 0; jj < 2; ++jj) {
-                        const int iy = ybi + jj;
-                        if (iy < 0 || iy >= 4) continue;
-                        const float wy = jj == 0 ? __fsub_rn(1.0f, fy) : fy;
-                        const float wxy = __fmul_rn(__fmul_rn(wm, wx), wy);
-                        const int cell = (iy * 4 + ix) * 8;
-                        const unsigned q0 = __float2uint_rn(__fmul_rn(wxy, wa0));
-                        const unsigned q1 = __float2uint_rn(__fmul_rn(wxy, wa1));
-                        if (q0) atomicAdd(&hist[cell + ia0], q0);
-                        if (q1) atomicAdd(&hist[cell + ia1], q1);
-                    }
+                for (int cc = 0; cc < 4; ++cc) {
+                    const float wx = (cc & 1) ? wx1 : wx0, wy = (cc & 2) ? wy1 : wy0;
+                    const int cell = (((cc & 2) ? cy1 : cy0) * 4 + ((cc & 1) ? cx1 : cx0)) * 8;
+                    const float wxy = __fmul_rn(__fmul_rn(wm, wx), wy);
+                    const unsigned q0 = __float2uint_rn(__fmul_rn(wxy, wa0));
+                    const unsigned q1 = __float2uint_rn(__fmul_rn(wxy, wa1));
+                    if (q0) atomicAdd(&hist[cell + ia0], q0);
+                    if (q1) atomicAdd(&hist[cell + ia1], q1);
                 }
             }
         }

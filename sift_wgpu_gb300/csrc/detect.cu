@@ -35,6 +35,19 @@ struct DogF32 {
         y = clampi(y, 0, H - 1);
         return base[(long long)l * plane + (long long)y * pitch + x];
     }
+    // Stages layers 0..L-1 of the clamped window [x0, x0+TW) x [y0, y0+TH)
+    // into tile[L][TH][TW]; warp w of nw loads rows w, w+nw, ...
+    __device__ __forceinline__ void stage(float* tile, int L, int x0, int y0, int TW, int TH, int warp, int nwarps,
+                                          int lane) const {
+        for (int l = 0; l < L; ++l) {
+            const float* pl = base + (long long)l * plane;
+            for (int yy = warp; yy < TH; yy += nwarps) {
+                const float* row = pl + (long long)clampi(y0 + yy, 0, H - 1) * pitch;
+                float* d = tile + (l * TH + yy) * TW;
+                for (int xx = lane; xx < TW; xx += 32) d[xx] = row[clampi(x0 + xx, 0, W - 1)];
+            }
+        }
+    }
 };
 
 // DoG recomputed in f32 from f16-stored Gaussian levels:
@@ -50,6 +63,21 @@ struct DogFromG16 {
         float a = __half2float(base[(long long)(l + 1) * plane + o]);
         float b = __half2float(base[(long long)l * plane + o]);
         return __fsub_rn(__fdiv_rn(a, 255.0f), __fdiv_rn(b, 255.0f));
+    }
+    __device__ __forceinline__ void stage(float* tile, int L, int x0, int y0, int TW, int TH, int warp, int nwarps,
+                                          int lane) const {
+        for (int yy = warp; yy < TH; yy += nwarps) {
+            const long long ro = (long long)clampi(y0 + yy, 0, H - 1) * pitch;
+            for (int xx = lane; xx < TW; xx += 32) {
+                const long long o = ro + clampi(x0 + xx, 0, W - 1);
+                float lower = __fdiv_rn(__half2float(base[o]), 255.0f);
+                for (int l = 0; l < L; ++l) {
+                    const float upper = __fdiv_rn(__half2float(base[(long long)(l + 1) * plane + o]), 255.0f);
+                    tile[(l * TH + yy) * TW + xx] = __fsub_rn(upper, lower);
+                    lower = upper;
+                }
+            }
+        }
     }
 };
 
@@ -76,48 +104,48 @@ __device__ __forceinline__ DogFromG16 make_dog<DogFromG16>(const void* arena, co
 constexpr int kExTX = 32, kExTY = 8, kExMaxLayers = 18;
 
 template <class Dog>
-__global__ void __launch_bounds__(kExTX* kExTY) k_extrema_mask(const void* arena, PyramidDev pyr, int o, int border,
-                                                              uint32_t* __restrict__ words) {
+__global__ void __launch_bounds__(kExTX* 8) k_extrema_mask(const void* arena, PyramidDev pyr, int o, int border,
+                                                          uint32_t* __restrict__ words) {
     extern __shared__ float tile[];  // [layers][kExTY + 2][kExTX + 2]
     const OctaveDev& od = pyr.oct[o];
     const Dog dog = make_dog<Dog>(arena, od);
     const int W = od.W, H = od.H, nw = od.nw, S = pyr.S, L = S + 2;
-    const int lane = threadIdx.x, ty = threadIdx.y;
+    const int lane = threadIdx.x, warp = threadIdx.y;
     const int c = blockIdx.x;
     const int x0 = c * kExTX, y0 = blockIdx.y * kExTY;
     constexpr int TW = kExTX + 2, TH = kExTY + 2;
-    for (int q = ty * kExTX + lane; q < L * TH * TW; q += kExTX * kExTY) {
-        const int l = q / (TH * TW), r = q % (TH * TW);
-        const int yy = r / TW, xx = r % TW;
-        tile[q] = dog.at(l, x0 - 1 + xx, y0 - 1 + yy);
-    }
+    dog.stage(tile, L, x0 - 1, y0 - 1, TW, TH, warp, 8, lane);
     __syncthreads();
-    const int x = x0 + lane, y = y0 + ty;
-    const bool inside = y >= border && y < H - border && x >= border && x < W - border;
-    // layer summaries, sliding over l
-    float Mp = 0.f, mp = 0.f, Mc = 0.f, mc = 0.f, m8c = 0.f, n8c = 0.f, vc = 0.f;
-    for (int l = 0; l < L; ++l) {
-        const float* t = tile + l * TH * TW + ty * TW + lane;  // top-left of the 3x3 block
-        const float a0 = t[0], a1 = t[1], a2 = t[2];
-        const float b0 = t[TW], b1 = t[TW + 1], b2 = t[TW + 2];
-        const float c0 = t[2 * TW], c1 = t[2 * TW + 1], c2 = t[2 * TW + 2];
-        const float mx8 = fmaxf(fmaxf(fmaxf(a0, a1), fmaxf(a2, b0)), fmaxf(fmaxf(b2, c0), fmaxf(c1, c2)));
-        const float mn8 = fminf(fminf(fminf(a0, a1), fminf(a2, b0)), fminf(fminf(b2, c0), fminf(c1, c2)));
-        const float M = fmaxf(mx8, b1), m = fminf(mn8, b1);
-        if (l >= 2) {
-            // layer l-1 is the centre layer s = l - 1 (1..S)
-            const int s = l - 1;
-            const bool ext = inside && ((vc > fmaxf(fmaxf(Mp, M), m8c)) || (vc < fminf(fminf(mp, m), n8c)));
-            const uint32_t w = __ballot_sync(0xffffffffu, ext);
-            if (lane == 0 && y < H) words[od.word_base + ((long long)(s - 1) * H + y) * nw + c] = w;
+    const int x = x0 + lane;
+    // each warp handles rows warp and warp + 8 of the tile
+    for (int ty = warp; ty < kExTY; ty += 8) {
+        const int y = y0 + ty;
+        const bool inside = y >= border && y < H - border && x >= border && x < W - border;
+        // layer summaries, sliding over l
+        float Mp = 0.f, mp = 0.f, Mc = 0.f, mc = 0.f, m8c = 0.f, n8c = 0.f, vc = 0.f;
+        for (int l = 0; l < L; ++l) {
+            const float* t = tile + (l * TH + ty) * TW + lane;  // top-left of the 3x3 block
+            const float a0 = t[0], a1 = t[1], a2 = t[2];
+            const float b0 = t[TW], b1 = t[TW + 1], b2 = t[TW + 2];
+            const float c0 = t[2 * TW], c1 = t[2 * TW + 1], c2 = t[2 * TW + 2];
+            const float mx8 = fmaxf(fmaxf(fmaxf(a0, a1), fmaxf(a2, b0)), fmaxf(fmaxf(b2, c0), fmaxf(c1, c2)));
+            const float mn8 = fminf(fminf(fminf(a0, a1), fminf(a2, b0)), fminf(fminf(b2, c0), fminf(c1, c2)));
+            const float M = fmaxf(mx8, b1), m = fminf(mn8, b1);
+            if (l >= 2) {
+                // layer l-1 is the centre layer s = l - 1 (1..S)
+                const int s = l - 1;
+                const bool ext = inside && ((vc > fmaxf(fmaxf(Mp, M), m8c)) || (vc < fminf(fminf(mp, m), n8c)));
+                const uint32_t wv = __ballot_sync(0xffffffffu, ext);
+                if (lane == 0 && y < H) words[od.word_base + ((long long)(s - 1) * H + y) * nw + c] = wv;
+            }
+            Mp = Mc;
+            mp = mc;
+            Mc = M;
+            mc = m;
+            m8c = mx8;
+            n8c = mn8;
+            vc = b1;
         }
-        Mp = Mc;
-        mp = mc;
-        Mc = M;
-        mc = m;
-        m8c = mx8;
-        n8c = mn8;
-        vc = b1;
     }
 }
 
@@ -314,9 +342,9 @@ int launch_extrema_mask(int storage, const void* arena, const PyramidDev& pyr, i
     dim3 grid(od.nw, (od.H + kExTY - 1) / kExTY);
     const size_t smem = sizeof(float) * (size_t)(pyr.S + 2) * (kExTY + 2) * (kExTX + 2);
     if (storage == SIFT_CUDA_STORAGE_F16)
-        k_extrema_mask<DogFromG16><<<grid, dim3(kExTX, kExTY), smem, st>>>(arena, pyr, o, border, words);
+        k_extrema_mask<DogFromG16><<<grid, dim3(kExTX, 8), smem, st>>>(arena, pyr, o, border, words);
     else
-        k_extrema_mask<DogF32><<<grid, dim3(kExTX, kExTY), smem, st>>>(arena, pyr, o, border, words);
+        k_extrema_mask<DogF32><<<grid, dim3(kExTX, 8), smem, st>>>(arena, pyr, o, border, words);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -171,13 +171,36 @@ struct Engine {
 
     uint32_t cap_cand = 0, cap_ori = 0;
 
-    DevMem d_img, d_G, d_D, d_tmp, d_ltmp, d_wts, d_ltab, d_lw;
+    DevMem d_img, d_G, d_D, d_tmp, d_tmp2, d_ltmp, d_wts, d_ltab, d_lw;
     DevMem d_words, d_cand_off, d_keep, d_keep_off, d_partials;
     DevMem d_cands, d_refined_at, d_refined, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
     HostPinned h_ctr, h_kps, h_desc;
     size_t img_pitch = 0;
     uint32_t launches = 0;
     bool last_desc = true;
+
+    // Second stream of the level DAG and its events (see enqueue_t), and the
+    // CUDA graph the whole run is replayed from.
+    cudaStream_t st2 = nullptr;
+    std::vector<cudaEvent_t> ev_level;  // per octave: level S written
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    struct GraphKey {
+        uint32_t W, H, cap_cand, cap_ori;
+        bool with_desc;
+        bool operator==(const GraphKey& o) const {
+            return W == o.W && H == o.H && cap_cand == o.cap_cand && cap_ori == o.cap_ori && with_desc == o.with_desc;
+        }
+    } gkey{};
+    uint32_t graph_launches = 0;
+
+    void drop_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        gexec = nullptr;
+        graph = nullptr;
+    }
 
     // Per-stage device time accounting (sift_cuda_profile_*): events recorded
     // on the stream at the stage boundaries of every run while enabled.
@@ -187,9 +210,14 @@ struct Engine {
     std::vector<std::vector<cudaEvent_t>> ev_runs;  // kStages + 1 events per run
 
     ~Engine() {
+        drop_graph();
         for (auto& r : ev_runs)
             for (auto e : r) cudaEventDestroy(e);
         for (auto e : ev_free) cudaEventDestroy(e);
+        for (auto e : ev_level) cudaEventDestroy(e);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (st2) cudaStreamDestroy(st2);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -243,6 +271,11 @@ struct Engine {
     int init() {
         if (int rc = set_device()) return rc;
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
+        ev_level.assign(kMaxOctaves, nullptr);
+        for (auto& e : ev_level) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
         CK(h_ctr.ensure(sizeof(Counters)), "cudaHostAlloc(counters)");
         CK(d_ctr.ensure(sizeof(Counters)), "cudaMalloc(counters)");
         return 0;
@@ -324,6 +357,8 @@ struct Engine {
         CK(d_G.ensure(goff * g_elem_size()), "cudaMalloc(G)");
         if (!f16()) CK(d_D.ensure(doff * sizeof(float)), "cudaMalloc(DoG)");
         CK(d_tmp.ensure(std::max<size_t>(tmpb, 16)), "cudaMalloc(tmp)");
+        CK(d_tmp2.ensure(std::max<size_t>(tmpb, 16)), "cudaMalloc(tmp2)");
+        drop_graph();
         CK(d_ltmp.ensure(std::max<size_t>(lt, 4) * sizeof(float)), "cudaMalloc(ltmp)");
         CK(d_wts.ensure(std::max<size_t>(wts.size(), 4) * sizeof(float)), "cudaMalloc(wts)");
         CK(d_ltab.ensure(std::max<size_t>(itab.size(), 4) * sizeof(int)), "cudaMalloc(ltab)");
@@ -359,6 +394,7 @@ struct Engine {
     }
 
     int ensure_lists() {
+        drop_graph();
         const size_t kp = sizeof(Keypoint);
         CK(d_cands.ensure((size_t)cap_cand * kp), "cudaMalloc(cands)");
         CK(d_refined_at.ensure((size_t)cap_cand * kp), "cudaMalloc(refined_at)");
@@ -375,13 +411,19 @@ struct Engine {
         return 0;
     }
 
+    // The run as a DAG on two streams (dag) or in order on one stream:
+    //   st : counters, base level, octave o levels 1..S, Lanczos(o) -> octave o+1
+    //   st2: after level S of octave o, levels S+1..S+2 and the extrema mask of
+    //        octave o (they feed nothing on the next octave's chain)
+    //   st : waits for st2, then the candidate list, refinement, orientation,
+    //        descriptors.
+    // Levels on st2 use their own horizontal-pass buffer (tmp2).
     template <typename TG>
-    int enqueue_t(const uint8_t* img, long long stride, bool with_desc) {
+    int enqueue_t(const uint8_t* img, long long stride, bool with_desc, bool dag) {
         const int O = pyr.num_octaves, S = pyr.S;
         TG* G = d_G.as<TG>();
         float* D = f16() ? nullptr : d_D.as<float>();
         const float* wts = d_wts.as<float>();
-        uint8_t* tmp = d_tmp.as<uint8_t>();
         launches = 0;
         auto ok = [&](int rc) {
             ++launches;
@@ -389,13 +431,35 @@ struct Engine {
         };
         std::vector<cudaEvent_t> run_ev;
         mark(&run_ev);
+        cudaStream_t s2 = dag ? st2 : st;
+        uint8_t* tmp_main = d_tmp.as<uint8_t>();
+        uint8_t* tmp_aux = dag ? d_tmp2.as<uint8_t>() : tmp_main;
         CK(cudaMemsetAsync(d_ctr.p, 0, sizeof(Counters), st), "memset counters");
+        const void* arena = f16() ? (const void*)d_G.p : (const void*)d_D.p;
         const OctaveDev& o0 = pyr.oct[0];
+        auto level = [&](int o, int s, cudaStream_t q, uint8_t* tmp) -> int {
+            const OctaveDev& od = pyr.oct[o];
+            const LevelBlur& b = lv[o][s - 1];
+            const TG* prev = G + od.g_off + (long long)(s - 1) * od.plane;
+            TG* out = G + od.g_off + (long long)s * od.plane;
+            float* dog = D ? D + od.d_off + (long long)(s - 1) * od.plane : nullptr;
+            if (b.sigma <= 0.0f) {
+                if (ok(launch_copy_level<TG>(prev, out, dog, od.pitch, od.W, od.H, q)))
+                    return cuda_fail(cudaGetLastError(), "copy level");
+                return 0;
+            }
+            int nl = 0;
+            if (launch_blur_level<TG, TG>(prev, od.pitch, tmp, out, dog, od.pitch, od.W, od.H, b.radius, wts + b.woff,
+                                          round_mode, q, &nl))
+                return cuda_fail(cudaGetLastError(), "blur level");
+            launches += nl;
+            return 0;
+        };
         if (o0.W > 0 && o0.H > 0) {
             // base image (src/sift.rs:1204-1214)
             if (base.sigma > 0.0f) {
                 int nl = 0;
-                if (launch_blur_level<uint8_t, TG>(img, stride, tmp, G + o0.g_off, nullptr, o0.pitch, o0.W, o0.H,
+                if (launch_blur_level<uint8_t, TG>(img, stride, tmp_main, G + o0.g_off, nullptr, o0.pitch, o0.W, o0.H,
                                                    base.radius, wts + base.woff, round_mode, st, &nl))
                     return cuda_fail(cudaGetLastError(), "blur (base)");
                 launches += nl;
@@ -404,24 +468,23 @@ struct Engine {
                     return cuda_fail(cudaGetLastError(), "base copy");
             }
         }
+        bool aux_used = false;
         for (int o = 0; o < O; ++o) {
             const OctaveDev& od = pyr.oct[o];
             if (od.W == 0 || od.H == 0) break;
-            for (int s = 1; s < S + 3; ++s) {
-                const LevelBlur& b = lv[o][s - 1];
-                const TG* prev = G + od.g_off + (long long)(s - 1) * od.plane;
-                TG* out = G + od.g_off + (long long)s * od.plane;
-                float* dog = D ? D + od.d_off + (long long)(s - 1) * od.plane : nullptr;
-                if (b.sigma <= 0.0f) {
-                    if (ok(launch_copy_level<TG>(prev, out, dog, od.pitch, od.W, od.H, st)))
-                        return cuda_fail(cudaGetLastError(), "copy level");
-                    continue;
-                }
-                int nl = 0;
-                if (launch_blur_level<TG, TG>(prev, od.pitch, tmp, out, dog, od.pitch, od.W, od.H, b.radius,
-                                              wts + b.woff, round_mode, st, &nl))
-                    return cuda_fail(cudaGetLastError(), "blur level");
-                launches += nl;
+            for (int s = 1; s <= S; ++s)
+                if (int rc = level(o, s, st, tmp_main)) return rc;
+            if (dag) {
+                CK(cudaEventRecord(ev_level[o], st), "event record");
+                CK(cudaStreamWaitEvent(st2, ev_level[o], 0), "stream wait");
+                aux_used = true;
+            }
+            for (int s = S + 1; s < S + 3; ++s)
+                if (int rc = level(o, s, s2, tmp_aux)) return rc;
+            if (!prof && od.nw > 0) {
+                if (ok(launch_extrema_mask(opt.storage, arena, pyr, o, (int)p.image_border_width,
+                                           d_words.as<uint32_t>(), s2)))
+                    return cuda_fail(cudaGetLastError(), "extrema mask");
             }
             if (o + 1 < O) {
                 const OctaveDev& nx = pyr.oct[o + 1];
@@ -436,17 +499,23 @@ struct Engine {
                 ++launches;
             }
         }
-        mark(&run_ev);
-        // (b) extrema -> (c) ordered candidates + refinement
-        const void* arena = f16() ? (const void*)d_G.p : (const void*)d_D.p;
-        Counters* ctr = d_ctr.as<Counters>();
-        for (int o = 0; o < O; ++o) {
-            const OctaveDev& od = pyr.oct[o];
-            if (od.W == 0 || od.H == 0 || od.nw == 0) continue;
-            if (ok(launch_extrema_mask(opt.storage, arena, pyr, o, (int)p.image_border_width, d_words.as<uint32_t>(),
-                                       st)))
-                return cuda_fail(cudaGetLastError(), "extrema mask");
+        if (aux_used) {
+            CK(cudaEventRecord(ev_join, st2), "event record");
+            CK(cudaStreamWaitEvent(st, ev_join, 0), "stream wait");
         }
+        mark(&run_ev);
+        if (prof) {
+            // profiled runs time the extrema masks as part of stage (b)
+            for (int o = 0; o < O; ++o) {
+                const OctaveDev& od = pyr.oct[o];
+                if (od.W == 0 || od.H == 0 || od.nw == 0) continue;
+                if (ok(launch_extrema_mask(opt.storage, arena, pyr, o, (int)p.image_border_width,
+                                           d_words.as<uint32_t>(), st)))
+                    return cuda_fail(cudaGetLastError(), "extrema mask");
+            }
+        }
+        // (b) extrema (above) -> (c) ordered candidates + refinement
+        Counters* ctr = d_ctr.as<Counters>();
         uint32_t* words = d_words.as<uint32_t>();
         if (scan_exclusive(words, SCAN_POPC, d_cand_off.as<uint32_t>(), (size_t)n_words, nullptr, &ctr->n_candidates,
                            d_partials.as<uint32_t>(), st))
@@ -490,8 +559,36 @@ struct Engine {
         return 0;
     }
 
-    int enqueue(const uint8_t* img, long long stride, bool with_desc) {
-        return f16() ? enqueue_t<__half>(img, stride, with_desc) : enqueue_t<float>(img, stride, with_desc);
+    int enqueue(const uint8_t* img, long long stride, bool with_desc, bool dag) {
+        return f16() ? enqueue_t<__half>(img, stride, with_desc, dag) : enqueue_t<float>(img, stride, with_desc, dag);
+    }
+
+    // One run on the image in d_img: replayed from the CUDA graph of this
+    // size (captured on first use), or launched in order with stage events
+    // when profiling.
+    int run(bool with_desc) {
+        const long long stride = (long long)img_pitch;
+        if (prof) return enqueue(d_img.as<uint8_t>(), stride, with_desc, false);
+        const GraphKey key{W, H, cap_cand, cap_ori, with_desc};
+        if (!gexec || !(key == gkey)) {
+            drop_graph();
+            CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+            int rc = enqueue(d_img.as<uint8_t>(), stride, with_desc, true);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "end capture");
+            graph = g;
+            CK(cudaGraphInstantiate(&gexec, graph, 0), "graph instantiate");
+            gkey = key;
+            graph_launches = launches;
+        }
+        launches = graph_launches;
+        CK(cudaGraphLaunch(gexec, st), "graph launch");
+        return 0;
     }
 
     // Reads the counters; grows the lists and reports 1 when a list overflowed.
@@ -514,26 +611,45 @@ struct Engine {
         return 0;
     }
 
-    int upload(const uint8_t* img, uint32_t w, uint32_t h, uint32_t stride) {
-        img_pitch = align_up(std::max<uint32_t>(w, 1), 128);
+    int upload(const uint8_t* img, uint32_t w, uint32_t h, uint32_t stride, cudaMemcpyKind kind) {
+        const size_t pitch = align_up(std::max<uint32_t>(w, 1), 128);
+        if (pitch != img_pitch || !d_img.p || d_img.bytes < pitch * std::max<uint32_t>(h, 1)) drop_graph();
+        img_pitch = pitch;
         CK(d_img.ensure(img_pitch * std::max<uint32_t>(h, 1)), "cudaMalloc(image)");
-        if (w && h)
-            CK(cudaMemcpy2DAsync(d_img.p, img_pitch, img, stride, w, h, cudaMemcpyHostToDevice, st), "H2D image");
+        if (w && h) CK(cudaMemcpy2DAsync(d_img.p, img_pitch, img, stride, w, h, kind, st), "copy image");
         return 0;
     }
 
     int detect_host(const uint8_t* img, uint32_t w, uint32_t h, uint32_t stride, bool with_desc,
-                    SiftCudaResult* out) {
+                    SiftCudaResult* out, bool view = false) {
         if (int rc = set_device()) return rc;
         if (int rc = ensure_geometry(w, h)) return rc;
-        if (int rc = upload(img, w, h, stride)) return rc;
+        if (int rc = upload(img, w, h, stride, cudaMemcpyHostToDevice)) return rc;
         for (int attempt = 0; attempt < 8; ++attempt) {
-            if (int rc = enqueue(d_img.as<uint8_t>(), (long long)img_pitch, with_desc)) return rc;
+            if (int rc = run(with_desc)) return rc;
             bool retry = false;
             if (int rc = check_counters(&retry)) return rc;
-            if (!retry) return fetch(with_desc, out);
+            if (!retry) return view ? fetch_view(with_desc, out) : fetch(with_desc, out);
         }
         return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint lists kept overflowing");
+    }
+
+    // Results copied into the engine's pinned buffers; out points at them.
+    int fetch_view(bool with_desc, SiftCudaResult* out) {
+        const uint32_t n = h_ctr.as<Counters>()->n_oriented;
+        CK(h_kps.ensure(sizeof(Keypoint) * std::max<uint32_t>(n, 1)), "cudaHostAlloc(kps)");
+        if (with_desc) CK(h_desc.ensure(sizeof(float) * kDescLen * std::max<uint32_t>(n, 1)), "cudaHostAlloc(desc)");
+        if (n) {
+            CK(cudaMemcpyAsync(h_kps.p, d_oriented.p, sizeof(Keypoint) * n, cudaMemcpyDeviceToHost, st), "D2H kps");
+            if (with_desc)
+                CK(cudaMemcpyAsync(h_desc.p, d_desc.p, sizeof(float) * kDescLen * n, cudaMemcpyDeviceToHost, st),
+                   "D2H desc");
+            CK(cudaStreamSynchronize(st), "D2H results");
+        }
+        out->n = n;
+        out->kps = h_kps.as<SiftCudaKeypoint>();
+        out->desc = with_desc ? h_desc.as<float>() : nullptr;
+        return 0;
     }
 
     int fetch(bool with_desc, SiftCudaResult* out) {
@@ -681,6 +797,14 @@ int sift_cuda_detect_and_compute(SiftCudaEngine* engine, const uint8_t* img, uin
     return engine->e.detect_host(img, width, height, stride, true, out);
 }
 
+int sift_cuda_detect_and_compute_view(SiftCudaEngine* engine, const uint8_t* img, uint32_t width, uint32_t height,
+                                      uint32_t stride, SiftCudaResult* out) {
+    sift::g_last_error.clear();
+    if (!out) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "out is NULL");
+    if (int rc = check_image(engine, img, width, height, stride, out)) return rc;
+    return engine->e.detect_host(img, width, height, stride, true, out, true);
+}
+
 int sift_cuda_detect(SiftCudaEngine* engine, const uint8_t* img, uint32_t width, uint32_t height, uint32_t stride,
                      SiftCudaResult* out) {
     sift::g_last_error.clear();
@@ -705,7 +829,8 @@ int sift_cuda_run_device(SiftCudaEngine* engine, const uint8_t* d_img, uint32_t 
     Engine& e = engine->e;
     if (int rc = e.set_device()) return rc;
     if (int rc = e.ensure_geometry(width, height)) return rc;
-    return e.enqueue(d_img, (long long)stride, with_descriptors != 0);
+    if (int rc = e.upload(d_img, width, height, stride, cudaMemcpyDeviceToDevice)) return rc;
+    return e.run(with_descriptors != 0);
 }
 
 int sift_cuda_device_outputs(SiftCudaEngine* engine, const uint32_t** d_count, const SiftCudaKeypoint** d_kps,
@@ -792,6 +917,18 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
     } else if (stage == SIFT_CUDA_STAGE_REFINED) {
         src = e.d_refined.as<sift::Keypoint>();
         n = std::min<uint64_t>(c.n_refined, e.cap_cand);
+    } else if (stage == SIFT_CUDA_STAGE_KEYPOINTS) {
+        src = e.d_oriented.as<sift::Keypoint>();
+        n = std::min<uint64_t>(c.n_oriented, e.cap_ori);
+    } else if (stage == SIFT_CUDA_STAGE_DESCRIPTORS) {
+        const uint64_t nd = std::min<uint64_t>(c.n_oriented, e.cap_ori) * sift::kDescLen;
+        *count = nd;
+        if (out && nd) {
+            if (cudaMemcpy(out, e.d_desc.p, std::min<uint64_t>(nd, capacity) * sizeof(float), cudaMemcpyDeviceToHost) !=
+                cudaSuccess)
+                return sift::cuda_fail(cudaGetLastError(), "D2H stage");
+        }
+        return 0;
     } else {
         return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "unknown stage");
     }

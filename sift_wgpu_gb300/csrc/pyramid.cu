@@ -55,7 +55,7 @@ __device__ __forceinline__ void store_level<__half>(__half* p, int v, float) {
     *p = __int2half_rn(v);
 }
 
-constexpr int kRowThreads = 256;
+constexpr int kRowThreads = 128;
 
 // One row per CTA. Shared layout: weights[taps] (padded to a multiple of 4),
 // then the row with r clamp-to-edge pixels on each side and 8 floats of slack.
@@ -209,12 +209,15 @@ size_t blur_fused_smem(int r) {
     return sizeof(float) * ((size_t)((taps + 3) & ~3) + 256 + rows * fused_row_stride(r) + rows * kFTX);
 }
 
-template <typename TIn, typename TG>
+// R > 0: the radius is a compile-time constant and every tap loop unrolls
+// (the vertical window then slides by register renaming); R == 0: run time.
+template <typename TIn, typename TG, int R>
 __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict__ in, long long in_pitch,
                                                           TG* __restrict__ out, float* __restrict__ dog, int pitch,
-                                                          int W, int H, int r, const float* __restrict__ wts,
+                                                          int W, int H, int r_rt, const float* __restrict__ wts,
                                                           int round_mode) {
     extern __shared__ __align__(16) float sm[];
+    const int r = R > 0 ? R : r_rt;
     const int taps = 2 * r + 1;
     const int wpad = (taps + 3) & ~3;
     const int RW = fused_row_stride(r);
@@ -241,6 +244,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict_
             float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
             float4 A = *reinterpret_cast<const float4*>(base);
             int i = 0;
+#pragma unroll
             for (; i + 4 <= taps; i += 4) {
                 const float4 B = *reinterpret_cast<const float4*>(base + i + 4);
                 const float4 K = *reinterpret_cast<const float4*>(kw + i);
@@ -262,6 +266,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict_
                 a3 = __fadd_rn(a3, __fmul_rn(B.z, K.w));
                 A = B;
             }
+#pragma unroll
             for (; i < taps; ++i) {
                 const float k = kw[i];
                 a0 = __fadd_rn(a0, __fmul_rn(base[i + 0], k));
@@ -285,6 +290,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict_
         acc[j] = 0.0f;
         win[j] = j < kFColRows - 1 ? hb[(size_t)(ly + j) * kFTX + col] : 0.0f;
     }
+#pragma unroll
     for (int i = 0; i < taps; ++i) {
         win[kFColRows - 1] = hb[(size_t)(ly + i + kFColRows - 1) * kFTX + col];
         const float k = kw[i];
@@ -413,14 +419,28 @@ int launch_blur_cols(const uint8_t* tmp, int tmp_pitch, const TG* prev, TG* out,
 template <typename TIn, typename TG>
 int launch_blur_level(const TIn* in, long long in_pitch, uint8_t* tmp, TG* out, float* dog, int pitch, int W, int H,
                       int r, const float* wts, int round_mode, cudaStream_t st, int* launches) {
+    // Fused only for small radii: its horizontal pass recomputes a 2r-row halo
+    // per 64-row tile. Large radii (the blur grows 2^o per octave) go to the
+    // two separable passes, which spread a small octave over many CTAs.
     const size_t smem = blur_fused_smem(r);
-    if (smem <= 160 * 1024) {
+    if (r <= 8 && smem <= 160 * 1024) {
+        void (*kern)(const TIn*, long long, TG*, float*, int, int, int, int, const float*, int);
+        switch (r) {
+            case 1: kern = k_blur_level<TIn, TG, 1>; break;
+            case 2: kern = k_blur_level<TIn, TG, 2>; break;
+            case 3: kern = k_blur_level<TIn, TG, 3>; break;
+            case 4: kern = k_blur_level<TIn, TG, 4>; break;
+            case 5: kern = k_blur_level<TIn, TG, 5>; break;
+            case 6: kern = k_blur_level<TIn, TG, 6>; break;
+            case 7: kern = k_blur_level<TIn, TG, 7>; break;
+            case 8: kern = k_blur_level<TIn, TG, 8>; break;
+            default: kern = k_blur_level<TIn, TG, 0>; break;
+        }
         if (smem > 48 * 1024 &&
-            cudaFuncSetAttribute(k_blur_level<TIn, TG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-                cudaSuccess)
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return -1;
         dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
-        k_blur_level<TIn, TG><<<grid, kFThreads, smem, st>>>(in, in_pitch, out, dog, pitch, W, H, r, wts, round_mode);
+        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, dog, pitch, W, H, r, wts, round_mode);
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }

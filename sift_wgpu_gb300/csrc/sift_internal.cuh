@@ -86,6 +86,32 @@ __device__ __forceinline__ float rem_euclid_2b(float a, float b) {
     return r < 0.0f ? __fadd_rn(r, b) : r;
 }
 
+// atan2 for the descriptor's gradient angles, written for this engine:
+// octant reduction to a = min(|x|,|y|) / max(|x|,|y|) in [0, 1], then
+// atan(a) = a * P(a^2) with a degree-7 polynomial fitted by iteratively
+// reweighted least squares on [0, 1] (relative error 1e-7 in f64, under 3 ulp
+// evaluated in f32), then the octant fix-ups. atan2(0, 0) = 0. Used where the
+// angle is interpolated linearly (descriptor bins); the orientation
+// histogram, whose bins are a hard floor, keeps atan2f.
+__device__ __forceinline__ float atan2_poly(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    const float a = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
+    const float t = a * a;
+    float p = -0.004693260882049799f;
+    p = fmaf(p, t, 0.024252355098724365f);
+    p = fmaf(p, t, -0.05948633328080177f);
+    p = fmaf(p, t, 0.0991428941488266f);
+    p = fmaf(p, t, -0.14019480347633362f);
+    p = fmaf(p, t, 0.19969724118709564f);
+    p = fmaf(p, t, -0.33331990242004395f);
+    p = fmaf(p, t, 0.9999998807907104f);
+    float r = p * a;
+    if (ay > ax) r = 1.5707963705062866f - r;
+    if (x < 0.0f) r = 3.1415927410125732f - r;
+    return copysignf(r, y);
+}
+
 // k / d and k % d for 0 <= k < 2^20, 0 < d < 2^10 without an integer divide:
 // (k + 0.5) / d is at least 0.5/d away from the next integer and the f32
 // product errs by far less.

@@ -166,6 +166,24 @@ class Engine:
     def detect(self, img) -> np.ndarray:
         return self._call(_capi.lib().sift_cuda_detect, img, False)[0]
 
+    def detect_and_compute_view(self, img) -> tuple[np.ndarray, np.ndarray]:
+        """Zero-copy form: numpy views of the engine's pinned result buffers,
+        valid until the next call on this engine."""
+        img = _as_gray(img)
+        h, w = img.shape
+        if img.strides[1] != 1:
+            img = np.ascontiguousarray(img)
+        res = _capi.Result()
+        _capi.check(_capi.lib().sift_cuda_detect_and_compute_view(
+            self.handle, img.ctypes.data if img.size else None, w, h, img.strides[0], C.byref(res)))
+        n = res.n
+        if n == 0:
+            return np.empty(0, KEYPOINT_DTYPE), np.empty((0, DESC_LEN), np.float32)
+        kbuf = (C.c_char * (n * KEYPOINT_DTYPE.itemsize)).from_address(C.cast(res.kps, C.c_void_p).value)
+        dbuf = (C.c_char * (n * DESC_LEN * 4)).from_address(C.cast(res.desc, C.c_void_p).value)
+        return (np.frombuffer(kbuf, dtype=KEYPOINT_DTYPE, count=n),
+                np.frombuffer(dbuf, dtype=np.float32, count=n * DESC_LEN).reshape(n, DESC_LEN))
+
     # device-resident form -------------------------------------------------
     def run_device(self, d_img: int, width: int, height: int, stride: int, with_descriptors: bool = True) -> None:
         _capi.check(_capi.lib().sift_cuda_run_device(self.handle, C.c_void_p(d_img), width, height, stride,
@@ -205,12 +223,14 @@ class Engine:
         _capi.check(L.sift_cuda_debug_stage(self.handle, stage, None, 0, C.byref(n)))
         if stage == _capi.STAGE_PYRAMID:
             out = np.empty(n.value, dtype=np.uint8)
-        elif stage == _capi.STAGE_DOG:
+        elif stage in (_capi.STAGE_DOG, _capi.STAGE_DESCRIPTORS):
             out = np.empty(n.value, dtype=np.float32)
         else:
             out = np.empty(n.value, dtype=KEYPOINT_DTYPE)
         _capi.check(L.sift_cuda_debug_stage(self.handle, stage, out.ctypes.data if n.value else None,
                                             n.value, C.byref(n)))
+        if stage == _capi.STAGE_DESCRIPTORS:
+            out = out.reshape(-1, DESC_LEN)
         return out
 
 

@@ -193,3 +193,33 @@ def test_large_6_octave_properties(sgb):
     assert np.all((k1["x"] >= -1) & (k1["x"] <= 4097) & (k1["y"] >= -1) & (k1["y"] <= 4097))
     k16, d16 = engine_for(sgb, args, "f16").detect_and_compute(img)
     assert k16.tobytes() == k1.tobytes() and d16.tobytes() == d1.tobytes()
+
+
+def test_all_call_forms_agree(sgb):
+    """The copying call, the zero-copy view, the device-resident run (CUDA
+    graph replay) and a profiled run (in-order launches with stage events)
+    give bit-identical keypoints and descriptors."""
+    import torch
+    img = image(sgb, 800, 600, 31)
+    eng = sgb.Engine(sgb.Sift.default())
+    k1, d1 = eng.detect_and_compute(img)
+    kv, dv = eng.detect_and_compute_view(img)
+    assert kv.tobytes() == k1.tobytes() and dv.tobytes() == d1.tobytes()
+    dimg = torch.from_numpy(img).cuda()
+    torch.cuda.synchronize()
+    eng.run_device(dimg.data_ptr(), 800, 600, 800)
+    eng.synchronize()
+    kd = eng.debug_stage(sgb.STAGE_KEYPOINTS)
+    dd = eng.debug_stage(sgb.STAGE_DESCRIPTORS)
+    assert kd.tobytes() == k1.tobytes() and dd.tobytes() == d1.tobytes()
+    eng.profile(True)
+    k2, d2 = eng.detect_and_compute(img)
+    times, runs = eng.profile_read()
+    eng.profile(False)
+    assert runs == 1 and all(t > 0 for t in times.values())
+    assert k2.tobytes() == k1.tobytes() and d2.tobytes() == d1.tobytes()
+    # a different size re-captures; going back reuses a valid graph
+    k3, _ = eng.detect_and_compute(image(sgb, 640, 480, 4))
+    k4, d4 = eng.detect_and_compute(img)
+    assert k4.tobytes() == k1.tobytes() and d4.tobytes() == d1.tobytes()
+    eng.close()
