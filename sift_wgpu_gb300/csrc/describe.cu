@@ -87,12 +87,53 @@ __device__ __forceinline__ void fill_lut(float* lut) {
         lut[i] = __fdiv_rn((float)i, 255.0f);
 }
 
+// The orientation window of one keypoint (src/sift.rs:640-662), lane-strided:
+// each lane adds into its own column of the bin-major histogram hist[bin][32].
+// Index and rounding arithmetic stays on the FMA pipe and is exact.
+template <typename TG, bool CHECK>
+__device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, float yo, int r, float wd, float* hist,
+                                           int lane) {
+    const float two_pi = 2.0f * kPi;
+    const int side = 2 * r + 1;
+    const int total = side * side;
+    const float inv_side = 1.0f / (float)side;
+    const float side_f = (float)side, r_f = (float)r;
+    float kf = (float)lane;
+    for (int k = lane; k < total; k += 32, kf += 32.0f) {
+        int q;
+        const float qf = floor_fi((kf + 0.5f) * inv_side, &q);
+        const float fdy = qf - r_f;
+        const float fdx = kf - qf * side_f - r_f;
+        int xi = round_away_i(__fadd_rn(xo, fdx));
+        int yi = round_away_i(__fadd_rn(yo, fdy));
+        bool in = true;
+        if (CHECK) {
+            in = !(xi < 1 || xi >= g.W - 1 || yi < 1 || yi >= g.H - 1);
+            xi = clampi(xi, 1, g.W - 2);
+            yi = clampi(yi, 1, g.H - 2);
+        }
+        const float gx = __fsub_rn(g.px_in(xi + 1, yi), g.px_in(xi - 1, yi));
+        const float gy = __fsub_rn(g.px_in(xi, yi + 1), g.px_in(xi, yi - 1));
+        const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
+        const float ang = atan2f(gy, gx);
+        const float wgt = expf(__fdiv_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), wd));
+        const float an = ang < 0.0f ? __fadd_rn(ang, two_pi) : ang;
+        const float bf = __fdiv_rn(__fmul_rn(an, (float)kOriBins), two_pi);  // in [0, 36]
+        const int fl = floor_i(bf);
+        const int bin = fl >= kOriBins ? fl - kOriBins : fl;
+        const float v = __fmul_rn(mag, wgt);
+        float* h = hist + bin * 32 + lane;
+        *h = __fadd_rn(*h, in ? v : 0.0f);
+    }
+}
+
 template <typename TG>
 __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
                                                                    const Keypoint* __restrict__ refined,
-                                                                   const Counters* __restrict__ ctr,
+                                                                   Counters* __restrict__ ctr_w,
                                                                    float* __restrict__ ori_angle,
                                                                    uint32_t* __restrict__ ori_count) {
+    const Counters* ctr = ctr_w;
     __shared__ float lut[256];
     __shared__ float hist[kWarpsPerCta][kOriBins][32];
     __shared__ float hs[kWarpsPerCta][kOriBins];
@@ -102,7 +143,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
     const uint32_t n = ctr->n_refined;
     const float two_pi = 2.0f * kPi;
     const float bin_w = 2.0f * kPi / (float)kOriBins;
-    for (uint32_t i = blockIdx.x * kWarpsPerCta + wid; i < n; i += gridDim.x * kWarpsPerCta) {
+    for (;;) {
+        uint32_t i = 0;
+        if (lane == 0) i = atomicAdd(&ctr_w->next_ori, 1u);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= n) break;
         const Keypoint kp = refined[i];
         const int o = kp.octave;
         uint32_t cnt = 0;
@@ -117,31 +162,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                 const float wd = __fmul_rn(__fmul_rn(2.0f, ws), ws);
 #pragma unroll
                 for (int b = 0; b < kOriBins; ++b) hist[wid][b][lane] = 0.0f;
-                const int side = 2 * r + 1;
-                const int total = side * side;
-                const float inv_side = 1.0f / (float)side;
-                // Branch-free: samples outside the level add +0.0, which leaves
-                // the bin bit-identical; their loads use clamped coordinates.
-                for (int k = lane; k < total; k += 32) {
-                    const int q = small_div(k, inv_side);
-                    const int dy = q - r, dx = k - q * side - r;
-                    const int xi = rust_as_i32(roundf(__fadd_rn(xo, (float)dx)));
-                    const int yi = rust_as_i32(roundf(__fadd_rn(yo, (float)dy)));
-                    const bool in = !(xi < 1 || xi >= g.W - 1 || yi < 1 || yi >= g.H - 1);
-                    const int xc = clampi(xi, 1, g.W - 2), yc = clampi(yi, 1, g.H - 2);
-                    const float gx = __fsub_rn(g.px_in(xc + 1, yc), g.px_in(xc - 1, yc));
-                    const float gy = __fsub_rn(g.px_in(xc, yc + 1), g.px_in(xc, yc - 1));
-                    const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
-                    const float ang = atan2f(gy, gx);
-                    const float fdx = (float)dx, fdy = (float)dy;
-                    const float wgt = expf(__fdiv_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), wd));
-                    const float an = ang < 0.0f ? __fadd_rn(ang, two_pi) : ang;
-                    const float bf = __fdiv_rn(__fmul_rn(an, (float)kOriBins), two_pi);
-                    const float fl = floorf(bf);
-                    const unsigned bin = (fl <= 0.0f ? 0u : (unsigned)fl) % kOriBins;
-                    const float v = in ? __fmul_rn(mag, wgt) : 0.0f;
-                    hist[wid][bin][lane] = __fadd_rn(hist[wid][bin][lane], v);
-                }
+                // Windows entirely inside the level (most keypoints) take the
+                // loop without bounds checks; the others add +0.0 for samples
+                // outside, which leaves a bin bit-identical.
+                const bool interior = xo - (float)r >= 2.5f && xo + (float)r <= (float)(g.W - 3) - 0.5f &&
+                                      yo - (float)r >= 2.5f && yo + (float)r <= (float)(g.H - 3) - 0.5f;
+                if (interior)
+                    ori_window<TG, false>(g, xo, yo, r, wd, &hist[wid][0][0], lane);
+                else
+                    ori_window<TG, true>(g, xo, yo, r, wd, &hist[wid][0][0], lane);
                 __syncwarp();
                 // Column sums, bins lane and lane+32.
                 for (int b = lane; b < kOriBins; b += 32) {
@@ -218,6 +247,9 @@ __global__ void k_orient_emit(const Keypoint* __restrict__ refined, const Counte
 }
 
 constexpr int kDescThreads = 128;
+constexpr int kHistRow = 9;      // 8 angle bins + 1 pad per cell
+constexpr int kHistCopies = 8;   // one copy per 4 lanes (lane >> 2)
+constexpr int kHistStride = 148; // >= 16 * kHistRow; 148 % 32 = 20 puts a bin's 8 copies in 8 banks
 constexpr int kDescRadGrid = 31;                      // largest radius served from the grid
 constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad+1
 
@@ -233,14 +265,18 @@ constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad
 // Radii above the grid (not reachable with the default sigma) fall back to
 // per-sample bilinears from the level itself.
 template <typename TG>
-__global__ void __launch_bounds__(kDescThreads, 6) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
+__global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
                                                               const Keypoint* __restrict__ oriented,
-                                                              const Counters* __restrict__ ctr,
+                                                              Counters* __restrict__ ctr_w,
                                                               float* __restrict__ desc, uint32_t cap) {
+    const Counters* ctr = ctr_w;
     __shared__ float lut[256];
     __shared__ float grid[kDescGridSide * kDescGridSide];
-    __shared__ float patch[(kDescGridSide + 1) * (kDescGridSide + 1)];
-    __shared__ unsigned int hist[kDescLen];
+    // Neighbouring samples land in the same bins, so the lanes of a warp add
+    // into kHistCopies copies of the histogram (lane >> 2 picks one): adds
+    // to one address serialise, adds to distinct copies do not. The copies
+    // are summed in a fixed order; integer sums make the order irrelevant.
+    __shared__ unsigned int hist[kHistCopies * kHistStride];
     __shared__ float red_lo[kDescThreads / 32], red_hi[kDescThreads / 32];
     fill_lut(lut);
     __syncthreads();
@@ -249,10 +285,16 @@ __global__ void __launch_bounds__(kDescThreads, 6) k_descriptor(const TG* __rest
     if (n > cap) n = cap;
     const float two_pi = 2.0f * kPi;
     const float sqrt2 = __fsqrt_rn(2.0f);
-    for (uint32_t i = blockIdx.x; i < n; i += gridDim.x) {
+    __shared__ uint32_t next;
+    for (;;) {
+        // keypoints differ ~4x in window area: take them from a queue
+        if (tid == 0) next = atomicAdd(&ctr_w->next_desc, 1u);
+        __syncthreads();
+        const uint32_t i = next;
+        if (i >= n) break;
         const Keypoint kp = oriented[i];
         const int o = kp.octave;
-        if (tid < kDescLen) hist[tid] = 0u;
+        for (int i = tid; i < kHistCopies * kHistStride; i += kDescThreads) hist[i] = 0u;
         const bool valid_oct = o >= 0 && o < pyr.num_octaves;
         const float scale = valid_oct ? __int_as_float((127 + o) << 23) : 1.0f;
         const float so = valid_oct ? __fdiv_rn(kp.size, scale) : 0.0f;
@@ -275,31 +317,37 @@ __global__ void __launch_bounds__(kDescThreads, 6) k_descriptor(const TG* __rest
             const int gs = side + 2;
             float lo = 1.0f, hi = 0.0f;
             if (use_grid) {
-                // Stage the clamped patch of the level (get_gauss_pixel_value
-                // clamps), then bilinear samples at the window's integer
-                // offsets. All of them share the fraction of (xo, yo): the
-                // reference's sample positions xo + i differ from it only by
-                // the rounding of that sum.
+                // Bilinear samples at the window's integer offsets, straight
+                // from the level (the patch stays in L1). All of them share the
+                // fraction of (xo, yo): the reference's sample positions xo + i
+                // differ from it only by the rounding of that sum. Clamped
+                // reads (get_gauss_pixel_value) only for windows at the border.
                 const float xf = floorf(xo), yf = floorf(yo);
-                const float fdx = __fsub_rn(xo, xf), fdy = __fsub_rn(yo, yf);
-                const float omx = __fsub_rn(1.0f, fdx), omy = __fsub_rn(1.0f, fdy);
+                const float fdx = xo - xf, fdy = yo - yf;
                 const int px0 = (int)xf - (rad + 1), py0 = (int)yf - (rad + 1);
-                const int ps = gs + 1;
-                for (int jj = tid >> 5; jj < ps; jj += kDescThreads / 32) {
-                    const int yy = clampi(py0 + jj, 0, g.H - 1);
-                    for (int ii = tid & 31; ii < ps; ii += 32) patch[jj * ps + ii] = g.px_in(clampi(px0 + ii, 0, g.W - 1), yy);
-                }
-                __syncthreads();
+                const bool inner = px0 >= 0 && py0 >= 0 && px0 + gs < g.W && py0 + gs < g.H;
                 const float inv_gs = 1.0f / (float)gs;
-                for (int q = tid; q < gs * gs; q += kDescThreads) {
-                    const int qy = small_div(q, inv_gs);
+                float qf = (float)tid;
+                for (int q = tid; q < gs * gs; q += kDescThreads, qf += (float)kDescThreads) {
+                    const int qy = floor_i((qf + 0.5f) * inv_gs);
                     const int qx = q - qy * gs;
-                    const float* pp = patch + qy * ps + qx;
-                    const float q11 = pp[0], q21 = pp[1], q12 = pp[ps], q22 = pp[ps + 1];
-                    float b = __fmul_rn(__fmul_rn(q11, omx), omy);
-                    b = __fadd_rn(b, __fmul_rn(__fmul_rn(q21, fdx), omy));
-                    b = __fadd_rn(b, __fmul_rn(__fmul_rn(q12, omx), fdy));
-                    b = __fadd_rn(b, __fmul_rn(__fmul_rn(q22, fdx), fdy));
+                    float q11, q21, q12, q22;
+                    if (inner) {
+                        const TG* pp = g.base + (py0 + qy) * g.pitch + (px0 + qx);
+                        q11 = gnorm(pp, lut);
+                        q21 = gnorm(pp + 1, lut);
+                        q12 = gnorm(pp + g.pitch, lut);
+                        q22 = gnorm(pp + g.pitch + 1, lut);
+                    } else {
+                        q11 = g.px(px0 + qx, py0 + qy);
+                        q21 = g.px(px0 + qx + 1, py0 + qy);
+                        q12 = g.px(px0 + qx, py0 + qy + 1);
+                        q22 = g.px(px0 + qx + 1, py0 + qy + 1);
+                    }
+                    // the reference's bilinear blend as two lerps (within the
+                    // descriptor tolerance)
+                    const float r0 = fmaf(fdx, q21 - q11, q11), r1 = fmaf(fdx, q22 - q12, q12);
+                    const float b = fmaf(fdy, r1 - r0, r0);
                     grid[q] = b;
                     lo = fminf(lo, b);
                     hi = fmaxf(hi, b);
@@ -325,65 +373,80 @@ __global__ void __launch_bounds__(kDescThreads, 6) k_descriptor(const TG* __rest
             lo = fminf(fminf(red_lo[0], red_lo[1]), fminf(red_lo[2], red_lo[3]));
             hi = fmaxf(fmaxf(red_hi[0], red_hi[1]), fmaxf(red_hi[2], red_hi[3]));
             const float range = fmaxf(hi - lo, 1.0f / 65536.0f);
-            const int fbits = max(0, min(40, (int)floorf(log2f(4.0e9f / (1.4143f * range * (float)total)))));
+            // and every single contribution (<= sqrt(2) * range) below 2^23,
+            // where the rounding add below converts it exactly
+            const float per = 1.4143f * range;
+            const int fbits = max(0, min(40, min(floor_i(log2f(4.0e9f / (per * (float)total))),
+                                                 floor_i(log2f(8.0e6f / per)))));
             const float to_fix = __int_as_float((127 + fbits) << 23);
             inv_fix = __int_as_float((127 - fbits) << 23);
-            // Per-sample divisions become products with reciprocals here: the
-            // bins are interpolated linearly, so an ulp in xb/yb/ab or in the
-            // Gaussian weight moves the descriptor by ~1e-7.
-            const float inv_bw = 1.0f / bw, inv_wd = 1.0f / wd, inv_side = 1.0f / (float)side;
+            // Descriptor samples are interpolated linearly into their bins, so
+            // this loop is written for speed within the descriptor tolerance:
+            // fused multiply-adds, reciprocal products instead of divisions,
+            // exp2 with the scale folded in, and the relative angle binned
+            // directly from (pa - angle) * 8 / (2 pi) (floor and & 7 give the
+            // rem_euclid bins). Each changes a descriptor value by ~1e-7.
+            const float inv_bw = 1.0f / bw, inv_side = 1.0f / (float)side;
             const float to_bins = 8.0f / two_pi;
-            // Branch-free sample loop: samples outside the rotated 4x4 window
-            // or the level carry weight 0 and their adds are predicated off,
-            // so the lanes of a warp never split.
-            for (int k = tid; k < total; k += kDescThreads) {
-                const int q = small_div(k, inv_side);
-                const int dyi = q - rad, dxi = k - q * side - rad;
-                const float px = (float)dxi, py = (float)dyi;
-                const float rx = __fadd_rn(__fmul_rn(ca, px), __fmul_rn(sa, py));
-                const float ry = __fadd_rn(__fmul_rn(-sa, px), __fmul_rn(ca, py));
-                const float xb = __fsub_rn(__fadd_rn(__fmul_rn(rx, inv_bw), 2.0f), 0.5f);
-                const float yb = __fsub_rn(__fadd_rn(__fmul_rn(ry, inv_bw), 2.0f), 0.5f);
-                const float xs = __fadd_rn(xo, px), ys = __fadd_rn(yo, py);
+            const float wexp = -1.4426950408889634f / wd;  // exp(-d2/wd) = exp2(d2 * wexp)
+            unsigned int* hcopy = hist + ((tid & 31) >> 2) * kHistStride;
+            // Branch-free: samples outside the rotated 4x4 window or the level
+            // carry weight 0 and their adds are predicated off, so the lanes of
+            // a warp never split.
+            // Loop indices without int<->float conversions: k is mirrored in an
+            // exact float counter; q = k / side by the floor add, px and py are
+            // exact small integers in f32, and the grid index of (px, py) is
+            // (py + rad + 1) * gs + px + rad + 1 = k + 2 q + gs + 1.
+            const float side_f = (float)side, rad_f = (float)rad;
+            float kf = (float)tid;
+            for (int k = tid; k < total; k += kDescThreads, kf += (float)kDescThreads) {
+                int q;
+                const float qf = floor_fi((kf + 0.5f) * inv_side, &q);
+                const float py = qf - rad_f;
+                const float px = kf - qf * side_f - rad_f;
+                const float rx = fmaf(ca, px, sa * py);
+                const float ry = fmaf(-sa, px, ca * py);
+                const float xb = fmaf(rx, inv_bw, 1.5f);
+                const float yb = fmaf(ry, inv_bw, 1.5f);
+                const float xs = xo + px, ys = yo + py;
                 const bool in = (xb > -1.0f && xb < 4.0f && yb > -1.0f && yb < 4.0f) &&
                                 !(xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1);
                 float gx, gy;
                 if (use_grid) {
-                    const int c = (dyi + rad + 1) * gs + (dxi + rad + 1);
-                    gx = __fsub_rn(grid[c + 1], grid[c - 1]);
-                    gy = __fsub_rn(grid[c + gs], grid[c - gs]);
+                    const int c = k + 2 * q + gs + 1;
+                    gx = grid[c + 1] - grid[c - 1];
+                    gy = grid[c + gs] - grid[c - gs];
                 } else {
                     gx = __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
                     gy = __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
                 }
-                const float m2 = __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy));
+                const float m2 = fmaf(gx, gx, gy * gy);
                 const float mag = m2 > 0.0f ? m2 * rsqrtf(m2) : 0.0f;
                 const float pa = atan2_poly(gy, gx);
-                const float ar = rem_euclid_2b(__fsub_rn(pa, ang), two_pi);  // |pa - ang| <= 2 pi
-                const float wgt = __expf(__fmul_rn(-__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)), inv_wd));
-                const float wm = in ? __fmul_rn(mag, wgt) : 0.0f;
-                const float ab = __fmul_rn(ar, to_bins);
-                const float xbf = floorf(xb), ybf = floorf(yb), abf = floorf(ab);
-                const int xbi = (int)xbf, ybi = (int)ybf, abi = (int)abf;
-                const float fx = __fsub_rn(xb, xbf), fy = __fsub_rn(yb, ybf), fa = __fsub_rn(ab, abf);
+                const float wgt = exp2f(fmaf(px, px, py * py) * wexp);
+                const float wm = in ? mag * wgt : 0.0f;
+                const float ab = (pa - ang) * to_bins;  // in [-8, 8]
+                int xbi, ybi, abi;
+                const float xbf = floor_fi(xb, &xbi), ybf = floor_fi(yb, &ybi), abf = floor_fi(ab, &abi);
+                const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
                 const int ia0 = abi & 7, ia1 = (abi + 1) & 7;
-                const float wa0 = __fmul_rn(__fsub_rn(1.0f, fa), to_fix), wa1 = __fmul_rn(fa, to_fix);
+                const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
                 // cells (xbi + i, ybi + j), i, j in {0, 1}, inside 0..3
-                const float wx0 = xbi >= 0 && xbi <= 3 ? __fsub_rn(1.0f, fx) : 0.0f;
-                const float wx1 = xbi >= -1 && xbi <= 2 ? fx : 0.0f;
-                const float wy0 = ybi >= 0 && ybi <= 3 ? __fsub_rn(1.0f, fy) : 0.0f;
-                const float wy1 = ybi >= -1 && ybi <= 2 ? fy : 0.0f;
+                const float wx0 = (unsigned)xbi <= 3u ? 1.0f - fx : 0.0f;
+                const float wx1 = (unsigned)(xbi + 1) <= 3u ? fx : 0.0f;
+                const float wy0 = (unsigned)ybi <= 3u ? wm * (1.0f - fy) : 0.0f;
+                const float wy1 = (unsigned)(ybi + 1) <= 3u ? wm * fy : 0.0f;
                 const int cx0 = clampi(xbi, 0, 3), cx1 = clampi(xbi + 1, 0, 3);
-                const int cy0 = clampi(ybi, 0, 3), cy1 = clampi(ybi + 1, 0, 3);
+                const int cy0 = clampi(ybi, 0, 3) * 4, cy1 = clampi(ybi + 1, 0, 3) * 4;
 #pragma unroll
                 for (int cc = 0; cc < 4; ++cc) {
-                    const float wx = (cc & 1) ? wx1 : wx0, wy = (cc & 2) ? wy1 : wy0;
-                    const int cell = (((cc & 2) ? cy1 : cy0) * 4 + ((cc & 1) ? cx1 : cx0)) * 8;
-                    const float wxy = __fmul_rn(__fmul_rn(wm, wx), wy);
-                    const unsigned q0 = __float2uint_rn(__fmul_rn(wxy, wa0));
-                    const unsigned q1 = __float2uint_rn(__fmul_rn(wxy, wa1));
-                    if (q0) atomicAdd(&hist[cell + ia0], q0);
-                    if (q1) atomicAdd(&hist[cell + ia1], q1);
+                    const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
+                    const int cell = (((cc & 2) ? cy1 : cy0) + ((cc & 1) ? cx1 : cx0)) * kHistRow;
+                    // round to the nearest integer (< 2^23 by the scale choice)
+                    const unsigned q0 = __float_as_uint(__fadd_rn(wxy * wa0, kMagic)) - 0x4B000000u;
+                    const unsigned q1 = __float_as_uint(__fadd_rn(wxy * wa1, kMagic)) - 0x4B000000u;
+                    if (q0) atomicAdd(&hcopy[cell + ia0], q0);
+                    if (q1) atomicAdd(&hcopy[cell + ia1], q1);
                 }
             }
         }
@@ -392,7 +455,14 @@ __global__ void __launch_bounds__(kDescThreads, 6) k_descriptor(const TG* __rest
         if (tid < 32) {
             float d[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) d[q] = __fmul_rn((float)hist[tid + 32 * q], inv_fix);
+            for (int q = 0; q < 4; ++q) {
+                const int bin = tid + 32 * q;
+                const int at = (bin >> 3) * kHistRow + (bin & 7);
+                unsigned v = 0u;
+#pragma unroll
+                for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at];
+                d[q] = __fmul_rn((float)v, inv_fix);
+            }
             float ss = 0.0f;
 #pragma unroll
             for (int q = 0; q < 4; ++q) ss = __fadd_rn(ss, __fmul_rn(d[q], d[q]));
@@ -430,7 +500,8 @@ int describe_grid() { return 152 * 4; }
 template <typename TG>
 int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, const Counters* ctr,
                        float* ori_angle, uint32_t* ori_count, cudaStream_t st) {
-    k_orientation<TG><<<describe_grid(), dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined, ctr, ori_angle,
+    k_orientation<TG><<<describe_grid(), dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined,
+                                                                         const_cast<Counters*>(ctr), ori_angle,
                                                                          ori_count);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -445,7 +516,7 @@ int launch_orient_emit(const Keypoint* refined, const Counters* ctr, const float
 template <typename TG>
 int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, const Counters* ctr,
                       float* desc, uint32_t cap, cudaStream_t st) {
-    k_descriptor<TG><<<152 * 12, kDescThreads, 0, st>>>(arena, pyr, oriented, ctr, desc, cap);
+    k_descriptor<TG><<<152 * 8, kDescThreads, 0, st>>>(arena, pyr, oriented, const_cast<Counters*>(ctr), desc, cap);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

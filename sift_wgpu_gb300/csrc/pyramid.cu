@@ -30,7 +30,7 @@ template <typename T>
 __device__ __forceinline__ float load_v(const T* p);
 template <>
 __device__ __forceinline__ float load_v<float>(const float* p) {
-    return rintf(__fmul_rn(*p, 255.0f));
+    return rint_pos(__fmul_rn(*p, 255.0f));
 }
 template <>
 __device__ __forceinline__ float load_v<__half>(const __half* p) {
@@ -38,7 +38,7 @@ __device__ __forceinline__ float load_v<__half>(const __half* p) {
 }
 template <>
 __device__ __forceinline__ float load_v<uint8_t>(const uint8_t* p) {
-    return (float)(unsigned)(*p);
+    return float_of_u8(*p);
 }
 
 // v / 255 in f32 (IEEE division, as the reference computes it).
@@ -116,10 +116,14 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const TIn* __restrict
             a2 = __fadd_rn(a2, __fmul_rn(base[i + 2], k));
             a3 = __fadd_rn(a3, __fmul_rn(base[i + 3], k));
         }
-        dst[x0] = (uint8_t)clamp_u8(a0, round_mode);
-        if (x0 + 1 < W) dst[x0 + 1] = (uint8_t)clamp_u8(a1, round_mode);
-        if (x0 + 2 < W) dst[x0 + 2] = (uint8_t)clamp_u8(a2, round_mode);
-        if (x0 + 3 < W) dst[x0 + 3] = (uint8_t)clamp_u8(a3, round_mode);
+        const int v0 = round_mode ? clamp_u8(a0, 1) : int_of(clamp_u8f(a0));
+        const int v1 = round_mode ? clamp_u8(a1, 1) : int_of(clamp_u8f(a1));
+        const int v2 = round_mode ? clamp_u8(a2, 1) : int_of(clamp_u8f(a2));
+        const int v3 = round_mode ? clamp_u8(a3, 1) : int_of(clamp_u8f(a3));
+        dst[x0] = (uint8_t)v0;
+        if (x0 + 1 < W) dst[x0 + 1] = (uint8_t)v1;
+        if (x0 + 2 < W) dst[x0 + 2] = (uint8_t)v2;
+        if (x0 + 3 < W) dst[x0 + 3] = (uint8_t)v3;
     }
 }
 
@@ -153,7 +157,7 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
     const int xg = min(x0 + (int)threadIdx.x, W - 1);
     for (int k = threadIdx.y; k < rows; k += kColTY) {
         int ys = clampi(y0 - r + k, 0, H - 1);
-        tile[k * kColTX + threadIdx.x] = (float)(unsigned)tmp[(long long)ys * tmp_pitch + xg];
+        tile[k * kColTX + threadIdx.x] = float_of_u8(tmp[(long long)ys * tmp_pitch + xg]);
     }
     __syncthreads();
     const int x = x0 + threadIdx.x;
@@ -179,11 +183,11 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
     for (int j = 0; j < kColRPT; ++j) {
         const int y = y0 + ly + j;
         if (y < H) {
-            const int v = clamp_u8(acc[j], round_mode);
+            const int v = round_mode ? clamp_u8(acc[j], 1) : int_of(clamp_u8f(acc[j]));
             const long long o = (long long)y * pitch + x;
             store_level(out + o, v, lut[v]);
             if (dog) {
-                const int pv = (int)load_v(prev + o);
+                const int pv = int_of(load_v(prev + o));
                 dog[o] = __fsub_rn(lut[v], lut[pv]);
             }
         }
@@ -274,8 +278,9 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict_
                 a2 = __fadd_rn(a2, __fmul_rn(base[i + 2], k));
                 a3 = __fadd_rn(a3, __fmul_rn(base[i + 3], k));
             }
-            float4 o4 = make_float4((float)clamp_u8(a0, round_mode), (float)clamp_u8(a1, round_mode),
-                                    (float)clamp_u8(a2, round_mode), (float)clamp_u8(a3, round_mode));
+            float4 o4 = round_mode ? make_float4((float)clamp_u8(a0, 1), (float)clamp_u8(a1, 1),
+                                                 (float)clamp_u8(a2, 1), (float)clamp_u8(a3, 1))
+                                   : make_float4(clamp_u8f(a0), clamp_u8f(a1), clamp_u8f(a2), clamp_u8f(a3));
             *reinterpret_cast<float4*>(hb + (size_t)yy * kFTX + xq) = o4;
         }
     }
@@ -305,11 +310,11 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict_
     for (int j = 0; j < kFColRows; ++j) {
         const int y = y0 + ly + j;
         if (y < H) {
-            const int v = clamp_u8(acc[j], round_mode);
+            const int v = round_mode ? clamp_u8(acc[j], 1) : int_of(clamp_u8f(acc[j]));
             const long long o = (long long)y * pitch + x;
             store_level(out + o, v, lut[v]);
             if (dog) {
-                const int pv = (int)src[(size_t)(r + ly + j) * RW + r + col];
+                const int pv = int_of(src[(size_t)(r + ly + j) * RW + r + col]);
                 dog[o] = __fsub_rn(lut[v], lut[pv]);
             }
         }

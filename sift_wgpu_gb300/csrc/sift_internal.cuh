@@ -30,7 +30,10 @@ struct Counters {
     uint32_t n_candidates;
     uint32_t n_refined;
     uint32_t n_oriented;
-    uint32_t overflow;  // bit 0 candidates, 1 refined, 2 oriented
+    uint32_t overflow;   // bit 0 candidates, 1 refined, 2 oriented
+    uint32_t next_ori;   // work queues of the persistent gather kernels
+    uint32_t next_desc;
+    uint32_t pad[2];
 };
 
 // Geometry of one octave in the device arena.
@@ -49,6 +52,37 @@ struct PyramidDev {
     int levels;               // S + 3
     OctaveDev oct[kMaxOctaves];
 };
+
+// Exact integer rounding on the FMA pipe. Conversions (F2I/I2F/FRND) run on
+// the quarter-rate XU pipe; for |x| < 2^22 adding a power of two of the right
+// size in a directed rounding mode leaves the rounded value in the low
+// mantissa bits, exactly.
+//   floor:  RD(x + 1.5*2^23) - 1.5*2^23   (1.5*2^23 keeps negatives in the binade)
+//   trunc:  RZ(x + 2^23) - 2^23           (x >= 0)
+//   rint:   RN(x + 2^23) - 2^23           (x >= 0, ties to even)
+constexpr float kMagic = 8388608.0f;         // 2^23
+constexpr float kMagic15 = 12582912.0f;      // 1.5 * 2^23
+__device__ __forceinline__ float floor_fi(float x, int* xi) {
+    const float t = __fadd_rd(x, kMagic15);
+    *xi = __float_as_int(t) - 0x4B400000;
+    return __fsub_rn(t, kMagic15);
+}
+__device__ __forceinline__ int floor_i(float x) { return __float_as_int(__fadd_rd(x, kMagic15)) - 0x4B400000; }
+__device__ __forceinline__ float trunc_pos(float x) { return __fsub_rn(__fadd_rz(x, kMagic), kMagic); }
+__device__ __forceinline__ float rint_pos(float x) { return __fsub_rn(__fadd_rn(x, kMagic), kMagic); }
+// integer value of a float holding an integer in [0, 2^23)
+__device__ __forceinline__ int int_of(float v) { return __float_as_int(__fadd_rn(v, kMagic)) - 0x4B000000; }
+// u8 -> float without a conversion
+__device__ __forceinline__ float float_of_u8(unsigned b) { return __fsub_rn(__uint_as_float(0x4B000000u | b), kMagic); }
+// round half away from zero (f32::round) to int, |x| < 2^22
+__device__ __forceinline__ int round_away_i(float x) {
+    const int m = floor_i(__fadd_rn(fabsf(x), 0.5f));
+    return x < 0.0f ? -m : m;
+}
+
+// imageproc's Clamp<f32> for u8 on the truncation path, as a float:
+// min(max(trunc(a), 0), 255) (trunc of a negative a is <= 0).
+__device__ __forceinline__ float clamp_u8f(float a) { return fminf(fmaxf(trunc_pos(a), 0.0f), 255.0f); }
 
 // f32 -> u8 the way imageproc's Clamp<f32> for u8 does it: truncation of
 // values strictly inside (0, 255), saturation outside. round_mode 1 rounds
