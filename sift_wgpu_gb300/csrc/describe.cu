@@ -130,22 +130,21 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
 template <typename TG>
 __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
                                                                    const Keypoint* __restrict__ refined,
-                                                                   Counters* __restrict__ ctr_w,
+                                                                   OctCounters* __restrict__ oc,
                                                                    float* __restrict__ ori_angle,
                                                                    uint32_t* __restrict__ ori_count) {
-    const Counters* ctr = ctr_w;
     __shared__ float lut[256];
     __shared__ float hist[kWarpsPerCta][kOriBins][32];
     __shared__ float hs[kWarpsPerCta][kOriBins];
     fill_lut(lut);
     __syncthreads();
     const int lane = threadIdx.x, wid = threadIdx.y;
-    const uint32_t n = ctr->n_refined;
+    const uint32_t n = oc->n_ref;
     const float two_pi = 2.0f * kPi;
     const float bin_w = 2.0f * kPi / (float)kOriBins;
     for (;;) {
         uint32_t i = 0;
-        if (lane == 0) i = atomicAdd(&ctr_w->next_ori, 1u);
+        if (lane == 0) i = atomicAdd(&oc->next_ori, 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= n) break;
         const Keypoint kp = refined[i];
@@ -227,19 +226,27 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
     }
 }
 
-__global__ void k_orient_emit(const Keypoint* __restrict__ refined, const Counters* __restrict__ ctr,
+// Octave o's oriented keypoints go after those of octaves 0..o-1 (whose
+// counts are final: their orientation scans precede this kernel).
+__global__ void k_orient_emit(const Keypoint* __restrict__ refined, int o, Counters* __restrict__ ctr,
                               const float* __restrict__ ori_angle, const uint32_t* __restrict__ ori_count,
-                              const uint32_t* __restrict__ ori_off, Keypoint* __restrict__ oriented, uint32_t cap,
-                              Counters* __restrict__ ctr_w) {
-    const uint32_t n = ctr->n_refined;
+                              const uint32_t* __restrict__ ori_off, Keypoint* __restrict__ oriented, uint32_t cap) {
+    OctCounters* oc = &ctr->oct[o];
+    uint32_t base = 0;
+    for (int q = 0; q < o; ++q) base += ctr->oct[q].n_ori;
+    const uint32_t n = oc->n_ref;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        oc->out_base = base;
+        atomicAdd(&ctr->n_candidates, oc->n_cand);
+        atomicAdd(&ctr->n_refined, n);
+        atomicMax(&ctr->n_oriented, base + oc->n_ori);
+        if (base + oc->n_ori > cap) atomicOr(&ctr->overflow, 4u);
+    }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t c = ori_count[i], off = ori_off[i];
+        const uint32_t c = ori_count[i], off = base + ori_off[i];
         Keypoint k = refined[i];
         for (uint32_t j = 0; j < c; ++j) {
-            if (off + j >= cap) {
-                atomicOr(&ctr_w->overflow, 4u);
-                break;
-            }
+            if (off + j >= cap) break;
             k.angle = ori_angle[(size_t)i * kOriMaxPeaks + j];
             oriented[off + j] = k;
         }
@@ -267,9 +274,8 @@ constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad
 template <typename TG>
 __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
                                                               const Keypoint* __restrict__ oriented,
-                                                              Counters* __restrict__ ctr_w,
+                                                              OctCounters* __restrict__ oc,
                                                               float* __restrict__ desc, uint32_t cap) {
-    const Counters* ctr = ctr_w;
     __shared__ float lut[256];
     __shared__ float grid[kDescGridSide * kDescGridSide];
     // Neighbouring samples land in the same bins, so the lanes of a warp add
@@ -281,17 +287,19 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     fill_lut(lut);
     __syncthreads();
     const int tid = threadIdx.x;
-    uint32_t n = ctr->n_oriented;
-    if (n > cap) n = cap;
+    const uint32_t base = oc->out_base;
+    uint32_t n = oc->n_ori;
+    if (base >= cap) n = 0;
+    else if (n > cap - base) n = cap - base;
     const float two_pi = 2.0f * kPi;
     const float sqrt2 = __fsqrt_rn(2.0f);
     __shared__ uint32_t next;
     for (;;) {
         // keypoints differ ~4x in window area: take them from a queue
-        if (tid == 0) next = atomicAdd(&ctr_w->next_desc, 1u);
+        if (tid == 0) next = atomicAdd(&oc->next_desc, 1u);
         __syncthreads();
-        const uint32_t i = next;
-        if (i >= n) break;
+        if (next >= n) break;
+        const uint32_t i = base + next;
         const Keypoint kp = oriented[i];
         const int o = kp.octave;
         for (int i = tid; i < kHistCopies * kHistStride; i += kDescThreads) hist[i] = 0u;
@@ -498,35 +506,33 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
 int describe_grid() { return 152 * 4; }
 
 template <typename TG>
-int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, const Counters* ctr,
-                       float* ori_angle, uint32_t* ori_count, cudaStream_t st) {
-    k_orientation<TG><<<describe_grid(), dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined,
-                                                                         const_cast<Counters*>(ctr), ori_angle,
-                                                                         ori_count);
+int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, OctCounters* oc,
+                       float* ori_angle, uint32_t* ori_count, int grid, cudaStream_t st) {
+    k_orientation<TG><<<grid, dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined, oc, ori_angle, ori_count);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_orient_emit(const Keypoint* refined, const Counters* ctr, const float* ori_angle,
+int launch_orient_emit(const Keypoint* refined, int o, Counters* ctr, const float* ori_angle,
                        const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
-                       Counters* ctr_w, cudaStream_t st) {
-    k_orient_emit<<<152 * 2, 256, 0, st>>>(refined, ctr, ori_angle, ori_count, ori_off, oriented, cap, ctr_w);
+                       cudaStream_t st) {
+    k_orient_emit<<<152, 256, 0, st>>>(refined, o, ctr, ori_angle, ori_count, ori_off, oriented, cap);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 template <typename TG>
-int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, const Counters* ctr,
-                      float* desc, uint32_t cap, cudaStream_t st) {
-    k_descriptor<TG><<<152 * 8, kDescThreads, 0, st>>>(arena, pyr, oriented, const_cast<Counters*>(ctr), desc, cap);
+int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
+                      uint32_t cap, int grid, cudaStream_t st) {
+    k_descriptor<TG><<<grid, kDescThreads, 0, st>>>(arena, pyr, oriented, oc, desc, cap);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-template int launch_orientation<float>(const float*, const PyramidDev&, const Keypoint*, const Counters*, float*,
-                                       uint32_t*, cudaStream_t);
-template int launch_orientation<__half>(const __half*, const PyramidDev&, const Keypoint*, const Counters*, float*,
-                                        uint32_t*, cudaStream_t);
-template int launch_descriptor<float>(const float*, const PyramidDev&, const Keypoint*, const Counters*, float*,
-                                      uint32_t, cudaStream_t);
-template int launch_descriptor<__half>(const __half*, const PyramidDev&, const Keypoint*, const Counters*, float*,
-                                       uint32_t, cudaStream_t);
+template int launch_orientation<float>(const float*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
+                                       uint32_t*, int, cudaStream_t);
+template int launch_orientation<__half>(const __half*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
+                                        uint32_t*, int, cudaStream_t);
+template int launch_descriptor<float>(const float*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
+                                      uint32_t, int, cudaStream_t);
+template int launch_descriptor<__half>(const __half*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
+                                       uint32_t, int, cudaStream_t);
 
 }  // namespace sift

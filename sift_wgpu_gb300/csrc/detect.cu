@@ -36,15 +36,27 @@ struct DogF32 {
         return base[(long long)l * plane + (long long)y * pitch + x];
     }
     // Stages layers 0..L-1 of the clamped window [x0, x0+TW) x [y0, y0+TH)
-    // into tile[L][TH][TW]; warp w of nw loads rows w, w+nw, ...
+    // into tile[L][TH][TW]; warp w of nw loads rows w, w+nw, ... Windows inside
+    // the plane (x0 % 4 == 0, TW % 4 == 0) go as aligned float4 loads.
     __device__ __forceinline__ void stage(float* tile, int L, int x0, int y0, int TW, int TH, int warp, int nwarps,
                                           int lane) const {
+        const bool inner = x0 >= 0 && y0 >= 0 && x0 + TW <= W && y0 + TH <= H && (x0 & 3) == 0 && (TW & 3) == 0 &&
+                           (pitch & 3) == 0;
         for (int l = 0; l < L; ++l) {
             const float* pl = base + (long long)l * plane;
-            for (int yy = warp; yy < TH; yy += nwarps) {
-                const float* row = pl + (long long)clampi(y0 + yy, 0, H - 1) * pitch;
-                float* d = tile + (l * TH + yy) * TW;
-                for (int xx = lane; xx < TW; xx += 32) d[xx] = row[clampi(x0 + xx, 0, W - 1)];
+            if (inner) {
+                const int q4 = TW >> 2;
+                for (int q = warp * 32 + lane; q < TH * q4; q += nwarps * 32) {
+                    const int yy = q / q4, xx = (q - yy * q4) * 4;
+                    const float4 v = *reinterpret_cast<const float4*>(pl + (long long)(y0 + yy) * pitch + x0 + xx);
+                    *reinterpret_cast<float4*>(tile + (l * TH + yy) * TW + xx) = v;
+                }
+            } else {
+                for (int yy = warp; yy < TH; yy += nwarps) {
+                    const float* row = pl + (long long)clampi(y0 + yy, 0, H - 1) * pitch;
+                    float* d = tile + (l * TH + yy) * TW;
+                    for (int xx = lane; xx < TW; xx += 32) d[xx] = row[clampi(x0 + xx, 0, W - 1)];
+                }
             }
         }
     }
@@ -94,57 +106,79 @@ __device__ __forceinline__ DogFromG16 make_dog<DogFromG16>(const void* arena, co
 
 // ---------------------------------------------------------------------------
 // Extrema of one octave, all layers s = 1..S at once. The CTA stages the
-// (32+2) x (8+2) neighbourhood of its 32 x 8 pixels for every DoG layer
-// 0..S+1 in shared memory (clamped coordinates, as get_pixel_value clamps);
-// each thread reduces every layer's 3x3 block to (max, min) and its 8-ring to
-// (max8, min8) once, then
-//   strict max  <=>  v > max(M_{s-1}, M_{s+1}, max8_s)
-//   strict min  <=>  v < min(m_{s-1}, m_{s+1}, min8_s)
+// neighbourhood of its 64 x 16 pixels for every DoG layer 0..S+1 in shared
+// memory (aligned float4 loads for interior tiles; clamped coordinates, as
+// get_pixel_value clamps, at the image border). Each thread owns one column
+// and 4 rows: per layer it forms the horizontal 3-max/3-min of 6 rows once and
+// reuses them for the 3x3 block max/min and the 8-ring max/min of its 4 pixels:
+//   strict max  <=>  v > max(M_{s-1}, M_{s+1}, ring8max_s)
+//   strict min  <=>  v < min(m_{s-1}, m_{s+1}, ring8min_s)
 // which is the reference's 26 strict comparisons (ties reject).
-constexpr int kExTX = 32, kExTY = 8, kExMaxLayers = 18;
+constexpr int kExTX = 64, kExTY = 16, kExRows = 4, kExMaxLayers = 18;
+constexpr int kExSW = kExTX + 8;  // staged width: x0-4 .. x0+68 (float4 aligned)
+constexpr int kExSH = kExTY + 2;
 
 template <class Dog>
-__global__ void __launch_bounds__(kExTX* 8) k_extrema_mask(const void* arena, PyramidDev pyr, int o, int border,
-                                                          uint32_t* __restrict__ words) {
-    extern __shared__ float tile[];  // [layers][kExTY + 2][kExTX + 2]
+__global__ void __launch_bounds__(256) k_extrema_mask(const void* arena, PyramidDev pyr, int o, int border,
+                                                      uint32_t* __restrict__ words) {
+    extern __shared__ float tile[];  // [layers][kExSH][kExSW]
     const OctaveDev& od = pyr.oct[o];
     const Dog dog = make_dog<Dog>(arena, od);
     const int W = od.W, H = od.H, nw = od.nw, S = pyr.S, L = S + 2;
-    const int lane = threadIdx.x, warp = threadIdx.y;
-    const int c = blockIdx.x;
-    const int x0 = c * kExTX, y0 = blockIdx.y * kExTY;
-    constexpr int TW = kExTX + 2, TH = kExTY + 2;
-    dog.stage(tile, L, x0 - 1, y0 - 1, TW, TH, warp, 8, lane);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int x0 = blockIdx.x * kExTX, y0 = blockIdx.y * kExTY;
+    dog.stage(tile, L, x0 - 4, y0 - 1, kExSW, kExSH, warp, 8, lane);
     __syncthreads();
-    const int x = x0 + lane;
-    // each warp handles rows warp and warp + 8 of the tile
-    for (int ty = warp; ty < kExTY; ty += 8) {
-        const int y = y0 + ty;
-        const bool inside = y >= border && y < H - border && x >= border && x < W - border;
-        // layer summaries, sliding over l
-        float Mp = 0.f, mp = 0.f, Mc = 0.f, mc = 0.f, m8c = 0.f, n8c = 0.f, vc = 0.f;
-        for (int l = 0; l < L; ++l) {
-            const float* t = tile + (l * TH + ty) * TW + lane;  // top-left of the 3x3 block
-            const float a0 = t[0], a1 = t[1], a2 = t[2];
-            const float b0 = t[TW], b1 = t[TW + 1], b2 = t[TW + 2];
-            const float c0 = t[2 * TW], c1 = t[2 * TW + 1], c2 = t[2 * TW + 2];
-            const float mx8 = fmaxf(fmaxf(fmaxf(a0, a1), fmaxf(a2, b0)), fmaxf(fmaxf(b2, c0), fmaxf(c1, c2)));
-            const float mn8 = fminf(fminf(fminf(a0, a1), fminf(a2, b0)), fminf(fminf(b2, c0), fminf(c1, c2)));
-            const float M = fmaxf(mx8, b1), m = fminf(mn8, b1);
-            if (l >= 2) {
-                // layer l-1 is the centre layer s = l - 1 (1..S)
-                const int s = l - 1;
-                const bool ext = inside && ((vc > fmaxf(fmaxf(Mp, M), m8c)) || (vc < fminf(fminf(mp, m), n8c)));
+    const int col = tid & (kExTX - 1);          // 0..63
+    const int r0 = (tid >> 6) * kExRows;       // 0, 4, 8, 12
+    const int x = x0 + col;
+    const int tx = col + 4;                     // staged column of x
+    const int word = (x0 >> 5) + ((tid >> 5) & 1);  // this warp's 32 columns
+    // Sliding window over the layers: p = l-2, c = l-1, n = l.
+    float BMp[kExRows], Bmp[kExRows], BMc[kExRows], Bmc[kExRows], RMc[kExRows], Rmc[kExRows], Vc[kExRows];
+#pragma unroll
+    for (int j = 0; j < kExRows; ++j) BMp[j] = Bmp[j] = BMc[j] = Bmc[j] = RMc[j] = Rmc[j] = Vc[j] = 0.0f;
+    for (int l = 0; l < L; ++l) {
+        const float* t = tile + (l * kExSH + r0) * kExSW + tx;  // staged row y0 + r0 - 1
+        float left[kExRows + 2], mid[kExRows + 2], right[kExRows + 2], hM[kExRows + 2], hm[kExRows + 2];
+#pragma unroll
+        for (int j = 0; j < kExRows + 2; ++j) {
+            left[j] = t[j * kExSW - 1];
+            mid[j] = t[j * kExSW];
+            right[j] = t[j * kExSW + 1];
+            hM[j] = fmaxf(fmaxf(left[j], mid[j]), right[j]);
+            hm[j] = fminf(fminf(left[j], mid[j]), right[j]);
+        }
+        float BMn[kExRows], Bmn[kExRows], RMn[kExRows], Rmn[kExRows];
+#pragma unroll
+        for (int j = 0; j < kExRows; ++j) {
+            BMn[j] = fmaxf(fmaxf(hM[j], hM[j + 1]), hM[j + 2]);
+            Bmn[j] = fminf(fminf(hm[j], hm[j + 1]), hm[j + 2]);
+            RMn[j] = fmaxf(fmaxf(hM[j], hM[j + 2]), fmaxf(left[j + 1], right[j + 1]));
+            Rmn[j] = fminf(fminf(hm[j], hm[j + 2]), fminf(left[j + 1], right[j + 1]));
+        }
+        if (l >= 2) {
+            const int s = l - 1;  // centre layer
+#pragma unroll
+            for (int j = 0; j < kExRows; ++j) {
+                const int y = y0 + r0 + j;
+                const float v = Vc[j];
+                const bool inside = y >= border && y < H - border && x >= border && x < W - border;
+                const bool ext = inside && ((v > fmaxf(fmaxf(BMp[j], BMn[j]), RMc[j])) ||
+                                            (v < fminf(fminf(Bmp[j], Bmn[j]), Rmc[j])));
                 const uint32_t wv = __ballot_sync(0xffffffffu, ext);
-                if (lane == 0 && y < H) words[od.word_base + ((long long)(s - 1) * H + y) * nw + c] = wv;
+                if (lane == 0 && y < H && word < nw) words[od.word_base + ((long long)(s - 1) * H + y) * nw + word] = wv;
             }
-            Mp = Mc;
-            mp = mc;
-            Mc = M;
-            mc = m;
-            m8c = mx8;
-            n8c = mn8;
-            vc = b1;
+        }
+#pragma unroll
+        for (int j = 0; j < kExRows; ++j) {
+            BMp[j] = BMc[j];
+            Bmp[j] = Bmc[j];
+            BMc[j] = BMn[j];
+            Bmc[j] = Bmn[j];
+            RMc[j] = RMn[j];
+            Rmc[j] = Rmn[j];
+            Vc[j] = mid[j + 1];
         }
     }
 }
@@ -251,31 +285,24 @@ __device__ bool refine_one(const Dog& dog, int o, int x, int y, int s, const Ref
     return false;
 }
 
-__device__ __forceinline__ int find_octave(const PyramidDev& pyr, long long w) {
-    int o = 0;
-    for (int k = 1; k < pyr.num_octaves; ++k)
-        if (pyr.oct[k].word_base <= w) o = k;
-    return o;
-}
-
-// One thread per mask word: the candidates of the word go to their scanned
-// slots, in x order within the word, i.e. (octave, layer, y, x) overall.
+// One thread per mask word of octave o: the candidates of the word go to
+// their scanned slots in the octave's list, in x order within the word, i.e.
+// (layer, y, x) within the octave.
 template <class Dog>
-__global__ void __launch_bounds__(256) k_emit(const void* arena, PyramidDev pyr, long long n_words,
+__global__ void __launch_bounds__(256) k_emit(const void* arena, PyramidDev pyr, int o,
                                               const uint32_t* __restrict__ words,
                                               const uint32_t* __restrict__ cand_off,
                                               Keypoint* __restrict__ cands, uint32_t cap,
                                               Counters* __restrict__ ctr) {
+    const OctaveDev& od = pyr.oct[o];
+    const long long nwo = (long long)pyr.S * od.H * od.nw;
     const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= n_words) return;
+    if (w >= nwo) return;
     uint32_t word = words[w];
     if (word == 0u) return;
-    const int o = find_octave(pyr, w);
-    const OctaveDev& od = pyr.oct[o];
     const Dog dog = make_dog<Dog>(arena, od);
-    const long long local = w - od.word_base;
-    const int c = (int)(local % od.nw);
-    const long long rowid = local / od.nw;
+    const int c = (int)(w % od.nw);
+    const long long rowid = w / od.nw;
     const int y = (int)(rowid % od.H);
     const int s = (int)(rowid / od.H) + 1;
     const float scale = __int_as_float((127 + o) << 23);
@@ -300,19 +327,18 @@ __global__ void __launch_bounds__(256) k_emit(const void* arena, PyramidDev pyr,
     }
 }
 
-// One thread per candidate (persistent grid over the device-side count).
+// One thread per candidate of octave o (persistent grid over its count).
 template <class Dog>
-__global__ void __launch_bounds__(256) k_refine(const void* arena, PyramidDev pyr, RefineParams rp,
+__global__ void __launch_bounds__(256) k_refine(const void* arena, PyramidDev pyr, int o, RefineParams rp,
                                                 const Keypoint* __restrict__ cands,
                                                 Keypoint* __restrict__ refined_at, uint32_t* __restrict__ keep,
-                                                uint32_t cap, const Counters* __restrict__ ctr) {
-    const uint32_t n = min(ctr->n_candidates, cap);
+                                                uint32_t cap, const OctCounters* __restrict__ oc) {
+    const uint32_t n = min(oc->n_cand, cap);
+    const Dog dog = make_dog<Dog>(arena, pyr.oct[o]);
+    const float scale = __int_as_float((127 + o) << 23);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const Keypoint k = cands[i];
-        const int o = k.octave;
-        const float scale = __int_as_float((127 + o) << 23);
         const int x = rust_as_i32(__fdiv_rn(k.x, scale)), y = rust_as_i32(__fdiv_rn(k.y, scale));
-        const Dog dog = make_dog<Dog>(arena, pyr.oct[o]);
         Keypoint r;
         const bool ok = refine_one(dog, o, x, y, k.layer, rp, &r);
         if (ok) refined_at[i] = r;
@@ -324,8 +350,8 @@ __global__ void __launch_bounds__(256) k_compact(const uint32_t* __restrict__ ke
                                                  const uint32_t* __restrict__ keep_off,
                                                  const Keypoint* __restrict__ refined_at,
                                                  Keypoint* __restrict__ refined, uint32_t cap,
-                                                 const Counters* __restrict__ ctr) {
-    const uint32_t n = min(ctr->n_candidates, cap);
+                                                 const OctCounters* __restrict__ oc) {
+    const uint32_t n = min(oc->n_cand, cap);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         if (keep[i]) refined[keep_off[i]] = refined_at[i];
 }
@@ -339,42 +365,48 @@ int launch_extrema_mask(int storage, const void* arena, const PyramidDev& pyr, i
     const OctaveDev& od = pyr.oct[o];
     if (od.W <= 0 || od.H <= 0) return 0;
     if (pyr.S + 2 > kExMaxLayers) return -1;
-    dim3 grid(od.nw, (od.H + kExTY - 1) / kExTY);
-    const size_t smem = sizeof(float) * (size_t)(pyr.S + 2) * (kExTY + 2) * (kExTX + 2);
+    dim3 grid((od.W + kExTX - 1) / kExTX, (od.H + kExTY - 1) / kExTY);
+    const size_t smem = sizeof(float) * (size_t)(pyr.S + 2) * kExSH * kExSW;
+    if (smem > 48 * 1024) {
+        auto k = storage == SIFT_CUDA_STORAGE_F16 ? k_extrema_mask<DogFromG16> : k_extrema_mask<DogF32>;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    }
     if (storage == SIFT_CUDA_STORAGE_F16)
-        k_extrema_mask<DogFromG16><<<grid, dim3(kExTX, 8), smem, st>>>(arena, pyr, o, border, words);
+        k_extrema_mask<DogFromG16><<<grid, 256, smem, st>>>(arena, pyr, o, border, words);
     else
-        k_extrema_mask<DogF32><<<grid, dim3(kExTX, 8), smem, st>>>(arena, pyr, o, border, words);
+        k_extrema_mask<DogF32><<<grid, 256, smem, st>>>(arena, pyr, o, border, words);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_emit(int storage, const void* arena, const PyramidDev& pyr, long long n_words, const uint32_t* words,
+int launch_emit(int storage, const void* arena, const PyramidDev& pyr, int o, const uint32_t* words,
                 const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st) {
-    if (n_words <= 0) return 0;
-    unsigned grid = (unsigned)((n_words + 255) / 256);
+    const OctaveDev& od = pyr.oct[o];
+    const long long nwo = (long long)pyr.S * od.H * od.nw;
+    if (nwo <= 0) return 0;
+    unsigned grid = (unsigned)((nwo + 255) / 256);
     if (storage == SIFT_CUDA_STORAGE_F16)
-        k_emit<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, n_words, words, cand_off, cands, cap, ctr);
+        k_emit<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, o, words, cand_off, cands, cap, ctr);
     else
-        k_emit<DogF32><<<grid, 256, 0, st>>>(arena, pyr, n_words, words, cand_off, cands, cap, ctr);
+        k_emit<DogF32><<<grid, 256, 0, st>>>(arena, pyr, o, words, cand_off, cands, cap, ctr);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_refine(int storage, const void* arena, const PyramidDev& pyr, float sigma, float contrast, float edge,
-                  const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap, const Counters* ctr,
-                  cudaStream_t st) {
+int launch_refine(int storage, const void* arena, const PyramidDev& pyr, int o, float sigma, float contrast,
+                  float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
+                  const OctCounters* oc, cudaStream_t st) {
     RefineParams rp{sigma, contrast, edge, pyr.S, pyr.S + 2};
-    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 4);
+    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 2);
     if (storage == SIFT_CUDA_STORAGE_F16)
-        k_refine<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, rp, cands, refined_at, keep, cap, ctr);
+        k_refine<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, o, rp, cands, refined_at, keep, cap, oc);
     else
-        k_refine<DogF32><<<grid, 256, 0, st>>>(arena, pyr, rp, cands, refined_at, keep, cap, ctr);
+        k_refine<DogF32><<<grid, 256, 0, st>>>(arena, pyr, o, rp, cands, refined_at, keep, cap, oc);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_compact(const uint32_t* keep, const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined,
-                   uint32_t cap, const Counters* ctr, cudaStream_t st) {
-    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 4);
-    k_compact<<<grid, 256, 0, st>>>(keep, keep_off, refined_at, refined, cap, ctr);
+                   uint32_t cap, const OctCounters* oc, cudaStream_t st) {
+    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 2);
+    k_compact<<<grid, 256, 0, st>>>(keep, keep_off, refined_at, refined, cap, oc);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -48,25 +48,27 @@ int launch_blur_level(const TIn* in, long long in_pitch, uint8_t* tmp, TG* out, 
 template <typename TG>
 int launch_lanczos(const TG* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst, int dst_pitch,
                    int nW, int nH, const int* vtab, const float* vw, const int* htab, const float* hw,
-                   cudaStream_t st);
+                   cudaStream_t st, bool fused);
+int lanczos_fused_span();
+int lanczos_fused_tile();
 int launch_extrema_mask(int storage, const void* arena, const PyramidDev& pyr, int o, int border, uint32_t* words,
                         cudaStream_t st);
-int launch_emit(int storage, const void* arena, const PyramidDev& pyr, long long n_words, const uint32_t* words,
+int launch_emit(int storage, const void* arena, const PyramidDev& pyr, int o, const uint32_t* words,
                 const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st);
-int launch_refine(int storage, const void* arena, const PyramidDev& pyr, float sigma, float contrast, float edge,
-                  const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap, const Counters* ctr,
-                  cudaStream_t st);
+int launch_refine(int storage, const void* arena, const PyramidDev& pyr, int o, float sigma, float contrast,
+                  float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
+                  const OctCounters* oc, cudaStream_t st);
 int launch_compact(const uint32_t* keep, const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined,
-                   uint32_t cap, const Counters* ctr, cudaStream_t st);
+                   uint32_t cap, const OctCounters* oc, cudaStream_t st);
 template <typename TG>
-int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, const Counters* ctr,
-                       float* ori_angle, uint32_t* ori_count, cudaStream_t st);
-int launch_orient_emit(const Keypoint* refined, const Counters* ctr, const float* ori_angle,
+int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, OctCounters* oc,
+                       float* ori_angle, uint32_t* ori_count, int grid, cudaStream_t st);
+int launch_orient_emit(const Keypoint* refined, int o, Counters* ctr, const float* ori_angle,
                        const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
-                       Counters* ctr_w, cudaStream_t st);
+                       cudaStream_t st);
 template <typename TG>
-int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, const Counters* ctr,
-                      float* desc, uint32_t cap, cudaStream_t st);
+int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
+                      uint32_t cap, int grid, cudaStream_t st);
 template <typename TG>
 int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, int pitch, int W, int H, cudaStream_t st);
 
@@ -166,12 +168,19 @@ struct Engine {
     std::vector<std::vector<LevelBlur>> lv;  // [o][s-1]
     struct LTab {
         size_t vtab, vw, htab, hw;  // element offsets in d_ltab / d_lw
+        bool fused;                 // every output tile's source window fits the fused kernel
     };
     std::vector<LTab> ltab;  // [o] for o -> o+1
 
+    // Lists. Octave o owns [cb[o], cb[o] + cap_c[o]) of the candidate-sized
+    // lists (candidates, refined, keep flags, orientation scratch) and its own
+    // scan scratch; the output lists (oriented keypoints, descriptors) are
+    // shared, octave after octave.
+    std::vector<uint32_t> cap_c, cb;
+    std::vector<size_t> pb, tb;  // scan-partials and horizontal-pass buffer offsets
     uint32_t cap_cand = 0, cap_ori = 0;
 
-    DevMem d_img, d_G, d_D, d_tmp, d_tmp2, d_ltmp, d_wts, d_ltab, d_lw;
+    DevMem d_img, d_G, d_D, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
     DevMem d_words, d_cand_off, d_keep, d_keep_off, d_partials;
     DevMem d_cands, d_refined_at, d_refined, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
     HostPinned h_ctr, h_kps, h_desc;
@@ -179,18 +188,18 @@ struct Engine {
     uint32_t launches = 0;
     bool last_desc = true;
 
-    // Second stream of the level DAG and its events (see enqueue_t), and the
-    // CUDA graph the whole run is replayed from.
-    cudaStream_t st2 = nullptr;
-    std::vector<cudaEvent_t> ev_level;  // per octave: level S written
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // One stream per octave for the level DAG and its events (see enqueue_t),
+    // and the CUDA graph the whole run is replayed from.
+    std::vector<cudaStream_t> st_oct;
+    std::vector<cudaEvent_t> ev_level, ev_ori, ev_done;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     struct GraphKey {
-        uint32_t W, H, cap_cand, cap_ori;
-        bool with_desc;
+        uint32_t W = 0, H = 0, cap_ori = 0;
+        std::vector<uint32_t> cap_c;
+        bool with_desc = false;
         bool operator==(const GraphKey& o) const {
-            return W == o.W && H == o.H && cap_cand == o.cap_cand && cap_ori == o.cap_ori && with_desc == o.with_desc;
+            return W == o.W && H == o.H && cap_ori == o.cap_ori && cap_c == o.cap_c && with_desc == o.with_desc;
         }
     } gkey{};
     uint32_t graph_launches = 0;
@@ -214,10 +223,11 @@ struct Engine {
         for (auto& r : ev_runs)
             for (auto e : r) cudaEventDestroy(e);
         for (auto e : ev_free) cudaEventDestroy(e);
-        for (auto e : ev_level) cudaEventDestroy(e);
-        if (ev_fork) cudaEventDestroy(ev_fork);
-        if (ev_join) cudaEventDestroy(ev_join);
-        if (st2) cudaStreamDestroy(st2);
+        for (auto* v : {&ev_level, &ev_ori, &ev_done})
+            for (auto e : *v)
+                if (e) cudaEventDestroy(e);
+        for (auto q : st_oct)
+            if (q) cudaStreamDestroy(q);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -271,15 +281,18 @@ struct Engine {
     int init() {
         if (int rc = set_device()) return rc;
         CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
-        CK(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking), "cudaStreamCreate");
-        CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming), "cudaEventCreate");
-        CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming), "cudaEventCreate");
-        ev_level.assign(kMaxOctaves, nullptr);
-        for (auto& e : ev_level) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        st_oct.assign(kMaxOctaves, nullptr);
+        for (auto& q : st_oct) CK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto* v : {&ev_level, &ev_ori, &ev_done}) {
+            v->assign(kMaxOctaves, nullptr);
+            for (auto& e : *v) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        }
         CK(h_ctr.ensure(sizeof(Counters)), "cudaHostAlloc(counters)");
         CK(d_ctr.ensure(sizeof(Counters)), "cudaMalloc(counters)");
         return 0;
     }
+
+    long long octave_words(int o) const { return (long long)pyr.S * pyr.oct[o].H * pyr.oct[o].nw; }
 
     // Lays out the arena for a width x height image and builds the tables.
     int ensure_geometry(uint32_t w, uint32_t h) {
@@ -290,7 +303,8 @@ struct Engine {
         g.num_octaves = O;
         g.S = S;
         g.levels = S + 3;
-        size_t goff = 0, doff = 0, wbase = 0, tmpb = 0, lt = 0;
+        size_t goff = 0, doff = 0, wbase = 0, tmpb = 0, lt = 0, tmpo = 0;
+        std::vector<size_t> tbo(O, 0);
         uint32_t ow = w, oh = h;
         for (int o = 0; o < O; ++o) {
             OctaveDev& od = g.oct[o];
@@ -306,6 +320,8 @@ struct Engine {
             doff += f16() ? 0 : (size_t)od.plane * (S + 2);
             wbase += (size_t)S * oh * od.nw;
             tmpb = std::max(tmpb, (size_t)od.pitch * oh);
+            tbo[o] = tmpo;
+            tmpo += align_up((size_t)od.pitch * oh, 256);
             if (o + 1 < O) lt = std::max(lt, (size_t)od.pitch * (oh / 2));
             ow /= 2;
             oh /= 2;
@@ -330,7 +346,16 @@ struct Engine {
         // Lanczos tables
         std::vector<int> itab;
         std::vector<float> ftab;
-        ltab.assign(O, LTab{0, 0, 0, 0});
+        ltab.assign(O, LTab{0, 0, 0, 0, false});
+        auto max_span = [](const AxisTaps& t) {
+            const int T = lanczos_fused_tile(), n = (int)t.left.size();
+            int m = 0;
+            for (int a = 0; a < n; a += T) {
+                const int b = std::min(a + T, n) - 1;
+                m = std::max(m, t.left[b] + t.count[b] - t.left[a]);
+            }
+            return m;
+        };
         for (int o = 0; o + 1 < O; ++o) {
             const OctaveDev& a = g.oct[o];
             const int nW = g.oct[o + 1].W, nH = g.oct[o + 1].H;
@@ -350,15 +375,16 @@ struct Engine {
             itab.insert(itab.end(), th.woff.begin(), th.woff.end());
             t.hw = ftab.size();
             ftab.insert(ftab.end(), th.w.begin(), th.w.end());
+            t.fused = max_span(tv) <= lanczos_fused_span() && max_span(th) <= lanczos_fused_span();
             ltab[o] = t;
         }
         // allocate
+        drop_graph();
         n_words = (long long)wbase;
         CK(d_G.ensure(goff * g_elem_size()), "cudaMalloc(G)");
         if (!f16()) CK(d_D.ensure(doff * sizeof(float)), "cudaMalloc(DoG)");
         CK(d_tmp.ensure(std::max<size_t>(tmpb, 16)), "cudaMalloc(tmp)");
-        CK(d_tmp2.ensure(std::max<size_t>(tmpb, 16)), "cudaMalloc(tmp2)");
-        drop_graph();
+        CK(d_tmpo.ensure(std::max<size_t>(tmpo, 16)), "cudaMalloc(tmp per octave)");
         CK(d_ltmp.ensure(std::max<size_t>(lt, 4) * sizeof(float)), "cudaMalloc(ltmp)");
         CK(d_wts.ensure(std::max<size_t>(wts.size(), 4) * sizeof(float)), "cudaMalloc(wts)");
         CK(d_ltab.ensure(std::max<size_t>(itab.size(), 4) * sizeof(int)), "cudaMalloc(ltab)");
@@ -379,22 +405,36 @@ struct Engine {
         d_elems = doff;
         tmp_bytes = tmpb;
         ltmp_elems = lt;
+        tb = tbo;
         W = w;
         H = h;
         have_geom = true;
-        if (cap_cand == 0) {
-            // Initial list capacity: 1/64 of the scanned positions (measured
-            // densities on natural and synthetic images are far below it);
-            // grown on overflow.
-            size_t positions = (size_t)n_words * 32;
-            cap_cand = (uint32_t)std::min<size_t>(std::max<size_t>(positions / 64, 4096), 1u << 30);
-            cap_ori = cap_cand;
-        }
+        // Initial list capacities: 1/64 of each octave's scanned positions
+        // (measured densities on natural and synthetic images are far below
+        // it), at least 1024; grown on overflow.
+        cap_c.assign(O, 0);
+        for (int o = 0; o < O; ++o)
+            cap_c[o] = (uint32_t)std::min<size_t>(std::max<size_t>((size_t)octave_words(o) * 32 / 64, 1024), 1u << 28);
+        size_t tot = 0;
+        for (auto c : cap_c) tot += c;
+        cap_ori = std::max<uint32_t>(cap_ori, (uint32_t)std::min<size_t>(tot, 1u << 30));
         return ensure_lists();
     }
 
     int ensure_lists() {
         drop_graph();
+        const int O = pyr.num_octaves;
+        cb.assign(O, 0);
+        pb.assign(O, 0);
+        size_t c = 0, pp = 0;
+        for (int o = 0; o < O; ++o) {
+            cb[o] = (uint32_t)c;
+            c += cap_c[o];
+            pb[o] = pp;
+            pp += align_up(scan_partials_size(std::max<size_t>({(size_t)octave_words(o), (size_t)cap_c[o], 1})), 64);
+        }
+        if (c > (1u << 30)) return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint lists above 2^30");
+        cap_cand = (uint32_t)c;
         const size_t kp = sizeof(Keypoint);
         CK(d_cands.ensure((size_t)cap_cand * kp), "cudaMalloc(cands)");
         CK(d_refined_at.ensure((size_t)cap_cand * kp), "cudaMalloc(refined_at)");
@@ -406,24 +446,28 @@ struct Engine {
         CK(d_keep_off.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(keep_off)");
         CK(d_oriented.ensure((size_t)cap_ori * kp), "cudaMalloc(oriented)");
         CK(d_desc.ensure((size_t)cap_ori * kDescLen * sizeof(float)), "cudaMalloc(desc)");
-        size_t np = scan_partials_size(std::max<size_t>({(size_t)n_words, (size_t)cap_cand, 1}));
-        CK(d_partials.ensure(np * sizeof(uint32_t)), "cudaMalloc(partials)");
+        CK(d_partials.ensure(std::max<size_t>(pp, 1) * sizeof(uint32_t)), "cudaMalloc(partials)");
         return 0;
     }
 
-    // The run as a DAG on two streams (dag) or in order on one stream:
-    //   st : counters, base level, octave o levels 1..S, Lanczos(o) -> octave o+1
-    //   st2: after level S of octave o, levels S+1..S+2 and the extrema mask of
-    //        octave o (they feed nothing on the next octave's chain)
-    //   st : waits for st2, then the candidate list, refinement, orientation,
-    //        descriptors.
-    // Levels on st2 use their own horizontal-pass buffer (tmp2).
+    // The run as a DAG (dag) or in stage order on one stream (profiling):
+    //   st        counters, base level, octave o levels 1..S, Lanczos(o) ->
+    //             octave o+1 ...
+    //   st_oct[o] after level S of octave o: levels S+1..S+2, the extrema
+    //             mask, the ordered candidate list, refinement, orientation;
+    //             then, once octaves 0..o-1 know their oriented counts, the
+    //             output slots and the descriptors of octave o.
+    //   st        waits for every octave's chain.
+    // Octave 0's descriptors (most of the work) overlap the smaller octaves'
+    // pyramid. Levels on st_oct[o] use their own horizontal-pass buffer.
     template <typename TG>
     int enqueue_t(const uint8_t* img, long long stride, bool with_desc, bool dag) {
         const int O = pyr.num_octaves, S = pyr.S;
         TG* G = d_G.as<TG>();
         float* D = f16() ? nullptr : d_D.as<float>();
         const float* wts = d_wts.as<float>();
+        Counters* ctr = d_ctr.as<Counters>();
+        const void* arena = f16() ? (const void*)d_G.p : (const void*)d_D.p;
         launches = 0;
         auto ok = [&](int rc) {
             ++launches;
@@ -431,12 +475,10 @@ struct Engine {
         };
         std::vector<cudaEvent_t> run_ev;
         mark(&run_ev);
-        cudaStream_t s2 = dag ? st2 : st;
-        uint8_t* tmp_main = d_tmp.as<uint8_t>();
-        uint8_t* tmp_aux = dag ? d_tmp2.as<uint8_t>() : tmp_main;
         CK(cudaMemsetAsync(d_ctr.p, 0, sizeof(Counters), st), "memset counters");
-        const void* arena = f16() ? (const void*)d_G.p : (const void*)d_D.p;
-        const OctaveDev& o0 = pyr.oct[0];
+        int O_used = 0;
+        for (int o = 0; o < O && pyr.oct[o].W > 0 && pyr.oct[o].H > 0; ++o) O_used = o + 1;
+
         auto level = [&](int o, int s, cudaStream_t q, uint8_t* tmp) -> int {
             const OctaveDev& od = pyr.oct[o];
             const LevelBlur& b = lv[o][s - 1];
@@ -455,12 +497,90 @@ struct Engine {
             launches += nl;
             return 0;
         };
-        if (o0.W > 0 && o0.H > 0) {
+        auto lanczos = [&](int o) -> int {
+            const OctaveDev& od = pyr.oct[o];
+            const OctaveDev& nx = pyr.oct[o + 1];
+            const LTab& t = ltab[o];
+            const int* it = d_ltab.as<int>();
+            const float* ft = d_lw.as<float>();
+            if (ok(launch_lanczos<TG>(G + od.g_off + (long long)S * od.plane, od.pitch, od.W, od.H, d_ltmp.as<float>(),
+                                      od.pitch, G + nx.g_off, nx.pitch, nx.W, nx.H, it + t.vtab, ft + t.vw,
+                                      it + t.htab, ft + t.hw, st, t.fused)))
+                return cuda_fail(cudaGetLastError(), "lanczos");
+            if (!t.fused) ++launches;
+            return 0;
+        };
+        // (b)+(c): extrema, ordered candidates, refinement of octave o
+        auto detect = [&](int o, cudaStream_t q) -> int {
+            const OctaveDev& od = pyr.oct[o];
+            OctCounters* oc = &ctr->oct[o];
+            uint32_t* partials = d_partials.as<uint32_t>() + pb[o];
+            const long long nwo = octave_words(o);
+            if (od.nw > 0 && ok(launch_extrema_mask(opt.storage, arena, pyr, o, (int)p.image_border_width,
+                                                    d_words.as<uint32_t>(), q)))
+                return cuda_fail(cudaGetLastError(), "extrema mask");
+            if (scan_exclusive(d_words.as<uint32_t>() + od.word_base, SCAN_POPC,
+                               d_cand_off.as<uint32_t>() + od.word_base, (size_t)nwo, nullptr, &oc->n_cand, partials,
+                               q))
+                return cuda_fail(cudaGetLastError(), "scan candidates");
+            launches += nwo > 0 ? 3 : 0;
+            if (ok(launch_emit(opt.storage, arena, pyr, o, d_words.as<uint32_t>() + od.word_base,
+                               d_cand_off.as<uint32_t>() + od.word_base, d_cands.as<Keypoint>() + cb[o], cap_c[o], ctr,
+                               q)))
+                return cuda_fail(cudaGetLastError(), "emit");
+            if (ok(launch_refine(opt.storage, arena, pyr, o, p.sigma, p.contrast_threshold, p.edge_threshold,
+                                 d_cands.as<Keypoint>() + cb[o], d_refined_at.as<Keypoint>() + cb[o],
+                                 d_keep.as<uint32_t>() + cb[o], cap_c[o], oc, q)))
+                return cuda_fail(cudaGetLastError(), "refine");
+            if (scan_exclusive(d_keep.as<uint32_t>() + cb[o], SCAN_U32, d_keep_off.as<uint32_t>() + cb[o],
+                               (size_t)cap_c[o], &oc->n_cand, &oc->n_ref, partials, q))
+                return cuda_fail(cudaGetLastError(), "scan refined");
+            launches += 3;
+            if (ok(launch_compact(d_keep.as<uint32_t>() + cb[o], d_keep_off.as<uint32_t>() + cb[o],
+                                  d_refined_at.as<Keypoint>() + cb[o], d_refined.as<Keypoint>() + cb[o], cap_c[o], oc,
+                                  q)))
+                return cuda_fail(cudaGetLastError(), "compact");
+            return 0;
+        };
+        // (d) orientation histograms and their scan
+        auto orient = [&](int o, cudaStream_t q) -> int {
+            OctCounters* oc = &ctr->oct[o];
+            const int grid = (int)std::min<uint32_t>(std::max<uint32_t>(cap_c[o] / 64, 32), 152 * 4);
+            if (ok(launch_orientation<TG>(G, pyr, d_refined.as<Keypoint>() + cb[o], oc,
+                                          d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
+                                          d_ori_count.as<uint32_t>() + cb[o], grid, q)))
+                return cuda_fail(cudaGetLastError(), "orientation");
+            if (scan_exclusive(d_ori_count.as<uint32_t>() + cb[o], SCAN_U32, d_ori_off.as<uint32_t>() + cb[o],
+                               (size_t)cap_c[o], &oc->n_ref, &oc->n_ori, d_partials.as<uint32_t>() + pb[o], q))
+                return cuda_fail(cudaGetLastError(), "scan orientations");
+            launches += 3;
+            return 0;
+        };
+        // output slots of octave o (after octaves 0..o-1) and its descriptors
+        auto emit_out = [&](int o, cudaStream_t q) -> int {
+            if (ok(launch_orient_emit(d_refined.as<Keypoint>() + cb[o], o, ctr,
+                                      d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
+                                      d_ori_count.as<uint32_t>() + cb[o], d_ori_off.as<uint32_t>() + cb[o],
+                                      d_oriented.as<Keypoint>(), cap_ori, q)))
+                return cuda_fail(cudaGetLastError(), "orientation emit");
+            return 0;
+        };
+        auto describe = [&](int o, cudaStream_t q) -> int {
+            if (!with_desc) return 0;
+            const int grid = (int)std::min<uint32_t>(std::max<uint32_t>(cap_c[o] / 16, 64), 152 * 8);
+            if (ok(launch_descriptor<TG>(G, pyr, d_oriented.as<Keypoint>(), &ctr->oct[o], d_desc.as<float>(), cap_ori,
+                                         grid, q)))
+                return cuda_fail(cudaGetLastError(), "descriptor");
+            return 0;
+        };
+
+        const OctaveDev& o0 = pyr.oct[0];
+        if (O_used > 0) {
             // base image (src/sift.rs:1204-1214)
             if (base.sigma > 0.0f) {
                 int nl = 0;
-                if (launch_blur_level<uint8_t, TG>(img, stride, tmp_main, G + o0.g_off, nullptr, o0.pitch, o0.W, o0.H,
-                                                   base.radius, wts + base.woff, round_mode, st, &nl))
+                if (launch_blur_level<uint8_t, TG>(img, stride, d_tmp.as<uint8_t>(), G + o0.g_off, nullptr, o0.pitch,
+                                                   o0.W, o0.H, base.radius, wts + base.woff, round_mode, st, &nl))
                     return cuda_fail(cudaGetLastError(), "blur (base)");
                 launches += nl;
             } else {
@@ -468,90 +588,50 @@ struct Engine {
                     return cuda_fail(cudaGetLastError(), "base copy");
             }
         }
-        bool aux_used = false;
-        for (int o = 0; o < O; ++o) {
-            const OctaveDev& od = pyr.oct[o];
-            if (od.W == 0 || od.H == 0) break;
-            for (int s = 1; s <= S; ++s)
-                if (int rc = level(o, s, st, tmp_main)) return rc;
-            if (dag) {
+        if (dag) {
+            for (int o = 0; o < O_used; ++o) {
+                cudaStream_t q = st_oct[o];
+                uint8_t* tmp_o = d_tmpo.as<uint8_t>() + tb[o];
+                for (int s = 1; s <= S; ++s)
+                    if (int rc = level(o, s, st, d_tmp.as<uint8_t>())) return rc;
                 CK(cudaEventRecord(ev_level[o], st), "event record");
-                CK(cudaStreamWaitEvent(st2, ev_level[o], 0), "stream wait");
-                aux_used = true;
+                CK(cudaStreamWaitEvent(q, ev_level[o], 0), "stream wait");
+                for (int s = S + 1; s < S + 3; ++s)
+                    if (int rc = level(o, s, q, tmp_o)) return rc;
+                if (int rc = detect(o, q)) return rc;
+                if (int rc = orient(o, q)) return rc;
+                CK(cudaEventRecord(ev_ori[o], q), "event record");
+                for (int k = 0; k < o; ++k) CK(cudaStreamWaitEvent(q, ev_ori[k], 0), "stream wait");
+                if (int rc = emit_out(o, q)) return rc;
+                if (int rc = describe(o, q)) return rc;
+                CK(cudaEventRecord(ev_done[o], q), "event record");
+                if (o + 1 < O_used)
+                    if (int rc = lanczos(o)) return rc;
             }
-            for (int s = S + 1; s < S + 3; ++s)
-                if (int rc = level(o, s, s2, tmp_aux)) return rc;
-            if (!prof && od.nw > 0) {
-                if (ok(launch_extrema_mask(opt.storage, arena, pyr, o, (int)p.image_border_width,
-                                           d_words.as<uint32_t>(), s2)))
-                    return cuda_fail(cudaGetLastError(), "extrema mask");
+            for (int o = 0; o < O_used; ++o) CK(cudaStreamWaitEvent(st, ev_done[o], 0), "stream wait");
+        } else {
+            for (int o = 0; o < O_used; ++o) {
+                for (int s = 1; s < S + 3; ++s)
+                    if (int rc = level(o, s, st, d_tmp.as<uint8_t>())) return rc;
+                if (o + 1 < O_used)
+                    if (int rc = lanczos(o)) return rc;
             }
-            if (o + 1 < O) {
-                const OctaveDev& nx = pyr.oct[o + 1];
-                if (nx.W == 0 || nx.H == 0) break;
-                const LTab& t = ltab[o];
-                const int* it = d_ltab.as<int>();
-                const float* ft = d_lw.as<float>();
-                if (ok(launch_lanczos<TG>(G + od.g_off + (long long)S * od.plane, od.pitch, od.W, od.H,
-                                          d_ltmp.as<float>(), od.pitch, G + nx.g_off, nx.pitch, nx.W, nx.H,
-                                          it + t.vtab, ft + t.vw, it + t.htab, ft + t.hw, st)))
-                    return cuda_fail(cudaGetLastError(), "lanczos");
-                ++launches;
-            }
+            mark(&run_ev);
+            for (int o = 0; o < O_used; ++o)
+                if (int rc = detect(o, st)) return rc;
+            mark(&run_ev);
+            for (int o = 0; o < O_used; ++o)
+                if (int rc = orient(o, st)) return rc;
+            for (int o = 0; o < O_used; ++o)
+                if (int rc = emit_out(o, st)) return rc;
+            mark(&run_ev);
+            for (int o = 0; o < O_used; ++o)
+                if (int rc = describe(o, st)) return rc;
         }
-        if (aux_used) {
-            CK(cudaEventRecord(ev_join, st2), "event record");
-            CK(cudaStreamWaitEvent(st, ev_join, 0), "stream wait");
-        }
-        mark(&run_ev);
-        if (prof) {
-            // profiled runs time the extrema masks as part of stage (b)
-            for (int o = 0; o < O; ++o) {
-                const OctaveDev& od = pyr.oct[o];
-                if (od.W == 0 || od.H == 0 || od.nw == 0) continue;
-                if (ok(launch_extrema_mask(opt.storage, arena, pyr, o, (int)p.image_border_width,
-                                           d_words.as<uint32_t>(), st)))
-                    return cuda_fail(cudaGetLastError(), "extrema mask");
-            }
-        }
-        // (b) extrema (above) -> (c) ordered candidates + refinement
-        Counters* ctr = d_ctr.as<Counters>();
-        uint32_t* words = d_words.as<uint32_t>();
-        if (scan_exclusive(words, SCAN_POPC, d_cand_off.as<uint32_t>(), (size_t)n_words, nullptr, &ctr->n_candidates,
-                           d_partials.as<uint32_t>(), st))
-            return cuda_fail(cudaGetLastError(), "scan candidates");
-        launches += 3;
-        if (ok(launch_emit(opt.storage, arena, pyr, n_words, words, d_cand_off.as<uint32_t>(), d_cands.as<Keypoint>(),
-                           cap_cand, ctr, st)))
-            return cuda_fail(cudaGetLastError(), "emit");
-        if (ok(launch_refine(opt.storage, arena, pyr, p.sigma, p.contrast_threshold, p.edge_threshold,
-                             d_cands.as<Keypoint>(), d_refined_at.as<Keypoint>(), d_keep.as<uint32_t>(), cap_cand, ctr,
-                             st)))
-            return cuda_fail(cudaGetLastError(), "refine");
-        if (scan_exclusive(d_keep.as<uint32_t>(), SCAN_U32, d_keep_off.as<uint32_t>(), (size_t)cap_cand,
-                           &ctr->n_candidates, &ctr->n_refined, d_partials.as<uint32_t>(), st))
-            return cuda_fail(cudaGetLastError(), "scan refined");
-        launches += 3;
-        if (ok(launch_compact(d_keep.as<uint32_t>(), d_keep_off.as<uint32_t>(), d_refined_at.as<Keypoint>(),
-                              d_refined.as<Keypoint>(), cap_cand, ctr, st)))
-            return cuda_fail(cudaGetLastError(), "compact");
-        mark(&run_ev);
-        // (d) orientation
-        if (ok(launch_orientation<TG>(G, pyr, d_refined.as<Keypoint>(), ctr, d_ori_angle.as<float>(),
-                                      d_ori_count.as<uint32_t>(), st)))
-            return cuda_fail(cudaGetLastError(), "orientation");
-        if (scan_exclusive(d_ori_count.as<uint32_t>(), SCAN_U32, d_ori_off.as<uint32_t>(), (size_t)cap_cand,
-                           &ctr->n_refined, &ctr->n_oriented, d_partials.as<uint32_t>(), st))
-            return cuda_fail(cudaGetLastError(), "scan orientations");
-        launches += 3;
-        if (ok(launch_orient_emit(d_refined.as<Keypoint>(), ctr, d_ori_angle.as<float>(), d_ori_count.as<uint32_t>(),
-                                  d_ori_off.as<uint32_t>(), d_oriented.as<Keypoint>(), cap_ori, ctr, st)))
-            return cuda_fail(cudaGetLastError(), "orientation emit");
-        mark(&run_ev);
-        // (e) descriptors
-        if (with_desc) {
-            if (ok(launch_descriptor<TG>(G, pyr, d_oriented.as<Keypoint>(), ctr, d_desc.as<float>(), cap_ori, st)))
-                return cuda_fail(cudaGetLastError(), "descriptor");
+        if (O_used == 0) {
+            mark(&run_ev);
+            mark(&run_ev);
+            mark(&run_ev);
         }
         mark(&run_ev);
         if (prof) ev_runs.push_back(std::move(run_ev));
@@ -569,7 +649,12 @@ struct Engine {
     int run(bool with_desc) {
         const long long stride = (long long)img_pitch;
         if (prof) return enqueue(d_img.as<uint8_t>(), stride, with_desc, false);
-        const GraphKey key{W, H, cap_cand, cap_ori, with_desc};
+        GraphKey key;
+        key.W = W;
+        key.H = H;
+        key.cap_ori = cap_ori;
+        key.cap_c = cap_c;
+        key.with_desc = with_desc;
         if (!gexec || !(key == gkey)) {
             drop_graph();
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -591,20 +676,30 @@ struct Engine {
         return 0;
     }
 
-    // Reads the counters; grows the lists and reports 1 when a list overflowed.
+    // Reads the counters; grows the lists and reports a retry when one
+    // overflowed.
     int check_counters(bool* retry) {
         *retry = false;
         CK(cudaMemcpyAsync(h_ctr.p, d_ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, st), "D2H counters");
         CK(cudaStreamSynchronize(st), "run");
-        const Counters c = *h_ctr.as<Counters>();
-        bool grow = c.overflow != 0 || c.n_candidates > cap_cand || c.n_oriented > cap_ori;
-        if (grow) {
-            size_t nc = std::max<size_t>((size_t)cap_cand, (size_t)c.n_candidates + c.n_candidates / 4 + 1024);
-            size_t no = std::max<size_t>((size_t)cap_ori, (size_t)c.n_oriented + c.n_oriented / 4 + 1024);
-            if (c.overflow & 4u) no = std::max<size_t>(no, (size_t)cap_ori * 2);
-            if (nc > (1u << 30) || no > (1u << 30)) return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint lists above 2^30");
-            cap_cand = (uint32_t)nc;
+        const Counters& c = *h_ctr.as<Counters>();
+        bool grow = false;
+        for (int o = 0; o < pyr.num_octaves; ++o) {
+            const uint32_t n = c.oct[o].n_cand;
+            if (n > cap_c[o]) {
+                const size_t nc = (size_t)n + n / 4 + 1024;
+                if (nc > (1u << 28)) return fail(SIFT_CUDA_ERR_CAPACITY, "candidate list above 2^28");
+                cap_c[o] = (uint32_t)nc;
+                grow = true;
+            }
+        }
+        if ((c.overflow & 4u) || c.n_oriented > cap_ori) {
+            const size_t no = std::max<size_t>((size_t)cap_ori * 2, (size_t)c.n_oriented + c.n_oriented / 4 + 1024);
+            if (no > (1u << 30)) return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint list above 2^30");
             cap_ori = (uint32_t)no;
+            grow = true;
+        }
+        if (grow) {
             if (int rc = ensure_lists()) return rc;
             *retry = true;
         }
@@ -653,8 +748,7 @@ struct Engine {
     }
 
     int fetch(bool with_desc, SiftCudaResult* out) {
-        const Counters c = *h_ctr.as<Counters>();
-        const uint32_t n = c.n_oriented;
+        const uint32_t n = h_ctr.as<Counters>()->n_oriented;
         out->n = n;
         out->kps = (SiftCudaKeypoint*)std::malloc(sizeof(SiftCudaKeypoint) * std::max<uint32_t>(n, 1));
         out->desc = with_desc ? (float*)std::malloc(sizeof(float) * kDescLen * std::max<uint32_t>(n, 1)) : nullptr;
@@ -911,12 +1005,25 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
     }
     const sift::Keypoint* src = nullptr;
     uint64_t n = 0;
-    if (stage == SIFT_CUDA_STAGE_CANDIDATES) {
-        src = e.d_cands.as<sift::Keypoint>();
-        n = std::min<uint64_t>(c.n_candidates, e.cap_cand);
-    } else if (stage == SIFT_CUDA_STAGE_REFINED) {
-        src = e.d_refined.as<sift::Keypoint>();
-        n = std::min<uint64_t>(c.n_refined, e.cap_cand);
+    if (stage == SIFT_CUDA_STAGE_CANDIDATES || stage == SIFT_CUDA_STAGE_REFINED) {
+        // per-octave regions, concatenated in octave order
+        const bool cand = stage == SIFT_CUDA_STAGE_CANDIDATES;
+        const sift::Keypoint* base = cand ? e.d_cands.as<sift::Keypoint>() : e.d_refined.as<sift::Keypoint>();
+        uint64_t total = 0;
+        for (int o = 0; o < g.num_octaves; ++o)
+            total += std::min<uint64_t>(cand ? c.oct[o].n_cand : c.oct[o].n_ref, e.cap_c[o]);
+        *count = total;
+        if (!out) return 0;
+        uint64_t pos = 0;
+        for (int o = 0; o < g.num_octaves && pos < capacity; ++o) {
+            const uint64_t no = std::min<uint64_t>(cand ? c.oct[o].n_cand : c.oct[o].n_ref, e.cap_c[o]);
+            const uint64_t m = std::min<uint64_t>(no, capacity - pos);
+            if (m && cudaMemcpy((sift::Keypoint*)out + pos, base + e.cb[o], m * sizeof(sift::Keypoint),
+                                cudaMemcpyDeviceToHost) != cudaSuccess)
+                return sift::cuda_fail(cudaGetLastError(), "D2H stage");
+            pos += m;
+        }
+        return 0;
     } else if (stage == SIFT_CUDA_STAGE_KEYPOINTS) {
         src = e.d_oriented.as<sift::Keypoint>();
         n = std::min<uint64_t>(c.n_oriented, e.cap_ori);

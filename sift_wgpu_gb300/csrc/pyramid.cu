@@ -132,10 +132,15 @@ constexpr int kColTY = 8;
 constexpr int kColRPT = 8;                 // output rows per thread
 constexpr int kColRows = kColTY * kColRPT;  // output rows per CTA
 
-// Vertical pass over a 32 x 64 output tile. Shared layout: weights[taps],
-// lut[256] (v / 255 in f32), then (64 + 2r) rows x 32 floats of the u8
-// intermediate with clamp-to-edge rows. Writes level s (TG) and, when
-// dog != nullptr, DoG(s-1) = G_s/255 - G_{s-1}/255 (src/sift.rs:92-124).
+// Vertical pass over a 32 x 64 output tile. Shared layout: weights padded
+// with zeros to a multiple of 8, lut[256] (v / 255 in f32), then
+// (64 + taps8 - 1) rows x 32 floats of the u8 intermediate with
+// clamp-to-edge rows. Taps go in unrolled groups of 8 from a 15-row register
+// window; the zero taps at the end add +0 to a non-negative sum, which leaves
+// it unchanged. Writes level s (TG) and, when dog != nullptr,
+// DoG(s-1) = G_s/255 - G_{s-1}/255 (src/sift.rs:92-124).
+__host__ __device__ constexpr int taps8(int r) { return ((2 * r + 1) + 7) & ~7; }
+
 template <typename TG>
 __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __restrict__ tmp, int tmp_pitch,
                                                              const TG* __restrict__ prev, TG* __restrict__ out,
@@ -144,16 +149,17 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
                                                              int round_mode) {
     extern __shared__ __align__(16) float sm[];
     const int taps = 2 * r + 1;
+    const int tp = taps8(r);
     float* kw = sm;
-    float* lut = sm + ((taps + 3) & ~3);
+    float* lut = sm + tp;
     float* tile = lut + 256;
     const int tid = threadIdx.y * kColTX + threadIdx.x;
     const int nthreads = kColTX * kColTY;
     const int x0 = blockIdx.x * kColTX;
     const int y0 = blockIdx.y * kColRows;
-    for (int i = tid; i < taps; i += nthreads) kw[i] = wts[i];
+    for (int i = tid; i < tp; i += nthreads) kw[i] = i < taps ? wts[i] : 0.0f;
     for (int i = tid; i < 256; i += nthreads) lut[i] = __fdiv_rn((float)i, 255.0f);
-    const int rows = kColRows + 2 * r;
+    const int rows = kColRows + tp - 1;
     const int xg = min(x0 + (int)threadIdx.x, W - 1);
     for (int k = threadIdx.y; k < rows; k += kColTY) {
         int ys = clampi(y0 - r + k, 0, H - 1);
@@ -163,20 +169,20 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
     const int x = x0 + threadIdx.x;
     const int ly = threadIdx.y * kColRPT;  // first local output row
     float acc[kColRPT];
-    float win[kColRPT];
 #pragma unroll
-    for (int j = 0; j < kColRPT; ++j) {
-        acc[j] = 0.0f;
-        win[j] = j < kColRPT - 1 ? tile[(ly + j) * kColTX + threadIdx.x] : 0.0f;
-    }
-    for (int i = 0; i < taps; ++i) {
-        // window rows ly+i .. ly+i+7
-        win[kColRPT - 1] = tile[(ly + i + kColRPT - 1) * kColTX + threadIdx.x];
-        const float k = kw[i];
+    for (int j = 0; j < kColRPT; ++j) acc[j] = 0.0f;
+    const float* col = tile + ly * kColTX + threadIdx.x;
+    for (int i0 = 0; i0 < tp; i0 += 8) {
+        float w[kColRPT + 7];
 #pragma unroll
-        for (int j = 0; j < kColRPT; ++j) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], k));
+        for (int m = 0; m < kColRPT + 7; ++m) w[m] = col[(i0 + m) * kColTX];
+        const float4 ka = *reinterpret_cast<const float4*>(kw + i0);
+        const float4 kb = *reinterpret_cast<const float4*>(kw + i0 + 4);
+        const float k8[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
 #pragma unroll
-        for (int j = 0; j < kColRPT - 1; ++j) win[j] = win[j + 1];
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int j = 0; j < kColRPT; ++j) acc[j] = __fadd_rn(acc[j], __fmul_rn(w[q + j], k8[q]));
     }
     if (x >= W) return;
 #pragma unroll
@@ -345,6 +351,62 @@ __global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride,
     store_level(out + (long long)y * pitch + x, v, norm255(v));
 }
 
+// Both Lanczos3 passes of the 2x resize in one kernel (image 0.25.6
+// vertical_sample then horizontal_sample): a 32 x 32 output tile stages its
+// source window (at most kLzSpan x kLzSpan, checked on the host), runs the
+// vertical pass for the columns the horizontal pass reads, then the
+// horizontal pass; every value is formed exactly as in the two-kernel form.
+constexpr int kLzT = 32, kLzSpan = 80;
+
+template <typename TG>
+__global__ void __launch_bounds__(256) k_lanczos_fused(const TG* __restrict__ src, int src_pitch, TG* __restrict__ dst,
+                                                       int dst_pitch, int nW, int nH, const int* __restrict__ vtab,
+                                                       const float* __restrict__ vw, const int* __restrict__ htab,
+                                                       const float* __restrict__ hw) {
+    __shared__ float in[kLzSpan][kLzSpan];
+    __shared__ float mid[kLzT][kLzSpan];
+    const int* vleft = vtab;
+    const int* vcount = vtab + nH;
+    const int* voff = vtab + 2 * nH;
+    const int* hleft = htab;
+    const int* hcount = htab + nW;
+    const int* hoff = htab + 2 * nW;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ox0 = blockIdx.x * kLzT, oy0 = blockIdx.y * kLzT;
+    const int ox1 = min(ox0 + kLzT, nW), oy1 = min(oy0 + kLzT, nH);
+    const int x_lo = hleft[ox0], x_hi = hleft[ox1 - 1] + hcount[ox1 - 1];
+    const int y_lo = vleft[oy0], y_hi = vleft[oy1 - 1] + vcount[oy1 - 1];
+    const int sw = x_hi - x_lo, sh = y_hi - y_lo;
+    for (int yy = warp; yy < sh; yy += 8) {
+        const TG* row = src + (long long)(y_lo + yy) * src_pitch + x_lo;
+        for (int xx = lane; xx < sw; xx += 32) in[yy][xx] = load_v(row + xx);
+    }
+    __syncthreads();
+    // vertical pass: rows oy0..oy1-1 (one warp per row), columns x_lo..x_hi-1
+    for (int oyl = warp; oyl < oy1 - oy0; oyl += 8) {
+        const int oy = oy0 + oyl;
+        const int l = vleft[oy] - y_lo, c = vcount[oy], o = voff[oy];
+        for (int xx = lane; xx < sw; xx += 32) {
+            float t = 0.0f;
+            for (int i = 0; i < c; ++i) t = __fadd_rn(t, __fmul_rn(in[l + i][xx], vw[o + i]));
+            mid[oyl][xx] = t;
+        }
+    }
+    __syncthreads();
+    // horizontal pass
+    for (int q = tid; q < (oy1 - oy0) * kLzT; q += 256) {
+        const int oyl = q >> 5, oxl = q & 31;
+        const int ox = ox0 + oxl;
+        if (ox >= ox1) continue;
+        const int l = hleft[ox] - x_lo, c = hcount[ox], o = hoff[ox];
+        float t = 0.0f;
+        for (int i = 0; i < c; ++i) t = __fadd_rn(t, __fmul_rn(mid[oyl][l + i], hw[o + i]));
+        t = t < 0.0f ? 0.0f : (t > 255.0f ? 255.0f : t);
+        const int v = (int)roundf(t);
+        store_level(dst + (long long)(oy0 + oyl) * dst_pitch + ox, v, norm255(v));
+    }
+}
+
 // Lanczos3 vertical pass (image 0.25.6 vertical_sample): tmp[oy][x] =
 // sum_i G[left+i][x] * w_i, accumulated from 0 in tap order, kept in f32.
 template <typename TG>
@@ -388,8 +450,7 @@ size_t blur_rows_smem(int W, int r) {
     return sizeof(float) * ((size_t)((taps + 3) & ~3) + (size_t)W + 2 * (size_t)r + 8);
 }
 size_t blur_cols_smem(int r) {
-    int taps = 2 * r + 1;
-    return sizeof(float) * ((size_t)((taps + 3) & ~3) + 256 + (size_t)(kColRows + 2 * r) * kColTX);
+    return sizeof(float) * ((size_t)taps8(r) + 256 + (size_t)(kColRows + taps8(r) - 1) * kColTX);
 }
 
 template <typename TIn>
@@ -471,7 +532,12 @@ int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, int pitch,
 template <typename TG>
 int launch_lanczos(const TG* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst, int dst_pitch,
                    int nW, int nH, const int* vtab, const float* vw, const int* htab, const float* hw,
-                   cudaStream_t st) {
+                   cudaStream_t st, bool fused) {
+    if (fused) {
+        dim3 g((nW + kLzT - 1) / kLzT, (nH + kLzT - 1) / kLzT);
+        k_lanczos_fused<TG><<<g, 256, 0, st>>>(src, src_pitch, dst, dst_pitch, nW, nH, vtab, vw, htab, hw);
+        return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+    }
     // vtab: left[nH], count[nH], woff[nH]; htab: left[nW], count[nW], woff[nW]
     dim3 gv((W + 127) / 128, nH);
     k_lanczos_v<TG><<<gv, 128, 0, st>>>(src, src_pitch, tmp, tmp_pitch, W, nH, vtab, vtab + nH, vtab + 2 * nH, vw);
@@ -504,8 +570,10 @@ template int launch_copy_level<__half>(const __half*, __half*, float*, int, int,
 template int launch_u8_to_level<float>(const uint8_t*, long long, float*, int, int, int, cudaStream_t);
 template int launch_u8_to_level<__half>(const uint8_t*, long long, __half*, int, int, int, cudaStream_t);
 template int launch_lanczos<float>(const float*, int, int, int, float*, int, float*, int, int, int, const int*,
-                                   const float*, const int*, const float*, cudaStream_t);
+                                   const float*, const int*, const float*, cudaStream_t, bool);
 template int launch_lanczos<__half>(const __half*, int, int, int, float*, int, __half*, int, int, int, const int*,
-                                    const float*, const int*, const float*, cudaStream_t);
+                                    const float*, const int*, const float*, cudaStream_t, bool);
+int lanczos_fused_span() { return kLzSpan; }
+int lanczos_fused_tile() { return kLzT; }
 
 }  // namespace sift

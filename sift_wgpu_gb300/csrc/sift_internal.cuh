@@ -25,15 +25,26 @@ constexpr int kMaxOctaves = 16;
 
 using Keypoint = SiftCudaKeypoint;
 
-// Device counters of one run. Zeroed at the start of every run.
-struct Counters {
-    uint32_t n_candidates;
-    uint32_t n_refined;
-    uint32_t n_oriented;
-    uint32_t overflow;   // bit 0 candidates, 1 refined, 2 oriented
-    uint32_t next_ori;   // work queues of the persistent gather kernels
+// Device counters of one run, zeroed at its start. Each octave has its own
+// lists and counters (its detection chain runs as soon as its levels exist);
+// the final keypoints of octave o go after those of octaves 0..o-1.
+struct OctCounters {
+    uint32_t n_cand;    // candidates (find_scale_space_extrema)
+    uint32_t n_ref;     // refined keypoints
+    uint32_t n_ori;     // oriented keypoints
+    uint32_t out_base;  // first output slot of the octave
+    uint32_t next_ori;  // work queues of the persistent gather kernels
     uint32_t next_desc;
     uint32_t pad[2];
+};
+
+struct Counters {
+    uint32_t n_candidates;  // totals (filled by the last octave's chain)
+    uint32_t n_refined;
+    uint32_t n_oriented;    // keypoints in the output
+    uint32_t overflow;      // bit 0 candidates, 2 oriented
+    uint32_t pad[4];
+    OctCounters oct[kMaxOctaves];
 };
 
 // Geometry of one octave in the device arena.
