@@ -35,31 +35,6 @@ struct DogF32 {
         y = clampi(y, 0, H - 1);
         return base[(long long)l * plane + (long long)y * pitch + x];
     }
-    // Stages layers 0..L-1 of the clamped window [x0, x0+TW) x [y0, y0+TH)
-    // into tile[L][TH][TW]; warp w of nw loads rows w, w+nw, ... Windows inside
-    // the plane (x0 % 4 == 0, TW % 4 == 0) go as aligned float4 loads.
-    __device__ __forceinline__ void stage(float* tile, int L, int x0, int y0, int TW, int TH, int warp, int nwarps,
-                                          int lane) const {
-        const bool inner = x0 >= 0 && y0 >= 0 && x0 + TW <= W && y0 + TH <= H && (x0 & 3) == 0 && (TW & 3) == 0 &&
-                           (pitch & 3) == 0;
-        for (int l = 0; l < L; ++l) {
-            const float* pl = base + (long long)l * plane;
-            if (inner) {
-                const int q4 = TW >> 2;
-                for (int q = warp * 32 + lane; q < TH * q4; q += nwarps * 32) {
-                    const int yy = q / q4, xx = (q - yy * q4) * 4;
-                    const float4 v = *reinterpret_cast<const float4*>(pl + (long long)(y0 + yy) * pitch + x0 + xx);
-                    *reinterpret_cast<float4*>(tile + (l * TH + yy) * TW + xx) = v;
-                }
-            } else {
-                for (int yy = warp; yy < TH; yy += nwarps) {
-                    const float* row = pl + (long long)clampi(y0 + yy, 0, H - 1) * pitch;
-                    float* d = tile + (l * TH + yy) * TW;
-                    for (int xx = lane; xx < TW; xx += 32) d[xx] = row[clampi(x0 + xx, 0, W - 1)];
-                }
-            }
-        }
-    }
 };
 
 // DoG recomputed in f32 from f16-stored Gaussian levels:
@@ -76,21 +51,6 @@ struct DogFromG16 {
         float b = __half2float(base[(long long)l * plane + o]);
         return __fsub_rn(__fdiv_rn(a, 255.0f), __fdiv_rn(b, 255.0f));
     }
-    __device__ __forceinline__ void stage(float* tile, int L, int x0, int y0, int TW, int TH, int warp, int nwarps,
-                                          int lane) const {
-        for (int yy = warp; yy < TH; yy += nwarps) {
-            const long long ro = (long long)clampi(y0 + yy, 0, H - 1) * pitch;
-            for (int xx = lane; xx < TW; xx += 32) {
-                const long long o = ro + clampi(x0 + xx, 0, W - 1);
-                float lower = __fdiv_rn(__half2float(base[o]), 255.0f);
-                for (int l = 0; l < L; ++l) {
-                    const float upper = __fdiv_rn(__half2float(base[(long long)(l + 1) * plane + o]), 255.0f);
-                    tile[(l * TH + yy) * TW + xx] = __fsub_rn(upper, lower);
-                    lower = upper;
-                }
-            }
-        }
-    }
 };
 
 template <class Dog>
@@ -104,30 +64,79 @@ __device__ __forceinline__ DogFromG16 make_dog<DogFromG16>(const void* arena, co
     return DogFromG16{(const __half*)arena + od.g_off, od.plane, od.pitch, od.W, od.H};
 }
 
+// DoG staged from the u8 copies of the Gaussian levels of one octave:
+// D_l = lut[G_{l+1}] - lut[G_l] with lut[v] = v/255 in f32, which is the
+// stored f32 DoG bit for bit (src/sift.rs:92-124) at a quarter of the bytes.
+// Stages layers 0..L-1 of the clamped window [x0, x0+TW) x [y0, y0+TH) into
+// tile[L][TH][TW]; windows inside the plane go as aligned 4-byte words, all
+// L+1 levels of a word per thread.
+__device__ __forceinline__ void stage_dog_u8(float* tile, const float* lut, const uint8_t* base, long long plane,
+                                             int pitch, int W, int H, int L, int x0, int y0, int TW, int TH, int tid,
+                                             int nthreads) {
+    const bool inner = x0 >= 0 && y0 >= 0 && x0 + TW <= W && y0 + TH <= H && (x0 & 3) == 0 && (TW & 3) == 0 &&
+                       (pitch & 3) == 0;
+    if (inner) {
+        const int q4 = TW >> 2;
+        for (int q = tid; q < TH * q4; q += nthreads) {
+            const int yy = q / q4, xx = (q - yy * q4) * 4;
+            const uint8_t* p = base + (long long)(y0 + yy) * pitch + x0 + xx;
+            const unsigned b0 = *reinterpret_cast<const unsigned*>(p);
+            float lo0 = lut[b0 & 0xffu], lo1 = lut[(b0 >> 8) & 0xffu], lo2 = lut[(b0 >> 16) & 0xffu],
+                  lo3 = lut[b0 >> 24];
+            float* t = tile + yy * TW + xx;
+#pragma unroll 4
+            for (int l = 0; l < L; ++l) {
+                const unsigned b = *reinterpret_cast<const unsigned*>(p + (long long)(l + 1) * plane);
+                const float u0 = lut[b & 0xffu], u1 = lut[(b >> 8) & 0xffu], u2 = lut[(b >> 16) & 0xffu],
+                            u3 = lut[b >> 24];
+                *reinterpret_cast<float4*>(t + (size_t)l * TH * TW) =
+                    make_float4(__fsub_rn(u0, lo0), __fsub_rn(u1, lo1), __fsub_rn(u2, lo2), __fsub_rn(u3, lo3));
+                lo0 = u0;
+                lo1 = u1;
+                lo2 = u2;
+                lo3 = u3;
+            }
+        }
+    } else {
+        for (int q = tid; q < TH * TW; q += nthreads) {
+            const int yy = q / TW, xx = q - yy * TW;
+            const long long o = (long long)clampi(y0 + yy, 0, H - 1) * pitch + clampi(x0 + xx, 0, W - 1);
+            float lo = lut[base[o]];
+            for (int l = 0; l < L; ++l) {
+                const float up = lut[base[(long long)(l + 1) * plane + o]];
+                tile[(l * TH + yy) * TW + xx] = __fsub_rn(up, lo);
+                lo = up;
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Extrema of one octave, all layers s = 1..S at once. The CTA stages the
 // neighbourhood of its 64 x 16 pixels for every DoG layer 0..S+1 in shared
-// memory (aligned float4 loads for interior tiles; clamped coordinates, as
-// get_pixel_value clamps, at the image border). Each thread owns one column
-// and 4 rows: per layer it forms the horizontal 3-max/3-min of 6 rows once and
-// reuses them for the 3x3 block max/min and the 8-ring max/min of its 4 pixels:
+// memory, formed from the u8 levels (clamped coordinates, as get_pixel_value
+// clamps, at the image border). Each thread owns one column and 4 rows: per
+// layer it forms the horizontal 3-max/3-min of 6 rows once and reuses them for
+// the 3x3 block max/min and the 8-ring max/min of its 4 pixels:
 //   strict max  <=>  v > max(M_{s-1}, M_{s+1}, ring8max_s)
 //   strict min  <=>  v < min(m_{s-1}, m_{s+1}, ring8min_s)
 // which is the reference's 26 strict comparisons (ties reject).
 constexpr int kExTX = 64, kExTY = 16, kExRows = 4, kExMaxLayers = 18;
-constexpr int kExSW = kExTX + 8;  // staged width: x0-4 .. x0+68 (float4 aligned)
+constexpr int kExSW = kExTX + 8;  // staged width: x0-4 .. x0+68 (word aligned)
 constexpr int kExSH = kExTY + 2;
 
-template <class Dog>
-__global__ void __launch_bounds__(256) k_extrema_mask(const void* arena, PyramidDev pyr, int o, int border,
-                                                      uint32_t* __restrict__ words) {
-    extern __shared__ float tile[];  // [layers][kExSH][kExSW]
+__global__ void __launch_bounds__(256) k_extrema_mask(const uint8_t* __restrict__ u8arena,
+                                                      const float* __restrict__ lut255, PyramidDev pyr, int o,
+                                                      int border, uint32_t* __restrict__ words) {
+    extern __shared__ __align__(16) float tile[];  // [layers][kExSH][kExSW], then lut[256]
     const OctaveDev& od = pyr.oct[o];
-    const Dog dog = make_dog<Dog>(arena, od);
     const int W = od.W, H = od.H, nw = od.nw, S = pyr.S, L = S + 2;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int x0 = blockIdx.x * kExTX, y0 = blockIdx.y * kExTY;
-    dog.stage(tile, L, x0 - 4, y0 - 1, kExSW, kExSH, warp, 8, lane);
+    float* lut = tile + L * kExSH * kExSW;
+    lut[tid] = lut255[tid];
+    __syncthreads();
+    stage_dog_u8(tile, lut, u8arena + od.u_off, od.plane, od.pitch, W, H, L, x0 - 4, y0 - 1, kExSW, kExSH, tid, 256);
     __syncthreads();
     const int col = tid & (kExTX - 1);          // 0..63
     const int r0 = (tid >> 6) * kExRows;       // 0, 4, 8, 12
@@ -360,21 +369,17 @@ __global__ void __launch_bounds__(256) k_compact(const uint32_t* __restrict__ ke
 
 // ---- launchers -------------------------------------------------------------
 
-int launch_extrema_mask(int storage, const void* arena, const PyramidDev& pyr, int o, int border, uint32_t* words,
-                        cudaStream_t st) {
+int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
+                        uint32_t* words, cudaStream_t st) {
     const OctaveDev& od = pyr.oct[o];
     if (od.W <= 0 || od.H <= 0) return 0;
     if (pyr.S + 2 > kExMaxLayers) return -1;
     dim3 grid((od.W + kExTX - 1) / kExTX, (od.H + kExTY - 1) / kExTY);
-    const size_t smem = sizeof(float) * (size_t)(pyr.S + 2) * kExSH * kExSW;
-    if (smem > 48 * 1024) {
-        auto k = storage == SIFT_CUDA_STORAGE_F16 ? k_extrema_mask<DogFromG16> : k_extrema_mask<DogF32>;
-        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
-    }
-    if (storage == SIFT_CUDA_STORAGE_F16)
-        k_extrema_mask<DogFromG16><<<grid, 256, smem, st>>>(arena, pyr, o, border, words);
-    else
-        k_extrema_mask<DogF32><<<grid, 256, smem, st>>>(arena, pyr, o, border, words);
+    const size_t smem = sizeof(float) * ((size_t)(pyr.S + 2) * kExSH * kExSW + 256);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_extrema_mask, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return -1;
+    k_extrema_mask<<<grid, 256, smem, st>>>(u8arena, lut255, pyr, o, border, words);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

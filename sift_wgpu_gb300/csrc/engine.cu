@@ -6,6 +6,8 @@
 //              plane pitch x H (pitch = width rounded up to 32 elements), f32
 //              or f16 (u8-valued either way)
 //   DoG arena  (S+2) f32 planes per octave (f32 storage only)
+//   U arena    (S+3) u8 planes per octave: every level as bytes, the input
+//              of the next level, of the resize and of the extrema scan
 //   tmp        one u8 plane for the horizontal blur pass (largest octave)
 //   ltmp       one f32 plane for the vertical Lanczos pass
 //   mask       per octave S x H x ceil(W/32) ballot words of extrema
@@ -34,25 +36,24 @@
 namespace sift {
 
 // launchers (pyramid.cu, detect.cu, describe.cu)
-template <typename TIn>
-int launch_blur_rows(const TIn* in, long long in_pitch, uint8_t* out, int out_pitch, int W, int H, int r,
-                     const float* wts, int round_mode, cudaStream_t st);
 template <typename TG>
-int launch_blur_cols(const uint8_t* tmp, int tmp_pitch, const TG* prev, TG* out, float* dog, int pitch, int W,
-                     int H, int r, const float* wts, int round_mode, cudaStream_t st);
+int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, float* dog, int pitch,
+                      int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
+                      int* launches);
 template <typename TG>
-int launch_copy_level(const TG* prev, TG* out, float* dog, int pitch, int W, int H, cudaStream_t st);
-template <typename TIn, typename TG>
-int launch_blur_level(const TIn* in, long long in_pitch, uint8_t* tmp, TG* out, float* dog, int pitch, int W, int H,
-                      int r, const float* wts, int round_mode, cudaStream_t st, int* launches);
+int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, float* dog, int pitch, int W,
+                      int H, cudaStream_t st);
 template <typename TG>
-int launch_lanczos(const TG* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst, int dst_pitch,
-                   int nW, int nH, const int* vtab, const float* vw, const int* htab, const float* hw,
-                   cudaStream_t st, bool fused);
+int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, uint8_t* out_u8, int pitch, int W, int H,
+                       cudaStream_t st);
+template <typename TG>
+int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst,
+                   uint8_t* dst_u8, int dst_pitch, int nW, int nH, const int* vtab, const float* vw, const int* htab,
+                   const float* hw, cudaStream_t st, bool fused, int* launches);
 int lanczos_fused_span();
 int lanczos_fused_tile();
-int launch_extrema_mask(int storage, const void* arena, const PyramidDev& pyr, int o, int border, uint32_t* words,
-                        cudaStream_t st);
+int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
+                        uint32_t* words, cudaStream_t st);
 int launch_emit(int storage, const void* arena, const PyramidDev& pyr, int o, const uint32_t* words,
                 const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st);
 int launch_refine(int storage, const void* arena, const PyramidDev& pyr, int o, float sigma, float contrast,
@@ -69,9 +70,6 @@ int launch_orient_emit(const Keypoint* refined, int o, Counters* ctr, const floa
 template <typename TG>
 int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
                       uint32_t cap, int grid, cudaStream_t st);
-template <typename TG>
-int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, int pitch, int W, int H, cudaStream_t st);
-
 namespace {
 
 thread_local std::string g_last_error;
@@ -163,7 +161,8 @@ struct Engine {
     bool have_geom = false;
     PyramidDev pyr{};
     long long n_words = 0;
-    size_t g_elems = 0, d_elems = 0, tmp_bytes = 0, ltmp_elems = 0;
+    size_t g_elems = 0, d_elems = 0, u_bytes = 0, tmp_bytes = 0, ltmp_elems = 0;
+    size_t lut_off = 0;  // v / 255 table (256 floats) in d_wts
     LevelBlur base{};
     std::vector<std::vector<LevelBlur>> lv;  // [o][s-1]
     struct LTab {
@@ -180,7 +179,7 @@ struct Engine {
     std::vector<size_t> pb, tb;  // scan-partials and horizontal-pass buffer offsets
     uint32_t cap_cand = 0, cap_ori = 0;
 
-    DevMem d_img, d_G, d_D, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
+    DevMem d_img, d_G, d_D, d_U, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
     DevMem d_words, d_cand_off, d_keep, d_keep_off, d_partials;
     DevMem d_cands, d_refined_at, d_refined, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
     HostPinned h_ctr, h_kps, h_desc;
@@ -303,7 +302,7 @@ struct Engine {
         g.num_octaves = O;
         g.S = S;
         g.levels = S + 3;
-        size_t goff = 0, doff = 0, wbase = 0, tmpb = 0, lt = 0, tmpo = 0;
+        size_t goff = 0, doff = 0, uoff = 0, wbase = 0, tmpb = 0, lt = 0, tmpo = 0;
         std::vector<size_t> tbo(O, 0);
         uint32_t ow = w, oh = h;
         for (int o = 0; o < O; ++o) {
@@ -316,7 +315,9 @@ struct Engine {
             od.g_off = (long long)goff;
             od.d_off = (long long)doff;
             od.word_base = (long long)wbase;
+            od.u_off = (long long)uoff;
             goff += (size_t)od.plane * (S + 3);
+            uoff += (size_t)od.plane * (S + 3);
             doff += f16() ? 0 : (size_t)od.plane * (S + 2);
             wbase += (size_t)S * oh * od.nw;
             tmpb = std::max(tmpb, (size_t)od.pitch * oh);
@@ -343,6 +344,10 @@ struct Engine {
         lv.assign(O, {});
         for (int o = 0; o < O; ++o)
             for (int s = 1; s < S + 3; ++s) lv[o].push_back(add_blur(bp.level[o][s - 1]));
+        // v / 255 in f32 (IEEE division): the normalised level value and the
+        // DoG operands (src/sift.rs:92-124)
+        const size_t lutw = wts.size();
+        for (int v = 0; v < 256; ++v) wts.push_back((float)v / 255.0f);
         // Lanczos tables
         std::vector<int> itab;
         std::vector<float> ftab;
@@ -383,6 +388,7 @@ struct Engine {
         n_words = (long long)wbase;
         CK(d_G.ensure(goff * g_elem_size()), "cudaMalloc(G)");
         if (!f16()) CK(d_D.ensure(doff * sizeof(float)), "cudaMalloc(DoG)");
+        CK(d_U.ensure(uoff + 64), "cudaMalloc(u8 levels)");
         CK(d_tmp.ensure(std::max<size_t>(tmpb, 16)), "cudaMalloc(tmp)");
         CK(d_tmpo.ensure(std::max<size_t>(tmpo, 16)), "cudaMalloc(tmp per octave)");
         CK(d_ltmp.ensure(std::max<size_t>(lt, 4) * sizeof(float)), "cudaMalloc(ltmp)");
@@ -403,6 +409,8 @@ struct Engine {
         pyr = g;
         g_elems = goff;
         d_elems = doff;
+        u_bytes = uoff;
+        lut_off = lutw;
         tmp_bytes = tmpb;
         ltmp_elems = lt;
         tb = tbo;
@@ -466,6 +474,8 @@ struct Engine {
         TG* G = d_G.as<TG>();
         float* D = f16() ? nullptr : d_D.as<float>();
         const float* wts = d_wts.as<float>();
+        const float* lut = wts + lut_off;
+        uint8_t* U = d_U.as<uint8_t>();
         Counters* ctr = d_ctr.as<Counters>();
         const void* arena = f16() ? (const void*)d_G.p : (const void*)d_D.p;
         launches = 0;
@@ -484,15 +494,17 @@ struct Engine {
             const LevelBlur& b = lv[o][s - 1];
             const TG* prev = G + od.g_off + (long long)(s - 1) * od.plane;
             TG* out = G + od.g_off + (long long)s * od.plane;
+            const uint8_t* prev_u8 = U + od.u_off + (long long)(s - 1) * od.plane;
+            uint8_t* out_u8 = U + od.u_off + (long long)s * od.plane;
             float* dog = D ? D + od.d_off + (long long)(s - 1) * od.plane : nullptr;
             if (b.sigma <= 0.0f) {
-                if (ok(launch_copy_level<TG>(prev, out, dog, od.pitch, od.W, od.H, q)))
+                if (ok(launch_copy_level<TG>(prev, prev_u8, out, out_u8, dog, od.pitch, od.W, od.H, q)))
                     return cuda_fail(cudaGetLastError(), "copy level");
                 return 0;
             }
             int nl = 0;
-            if (launch_blur_level<TG, TG>(prev, od.pitch, tmp, out, dog, od.pitch, od.W, od.H, b.radius, wts + b.woff,
-                                          round_mode, q, &nl))
+            if (launch_blur_level<TG>(prev_u8, od.pitch, tmp, out, out_u8, dog, od.pitch, od.W, od.H, b.radius,
+                                      wts + b.woff, lut, round_mode, q, &nl))
                 return cuda_fail(cudaGetLastError(), "blur level");
             launches += nl;
             return 0;
@@ -503,11 +515,12 @@ struct Engine {
             const LTab& t = ltab[o];
             const int* it = d_ltab.as<int>();
             const float* ft = d_lw.as<float>();
-            if (ok(launch_lanczos<TG>(G + od.g_off + (long long)S * od.plane, od.pitch, od.W, od.H, d_ltmp.as<float>(),
-                                      od.pitch, G + nx.g_off, nx.pitch, nx.W, nx.H, it + t.vtab, ft + t.vw,
-                                      it + t.htab, ft + t.hw, st, t.fused)))
+            int nl = 0;
+            if (launch_lanczos<TG>(U + od.u_off + (long long)S * od.plane, od.pitch, od.W, od.H, d_ltmp.as<float>(),
+                                   od.pitch, G + nx.g_off, U + nx.u_off, nx.pitch, nx.W, nx.H, it + t.vtab, ft + t.vw,
+                                   it + t.htab, ft + t.hw, st, t.fused, &nl))
                 return cuda_fail(cudaGetLastError(), "lanczos");
-            if (!t.fused) ++launches;
+            launches += nl;
             return 0;
         };
         // (b)+(c): extrema, ordered candidates, refinement of octave o
@@ -516,8 +529,8 @@ struct Engine {
             OctCounters* oc = &ctr->oct[o];
             uint32_t* partials = d_partials.as<uint32_t>() + pb[o];
             const long long nwo = octave_words(o);
-            if (od.nw > 0 && ok(launch_extrema_mask(opt.storage, arena, pyr, o, (int)p.image_border_width,
-                                                    d_words.as<uint32_t>(), q)))
+            if (od.nw > 0 && ok(launch_extrema_mask(U, lut, pyr, o, (int)p.image_border_width, d_words.as<uint32_t>(),
+                                                    q)))
                 return cuda_fail(cudaGetLastError(), "extrema mask");
             if (scan_exclusive(d_words.as<uint32_t>() + od.word_base, SCAN_POPC,
                                d_cand_off.as<uint32_t>() + od.word_base, (size_t)nwo, nullptr, &oc->n_cand, partials,
@@ -579,12 +592,13 @@ struct Engine {
             // base image (src/sift.rs:1204-1214)
             if (base.sigma > 0.0f) {
                 int nl = 0;
-                if (launch_blur_level<uint8_t, TG>(img, stride, d_tmp.as<uint8_t>(), G + o0.g_off, nullptr, o0.pitch,
-                                                   o0.W, o0.H, base.radius, wts + base.woff, round_mode, st, &nl))
+                if (launch_blur_level<TG>(img, (int)stride, d_tmp.as<uint8_t>(), G + o0.g_off, U + o0.u_off, nullptr,
+                                          o0.pitch, o0.W, o0.H, base.radius, wts + base.woff, lut, round_mode, st,
+                                          &nl))
                     return cuda_fail(cudaGetLastError(), "blur (base)");
                 launches += nl;
             } else {
-                if (ok(launch_u8_to_level<TG>(img, stride, G + o0.g_off, o0.pitch, o0.W, o0.H, st)))
+                if (ok(launch_u8_to_level<TG>(img, stride, G + o0.g_off, U + o0.u_off, o0.pitch, o0.W, o0.H, st)))
                     return cuda_fail(cudaGetLastError(), "base copy");
             }
         }

@@ -8,42 +8,30 @@
 // and every DoG value is bit-identical to the CPU path. Products and sums are
 // rounded one by one (__fmul_rn/__fadd_rn) in the reference's tap order.
 //
+// Every level is written three ways: the u8 plane (1 byte/pixel, what the next
+// level, the resize and the extrema scan read), the stored level in the
+// storage type (f32 v/255 or f16 v, read by the orientation and descriptor
+// stages) and, for f32 storage, the DoG level below it. Nothing in the chain
+// re-reads a 4-byte plane.
+//
 // Kernels
-//   k_blur_rows    horizontal pass, one row per CTA staged in shared memory
-//                  with clamp-to-edge padding; 4 outputs per thread fed by
-//                  16-byte shared loads (sliding window). u8 out.
-//   k_blur_cols    vertical pass on a 32-column tile staged in shared memory;
-//                  8 outputs per thread (sliding window); writes the level and
-//                  the DoG level below it (DoG fused, each scale read once).
-//   k_lanczos_v/h  the 2x Lanczos3 resize between octaves (f32 intermediate).
+//   k_blur_level   both separable passes of a level for r <= 8 (the first two
+//                  octaves at the default sigma): a 64 x 64 tile stages its
+//                  u8 window with 16-byte loads, the horizontal pass goes to
+//                  shared memory, the vertical pass writes level, DoG and u8.
+//   k_blur_rows    horizontal pass for larger radii, one row per CTA. u8 out.
+//   k_blur_cols    vertical pass for larger radii on a 32 x 64 tile.
+//   k_lanczos_fused  the 2x Lanczos3 resize between octaves, both passes.
 #include "sift_internal.cuh"
 
 namespace sift {
 namespace {
 
-// Level storage. An f32 level holds v/255 (the reference's
-// convert_u8_to_f32_gray value, src/sift.rs:92-101) for its u8 value v, so
-// DoG and the gradient stages read it directly; f16 holds v itself (v/255 is
-// not exact in f16). load_v returns v as a float for the blur and resize
-// passes: rint(255 * (v/255)) == v for every u8 v.
-template <typename T>
-__device__ __forceinline__ float load_v(const T* p);
-template <>
-__device__ __forceinline__ float load_v<float>(const float* p) {
-    return rint_pos(__fmul_rn(*p, 255.0f));
-}
-template <>
-__device__ __forceinline__ float load_v<__half>(const __half* p) {
-    return __half2float(*p);
-}
-template <>
-__device__ __forceinline__ float load_v<uint8_t>(const uint8_t* p) {
-    return float_of_u8(*p);
-}
-
 // v / 255 in f32 (IEEE division, as the reference computes it).
 __device__ __forceinline__ float norm255(int v) { return __fdiv_rn((float)v, 255.0f); }
 
+// Level storage: f32 holds v/255 (the reference's convert_u8_to_f32_gray
+// value, src/sift.rs:92-101), f16 holds v (v/255 is not exact in f16).
 template <typename T>
 __device__ __forceinline__ void store_level(T* p, int v, float vn);
 template <>
@@ -55,27 +43,49 @@ __device__ __forceinline__ void store_level<__half>(__half* p, int v, float) {
     *p = __int2half_rn(v);
 }
 
+__device__ __forceinline__ void unpack16(const uint4 b, float* v) {
+    const unsigned w[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        v[4 * e + 0] = float_of_u8(w[e] & 0xffu);
+        v[4 * e + 1] = float_of_u8((w[e] >> 8) & 0xffu);
+        v[4 * e + 2] = float_of_u8((w[e] >> 16) & 0xffu);
+        v[4 * e + 3] = float_of_u8(w[e] >> 24);
+    }
+}
+
+__device__ __forceinline__ int clamp_u8_any(float a, int round_mode) {
+    return round_mode ? clamp_u8(a, 1) : int_of(clamp_u8f(a));
+}
+
 constexpr int kRowThreads = 128;
 
 // One row per CTA. Shared layout: weights[taps] (padded to a multiple of 4),
 // then the row with r clamp-to-edge pixels on each side and 8 floats of slack.
-template <typename TIn>
-__global__ void __launch_bounds__(kRowThreads) k_blur_rows(const TIn* __restrict__ in, long long in_pitch,
-                                                           uint8_t* __restrict__ out, int out_pitch, int W,
-                                                           int r, const float* __restrict__ wts,
-                                                           int round_mode) {
+__global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __restrict__ in, int in_pitch,
+                                                           uint8_t* __restrict__ out, int out_pitch, int W, int r,
+                                                           const float* __restrict__ wts, int round_mode) {
     extern __shared__ __align__(16) float sm[];
     const int taps = 2 * r + 1;
     const int wpad = (taps + 3) & ~3;
     float* kw = sm;
     float* row = sm + wpad;
     const int y = blockIdx.x;
-    const TIn* src = in + (long long)y * in_pitch;
+    const uint8_t* src = in + (long long)y * in_pitch;
     for (int i = threadIdx.x; i < wpad; i += blockDim.x) kw[i] = i < taps ? wts[i] : 0.0f;
     const int padded = W + 2 * r;
+    const int nv = (in_pitch & 15) == 0 ? (W >> 4) : 0;  // 16-byte vectors of the interior
+#pragma unroll 2
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+        float v[16];
+        unpack16(*reinterpret_cast<const uint4*>(src + 16 * k), v);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) row[r + 16 * k + e] = v[e];
+    }
     for (int j = threadIdx.x; j < padded + 8; j += blockDim.x) {
-        int xs = clampi(j - r, 0, W - 1);
-        row[j] = load_v(src + xs);
+        const int xs = j - r;
+        if (xs >= 0 && xs < 16 * nv) continue;
+        row[j] = float_of_u8(src[clampi(xs, 0, W - 1)]);
     }
     __syncthreads();
     uint8_t* dst = out + (long long)y * out_pitch;
@@ -87,22 +97,18 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const TIn* __restrict
         for (; i + 4 <= taps; i += 4) {
             const float4 B = *reinterpret_cast<const float4*>(base + i + 4);
             const float4 K = *reinterpret_cast<const float4*>(kw + i);
-            // tap i+0: A.x A.y A.z A.w
             a0 = __fadd_rn(a0, __fmul_rn(A.x, K.x));
             a1 = __fadd_rn(a1, __fmul_rn(A.y, K.x));
             a2 = __fadd_rn(a2, __fmul_rn(A.z, K.x));
             a3 = __fadd_rn(a3, __fmul_rn(A.w, K.x));
-            // tap i+1: A.y A.z A.w B.x
             a0 = __fadd_rn(a0, __fmul_rn(A.y, K.y));
             a1 = __fadd_rn(a1, __fmul_rn(A.z, K.y));
             a2 = __fadd_rn(a2, __fmul_rn(A.w, K.y));
             a3 = __fadd_rn(a3, __fmul_rn(B.x, K.y));
-            // tap i+2: A.z A.w B.x B.y
             a0 = __fadd_rn(a0, __fmul_rn(A.z, K.z));
             a1 = __fadd_rn(a1, __fmul_rn(A.w, K.z));
             a2 = __fadd_rn(a2, __fmul_rn(B.x, K.z));
             a3 = __fadd_rn(a3, __fmul_rn(B.y, K.z));
-            // tap i+3: A.w B.x B.y B.z
             a0 = __fadd_rn(a0, __fmul_rn(A.w, K.w));
             a1 = __fadd_rn(a1, __fmul_rn(B.x, K.w));
             a2 = __fadd_rn(a2, __fmul_rn(B.y, K.w));
@@ -116,10 +122,8 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const TIn* __restrict
             a2 = __fadd_rn(a2, __fmul_rn(base[i + 2], k));
             a3 = __fadd_rn(a3, __fmul_rn(base[i + 3], k));
         }
-        const int v0 = round_mode ? clamp_u8(a0, 1) : int_of(clamp_u8f(a0));
-        const int v1 = round_mode ? clamp_u8(a1, 1) : int_of(clamp_u8f(a1));
-        const int v2 = round_mode ? clamp_u8(a2, 1) : int_of(clamp_u8f(a2));
-        const int v3 = round_mode ? clamp_u8(a3, 1) : int_of(clamp_u8f(a3));
+        const int v0 = clamp_u8_any(a0, round_mode), v1 = clamp_u8_any(a1, round_mode);
+        const int v2 = clamp_u8_any(a2, round_mode), v3 = clamp_u8_any(a3, round_mode);
         dst[x0] = (uint8_t)v0;
         if (x0 + 1 < W) dst[x0 + 1] = (uint8_t)v1;
         if (x0 + 2 < W) dst[x0 + 2] = (uint8_t)v2;
@@ -137,16 +141,17 @@ constexpr int kColRows = kColTY * kColRPT;  // output rows per CTA
 // (64 + taps8 - 1) rows x 32 floats of the u8 intermediate with
 // clamp-to-edge rows. Taps go in unrolled groups of 8 from a 15-row register
 // window; the zero taps at the end add +0 to a non-negative sum, which leaves
-// it unchanged. Writes level s (TG) and, when dog != nullptr,
+// it unchanged. Writes level s (TG and u8) and, when dog != nullptr,
 // DoG(s-1) = G_s/255 - G_{s-1}/255 (src/sift.rs:92-124).
 __host__ __device__ constexpr int taps8(int r) { return ((2 * r + 1) + 7) & ~7; }
 
 template <typename TG>
 __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __restrict__ tmp, int tmp_pitch,
-                                                             const TG* __restrict__ prev, TG* __restrict__ out,
-                                                             float* __restrict__ dog, int pitch, int W, int H,
-                                                             int r, const float* __restrict__ wts,
-                                                             int round_mode) {
+                                                             const uint8_t* __restrict__ prev_u8,
+                                                             TG* __restrict__ out, uint8_t* __restrict__ out_u8,
+                                                             float* __restrict__ dog, int pitch, int W, int H, int r,
+                                                             const float* __restrict__ wts,
+                                                             const float* __restrict__ lut255, int round_mode) {
     extern __shared__ __align__(16) float sm[];
     const int taps = 2 * r + 1;
     const int tp = taps8(r);
@@ -158,12 +163,26 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
     const int x0 = blockIdx.x * kColTX;
     const int y0 = blockIdx.y * kColRows;
     for (int i = tid; i < tp; i += nthreads) kw[i] = i < taps ? wts[i] : 0.0f;
-    for (int i = tid; i < 256; i += nthreads) lut[i] = __fdiv_rn((float)i, 255.0f);
+    for (int i = tid; i < 256; i += nthreads) lut[i] = lut255[i];
     const int rows = kColRows + tp - 1;
-    const int xg = min(x0 + (int)threadIdx.x, W - 1);
-    for (int k = threadIdx.y; k < rows; k += kColTY) {
-        int ys = clampi(y0 - r + k, 0, H - 1);
-        tile[k * kColTX + threadIdx.x] = float_of_u8(tmp[(long long)ys * tmp_pitch + xg]);
+    if (x0 + kColTX <= W && (tmp_pitch & 15) == 0) {
+        // two 16-byte loads per row, all rows of the tile in flight
+#pragma unroll 4
+        for (int q = tid; q < rows * 2; q += nthreads) {
+            const int k = q >> 1, h = q & 1;
+            const int ys = clampi(y0 - r + k, 0, H - 1);
+            float v[16];
+            unpack16(*reinterpret_cast<const uint4*>(tmp + (long long)ys * tmp_pitch + x0 + 16 * h), v);
+            float* d = tile + k * kColTX + 16 * h;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) d[e] = v[e];
+        }
+    } else {
+        const int xg = min(x0 + (int)threadIdx.x, W - 1);
+        for (int k = threadIdx.y; k < rows; k += kColTY) {
+            int ys = clampi(y0 - r + k, 0, H - 1);
+            tile[k * kColTX + threadIdx.x] = float_of_u8(tmp[(long long)ys * tmp_pitch + xg]);
+        }
     }
     __syncthreads();
     const int x = x0 + threadIdx.x;
@@ -189,13 +208,11 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
     for (int j = 0; j < kColRPT; ++j) {
         const int y = y0 + ly + j;
         if (y < H) {
-            const int v = round_mode ? clamp_u8(acc[j], 1) : int_of(clamp_u8f(acc[j]));
+            const int v = clamp_u8_any(acc[j], round_mode);
             const long long o = (long long)y * pitch + x;
             store_level(out + o, v, lut[v]);
-            if (dog) {
-                const int pv = int_of(load_v(prev + o));
-                dog[o] = __fsub_rn(lut[v], lut[pv]);
-            }
+            out_u8[o] = (uint8_t)v;
+            if (dog) dog[o] = __fsub_rn(lut[v], lut[prev_u8[o]]);
         }
     }
 }
@@ -203,11 +220,11 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
 // ---------------------------------------------------------------------------
 // Fused level kernel: both separable passes of one level in one launch. The
 // CTA stages the (64 + 2r) x (64 + 2r) clamp-to-edge neighbourhood of its
-// 64 x 64 output tile as u8 values in f32, runs the horizontal pass for all
-// 64 + 2r rows into shared memory (u8-truncated like imageproc's intermediate
-// image), then the vertical pass, and writes the level and the DoG below it;
-// the previous level's value for the DoG comes from the staged tile, so each
-// scale is read from memory once.
+// 64 x 64 output tile from the previous level's u8 plane, runs the horizontal
+// pass for all 64 + 2r rows into shared memory (u8-truncated like
+// imageproc's intermediate image), then the vertical pass, and writes the
+// level, its u8 plane and the DoG below it; the previous level's value for the
+// DoG comes from the staged tile, so each scale is read once, as bytes.
 constexpr int kFTX = 64, kFTY = 64, kFThreads = 256;
 constexpr int kFColRows = 16;  // vertical-pass outputs per thread
 
@@ -221,11 +238,12 @@ size_t blur_fused_smem(int r) {
 
 // R > 0: the radius is a compile-time constant and every tap loop unrolls
 // (the vertical window then slides by register renaming); R == 0: run time.
-template <typename TIn, typename TG, int R>
-__global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict__ in, long long in_pitch,
-                                                          TG* __restrict__ out, float* __restrict__ dog, int pitch,
-                                                          int W, int H, int r_rt, const float* __restrict__ wts,
-                                                          int round_mode) {
+template <typename TG, int R>
+__global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restrict__ in, int in_pitch,
+                                                          TG* __restrict__ out, uint8_t* __restrict__ out_u8,
+                                                          float* __restrict__ dog, int pitch, int W, int H, int r_rt,
+                                                          const float* __restrict__ wts,
+                                                          const float* __restrict__ lut255, int round_mode) {
     extern __shared__ __align__(16) float sm[];
     const int r = R > 0 ? R : r_rt;
     const int taps = 2 * r + 1;
@@ -239,11 +257,33 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict_
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * kFTX, y0 = blockIdx.y * kFTY;
     for (int i = tid; i < wpad; i += kFThreads) kw[i] = i < taps ? wts[i] : 0.0f;
-    for (int i = tid; i < 256; i += kFThreads) lut[i] = __fdiv_rn((float)i, 255.0f);
-    for (int yy = warp; yy < RH; yy += kFThreads / 32) {
-        const TIn* row = in + (long long)clampi(y0 - r + yy, 0, H - 1) * in_pitch;
-        float* d = src + (size_t)yy * RW;
-        for (int xx = lane; xx < RW; xx += 32) d[xx] = load_v(row + clampi(x0 - r + xx, 0, W - 1));
+    for (int i = tid; i < 256; i += kFThreads) lut[i] = lut255[i];
+    // Stage rows y0-r .. y0+63+r, columns x0-r .. (RW columns). Interior tiles
+    // load the bytes [x0-16, x0+80) of every row as six 16-byte vectors, all
+    // issued before use; border tiles clamp per element.
+    const bool interior = R > 0 && r <= 16 && x0 >= 16 && x0 + 80 <= W && y0 >= r && y0 + kFTY + r <= H &&
+                          (in_pitch & 15) == 0;
+    if (interior) {
+        constexpr int Q = 6;
+        const uint8_t* org = in + (long long)(y0 - r) * in_pitch + (x0 - 16);
+#pragma unroll 2
+        for (int q = tid; q < RH * Q; q += kFThreads) {
+            const int yy = q / Q, k = q - yy * Q;
+            float v[16];
+            unpack16(*reinterpret_cast<const uint4*>(org + (long long)yy * in_pitch + 16 * k), v);
+            float* d = src + (size_t)yy * RW;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int xx = 16 * k + e - 16 + r;
+                if (xx >= 0 && xx < RW) d[xx] = v[e];
+            }
+        }
+    } else {
+        for (int yy = warp; yy < RH; yy += kFThreads / 32) {
+            const uint8_t* row = in + (long long)clampi(y0 - r + yy, 0, H - 1) * in_pitch;
+            float* d = src + (size_t)yy * RW;
+            for (int xx = lane; xx < RW; xx += 32) d[xx] = float_of_u8(row[clampi(x0 - r + xx, 0, W - 1)]);
+        }
     }
     __syncthreads();
     // horizontal pass: 16 threads per row, 4 outputs each (float4 sliding window)
@@ -316,9 +356,10 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict_
     for (int j = 0; j < kFColRows; ++j) {
         const int y = y0 + ly + j;
         if (y < H) {
-            const int v = round_mode ? clamp_u8(acc[j], 1) : int_of(clamp_u8f(acc[j]));
+            const int v = clamp_u8_any(acc[j], round_mode);
             const long long o = (long long)y * pitch + x;
             store_level(out + o, v, lut[v]);
+            out_u8[o] = (uint8_t)v;
             if (dog) {
                 const int pv = int_of(src[(size_t)(r + ly + j) * RW + r + col]);
                 dog[o] = __fsub_rn(lut[v], lut[pv]);
@@ -330,25 +371,28 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const TIn* __restrict_
 // A level whose blur increment is below 1e-4 is a copy of the previous one
 // (src/sift.rs:152-154); its DoG is then exactly zero.
 template <typename TG>
-__global__ void k_copy_level(const TG* __restrict__ prev, TG* __restrict__ out, float* __restrict__ dog,
-                             int pitch, int W, int H) {
+__global__ void k_copy_level(const TG* __restrict__ prev, const uint8_t* __restrict__ prev_u8, TG* __restrict__ out,
+                             uint8_t* __restrict__ out_u8, float* __restrict__ dog, int pitch, int W, int H) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x >= W) return;
     long long o = (long long)y * pitch + x;
     out[o] = prev[o];
+    out_u8[o] = prev_u8[o];
     if (dog) dog[o] = 0.0f;
 }
 
 // Base level without a blur (sigma <= assumed_blur, src/sift.rs:1204-1214).
 template <typename TG>
-__global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride, TG* __restrict__ out, int pitch,
-                              int W, int H) {
+__global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride, TG* __restrict__ out,
+                              uint8_t* __restrict__ out_u8, int pitch, int W, int H) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x >= W) return;
     const int v = (int)img[(long long)y * stride + x];
-    store_level(out + (long long)y * pitch + x, v, norm255(v));
+    const long long o = (long long)y * pitch + x;
+    store_level(out + o, v, norm255(v));
+    out_u8[o] = (uint8_t)v;
 }
 
 // Both Lanczos3 passes of the 2x resize in one kernel (image 0.25.6
@@ -359,7 +403,8 @@ __global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride,
 constexpr int kLzT = 32, kLzSpan = 80;
 
 template <typename TG>
-__global__ void __launch_bounds__(256) k_lanczos_fused(const TG* __restrict__ src, int src_pitch, TG* __restrict__ dst,
+__global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict__ src, int src_pitch,
+                                                       TG* __restrict__ dst, uint8_t* __restrict__ dst_u8,
                                                        int dst_pitch, int nW, int nH, const int* __restrict__ vtab,
                                                        const float* __restrict__ vw, const int* __restrict__ htab,
                                                        const float* __restrict__ hw) {
@@ -377,9 +422,18 @@ __global__ void __launch_bounds__(256) k_lanczos_fused(const TG* __restrict__ sr
     const int x_lo = hleft[ox0], x_hi = hleft[ox1 - 1] + hcount[ox1 - 1];
     const int y_lo = vleft[oy0], y_hi = vleft[oy1 - 1] + vcount[oy1 - 1];
     const int sw = x_hi - x_lo, sh = y_hi - y_lo;
-    for (int yy = warp; yy < sh; yy += 8) {
-        const TG* row = src + (long long)(y_lo + yy) * src_pitch + x_lo;
-        for (int xx = lane; xx < sw; xx += 32) in[yy][xx] = load_v(row + xx);
+    // stage: aligned 4-byte words covering [x_lo, x_hi) of each source row
+    const int xa = x_lo & ~3;
+    const int nq = (x_hi - xa + 3) >> 2;
+    for (int q = tid; q < sh * nq; q += 256) {
+        const int yy = q / nq, k = q - yy * nq;
+        const uint8_t* p = src + (long long)(y_lo + yy) * src_pitch + xa + 4 * k;
+        const unsigned b = *reinterpret_cast<const unsigned*>(p);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int xx = xa + 4 * k + e - x_lo;
+            if (xx >= 0 && xx < sw) in[yy][xx] = float_of_u8((b >> (8 * e)) & 0xffu);
+        }
     }
     __syncthreads();
     // vertical pass: rows oy0..oy1-1 (one warp per row), columns x_lo..x_hi-1
@@ -403,14 +457,16 @@ __global__ void __launch_bounds__(256) k_lanczos_fused(const TG* __restrict__ sr
         for (int i = 0; i < c; ++i) t = __fadd_rn(t, __fmul_rn(mid[oyl][l + i], hw[o + i]));
         t = t < 0.0f ? 0.0f : (t > 255.0f ? 255.0f : t);
         const int v = (int)roundf(t);
-        store_level(dst + (long long)(oy0 + oyl) * dst_pitch + ox, v, norm255(v));
+        const long long od = (long long)(oy0 + oyl) * dst_pitch + ox;
+        store_level(dst + od, v, norm255(v));
+        dst_u8[od] = (uint8_t)v;
     }
 }
 
 // Lanczos3 vertical pass (image 0.25.6 vertical_sample): tmp[oy][x] =
 // sum_i G[left+i][x] * w_i, accumulated from 0 in tap order, kept in f32.
-template <typename TG>
-__global__ void k_lanczos_v(const TG* __restrict__ src, int src_pitch, float* __restrict__ dst, int dst_pitch,
+// Used when a tile's source window would not fit the fused kernel.
+__global__ void k_lanczos_v(const uint8_t* __restrict__ src, int src_pitch, float* __restrict__ dst, int dst_pitch,
                             int W, int nH, const int* __restrict__ left, const int* __restrict__ count,
                             const int* __restrict__ woff, const float* __restrict__ w) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -419,16 +475,17 @@ __global__ void k_lanczos_v(const TG* __restrict__ src, int src_pitch, float* __
     const int l = left[oy], c = count[oy], o = woff[oy];
     float t = 0.0f;
     for (int i = 0; i < c; ++i)
-        t = __fadd_rn(t, __fmul_rn(load_v(src + (long long)(l + i) * src_pitch + x), w[o + i]));
+        t = __fadd_rn(t, __fmul_rn(float_of_u8(src[(long long)(l + i) * src_pitch + x]), w[o + i]));
     dst[(long long)oy * dst_pitch + x] = t;
 }
 
 // Lanczos3 horizontal pass (image 0.25.6 horizontal_sample): clamp to
 // [0, 255], round half away from zero, store as the next octave's base level.
 template <typename TG>
-__global__ void k_lanczos_h(const float* __restrict__ src, int src_pitch, TG* __restrict__ dst, int dst_pitch,
-                            int nW, int nH, const int* __restrict__ left, const int* __restrict__ count,
-                            const int* __restrict__ woff, const float* __restrict__ w) {
+__global__ void k_lanczos_h(const float* __restrict__ src, int src_pitch, TG* __restrict__ dst,
+                            uint8_t* __restrict__ dst_u8, int dst_pitch, int nW, int nH, const int* __restrict__ left,
+                            const int* __restrict__ count, const int* __restrict__ woff,
+                            const float* __restrict__ w) {
     const int ox = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
     if (ox >= nW || y >= nH) return;
@@ -438,7 +495,9 @@ __global__ void k_lanczos_h(const float* __restrict__ src, int src_pitch, TG* __
     for (int i = 0; i < c; ++i) t = __fadd_rn(t, __fmul_rn(row[l + i], w[o + i]));
     t = t < 0.0f ? 0.0f : (t > 255.0f ? 255.0f : t);
     const int v = (int)roundf(t);
-    store_level(dst + (long long)y * dst_pitch + ox, v, norm255(v));
+    const long long od = (long long)y * dst_pitch + ox;
+    store_level(dst + od, v, norm255(v));
+    dst_u8[od] = (uint8_t)v;
 }
 
 }  // namespace
@@ -453,127 +512,97 @@ size_t blur_cols_smem(int r) {
     return sizeof(float) * ((size_t)taps8(r) + 256 + (size_t)(kColRows + taps8(r) - 1) * kColTX);
 }
 
-template <typename TIn>
-int launch_blur_rows(const TIn* in, long long in_pitch, uint8_t* out, int out_pitch, int W, int H, int r,
-                     const float* wts, int round_mode, cudaStream_t st) {
-    size_t smem = blur_rows_smem(W, r);
-    if (smem > 48 * 1024) {
-        if (cudaFuncSetAttribute(k_blur_rows<TIn>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-            return -1;
-    }
-    k_blur_rows<TIn><<<H, kRowThreads, smem, st>>>(in, in_pitch, out, out_pitch, W, r, wts, round_mode);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+static int set_smem(const void* k, size_t smem) {
+    if (smem <= 48 * 1024) return 0;
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess ? 0 : -1;
 }
 
+// One level from the previous level's u8 plane: fused when r <= 8 (its
+// horizontal pass recomputes a 2r-row halo per 64-row tile), else the two
+// separable passes, which spread a small octave over many CTAs.
 template <typename TG>
-int launch_blur_cols(const uint8_t* tmp, int tmp_pitch, const TG* prev, TG* out, float* dog, int pitch, int W,
-                     int H, int r, const float* wts, int round_mode, cudaStream_t st) {
-    size_t smem = blur_cols_smem(r);
-    if (smem > 48 * 1024) {
-        if (cudaFuncSetAttribute(k_blur_cols<TG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-            return -1;
-    }
-    dim3 grid((W + kColTX - 1) / kColTX, (H + kColRows - 1) / kColRows);
-    k_blur_cols<TG><<<grid, dim3(kColTX, kColTY), smem, st>>>(tmp, tmp_pitch, prev, out, dog, pitch, W, H, r, wts,
-                                                            round_mode);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
-}
-
-// Fused level when its tile fits in shared memory, else the two passes.
-template <typename TIn, typename TG>
-int launch_blur_level(const TIn* in, long long in_pitch, uint8_t* tmp, TG* out, float* dog, int pitch, int W, int H,
-                      int r, const float* wts, int round_mode, cudaStream_t st, int* launches) {
-    // Fused only for small radii: its horizontal pass recomputes a 2r-row halo
-    // per 64-row tile. Large radii (the blur grows 2^o per octave) go to the
-    // two separable passes, which spread a small octave over many CTAs.
+int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, float* dog, int pitch,
+                      int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
+                      int* launches) {
     const size_t smem = blur_fused_smem(r);
     if (r <= 8 && smem <= 160 * 1024) {
-        void (*kern)(const TIn*, long long, TG*, float*, int, int, int, int, const float*, int);
+        void (*kern)(const uint8_t*, int, TG*, uint8_t*, float*, int, int, int, int, const float*, const float*, int);
         switch (r) {
-            case 1: kern = k_blur_level<TIn, TG, 1>; break;
-            case 2: kern = k_blur_level<TIn, TG, 2>; break;
-            case 3: kern = k_blur_level<TIn, TG, 3>; break;
-            case 4: kern = k_blur_level<TIn, TG, 4>; break;
-            case 5: kern = k_blur_level<TIn, TG, 5>; break;
-            case 6: kern = k_blur_level<TIn, TG, 6>; break;
-            case 7: kern = k_blur_level<TIn, TG, 7>; break;
-            case 8: kern = k_blur_level<TIn, TG, 8>; break;
-            default: kern = k_blur_level<TIn, TG, 0>; break;
+            case 1: kern = k_blur_level<TG, 1>; break;
+            case 2: kern = k_blur_level<TG, 2>; break;
+            case 3: kern = k_blur_level<TG, 3>; break;
+            case 4: kern = k_blur_level<TG, 4>; break;
+            case 5: kern = k_blur_level<TG, 5>; break;
+            case 6: kern = k_blur_level<TG, 6>; break;
+            case 7: kern = k_blur_level<TG, 7>; break;
+            case 8: kern = k_blur_level<TG, 8>; break;
+            default: kern = k_blur_level<TG, 0>; break;
         }
-        if (smem > 48 * 1024 &&
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return -1;
+        if (set_smem((const void*)kern, smem)) return -1;
         dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
-        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, dog, pitch, W, H, r, wts, round_mode);
+        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, out_u8, dog, pitch, W, H, r, wts, lut255, round_mode);
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
-    if (launch_blur_rows<TIn>(in, in_pitch, tmp, pitch, W, H, r, wts, round_mode, st)) return -1;
+    const size_t rs = blur_rows_smem(W, r), cs = blur_cols_smem(r);
+    if (set_smem((const void*)k_blur_rows, rs) || set_smem((const void*)k_blur_cols<TG>, cs)) return -1;
+    k_blur_rows<<<H, kRowThreads, rs, st>>>(in, in_pitch, tmp, pitch, W, r, wts, round_mode);
+    dim3 grid((W + kColTX - 1) / kColTX, (H + kColRows - 1) / kColRows);
+    k_blur_cols<TG><<<grid, dim3(kColTX, kColTY), cs, st>>>(tmp, pitch, in, out, out_u8, dog, pitch, W, H, r, wts,
+                                                            lut255, round_mode);
     *launches += 2;
-    return launch_blur_cols<TG>(tmp, pitch, (const TG*)in, out, dog, pitch, W, H, r, wts, round_mode, st);
-}
-
-template <typename TG>
-int launch_copy_level(const TG* prev, TG* out, float* dog, int pitch, int W, int H, cudaStream_t st) {
-    dim3 grid((W + 255) / 256, H);
-    k_copy_level<TG><<<grid, 256, 0, st>>>(prev, out, dog, pitch, W, H);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 template <typename TG>
-int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, int pitch, int W, int H, cudaStream_t st) {
+int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, float* dog, int pitch, int W,
+                      int H, cudaStream_t st) {
     dim3 grid((W + 255) / 256, H);
-    k_u8_to_level<TG><<<grid, 256, 0, st>>>(img, stride, out, pitch, W, H);
+    k_copy_level<TG><<<grid, 256, 0, st>>>(prev, prev_u8, out, out_u8, dog, pitch, W, H);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 template <typename TG>
-int launch_lanczos(const TG* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst, int dst_pitch,
-                   int nW, int nH, const int* vtab, const float* vw, const int* htab, const float* hw,
-                   cudaStream_t st, bool fused) {
+int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, uint8_t* out_u8, int pitch, int W, int H,
+                       cudaStream_t st) {
+    dim3 grid((W + 255) / 256, H);
+    k_u8_to_level<TG><<<grid, 256, 0, st>>>(img, stride, out, out_u8, pitch, W, H);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <typename TG>
+int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst,
+                   uint8_t* dst_u8, int dst_pitch, int nW, int nH, const int* vtab, const float* vw, const int* htab,
+                   const float* hw, cudaStream_t st, bool fused, int* launches) {
     if (fused) {
         dim3 g((nW + kLzT - 1) / kLzT, (nH + kLzT - 1) / kLzT);
-        k_lanczos_fused<TG><<<g, 256, 0, st>>>(src, src_pitch, dst, dst_pitch, nW, nH, vtab, vw, htab, hw);
+        k_lanczos_fused<TG><<<g, 256, 0, st>>>(src, src_pitch, dst, dst_u8, dst_pitch, nW, nH, vtab, vw, htab, hw);
+        *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
-    // vtab: left[nH], count[nH], woff[nH]; htab: left[nW], count[nW], woff[nW]
     dim3 gv((W + 127) / 128, nH);
-    k_lanczos_v<TG><<<gv, 128, 0, st>>>(src, src_pitch, tmp, tmp_pitch, W, nH, vtab, vtab + nH, vtab + 2 * nH, vw);
+    k_lanczos_v<<<gv, 128, 0, st>>>(src, src_pitch, tmp, tmp_pitch, W, nH, vtab, vtab + nH, vtab + 2 * nH, vw);
     dim3 gh((nW + 127) / 128, nH);
-    k_lanczos_h<TG><<<gh, 128, 0, st>>>(tmp, tmp_pitch, dst, dst_pitch, nW, nH, htab, htab + nW, htab + 2 * nW, hw);
+    k_lanczos_h<TG><<<gh, 128, 0, st>>>(tmp, tmp_pitch, dst, dst_u8, dst_pitch, nW, nH, htab, htab + nW,
+                                        htab + 2 * nW, hw);
     (void)H;
+    *launches += 2;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-template int launch_blur_rows<uint8_t>(const uint8_t*, long long, uint8_t*, int, int, int, int, const float*, int,
-                                       cudaStream_t);
-template int launch_blur_rows<float>(const float*, long long, uint8_t*, int, int, int, int, const float*, int,
-                                     cudaStream_t);
-template int launch_blur_rows<__half>(const __half*, long long, uint8_t*, int, int, int, int, const float*, int,
-                                      cudaStream_t);
-template int launch_blur_cols<float>(const uint8_t*, int, const float*, float*, float*, int, int, int, int,
-                                     const float*, int, cudaStream_t);
-template int launch_blur_cols<__half>(const uint8_t*, int, const __half*, __half*, float*, int, int, int, int,
-                                      const float*, int, cudaStream_t);
-template int launch_blur_level<uint8_t, float>(const uint8_t*, long long, uint8_t*, float*, float*, int, int, int,
-                                              int, const float*, int, cudaStream_t, int*);
-template int launch_blur_level<uint8_t, __half>(const uint8_t*, long long, uint8_t*, __half*, float*, int, int, int,
-                                               int, const float*, int, cudaStream_t, int*);
-template int launch_blur_level<float, float>(const float*, long long, uint8_t*, float*, float*, int, int, int, int,
-                                            const float*, int, cudaStream_t, int*);
-template int launch_blur_level<__half, __half>(const __half*, long long, uint8_t*, __half*, float*, int, int, int,
-                                              int, const float*, int, cudaStream_t, int*);
-template int launch_copy_level<float>(const float*, float*, float*, int, int, int, cudaStream_t);
-template int launch_copy_level<__half>(const __half*, __half*, float*, int, int, int, cudaStream_t);
-template int launch_u8_to_level<float>(const uint8_t*, long long, float*, int, int, int, cudaStream_t);
-template int launch_u8_to_level<__half>(const uint8_t*, long long, __half*, int, int, int, cudaStream_t);
-template int launch_lanczos<float>(const float*, int, int, int, float*, int, float*, int, int, int, const int*,
-                                   const float*, const int*, const float*, cudaStream_t, bool);
-template int launch_lanczos<__half>(const __half*, int, int, int, float*, int, __half*, int, int, int, const int*,
-                                    const float*, const int*, const float*, cudaStream_t, bool);
 int lanczos_fused_span() { return kLzSpan; }
 int lanczos_fused_tile() { return kLzT; }
+
+#define SIFT_INST(TG)                                                                                              \
+    template int launch_blur_level<TG>(const uint8_t*, int, uint8_t*, TG*, uint8_t*, float*, int, int, int, int,   \
+                                       const float*, const float*, int, cudaStream_t, int*);                       \
+    template int launch_copy_level<TG>(const TG*, const uint8_t*, TG*, uint8_t*, float*, int, int, int,            \
+                                       cudaStream_t);                                                              \
+    template int launch_u8_to_level<TG>(const uint8_t*, long long, TG*, uint8_t*, int, int, int, cudaStream_t);    \
+    template int launch_lanczos<TG>(const uint8_t*, int, int, int, float*, int, TG*, uint8_t*, int, int, int,      \
+                                    const int*, const float*, const int*, const float*, cudaStream_t, bool, int*);
+SIFT_INST(float)
+SIFT_INST(__half)
+#undef SIFT_INST
 
 }  // namespace sift

@@ -55,6 +55,7 @@ struct OctaveDev {
     long long d_off;          // element offset of DoG level 0 in the DoG arena
     long long plane;          // elements per plane (pitch * H)
     long long word_base;      // first word of this octave in the mask arena
+    long long u_off;          // byte offset of level 0 in the u8 level arena
 };
 
 struct PyramidDev {
