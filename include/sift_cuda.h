@@ -199,6 +199,30 @@ enum { SIFT_CUDA_PROFILE_STAGES = 4 };
 int sift_cuda_profile_enable(SiftCudaEngine* engine, int enable);
 int sift_cuda_profile_read(SiftCudaEngine* engine, float* stage_ms, uint32_t n_stages, uint32_t* runs);
 
+/* ---- blur without allocation ---------------------------------------------- */
+
+/* Gaussian blur of a u8 image in device memory into a caller-owned device
+ * buffer, with the arithmetic of every blur of the pyramid (imageproc 0.25.0
+ * gaussian_blur_f32 on u8: radius ceil(2 sigma), clamp-to-edge, horizontal
+ * then vertical pass, each truncated to u8). This entry point has no
+ * counterpart in the reference; it serves callers that must not allocate
+ * device memory on their path (a process whose memory pool has reserved the
+ * free device memory, or a loop that cannot take cudaFree's device-wide
+ * synchronisation). The horizontal pass's intermediate lives in a fixed
+ * 16 MiB device array inside this library, so the call allocates nothing.
+ *  - Limits: width <= 8192, align16(width) * height <= 16 MiB (4096 x 4096
+ *    fits), ceil(2 sigma) <= 64; beyond them SIFT_CUDA_ERR_UNSUPPORTED and
+ *    nothing runs. d_dst may equal d_src.
+ *  - The first call on a device looks the array's address up (and may make
+ *    the runtime load this library's device code there): make it before any
+ *    stream capture begins.
+ *  - Calls share the array: calls that can overlap on the device (different
+ *    streams, unordered threads) race and corrupt each other's output.
+ *  - Asynchronous on `stream` (a cudaStream_t; NULL = the default stream). */
+int sift_cuda_gaussian_blur_u8_noalloc(const uint8_t* d_src, uint32_t width, uint32_t height,
+                                       uint32_t src_stride, uint8_t* d_dst, uint32_t dst_stride,
+                                       float sigma, void* stream);
+
 /* ---- synthetic input -------------------------------------------------------- */
 
 /* Seeded synthetic image: background 128, n_blobs isotropic Gaussian blobs

@@ -116,6 +116,8 @@ def lib() -> C.CDLL:
         "sift_cuda_last_launch_count": (u32, [C.c_void_p]),
         "sift_cuda_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
         "sift_cuda_profile_read": (C.c_int, [C.c_void_p, P(f32), u32, P(u32)]),
+        "sift_cuda_gaussian_blur_u8_noalloc": (C.c_int, [C.c_void_p, u32, u32, u32, C.c_void_p, u32, f32,
+                                                         C.c_void_p]),
         "sift_synth_image": (None, [u64, u32, u32, u32, u32, C.c_void_p]),
         "sift_synth_density": (None, [u32, u32, P(u32), P(u32)]),
     }
@@ -136,7 +138,7 @@ def exported_symbols() -> list[str]:
         "sift_cuda_result_free", "sift_cuda_last_error", "sift_cuda_run_device",
         "sift_cuda_device_outputs", "sift_cuda_synchronize", "sift_cuda_stream",
         "sift_cuda_debug_stage", "sift_cuda_last_launch_count", "sift_cuda_profile_enable",
-        "sift_cuda_profile_read", "sift_synth_image",
+        "sift_cuda_profile_read", "sift_cuda_gaussian_blur_u8_noalloc", "sift_synth_image",
         "sift_synth_density",
     ]
 

@@ -88,6 +88,14 @@ int cuda_fail(cudaError_t e, const char* what) {
                 m);
 }
 
+}  // namespace
+
+// Sets the calling thread's sift_cuda_last_error message from another
+// translation unit of the library; returns code.
+int report_error(int code, const char* msg) { return fail(code, msg ? std::string(msg) : std::string()); }
+
+namespace {
+
 #define CK(call, what)                              \
     do {                                            \
         cudaError_t e_ = (call);                    \
