@@ -152,3 +152,14 @@ def test_extrema_match_numpy_restatement(oracle_mod, built_lib):
     got = [(int(k["octave"]), int(k["layer"]), int(k["y"] / 2 ** k["octave"]), int(k["x"] / 2 ** k["octave"]))
            for k in st.candidates]
     assert got == rows
+
+
+def test_oracle_reproduces_committed_fixture(oracle_mod):
+    """tests/golden/oracle_256_seed0.npz (make_oracle_fixtures.py): the oracle
+    still gives the committed keypoints and descriptors."""
+    from parity import match
+    fx = np.load(GOLDEN / "oracle_256_seed0.npz")
+    kps, desc = oracle_mod.detect_and_compute(fx["image"])
+    m = match(fx["keypoints"], fx["descriptors"], kps, desc)
+    assert len(kps) == len(fx["keypoints"]) and m.rate == 1.0 and m.same_order, m.summary()
+    assert float(m.desc_err.max()) <= 1e-6, m.summary()

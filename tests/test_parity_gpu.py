@@ -98,6 +98,17 @@ def test_keypoints_and_descriptors_match(sgb, oracle_mod, case):
     assert float(m.desc_err.max()) <= DESC_RTOL, m.summary()
 
 
+def test_committed_fixture(sgb):
+    """The CUDA path against the committed oracle fixture
+    (tests/golden/oracle_256_seed0.npz)."""
+    from pathlib import Path
+    fx = np.load(Path(__file__).resolve().parent / "golden" / "oracle_256_seed0.npz")
+    kps, desc = engine_for(sgb, (1.6, 4, 3, 0.5, 0.04, 10.0)).detect_and_compute(fx["image"])
+    m = match(fx["keypoints"], fx["descriptors"], kps, desc)
+    assert m.rate >= MATCH_RATE and m.same_order, m.summary()
+    assert float(m.desc_err.max()) <= DESC_RTOL, m.summary()
+
+
 def test_uniform_image_has_no_keypoints(sgb):
     """tests/integration_test.rs:205-226"""
     eng = engine_for(sgb, (1.6, 4, 3, 0.5, 0.04, 10.0))
