@@ -199,6 +199,93 @@ enum { SIFT_CUDA_PROFILE_STAGES = 4 };
 int sift_cuda_profile_enable(SiftCudaEngine* engine, int enable);
 int sift_cuda_profile_read(SiftCudaEngine* engine, float* stage_ms, uint32_t n_stages, uint32_t* runs);
 
+/* ---- serving: continuous batching over resident engines ------------------ */
+
+/* The serving and batching forms of SiftBackend::Cuda (no counterpart in the
+ * reference, whose GPU arms build a context per call, src/sift.rs:1262-1291).
+ * A server keeps one resident engine ("slot") per image size and in-flight
+ * request, admits requests by the device footprint of their slot against
+ * arena_bytes, and runs up to max_inflight of them concurrently on separate
+ * streams; a request that arrives while others run starts as soon as a slot
+ * of its size is idle or fits. One internal host thread issues all CUDA work.
+ * Results are bit-identical to sift_cuda_detect_and_compute on the same image
+ * and parameters, alone or in any mix. */
+typedef struct SiftCudaServer SiftCudaServer;
+
+typedef struct {
+    int32_t device;
+    int32_t storage;       /* SiftCudaStorage */
+    uint64_t arena_bytes;  /* device bytes the slots may hold (default 40 GiB) */
+    uint32_t max_inflight; /* requests on the device at once (default 8) */
+    uint32_t autotune;     /* 1: time launch shapes on the first slot of each size */
+    uint32_t reserved[4];
+} SiftCudaServerOptions;
+
+typedef struct {
+    uint64_t ticket;             /* pass to sift_cuda_server_release */
+    uint64_t tag;                /* the caller's tag from submit */
+    int32_t status;              /* 0 or a SiftCudaStatus */
+    uint32_t n;                  /* keypoints */
+    const SiftCudaKeypoint* kps; /* valid until released */
+    const float* desc;           /* n x 128, valid until released */
+    double submit_s, start_s, done_s; /* steady-clock seconds */
+} SiftCudaServed;
+
+typedef struct {
+    uint32_t slots, running, pending, reserved;
+    uint64_t device_bytes, completed, reruns, evicted, max_pending;
+} SiftCudaServerStats;
+
+enum { SIFT_CUDA_SUBMIT_BORROW = 1 }; /* img stays valid and unchanged until polled: no copy */
+
+void sift_cuda_server_options_default(SiftCudaServerOptions* out);
+int sift_cuda_server_create(const SiftCudaParams* params, const SiftCudaServerOptions* opts,
+                            SiftCudaServer** out);
+/* Waits for the requests in flight, then frees everything. */
+void sift_cuda_server_destroy(SiftCudaServer* server);
+/* Queues one image (copied unless SIFT_CUDA_SUBMIT_BORROW); *ticket names it. */
+int sift_cuda_server_submit(SiftCudaServer* server, const uint8_t* img, uint32_t width, uint32_t height,
+                            uint32_t stride, uint64_t tag, uint32_t flags, uint64_t* ticket);
+/* Next finished request: 1 and *out filled, 0 on timeout (timeout_us < 0
+ * waits without limit, 0 does not wait). */
+int sift_cuda_server_poll(SiftCudaServer* server, SiftCudaServed* out, int64_t timeout_us);
+/* Gives the request's slot back; its kps/desc pointers become invalid. */
+int sift_cuda_server_release(SiftCudaServer* server, uint64_t ticket);
+/* Runs `count` concurrent requests of this image (untimed warm-up): creates
+ * up to `count` slots of its size and captures their graphs. */
+int sift_cuda_server_warm(SiftCudaServer* server, const uint8_t* img, uint32_t width, uint32_t height,
+                          uint32_t stride, uint32_t count);
+int sift_cuda_server_stats(SiftCudaServer* server, SiftCudaServerStats* out);
+/* Launch shape chosen for a size by the autotuner: [fused blur radius limit,
+ * orientation CTAs/SM, descriptor CTAs/SM]; returns 1 if tuned, 0 if default. */
+int sift_cuda_server_tuning(SiftCudaServer* server, uint32_t width, uint32_t height, int32_t* knobs3);
+/* Device bytes a slot for a width x height image holds (admission estimate). */
+uint64_t sift_cuda_footprint_bytes(const SiftCudaParams* params, int32_t storage, uint32_t width,
+                                   uint32_t height);
+
+/* Open-loop replay of a request trace: request i is due at start +
+ * arrival_s and its latency runs from that due time until its result is in
+ * host memory. server != NULL drives the server (images are borrowed: keep
+ * them pinned for speed); server == NULL runs the plain path instead — one
+ * synchronous sift_cuda_detect_and_compute_view per request, in arrival
+ * order, on an engine per image size created from params/opts. */
+typedef struct {
+    const uint8_t* data;
+    uint32_t width, height, stride, reserved;
+} SiftCudaReplayImage;
+typedef struct {
+    double arrival_s;
+    uint32_t image, reserved;
+} SiftCudaReplayRequest;
+typedef struct {
+    double latency_s;
+    uint32_t n;
+    int32_t status;
+} SiftCudaReplayResult;
+int sift_cuda_replay(SiftCudaServer* server, const SiftCudaParams* params, const SiftCudaOptions* opts,
+                     const SiftCudaReplayImage* images, uint32_t n_images, const SiftCudaReplayRequest* reqs,
+                     uint32_t n_reqs, SiftCudaReplayResult* results, double* wall_s);
+
 /* ---- blur without allocation ---------------------------------------------- */
 
 /* Gaussian blur of a u8 image in device memory into a caller-owned device

@@ -85,6 +85,39 @@ class SiftCudaError(RuntimeError):
         self.code = code
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("device", C.c_int32), ("storage", C.c_int32), ("arena_bytes", C.c_uint64),
+                ("max_inflight", C.c_uint32), ("autotune", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+
+class Served(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32), ("n", C.c_uint32),
+                ("kps", C.c_void_p), ("desc", C.c_void_p), ("submit_s", C.c_double), ("start_s", C.c_double),
+                ("done_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("running", C.c_uint32), ("pending", C.c_uint32), ("reserved", C.c_uint32),
+                ("device_bytes", C.c_uint64), ("completed", C.c_uint64), ("reruns", C.c_uint64),
+                ("evicted", C.c_uint64), ("max_pending", C.c_uint64)]
+
+
+class ReplayImage(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("stride", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class ReplayRequest(C.Structure):
+    _fields_ = [("arrival_s", C.c_double), ("image", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class ReplayResult(C.Structure):
+    _fields_ = [("latency_s", C.c_double), ("n", C.c_uint32), ("status", C.c_int32)]
+
+
+SUBMIT_BORROW = 1
+
+
 def lib() -> C.CDLL:
     global _lib
     if _lib is not None:
@@ -118,6 +151,18 @@ def lib() -> C.CDLL:
         "sift_cuda_profile_read": (C.c_int, [C.c_void_p, P(f32), u32, P(u32)]),
         "sift_cuda_gaussian_blur_u8_noalloc": (C.c_int, [C.c_void_p, u32, u32, u32, C.c_void_p, u32, f32,
                                                          C.c_void_p]),
+        "sift_cuda_server_options_default": (None, [P(ServerOptions)]),
+        "sift_cuda_server_create": (C.c_int, [P(Params), P(ServerOptions), P(C.c_void_p)]),
+        "sift_cuda_server_destroy": (None, [C.c_void_p]),
+        "sift_cuda_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, u64, u32, P(u64)]),
+        "sift_cuda_server_poll": (C.c_int, [C.c_void_p, P(Served), C.c_int64]),
+        "sift_cuda_server_release": (C.c_int, [C.c_void_p, u64]),
+        "sift_cuda_server_warm": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, u32]),
+        "sift_cuda_server_stats": (C.c_int, [C.c_void_p, P(ServerStats)]),
+        "sift_cuda_server_tuning": (C.c_int, [C.c_void_p, u32, u32, P(i32)]),
+        "sift_cuda_footprint_bytes": (u64, [P(Params), i32, u32, u32]),
+        "sift_cuda_replay": (C.c_int, [C.c_void_p, P(Params), P(Options), P(ReplayImage), u32, P(ReplayRequest),
+                                       u32, P(ReplayResult), P(C.c_double)]),
         "sift_synth_image": (None, [u64, u32, u32, u32, u32, C.c_void_p]),
         "sift_synth_density": (None, [u32, u32, P(u32), P(u32)]),
     }
@@ -138,7 +183,10 @@ def exported_symbols() -> list[str]:
         "sift_cuda_result_free", "sift_cuda_last_error", "sift_cuda_run_device",
         "sift_cuda_device_outputs", "sift_cuda_synchronize", "sift_cuda_stream",
         "sift_cuda_debug_stage", "sift_cuda_last_launch_count", "sift_cuda_profile_enable",
-        "sift_cuda_profile_read", "sift_cuda_gaussian_blur_u8_noalloc", "sift_synth_image",
+        "sift_cuda_profile_read", "sift_cuda_server_options_default", "sift_cuda_server_create",
+        "sift_cuda_server_destroy", "sift_cuda_server_submit", "sift_cuda_server_poll", "sift_cuda_server_release",
+        "sift_cuda_server_warm", "sift_cuda_server_stats", "sift_cuda_server_tuning", "sift_cuda_footprint_bytes",
+        "sift_cuda_replay", "sift_cuda_gaussian_blur_u8_noalloc", "sift_synth_image",
         "sift_synth_density",
     ]
 

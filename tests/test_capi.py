@@ -87,3 +87,43 @@ def test_engine_errors_are_reported(built_lib):
     res = _capi.Result()
     rc = L.sift_cuda_detect_and_compute(None, None, 4, 4, 4, C.byref(res))
     assert rc == 1 and res.n == 0
+
+
+def footprint_restated(S, O, w, h, es):
+    """The admission estimate of a server slot, restated: the arena layout
+    (pitch = width rounded to 32; S+3 Gaussian, S+2 DoG (f32 only) and S+3 u8
+    planes per octave; horizontal-pass and resize scratch; two mask-word
+    arrays) plus list capacities of 1/64 of the scanned positions (>= 1024)
+    at 172 candidate-list bytes and 540 output bytes each, plus the padded
+    image and 1 MiB of tables."""
+    al = lambda v, a: (v + a - 1) // a * a
+    g = d = u = tmpb = tmpo = lt = words = caps = 0
+    ow, oh = w, h
+    for o in range(O):
+        pitch = al(max(ow, 1), 32)
+        plane, nw = pitch * oh, (ow + 31) // 32
+        g += plane * (S + 3) * es
+        d += plane * (S + 2) * 4 if es == 4 else 0
+        u += plane * (S + 3)
+        tmpb = max(tmpb, plane)
+        tmpo += al(plane, 256)
+        if o + 1 < O:
+            lt = max(lt, pitch * (oh // 2) * 4)
+        wo = S * oh * nw
+        words += wo * 8
+        caps += min(max(wo * 32 // 64, 1024), 1 << 28)
+        ow, oh = ow // 2, oh // 2
+    return al(max(w, 1), 128) * h + g + d + u + tmpb + tmpo + lt + words + caps * 172 + caps * 540 + (1 << 20)
+
+
+@pytest.mark.parametrize("shape", [(640, 480), (1920, 1080), (3840, 2160), (333, 217), (1, 1)])
+def test_server_footprint_estimate(built_lib, shape):
+    """Admission is by this estimate; it runs on the host (no GPU)."""
+    import sift_wgpu_gb300 as sg
+    w, h = shape
+    s = sg.Sift.default()
+    f32 = sg.footprint_bytes(s, w, h, "f32")
+    f16 = sg.footprint_bytes(s, w, h, "f16")
+    assert f32 == footprint_restated(3, 4, w, h, 4)
+    assert f16 == footprint_restated(3, 4, w, h, 2)
+    assert f16 < f32
