@@ -18,6 +18,16 @@ quoted on. Prints one JSON line.
   cpu_baseline  the C++ restatement of the reference CPU path (oracle/) on the
           host cores, bounded sample of the same frame.
 
+  serving  the continuous-batching server (sift_wgpu_gb300.Server) against
+          the plain one-call-per-image path on the same open-loop Poisson
+          trace of mixed resolutions (40% 640x480, 30% 1280x720, 20% 1920x1080,
+          10% 3840x2160): p50/p99 latency per offered rate, and the saturated
+          images/s of both (all requests due at once).
+
+--workload batch64 prints the batched form (64 images of uneven sizes in
+flight at once) against the plain path; --workload serve prints the full
+serving sweep (20000 requests per offered rate, 500-8000 req/s).
+
 --impl reference times that CPU path alone (the reference crate itself cannot
 be built here: no Rust toolchain), with the same metric and workload.
 Multi-GPU (torchrun): independent replicas, one engine per rank, no
@@ -34,6 +44,8 @@ import sys
 import threading
 import time
 from pathlib import Path
+
+import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
@@ -167,6 +179,144 @@ def cpu_baseline(img, args, budget_s: float = 15.0) -> dict:
                       f"rayon axes on {threads} threads)"}
 
 
+SERVE_MIX = [((640, 480), 0.4), ((1280, 720), 0.3), ((1920, 1080), 0.2), ((3840, 2160), 0.1)]
+
+
+def serve_pool(per_size: int = 4):
+    """Images of the serving mix: per_size distinct seeded frames per
+    resolution (seeds 4000000 + k), at the 512x512 density."""
+    from sift_wgpu_gb300 import synth_image
+    images, size_of = [], []
+    for si, ((w, h), _) in enumerate(SERVE_MIX):
+        for j in range(per_size):
+            images.append(synth_image(4_000_000 + si * per_size + j, w, h))
+            size_of.append(si)
+    return images, np.array(size_of)
+
+
+def serve_trace(n: int, rate: float, size_of, seed: int = 4):
+    """Poisson arrivals at `rate` req/s; each request draws a resolution from
+    the mix and one of that resolution's pooled images."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n)) if rate > 0 else np.zeros(n)
+    probs = np.array([p for _, p in SERVE_MIX])
+    sizes = rng.choice(len(SERVE_MIX), size=n, p=probs)
+    idx = np.empty(n, dtype=np.int64)
+    for si in range(len(SERVE_MIX)):
+        pool = np.nonzero(size_of == si)[0]
+        m = sizes == si
+        idx[m] = rng.choice(pool, size=int(m.sum()))
+    return arrivals, idx, sizes
+
+
+def lat_summary(lat, sizes=None):
+    ms = np.asarray(lat) * 1e3
+    out = {"p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+           "mean_ms": float(ms.mean())}
+    if sizes is not None:
+        m = sizes == 2  # 1920x1080
+        if m.any():
+            out["p50_1080p_ms"] = float(np.percentile(ms[m], 50))
+            out["p99_1080p_ms"] = float(np.percentile(ms[m], 99))
+    return out
+
+
+def serving_report(n_req: int, rates, max_inflight: int = 8, autotune: bool = False, device: int = 0) -> dict:
+    """Served vs plain on the same traces (both warmed, untimed)."""
+    import sift_wgpu_gb300 as sg
+    images, size_of = serve_pool()
+    rep = {"mix": "40% 640x480, 30% 1280x720, 20% 1920x1080, 10% 3840x2160; 4 pooled seeded frames per "
+                  "resolution; Poisson arrivals (seed 4); latency from due time to results in host memory",
+           "requests_per_rate": n_req, "max_inflight": max_inflight, "autotune": autotune, "rates": []}
+    with sg.Server(device=device, max_inflight=max_inflight, autotune=autotune) as srv:
+        for si in range(len(SERVE_MIX)):
+            srv.warm(images[int(np.nonzero(size_of == si)[0][0])], max_inflight)
+        # saturation: every request due at once
+        arr0, idx0, sz0 = serve_trace(n_req, 0, size_of)
+        lat, nk, wall = sg.replay(images, arr0, idx0, server=srv, device=device)
+        served_sat = n_req / wall
+        for rate in rates:
+            arr, idx, sz = serve_trace(n_req, rate, size_of)
+            lat, nk, wall = sg.replay(images, arr, idx, server=srv, device=device)
+            rep["rates"].append({"offered_req_s": rate, "served": dict(lat_summary(lat, sz),
+                                                                       images_s=n_req / wall)})
+        rep["server_stats"] = srv.stats()
+    lat, nk, wall = sg.replay(images, arr0, idx0, server=None, device=device)
+    plain_sat = n_req / wall
+    for k, rate in enumerate(rates):
+        arr, idx, sz = serve_trace(n_req, rate, size_of)
+        lat, nk, wall = sg.replay(images, arr, idx, server=None, device=device)
+        rep["rates"][k]["plain"] = dict(lat_summary(lat, sz), images_s=n_req / wall)
+    rep["saturated_images_s"] = {"served": served_sat, "plain": plain_sat, "ratio": served_sat / plain_sat}
+    return rep
+
+
+def batch64_images():
+    """64 images, width and height uniform over the multiples of 16 in
+    [320, 2560] (seed 2), image i made with seed 1000 + i."""
+    from sift_wgpu_gb300 import synth_image
+    rng = np.random.default_rng(2)
+    dims = rng.integers(20, 161, size=(64, 2)) * 16
+    return [synth_image(1000 + i, int(w), int(h)) for i, (w, h) in enumerate(dims)]
+
+
+def run_batch64(args, world, rank, local):
+    import sift_wgpu_gb300 as sg
+    import torch
+    images = []
+    for im in batch64_images():  # pinned host images, borrowed by the server
+        t = torch.from_numpy(im).pin_memory()
+        images.append(t.numpy())
+    px = sum(im.size for im in images)
+    with sg.Server(device=local, max_inflight=args.inflight, autotune=args.autotune) as srv:
+        srv.detect_batch(images, borrow=True)  # creates and captures a slot per size
+        for _ in range(max(0, args.warmup - 1)):
+            srv.detect_batch(images, borrow=True)
+        t = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            out = srv.detect_batch(images, borrow=True)
+            t.append(time.perf_counter() - t0)
+        nk = sum(len(k) for k, _ in out)
+        stats = srv.stats()
+    zero = np.zeros(len(images))
+    idx = np.arange(len(images))
+    sg.replay(images, zero, idx, server=None, device=local)  # warm the plain engines
+    tp = []
+    for _ in range(args.steps):
+        _, _, wall = sg.replay(images, zero, idx, server=None, device=local)
+        tp.append(wall)
+    value = len(images) / statistics.median(t)
+    plain = len(images) / statistics.median(tp)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "batch64 images/s", "value": value, "unit": "images/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(t),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "64 u8 images, W,H uniform multiples of 16 in [320, 2560], seeds 1000+i, "
+                                   "Sift::default()", "megapixels": px / 1e6, "keypoints": int(nk),
+                       "max_inflight": args.inflight, "autotune": bool(args.autotune)},
+            "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": int(px),
+                    "d2h_bytes_per_step": int(nk * (28 + 512))},
+            "plain_images_s": plain, "batched_over_plain": value / plain, "server_stats": stats,
+        }), flush=True)
+
+
+def run_serve(args, world, rank, local):
+    rep = serving_report(args.requests, [500, 1000, 2000, 4000, 8000], max_inflight=args.inflight,
+                         autotune=args.autotune, device=local)
+    if rank == 0:
+        best = min(rep["rates"], key=lambda r: r["served"]["p99_ms"])
+        print(json.dumps({
+            "metric": "served images/s (mixed-resolution Poisson stream)", "value": rep["saturated_images_s"]["served"],
+            "unit": "images/s", "n_gpus": world, "steps": args.requests, "warmup": 1, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "serving mix, 20000 requests per offered rate"}, "serving": rep,
+            "best_p99_ms": best["served"]["p99_ms"],
+        }), flush=True)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -199,7 +349,7 @@ def run_reference(args, world, rank):
         return
     from sift_wgpu_gb300 import synth_image
     from oracle import oracle
-    w, h, seed, sargs = WORKLOADS[args.workload]
+    w, h, seed, sargs = WORKLOADS.get(args.workload, WORKLOADS["1080p"])
     img = synth_image(seed, w, h)
     threads = os.cpu_count() or 1
     p = oracle.params(*sargs)
@@ -356,8 +506,13 @@ def run_cuda(args, world, rank, local):
         }
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(img, sargs, args.cpu_budget)
-        print(json.dumps(out), flush=True)
     eng.close()
+    if not args.no_serving:
+        srv = serving_report(args.serve_requests, [1000, 2000, 4000], max_inflight=args.inflight, device=local)
+        if rank == 0:
+            out["serving"] = srv
+    if rank == 0:
+        print(json.dumps(out), flush=True)
     return out
 
 
@@ -367,15 +522,24 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="1080p")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64", "serve"], default="1080p")
     ap.add_argument("--storage", choices=["f32", "f16"], default="f32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain section")
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--requests", type=int, default=20000, help="requests per rate (--workload serve)")
+    ap.add_argument("--inflight", type=int, default=8, help="server: requests on the device at once")
+    ap.add_argument("--autotune", action="store_true", help="server: tune launch shapes per image size")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "cuda" else args.warmup
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "batch64":
+        run_batch64(args, world, rank, local)
+    elif args.workload == "serve":
+        run_serve(args, world, rank, local)
     else:
         run_cuda(args, world, rank, local)
     if world > 1:

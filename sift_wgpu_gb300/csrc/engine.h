@@ -273,6 +273,10 @@ struct Engine {
         return 0;
     }
 
+    // CUDA stream priority of the engine's streams (0 = default; lower is
+    // more urgent). A graph launched into st runs at st's priority.
+    int priority = 0;
+
     bool f16() const { return opt.storage == SIFT_CUDA_STORAGE_F16; }
 
     // Device bytes held by the engine's arenas and lists.
@@ -293,9 +297,10 @@ struct Engine {
 
     int init() {
         if (int rc = set_device()) return rc;
-        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, priority), "cudaStreamCreate");
         st_oct.assign(kMaxOctaves, nullptr);
-        for (auto& q : st_oct) CK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto& q : st_oct)
+            CK(cudaStreamCreateWithPriority(&q, cudaStreamNonBlocking, priority), "cudaStreamCreate");
         for (auto* v : {&ev_level, &ev_ori, &ev_done}) {
             v->assign(kMaxOctaves, nullptr);
             for (auto& e : *v) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");

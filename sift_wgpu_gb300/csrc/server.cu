@@ -153,6 +153,7 @@ struct Server {
     std::vector<std::unique_ptr<Slot>> slots;
     std::multimap<size_t, void*> pinned_free;  // owned-copy buffers
     std::map<TuneKey, Engine::Tuning> tuned;
+    std::vector<std::pair<uint32_t, uint32_t>> creating;  // sizes of slots being created
     uint64_t next_ticket = 1, use_clock = 0, device_bytes = 0;
     uint32_t running = 0;
     bool stop = false;
@@ -182,7 +183,21 @@ struct Server {
 
     // -- slot management (service thread) ------------------------------------
 
-    int new_slot(uint32_t w, uint32_t h, Slot** out) {
+    // Smaller images get more urgent streams: while a large image runs, the
+    // block scheduler serves a small request's kernels first, so its latency
+    // stays near its solo time. Tiers: up to 0.5 Mpx, up to 2.1 Mpx (1080p),
+    // larger.
+    int priority_for(uint32_t w, uint32_t h) const {
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return 0;
+        const uint64_t area = (uint64_t)w * h;
+        const int tier = area <= 500000 ? 0 : (area <= 2100000 ? 1 : 2);
+        return std::min(least, greatest + tier);
+    }
+
+    // A new slot for w x h (service thread, lock NOT held: engine creation
+    // allocates and captures).
+    int make_slot(uint32_t w, uint32_t h, const Engine::Tuning* tune, std::unique_ptr<Slot>* out) {
         auto s = std::make_unique<Slot>();
         s->eng = std::make_unique<Engine>();
         s->eng->p = p;
@@ -191,28 +206,16 @@ struct Server {
         eo.device = opt.device;
         eo.storage = opt.storage;
         s->eng->opt = eo;
+        s->eng->priority = priority_for(w, h);
         if (int rc = s->eng->init()) return rc;
         if (int rc = s->eng->ensure_geometry(w, h)) return rc;
         CK(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming), "cudaEventCreate");
-        auto it = tuned.find(TuneKey{w, h});
-        if (it != tuned.end()) s->eng->tune = it->second;
+        if (tune) s->eng->tune = *tune;
         s->w = w;
         s->h = h;
         s->bytes = s->eng->device_bytes();
-        device_bytes += s->bytes;
-        slots.push_back(std::move(s));
-        *out = slots.back().get();
+        *out = std::move(s);
         return 0;
-    }
-
-    void evict(Slot* s) {
-        device_bytes -= s->bytes;
-        for (size_t i = 0; i < slots.size(); ++i)
-            if (slots[i].get() == s) {
-                slots.erase(slots.begin() + (long)i);
-                break;
-            }
-        ++n_evicted;
     }
 
     int ensure_export(Slot* s, uint32_t n) {
@@ -227,33 +230,46 @@ struct Server {
         return 0;
     }
 
-    // Finds a slot for r (lock held): an idle slot of its size, a new one that
-    // fits the budget, or a new one after evicting idle slots of other sizes.
-    // Returns 0 with *out == nullptr when r has to wait.
-    int find_slot(Request* r, Slot** out) {
+    // Admission of r (lock held). Returns 0 and either *out (an idle slot of
+    // r's size), or *create (a new slot of r's size fits: its estimated
+    // footprint is reserved in device_bytes; idle slots of other sizes may
+    // have been moved to *evicted to make room), or neither (r waits). A size
+    // never holds more than max_inflight slots.
+    int admit(Request* r, Slot** out, bool* create, std::vector<std::unique_ptr<Slot>>* evicted) {
         *out = nullptr;
-        Slot* best = nullptr;
+        *create = false;
+        uint32_t same = 0;
         for (auto& s : slots)
-            if (s->state == Slot::Idle && s->w == r->w && s->h == r->h) {
-                best = s.get();
-                break;
+            if (s->w == r->w && s->h == r->h) {
+                if (s->state == Slot::Idle) {
+                    *out = s.get();
+                    return 0;
+                }
+                ++same;
             }
-        if (best) {
-            *out = best;
-            return 0;
-        }
+        for (const auto& c : creating)
+            if (c.first == r->w && c.second == r->h) ++same;
+        if (same >= opt.max_inflight) return 0;
         const uint64_t need = footprint_estimate(p, opt.storage, r->w, r->h);
         if (need > opt.arena_bytes) return fail(SIFT_CUDA_ERR_CAPACITY, "image footprint above the arena budget");
         while (device_bytes + need > opt.arena_bytes) {
-            Slot* victim = nullptr;
-            for (auto& s : slots)
+            size_t victim = slots.size();
+            for (size_t i = 0; i < slots.size(); ++i) {
+                const Slot* s = slots[i].get();
                 if (s->state == Slot::Idle && (s->w != r->w || s->h != r->h) &&
-                    (!victim || s->last_use < victim->last_use))
-                    victim = s.get();
-            if (!victim) return 0;  // wait for a running slot to finish
-            evict(victim);
+                    (victim == slots.size() || s->last_use < slots[victim]->last_use))
+                    victim = i;
+            }
+            if (victim == slots.size()) return 0;  // wait for running slots to finish
+            device_bytes -= slots[victim]->bytes;
+            evicted->push_back(std::move(slots[victim]));
+            slots.erase(slots.begin() + (long)victim);
+            ++n_evicted;
         }
-        return new_slot(r->w, r->h, out);
+        device_bytes += need;
+        creating.emplace_back(r->w, r->h);
+        *create = true;
+        return 0;
     }
 
     // Times the slot's graph for a few launch shapes on the image already in
@@ -297,6 +313,7 @@ struct Server {
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         e.tune = best;
+        std::lock_guard<std::mutex> g(mu);
         tuned[TuneKey{s->w, s->h}] = best;
         return rc;
     }
@@ -304,7 +321,12 @@ struct Server {
     int launch(Slot* s, Request* r) {
         Engine& e = *s->eng;
         if (int rc = e.upload(r->img, r->w, r->h, r->stride, cudaMemcpyHostToDevice)) return rc;
-        if (opt.autotune && tuned.find(TuneKey{s->w, s->h}) == tuned.end())
+        bool tune = false;
+        if (opt.autotune) {
+            std::lock_guard<std::mutex> g(mu);
+            tune = tuned.find(TuneKey{s->w, s->h}) == tuned.end();
+        }
+        if (tune)
             if (int rc = autotune(s)) return rc;
         if (int rc = e.run(true)) return rc;
         return launch_export(s);
@@ -362,56 +384,137 @@ struct Server {
         ++n_done;
     }
 
+    // The service loop. The lock guards the queues and the slot states only;
+    // event polling, launches and slot creation or destruction run without
+    // it, so submit, poll and release never wait behind CUDA calls.
     void service() {
         cudaSetDevice(opt.device);
+        std::vector<Slot*> run_list, done_list;
+        std::vector<cudaError_t> done_q;
+        struct Start {
+            Request* r;
+            Slot* s;            // null: create a slot of r's size first
+            uint64_t reserved;  // footprint reserved for that creation
+        };
+        std::vector<Start> starts;
+        std::vector<std::unique_ptr<Slot>> evicted;
         std::unique_lock<std::mutex> lk(mu);
         while (true) {
-            bool progressed = false;
-            // completions
-            for (auto& sp : slots) {
-                Slot* s = sp.get();
-                if (s->state != Slot::Running) continue;
-                cudaError_t q = cudaEventQuery(s->done);
+            run_list.clear();
+            for (auto& sp : slots)
+                if (sp->state == Slot::Running && sp->req) run_list.push_back(sp.get());
+            lk.unlock();
+            done_list.clear();
+            done_q.clear();
+            for (Slot* s : run_list) {
+                const cudaError_t q = cudaEventQuery(s->done);
                 if (q == cudaErrorNotReady) continue;
-                progressed = true;
-                const int rc = q == cudaSuccess ? complete(s) : cuda_fail(q, "request");
+                done_list.push_back(s);
+                done_q.push_back(q);
+            }
+            lk.lock();
+            bool progressed = !done_list.empty();
+            for (size_t i = 0; i < done_list.size(); ++i) {
+                Slot* s = done_list[i];
+                const int rc = done_q[i] == cudaSuccess ? complete(s) : cuda_fail(done_q[i], "request");
                 if (rc) fail_request(s->req, rc);
             }
             if (!finished.empty()) cv_done.notify_all();
-            // admissions, FIFO; a request that cannot start does not block
-            // later requests of other sizes
+            // admissions in FIFO order; a request that has to wait does not
+            // hold back later requests of other sizes
+            starts.clear();
             for (auto it = pending.begin(); it != pending.end() && running < opt.max_inflight;) {
                 Request* r = *it;
                 Slot* s = nullptr;
-                int rc = find_slot(r, &s);
+                bool create = false;
+                const int rc = admit(r, &s, &create, &evicted);
                 if (rc) {
                     it = pending.erase(it);
                     fail_request(r, rc);
                     progressed = true;
                     continue;
                 }
-                if (!s) {
+                if (!s && !create) {
                     ++it;
                     continue;
                 }
                 it = pending.erase(it);
-                s->state = Slot::Running;
-                s->req = r;
-                s->last_use = ++use_clock;
-                r->slot = s;
+                if (s) {
+                    s->state = Slot::Running;
+                    s->req = nullptr;  // not polled until launched
+                    s->last_use = ++use_clock;
+                    r->slot = s;
+                }
                 r->t_start = now_s();
                 ++running;
                 progressed = true;
-                rc = launch(s, r);
-                if (rc) fail_request(r, rc);
+                starts.push_back(Start{r, s, create ? footprint_estimate(p, opt.storage, r->w, r->h) : 0});
             }
+            if (stop) {
+                // shutting down: requests not yet started fail
+                while (!pending.empty()) {
+                    Request* r = pending.front();
+                    pending.pop_front();
+                    r->status = SIFT_CUDA_ERR_INVALID_ARGUMENT;
+                    r->t_done = now_s();
+                    finished.push_back(r);
+                }
+            }
+            if (!finished.empty()) cv_done.notify_all();
             if (stop && running == 0) break;
+            lk.unlock();
+            evicted.clear();  // engines of evicted slots are destroyed without the lock
+            for (Start& st : starts) {
+                Request* r = st.r;
+                int rc = 0;
+                if (!st.s) {
+                    Engine::Tuning t{};
+                    bool have_tune = false;
+                    {
+                        std::lock_guard<std::mutex> g(mu);
+                        auto tt = tuned.find(TuneKey{r->w, r->h});
+                        if (tt != tuned.end()) {
+                            t = tt->second;
+                            have_tune = true;
+                        }
+                    }
+                    std::unique_ptr<Slot> fresh;
+                    rc = make_slot(r->w, r->h, have_tune ? &t : nullptr, &fresh);
+                    std::lock_guard<std::mutex> g(mu);
+                    device_bytes -= st.reserved;
+                    for (size_t k = 0; k < creating.size(); ++k)
+                        if (creating[k].first == r->w && creating[k].second == r->h) {
+                            creating.erase(creating.begin() + (long)k);
+                            break;
+                        }
+                    if (!rc) {
+                        Slot* s = fresh.get();
+                        device_bytes += s->bytes;
+                        s->state = Slot::Running;
+                        s->last_use = ++use_clock;
+                        r->slot = s;
+                        slots.push_back(std::move(fresh));
+                        st.s = s;
+                    }
+                }
+                if (!rc) rc = launch(st.s, r);
+                std::lock_guard<std::mutex> g(mu);
+                if (rc) {
+                    if (r->slot) r->slot->req = r;  // so that release frees the slot
+                    else --running;
+                    fail_request(r, rc);
+                    cv_done.notify_all();
+                } else {
+                    st.s->req = r;  // now visible to the completion poll
+                }
+            }
+            lk.lock();
             if (!progressed) {
                 if (running == 0) {
                     cv_work.wait_for(lk, std::chrono::milliseconds(5));
                 } else {
                     lk.unlock();
-                    std::this_thread::yield();
+                    std::this_thread::sleep_for(std::chrono::microseconds(5));
                     lk.lock();
                 }
             }
