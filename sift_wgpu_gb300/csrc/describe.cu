@@ -133,10 +133,10 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                                                                    OctCounters* __restrict__ oc,
                                                                    float* __restrict__ ori_angle,
                                                                    uint32_t* __restrict__ ori_count) {
-    __shared__ float lut[256];
+    __shared__ float lut[sizeof(TG) == 2 ? 256 : 1];
     __shared__ float hist[kWarpsPerCta][kOriBins][32];
     __shared__ float hs[kWarpsPerCta][kOriBins];
-    fill_lut(lut);
+    if constexpr (sizeof(TG) == 2) fill_lut(lut);
     __syncthreads();
     const int lane = threadIdx.x, wid = threadIdx.y;
     const uint32_t n = oc->n_ref;
@@ -161,6 +161,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                 const float wd = __fmul_rn(__fmul_rn(2.0f, ws), ws);
 #pragma unroll
                 for (int b = 0; b < kOriBins; ++b) hist[wid][b][lane] = 0.0f;
+
                 // Windows entirely inside the level (most keypoints) take the
                 // loop without bounds checks; the others add +0.0 for samples
                 // outside, which leaves a bin bit-identical.
@@ -254,9 +255,11 @@ __global__ void k_orient_emit(const Keypoint* __restrict__ refined, int o, Count
 }
 
 constexpr int kDescThreads = 128;
-constexpr int kHistRow = 9;      // 8 angle bins + 1 pad per cell
+constexpr int kHistRow = 9;      // 8 angle bins + slot 8, the share of bin 0 that wrapped from bin 7
+constexpr int kHistSide = 6;     // cells -1..4 per axis: the 4 x 4 window and a border that takes the
+                                 // trilinear spill, so no sample needs a clamp or a validity test
 constexpr int kHistCopies = 8;   // one copy per 4 lanes (lane >> 2)
-constexpr int kHistStride = 148; // >= 16 * kHistRow; 148 % 32 = 20 puts a bin's 8 copies in 8 banks
+constexpr int kHistStride = 324; // 36 * kHistRow; 324 % 32 = 4 puts a bin's 8 copies in 8 banks
 constexpr int kDescRadGrid = 31;                      // largest radius served from the grid
 constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad+1
 
@@ -276,7 +279,8 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                                                               const Keypoint* __restrict__ oriented,
                                                               OctCounters* __restrict__ oc,
                                                               float* __restrict__ desc, uint32_t cap) {
-    __shared__ float lut[256];
+    // v / 255 for f16 levels (f32 levels hold v / 255 already)
+    __shared__ float lut[sizeof(TG) == 2 ? 256 : 1];
     __shared__ float grid[kDescGridSide * kDescGridSide];
     // Neighbouring samples land in the same bins, so the lanes of a warp add
     // into kHistCopies copies of the histogram (lane >> 2 picks one): adds
@@ -284,7 +288,7 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     // are summed in a fixed order; integer sums make the order irrelevant.
     __shared__ unsigned int hist[kHistCopies * kHistStride];
     __shared__ float red_lo[kDescThreads / 32], red_hi[kDescThreads / 32];
-    fill_lut(lut);
+    if constexpr (sizeof(TG) == 2) fill_lut(lut);
     __syncthreads();
     const int tid = threadIdx.x;
     const uint32_t base = oc->out_base;
@@ -419,6 +423,8 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                 const float xs = xo + px, ys = yo + py;
                 const bool in = (xb > -1.0f && xb < 4.0f && yb > -1.0f && yb < 4.0f) &&
                                 !(xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1);
+                // warps whose 32 samples all fall outside skip the rest
+                if (!__any_sync(__activemask(), in)) continue;
                 float gx, gy;
                 if (use_grid) {
                     const int c = k + 2 * q + gs + 1;
@@ -437,24 +443,24 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                 int xbi, ybi, abi;
                 const float xbf = floor_fi(xb, &xbi), ybf = floor_fi(yb, &ybi), abf = floor_fi(ab, &abi);
                 const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
-                const int ia0 = abi & 7, ia1 = (abi + 1) & 7;
                 const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
-                // cells (xbi + i, ybi + j), i, j in {0, 1}, inside 0..3
-                const float wx0 = (unsigned)xbi <= 3u ? 1.0f - fx : 0.0f;
-                const float wx1 = (unsigned)(xbi + 1) <= 3u ? fx : 0.0f;
-                const float wy0 = (unsigned)ybi <= 3u ? wm * (1.0f - fy) : 0.0f;
-                const float wy1 = (unsigned)(ybi + 1) <= 3u ? wm * fy : 0.0f;
-                const int cx0 = clampi(xbi, 0, 3), cx1 = clampi(xbi + 1, 0, 3);
-                const int cy0 = clampi(ybi, 0, 3) * 4, cy1 = clampi(ybi + 1, 0, 3) * 4;
+                // cells (xbi + i, ybi + j), i, j in {0, 1}: xbi, ybi in -1..3 for
+                // samples inside, so all four lie in the padded 6 x 6 grid; a
+                // sample outside has weight 0 and its adds are skipped (its
+                // indices are pinned to 0 so that no address leaves the grid)
+                if (!in) xbi = ybi = 0;
+                const float wx0 = 1.0f - fx, wx1 = fx;
+                const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
+                unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
 #pragma unroll
                 for (int cc = 0; cc < 4; ++cc) {
                     const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
-                    const int cell = (((cc & 2) ? cy1 : cy0) + ((cc & 1) ? cx1 : cx0)) * kHistRow;
+                    unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
                     // round to the nearest integer (< 2^23 by the scale choice)
                     const unsigned q0 = __float_as_uint(__fadd_rn(wxy * wa0, kMagic)) - 0x4B000000u;
                     const unsigned q1 = __float_as_uint(__fadd_rn(wxy * wa1, kMagic)) - 0x4B000000u;
-                    if (q0) atomicAdd(&hcopy[cell + ia0], q0);
-                    if (q1) atomicAdd(&hcopy[cell + ia1], q1);
+                    if (q0) atomicAdd(hc, q0);
+                    if (q1) atomicAdd(hc + 1, q1);
                 }
             }
         }
@@ -464,11 +470,15 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
             float d[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const int bin = tid + 32 * q;
-                const int at = (bin >> 3) * kHistRow + (bin & 7);
+                const int bin = tid + 32 * q;  // (iy * 4 + ix) * 8 + ia
+                const int cell = bin >> 3, ia = bin & 7;
+                const int at = (((cell >> 2) + 1) * kHistSide + (cell & 3) + 1) * kHistRow + ia;
                 unsigned v = 0u;
 #pragma unroll
                 for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at];
+                if (ia == 0)
+#pragma unroll
+                    for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at + 8];
                 d[q] = __fmul_rn((float)v, inv_fix);
             }
             float ss = 0.0f;
