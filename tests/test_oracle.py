@@ -163,3 +163,37 @@ def test_oracle_reproduces_committed_fixture(oracle_mod):
     m = match(fx["keypoints"], fx["descriptors"], kps, desc)
     assert len(kps) == len(fx["keypoints"]) and m.rate == 1.0 and m.same_order, m.summary()
     assert float(m.desc_err.max()) <= 1e-6, m.summary()
+
+
+def test_fp64_model_is_the_reference_algorithm(oracle_mod):
+    """oracle/ideal64.py with the reference's u8 rounding and f32 DoG put back
+    reproduces the u8 oracle's pyramid, candidates and refined keypoints (up
+    to the few pixels where float64 and f32 accumulation truncate differently),
+    so the FP64 model of the precision statement differs from the reference
+    path only by those roundings."""
+    import sift_wgpu_gb300 as sg
+    from oracle.ideal64 import Ideal64
+    img = sg.synth_image(0, 512, 512)
+    m = Ideal64(quantize=True, dog_f32=True)
+    pyr = m.pyramid(img)
+    dog = m.dog(pyr)
+    st = oracle_mod.stages(img, oracle_mod.params())
+    off = diff = 0
+    for lv in pyr:
+        for g in lv:
+            n = g.size
+            diff += int(np.count_nonzero(st.pyramid[off: off + n].reshape(g.shape) != g))
+            off += n
+    assert diff < 1e-3 * off
+    cands = m.extrema(dog)
+    ref = {(int(k["octave"]), int(k["layer"]), float(k["x"]), float(k["y"])) for k in st.candidates}
+    got = {(o, s, (x + 0.5) * 2.0 ** o, (y + 0.5) * 2.0 ** o) for (o, s, x, y) in cands}
+    assert len(ref & got) >= 0.995 * len(ref)
+    refined = m.refine(cands, dog)
+    rx = np.array([k["x"] for k in refined])
+    ry = np.array([k["y"] for k in refined])
+    hit = 0
+    for k in st.refined:
+        d = np.hypot(rx - float(k["x"]), ry - float(k["y"]))
+        hit += int(d.min() < 1e-3)
+    assert hit >= 0.995 * len(st.refined)
