@@ -138,6 +138,33 @@ int sift_cuda_detect(SiftCudaEngine* engine, const uint8_t* img, uint32_t width,
 
 void sift_cuda_result_free(SiftCudaResult* result);
 
+/* ---- colour input ----------------------------------------------------------- */
+
+/* Pixel formats of sift_cuda_detect_and_compute_pixels. The conversion to
+ * 8-bit luma runs on the device:
+ *   GRAY8          as sift_cuda_detect_and_compute
+ *   RGB8, RGBA8    DynamicImage::to_luma8 (src/sift.rs:1202, 1256; image 0.25.6:
+ *                  (2126 r + 7152 g + 722 b) / 10000, integer, alpha ignored)
+ *   RGBA8_CANVAS   the WASM entry's img_from_raw (src/wasm.rs:79-104):
+ *                  0.299 r + 0.587 g + 0.114 b in f32, truncated to u8 */
+enum {
+    SIFT_CUDA_PIXELS_GRAY8 = 0,
+    SIFT_CUDA_PIXELS_RGB8 = 1,
+    SIFT_CUDA_PIXELS_RGBA8 = 2,
+    SIFT_CUDA_PIXELS_RGBA8_CANVAS = 3
+};
+
+/* detect_and_compute_with_backend on a colour image (`stride` in bytes,
+ * >= width x channels): the host->device copy moves the colour bytes and the
+ * luma conversion is one more kernel before the pipeline. */
+int sift_cuda_detect_and_compute_pixels(SiftCudaEngine* engine, const uint8_t* pixels, uint32_t width,
+                                        uint32_t height, uint32_t stride, int32_t format,
+                                        SiftCudaResult* out);
+/* The conversion alone, device to device, asynchronous on `stream`
+ * (a cudaStream_t; NULL = default stream). */
+int sift_cuda_to_luma(const uint8_t* d_pixels, uint32_t width, uint32_t height, uint32_t stride,
+                      int32_t format, uint8_t* d_out, uint32_t out_stride, void* stream);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* sift_cuda_last_error(void);
 

@@ -213,3 +213,22 @@ def get_blur_model() -> OracleBlurModel:
 
 def set_blur_model(m: OracleBlurModel) -> None:
     lib().oracle_set_blur_model(C.byref(m))
+
+
+def luma_u8(pixels: np.ndarray, fmt: int) -> np.ndarray:
+    """Colour to 8-bit luma, restated for the conversion kernel's parity test.
+
+    fmt 1 / 2 (RGB8 / RGBA8): image 0.25.6 DynamicImage::to_luma8, the path of
+    src/sift.rs:1202 and 1256 (the crate is not vendored): integer
+    (2126 r + 7152 g + 722 b) / 10000, truncating, alpha ignored.
+    fmt 3 (RGBA8 canvas): img_from_raw, src/wasm.rs:89-93: f32
+    0.299 r + 0.587 g + 0.114 b, each product and sum rounded to f32 in that
+    order, then `as u8` (truncation, saturating)."""
+    p = np.asarray(pixels)
+    r, g, b = (p[..., k].astype(np.uint32) for k in range(3))
+    if fmt in (1, 2):
+        return ((2126 * r + 7152 * g + 722 * b) // 10000).astype(np.uint8)
+    f = np.float32
+    rf, gf, bf = r.astype(f), g.astype(f), b.astype(f)
+    lum = (f(0.299) * rf + f(0.587) * gf) + f(0.114) * bf
+    return np.clip(np.trunc(lum), 0, 255).astype(np.uint8)

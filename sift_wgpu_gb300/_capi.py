@@ -27,6 +27,11 @@ STATUS = {
 STORAGE_F32 = 0
 STORAGE_F16 = 1
 
+PIXELS_GRAY8 = 0
+PIXELS_RGB8 = 1
+PIXELS_RGBA8 = 2
+PIXELS_RGBA8_CANVAS = 3
+
 STAGE_PYRAMID = 0
 STAGE_CANDIDATES = 1
 STAGE_REFINED = 2
@@ -139,6 +144,8 @@ def lib() -> C.CDLL:
         "sift_cuda_detect_and_compute": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, P(Result)]),
         "sift_cuda_detect": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, P(Result)]),
         "sift_cuda_detect_and_compute_view": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, P(Result)]),
+        "sift_cuda_detect_and_compute_pixels": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, i32, P(Result)]),
+        "sift_cuda_to_luma": (C.c_int, [C.c_void_p, u32, u32, u32, i32, C.c_void_p, u32, C.c_void_p]),
         "sift_cuda_result_free": (None, [P(Result)]),
         "sift_cuda_last_error": (C.c_char_p, []),
         "sift_cuda_run_device": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, C.c_int]),
@@ -179,7 +186,7 @@ def exported_symbols() -> list[str]:
     return [
         "sift_cuda_params_default", "sift_cuda_params_new", "sift_cuda_options_default",
         "sift_cuda_create", "sift_cuda_destroy", "sift_cuda_detect_and_compute", "sift_cuda_detect",
-        "sift_cuda_detect_and_compute_view",
+        "sift_cuda_detect_and_compute_view", "sift_cuda_detect_and_compute_pixels", "sift_cuda_to_luma",
         "sift_cuda_result_free", "sift_cuda_last_error", "sift_cuda_run_device",
         "sift_cuda_device_outputs", "sift_cuda_synchronize", "sift_cuda_stream",
         "sift_cuda_debug_stage", "sift_cuda_last_launch_count", "sift_cuda_profile_enable",

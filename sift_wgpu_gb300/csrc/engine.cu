@@ -156,6 +156,32 @@ int sift_cuda_detect(SiftCudaEngine* engine, const uint8_t* img, uint32_t width,
     return engine->e.detect_host(img, width, height, stride, false, out);
 }
 
+int sift_cuda_detect_and_compute_pixels(SiftCudaEngine* engine, const uint8_t* pixels, uint32_t width,
+                                        uint32_t height, uint32_t stride, int32_t format, SiftCudaResult* out) {
+    sift::g_last_error.clear();
+    if (!out) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "out is NULL");
+    const int ch = sift::pixel_channels(format);
+    if (ch == 0) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "unknown pixel format");
+    if ((uint64_t)stride < (uint64_t)width * (uint64_t)ch)
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "stride < width x channels");
+    if (int rc = check_image(engine, pixels, width, height, stride, out)) return rc;
+    return engine->e.detect_host(pixels, width, height, stride, true, out, false, format);
+}
+
+int sift_cuda_to_luma(const uint8_t* d_pixels, uint32_t width, uint32_t height, uint32_t stride, int32_t format,
+                      uint8_t* d_out, uint32_t out_stride, void* stream) {
+    sift::g_last_error.clear();
+    const int ch = sift::pixel_channels(format);
+    if (ch <= 1) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "format must be a colour format");
+    if (width == 0 || height == 0) return 0;
+    if (!d_pixels || !d_out || (uint64_t)stride < (uint64_t)width * ch || out_stride < width)
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "NULL pointer or stride too small");
+    if (sift::launch_to_luma(format, d_pixels, stride, (int)width, (int)height, d_out, out_stride,
+                             (cudaStream_t)stream))
+        return sift::cuda_fail(cudaGetLastError(), "luma conversion");
+    return 0;
+}
+
 void sift_cuda_result_free(SiftCudaResult* r) {
     if (!r) return;
     std::free(r->kps);

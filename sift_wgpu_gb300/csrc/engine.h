@@ -54,6 +54,9 @@ int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, 
                    const float* hw, cudaStream_t st, bool fused, int* launches);
 int lanczos_fused_span();
 int lanczos_fused_tile();
+int pixel_channels(int format);
+int launch_to_luma(int format, const uint8_t* px, long long stride, int W, int H, uint8_t* out, long long out_pitch,
+                   cudaStream_t st);
 int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
                         uint32_t* words, cudaStream_t st);
 int launch_emit(int storage, const void* arena, const PyramidDev& pyr, int o, const uint32_t* words,
@@ -167,6 +170,7 @@ struct Engine {
     std::vector<size_t> pb, tb;  // scan-partials and horizontal-pass buffer offsets
     uint32_t cap_cand = 0, cap_ori = 0;
 
+    DevMem d_px;  // colour input before its luma conversion
     DevMem d_img, d_G, d_D, d_U, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
     DevMem d_words, d_cand_off, d_keep, d_keep_off, d_partials;
     DevMem d_cands, d_refined_at, d_refined, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
@@ -753,15 +757,29 @@ struct Engine {
         if (pitch != img_pitch || !d_img.p || d_img.bytes < pitch * std::max<uint32_t>(h, 1)) drop_graph();
         img_pitch = pitch;
         CK(d_img.ensure(img_pitch * std::max<uint32_t>(h, 1)), "cudaMalloc(image)");
-        if (w && h) CK(cudaMemcpy2DAsync(d_img.p, img_pitch, img, stride, w, h, kind, st), "copy image");
+        if (w && h && img) CK(cudaMemcpy2DAsync(d_img.p, img_pitch, img, stride, w, h, kind, st), "copy image");
         return 0;
     }
 
     int detect_host(const uint8_t* img, uint32_t w, uint32_t h, uint32_t stride, bool with_desc,
-                    SiftCudaResult* out, bool view = false) {
+                    SiftCudaResult* out, bool view = false, int format = SIFT_CUDA_PIXELS_GRAY8) {
         if (int rc = set_device()) return rc;
         if (int rc = ensure_geometry(w, h)) return rc;
-        if (int rc = upload(img, w, h, stride, cudaMemcpyHostToDevice)) return rc;
+        if (format == SIFT_CUDA_PIXELS_GRAY8) {
+            if (int rc = upload(img, w, h, stride, cudaMemcpyHostToDevice)) return rc;
+        } else {
+            // colour bytes to the device, luma into the image plane
+            const size_t ch = (size_t)pixel_channels(format), row = (size_t)w * ch;
+            const size_t pitch = align_up(std::max<size_t>(row, 1), 128);
+            CK(d_px.ensure(pitch * std::max<uint32_t>(h, 1)), "cudaMalloc(colour image)");
+            if (int rc = upload(nullptr, w, h, 0, cudaMemcpyHostToDevice)) return rc;
+            if (w && h) {
+                CK(cudaMemcpy2DAsync(d_px.p, pitch, img, stride, row, h, cudaMemcpyHostToDevice, st), "copy pixels");
+                if (launch_to_luma(format, d_px.as<uint8_t>(), (long long)pitch, (int)w, (int)h, d_img.as<uint8_t>(),
+                                   (long long)img_pitch, st))
+                    return cuda_fail(cudaGetLastError(), "luma conversion");
+            }
+        }
         for (int attempt = 0; attempt < 8; ++attempt) {
             if (int rc = run(with_desc)) return rc;
             bool retry = false;

@@ -160,8 +160,39 @@ class Engine:
         return kps, desc
 
     def detect_and_compute(self, img) -> tuple[np.ndarray, np.ndarray]:
-        """Keypoints (structured array) and descriptors (n x 128 f32)."""
+        """Keypoints (structured array) and descriptors (n x 128 f32).
+        H x W x 3 (RGB) and H x W x 4 (RGBA) uint8 images are converted to
+        luma on the device the way DynamicImage::to_luma8 does."""
+        a = np.asarray(img)
+        if a.ndim == 3 and a.dtype == np.uint8 and a.shape[2] in (3, 4):
+            return self.detect_and_compute_pixels(a, _capi.PIXELS_RGB8 if a.shape[2] == 3 else _capi.PIXELS_RGBA8)
         return self._call(_capi.lib().sift_cuda_detect_and_compute, img, True)
+
+    def detect_and_compute_pixels(self, img, fmt: int) -> tuple[np.ndarray, np.ndarray]:
+        """A colour image (H x W x 3 for PIXELS_RGB8, H x W x 4 for PIXELS_RGBA8
+        or PIXELS_RGBA8_CANVAS) converted to luma on the device, then the
+        pipeline (sift_cuda_detect_and_compute_pixels)."""
+        a = np.asarray(img)
+        ch = {_capi.PIXELS_RGB8: 3, _capi.PIXELS_RGBA8: 4, _capi.PIXELS_RGBA8_CANVAS: 4}.get(fmt)
+        if ch is None or a.dtype != np.uint8 or a.ndim != 3 or a.shape[2] != ch:
+            raise SiftError(f"expected an H x W x {ch} uint8 image for pixel format {fmt}")
+        if a.strides[2] != 1 or a.strides[1] != ch:
+            a = np.ascontiguousarray(a)
+        h, w = a.shape[:2]
+        res = _capi.Result()
+        L = _capi.lib()
+        _capi.check(L.sift_cuda_detect_and_compute_pixels(self.handle, a.ctypes.data if a.size else None, w, h,
+                                                          a.strides[0], fmt, C.byref(res)))
+        try:
+            n = res.n
+            kps = np.empty(n, dtype=KEYPOINT_DTYPE)
+            desc = np.empty((n, DESC_LEN), dtype=np.float32)
+            if n:
+                C.memmove(kps.ctypes.data, res.kps, n * KEYPOINT_DTYPE.itemsize)
+                C.memmove(desc.ctypes.data, res.desc, n * DESC_LEN * 4)
+        finally:
+            L.sift_cuda_result_free(C.byref(res))
+        return kps, desc
 
     def detect(self, img) -> np.ndarray:
         return self._call(_capi.lib().sift_cuda_detect, img, False)[0]

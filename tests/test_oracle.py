@@ -197,3 +197,14 @@ def test_fp64_model_is_the_reference_algorithm(oracle_mod):
         d = np.hypot(rx - float(k["x"]), ry - float(k["y"]))
         hit += int(d.min() < 1e-3)
     assert hit >= 0.995 * len(st.refined)
+
+
+def test_luma_restatements(oracle_mod):
+    """Known answers of the two luma formulas (image 0.25.6 to_luma8 integer
+    weights; src/wasm.rs:89-93 in f32)."""
+    px = np.array([[[255, 255, 255, 0], [255, 0, 0, 9], [0, 255, 0, 9], [0, 0, 255, 9], [10, 20, 30, 0]]], np.uint8)
+    assert oracle_mod.luma_u8(px, 2).tolist() == [[255, 54, 182, 18, 18]]
+    f = np.float32
+    want = [int(np.trunc((f(0.299) * f(r) + f(0.587) * f(g)) + f(0.114) * f(b))) for r, g, b, _ in px[0]]
+    assert oracle_mod.luma_u8(px, 3).tolist() == [want]
+    assert oracle_mod.luma_u8(px[..., :3], 1).tolist() == oracle_mod.luma_u8(px, 2).tolist()
