@@ -115,10 +115,19 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
         const float gx = __fsub_rn(g.px_in(xi + 1, yi), g.px_in(xi - 1, yi));
         const float gy = __fsub_rn(g.px_in(xi, yi + 1), g.px_in(xi, yi - 1));
         const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
-        const float ang = atan2f(gy, gx);
         const float wgt = expf(__fdiv_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), wd));
-        const float an = ang < 0.0f ? __fadd_rn(ang, two_pi) : ang;
-        const float bf = __fdiv_rn(__fmul_rn(an, (float)kOriBins), two_pi);  // in [0, 36]
+        // Bin index: from the polynomial atan2 and a multiply by 36 / (2 pi)
+        // (a few ulp from the exact value), unless that lands within 1e-4 of
+        // a bin edge; then from atan2f and the IEEE division, the exact
+        // sequence. Away from the edges both floor to the same bin.
+        const float pa = atan2_poly(gy, gx);
+        const float pn = pa < 0.0f ? __fadd_rn(pa, two_pi) : pa;
+        float bf = __fmul_rn(pn, (float)kOriBins / two_pi);
+        if (fabsf(__fsub_rn(bf, rintf(bf))) < 1e-4f) {
+            const float ang = atan2f(gy, gx);
+            const float an = ang < 0.0f ? __fadd_rn(ang, two_pi) : ang;
+            bf = __fdiv_rn(__fmul_rn(an, (float)kOriBins), two_pi);  // in [0, 36]
+        }
         const int fl = floor_i(bf);
         const int bin = fl >= kOriBins ? fl - kOriBins : fl;
         const float v = __fmul_rn(mag, wgt);
@@ -445,22 +454,22 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                 const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
                 const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
                 // cells (xbi + i, ybi + j), i, j in {0, 1}: xbi, ybi in -1..3 for
-                // samples inside, so all four lie in the padded 6 x 6 grid; a
-                // sample outside has weight 0 and its adds are skipped (its
-                // indices are pinned to 0 so that no address leaves the grid)
-                if (!in) xbi = ybi = 0;
-                const float wx0 = 1.0f - fx, wx1 = fx;
-                const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
-                unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
+                // samples inside, so all four lie in the padded 6 x 6 grid.
+                // Samples outside add nothing; inside, the eight adds are
+                // unconditional (a zero share adds 0): one branch per sample
+                // instead of one per add.
+                if (in) {
+                    const float wx0 = 1.0f - fx, wx1 = fx;
+                    const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
+                    unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
 #pragma unroll
-                for (int cc = 0; cc < 4; ++cc) {
-                    const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
-                    unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
-                    // round to the nearest integer (< 2^23 by the scale choice)
-                    const unsigned q0 = __float_as_uint(__fadd_rn(wxy * wa0, kMagic)) - 0x4B000000u;
-                    const unsigned q1 = __float_as_uint(__fadd_rn(wxy * wa1, kMagic)) - 0x4B000000u;
-                    if (q0) atomicAdd(hc, q0);
-                    if (q1) atomicAdd(hc + 1, q1);
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
+                        unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
+                        // round to the nearest integer (< 2^23 by the scale choice)
+                        atomicAdd(hc, __float_as_uint(__fadd_rn(wxy * wa0, kMagic)) - 0x4B000000u);
+                        atomicAdd(hc + 1, __float_as_uint(__fadd_rn(wxy * wa1, kMagic)) - 0x4B000000u);
+                    }
                 }
             }
         }

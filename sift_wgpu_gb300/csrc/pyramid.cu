@@ -517,16 +517,17 @@ static int set_smem(const void* k, size_t smem) {
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess ? 0 : -1;
 }
 
-// One level from the previous level's u8 plane: fused when r <= 8 and
-// r <= fused_max_radius (its horizontal pass recomputes a 2r-row halo per
-// 64-row tile), else the two separable passes, which spread a small octave
-// over many CTAs.
+// One level from the previous level's u8 plane: fused when r <=
+// fused_max_radius and its tile fits in shared memory (the horizontal pass
+// recomputes a 2r-row halo per 64-row tile; radii up to 8 are compiled in,
+// larger ones take the run-time-radius kernel), else the two separable
+// passes, which spread a large-radius level over many CTAs.
 template <typename TG>
 int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, float* dog, int pitch,
                       int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
                       int* launches, int fused_max_radius) {
     const size_t smem = blur_fused_smem(r);
-    if (r <= 8 && r <= fused_max_radius && smem <= 160 * 1024) {
+    if (r <= fused_max_radius && smem <= 160 * 1024) {
         void (*kern)(const uint8_t*, int, TG*, uint8_t*, float*, int, int, int, int, const float*, const float*, int);
         switch (r) {
             case 1: kern = k_blur_level<TG, 1>; break;

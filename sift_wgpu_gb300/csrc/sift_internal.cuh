@@ -137,8 +137,8 @@ __device__ __forceinline__ float rem_euclid_2b(float a, float b) {
 // atan(a) = a * P(a^2) with a degree-7 polynomial fitted by iteratively
 // reweighted least squares on [0, 1] (relative error 1e-7 in f64, under 3 ulp
 // evaluated in f32), then the octant fix-ups. atan2(0, 0) = 0. Used where the
-// angle is interpolated linearly (descriptor bins); the orientation
-// histogram, whose bins are a hard floor, keeps atan2f.
+// angle is interpolated linearly (descriptor bins), and by the orientation
+// histogram, whose bins are a hard floor, only away from the bin edges.
 __device__ __forceinline__ float atan2_poly(float y, float x) {
     const float ax = fabsf(x), ay = fabsf(y);
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
