@@ -10,9 +10,10 @@
 //                   columns are summed in a fixed order, then the two [1,1,1]/3
 //                   smoothing passes and the peak test run one bin per lane;
 //                   peaks come out in bin order through a ballot.
-//   k_orient_emit   keypoint i with c_i peaks writes its c_i oriented copies at
-//                   the scanned offset, so the output order is the reference's
-//                   (keypoint, bin) order.
+//   k_orient_emit   candidate slot i with c_i peaks (0 if refinement rejected
+//                   it) writes its c_i oriented copies at the scanned offset,
+//                   so the output order is the reference's (keypoint, bin)
+//                   order.
 //   k_descriptor    one CTA per oriented keypoint: the bilinear samples of the
 //                   window are computed once into a shared grid, window samples
 //                   are split over the threads, trilinear contributions are
@@ -138,7 +139,8 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
 
 template <typename TG>
 __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
-                                                                   const Keypoint* __restrict__ refined,
+                                                                   const Keypoint* __restrict__ refined_at,
+                                                                   const uint32_t* __restrict__ keep, uint32_t ncap,
                                                                    OctCounters* __restrict__ oc,
                                                                    float* __restrict__ ori_angle,
                                                                    uint32_t* __restrict__ ori_count) {
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
     if constexpr (sizeof(TG) == 2) fill_lut(lut);
     __syncthreads();
     const int lane = threadIdx.x, wid = threadIdx.y;
-    const uint32_t n = oc->n_ref;
+    const uint32_t n = min(oc->n_cand, ncap);  // candidate slots; rejected ones get 0 peaks
     const float two_pi = 2.0f * kPi;
     const float bin_w = 2.0f * kPi / (float)kOriBins;
     for (;;) {
@@ -156,7 +158,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
         if (lane == 0) i = atomicAdd(&oc->next_ori, 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= n) break;
-        const Keypoint kp = refined[i];
+        if (!keep[i]) {
+            if (lane == 0) ori_count[i] = 0;
+            continue;
+        }
+        const Keypoint kp = refined_at[i];
         const int o = kp.octave;
         uint32_t cnt = 0;
         if (o >= 0 && o < pyr.num_octaves) {
@@ -237,24 +243,27 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
 }
 
 // Octave o's oriented keypoints go after those of octaves 0..o-1 (whose
-// counts are final: their orientation scans precede this kernel).
-__global__ void k_orient_emit(const Keypoint* __restrict__ refined, int o, Counters* __restrict__ ctr,
-                              const float* __restrict__ ori_angle, const uint32_t* __restrict__ ori_count,
-                              const uint32_t* __restrict__ ori_off, Keypoint* __restrict__ oriented, uint32_t cap) {
+// counts are final: their orientation scans precede this kernel). Candidate
+// slot i holds ori_count[i] peaks (0 for a rejected candidate).
+__global__ void k_orient_emit(const Keypoint* __restrict__ refined_at, uint32_t ncap, int o,
+                              Counters* __restrict__ ctr, const float* __restrict__ ori_angle,
+                              const uint32_t* __restrict__ ori_count, const uint32_t* __restrict__ ori_off,
+                              Keypoint* __restrict__ oriented, uint32_t cap) {
     OctCounters* oc = &ctr->oct[o];
     uint32_t base = 0;
     for (int q = 0; q < o; ++q) base += ctr->oct[q].n_ori;
-    const uint32_t n = oc->n_ref;
+    const uint32_t n = min(oc->n_cand, ncap);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         oc->out_base = base;
         atomicAdd(&ctr->n_candidates, oc->n_cand);
-        atomicAdd(&ctr->n_refined, n);
+        atomicAdd(&ctr->n_refined, oc->n_ref);
         atomicMax(&ctr->n_oriented, base + oc->n_ori);
         if (base + oc->n_ori > cap) atomicOr(&ctr->overflow, 4u);
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t c = ori_count[i], off = base + ori_off[i];
-        Keypoint k = refined[i];
+        if (c == 0) continue;
+        Keypoint k = refined_at[i];
         for (uint32_t j = 0; j < c; ++j) {
             if (off + j >= cap) break;
             k.angle = ori_angle[(size_t)i * kOriMaxPeaks + j];
@@ -525,16 +534,18 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
 int describe_grid() { return 152 * 4; }
 
 template <typename TG>
-int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, OctCounters* oc,
-                       float* ori_angle, uint32_t* ori_count, int grid, cudaStream_t st) {
-    k_orientation<TG><<<grid, dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined, oc, ori_angle, ori_count);
+int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
+                       uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,
+                       cudaStream_t st) {
+    k_orientation<TG><<<grid, dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined_at, keep, ncap, oc, ori_angle,
+                                                               ori_count);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_orient_emit(const Keypoint* refined, int o, Counters* ctr, const float* ori_angle,
+int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counters* ctr, const float* ori_angle,
                        const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
                        cudaStream_t st) {
-    k_orient_emit<<<152, 256, 0, st>>>(refined, o, ctr, ori_angle, ori_count, ori_off, oriented, cap);
+    k_orient_emit<<<152, 256, 0, st>>>(refined_at, ncap, o, ctr, ori_angle, ori_count, ori_off, oriented, cap);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -545,10 +556,10 @@ int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* or
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-template int launch_orientation<float>(const float*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
-                                       uint32_t*, int, cudaStream_t);
-template int launch_orientation<__half>(const __half*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
-                                        uint32_t*, int, cudaStream_t);
+template int launch_orientation<float>(const float*, const PyramidDev&, const Keypoint*, const uint32_t*, uint32_t,
+                                       OctCounters*, float*, uint32_t*, int, cudaStream_t);
+template int launch_orientation<__half>(const __half*, const PyramidDev&, const Keypoint*, const uint32_t*, uint32_t,
+                                        OctCounters*, float*, uint32_t*, int, cudaStream_t);
 template int launch_descriptor<float>(const float*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
                                       uint32_t, int, cudaStream_t);
 template int launch_descriptor<__half>(const __half*, const PyramidDev&, const Keypoint*, OctCounters*, float*,

@@ -11,8 +11,10 @@
 //   k_emit           one thread per word writes the word's candidates to their
 //                    slots.
 //   k_refine         one thread per candidate: the Newton refinement, contrast
-//                    and edge tests in the reference's f32 operation order.
-//   scan + k_compact survivors move to their final slots, order kept.
+//                    and edge tests in the reference's f32 operation order;
+//                    the result stays in the candidate's slot with a keep
+//                    flag (the orientation stage reads the slots in order and
+//                    skips the rejected ones, so no compaction pass is needed).
 //
 // All arithmetic is f32 with separately rounded operations (no FMA), so the
 // candidates and refined keypoints are bit-identical to the CPU path; the one
@@ -336,33 +338,31 @@ __global__ void __launch_bounds__(256) k_emit(const void* arena, PyramidDev pyr,
     }
 }
 
-// One thread per candidate of octave o (persistent grid over its count).
+// One thread per candidate of octave o (persistent grid over its count); the
+// survivors are counted per warp into oc->n_ref (a count, order-free).
 template <class Dog>
 __global__ void __launch_bounds__(256) k_refine(const void* arena, PyramidDev pyr, int o, RefineParams rp,
                                                 const Keypoint* __restrict__ cands,
                                                 Keypoint* __restrict__ refined_at, uint32_t* __restrict__ keep,
-                                                uint32_t cap, const OctCounters* __restrict__ oc) {
+                                                uint32_t cap, OctCounters* __restrict__ oc) {
     const uint32_t n = min(oc->n_cand, cap);
     const Dog dog = make_dog<Dog>(arena, pyr.oct[o]);
     const float scale = __int_as_float((127 + o) << 23);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const Keypoint k = cands[i];
-        const int x = rust_as_i32(__fdiv_rn(k.x, scale)), y = rust_as_i32(__fdiv_rn(k.y, scale));
-        Keypoint r;
-        const bool ok = refine_one(dog, o, x, y, k.layer, rp, &r);
-        if (ok) refined_at[i] = r;
-        keep[i] = ok ? 1u : 0u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        const uint32_t i = i0 + threadIdx.x;
+        bool ok = false;
+        if (i < n) {
+            const Keypoint k = cands[i];
+            const int x = rust_as_i32(__fdiv_rn(k.x, scale)), y = rust_as_i32(__fdiv_rn(k.y, scale));
+            Keypoint r;
+            ok = refine_one(dog, o, x, y, k.layer, rp, &r);
+            if (ok) refined_at[i] = r;
+            keep[i] = ok ? 1u : 0u;
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, ok);
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(&oc->n_ref, (uint32_t)__popc(m));
     }
-}
-
-__global__ void __launch_bounds__(256) k_compact(const uint32_t* __restrict__ keep,
-                                                 const uint32_t* __restrict__ keep_off,
-                                                 const Keypoint* __restrict__ refined_at,
-                                                 Keypoint* __restrict__ refined, uint32_t cap,
-                                                 const OctCounters* __restrict__ oc) {
-    const uint32_t n = min(oc->n_cand, cap);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        if (keep[i]) refined[keep_off[i]] = refined_at[i];
 }
 
 }  // namespace
@@ -398,20 +398,13 @@ int launch_emit(int storage, const void* arena, const PyramidDev& pyr, int o, co
 
 int launch_refine(int storage, const void* arena, const PyramidDev& pyr, int o, float sigma, float contrast,
                   float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
-                  const OctCounters* oc, cudaStream_t st) {
+                  OctCounters* oc, cudaStream_t st) {
     RefineParams rp{sigma, contrast, edge, pyr.S, pyr.S + 2};
     const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 2);
     if (storage == SIFT_CUDA_STORAGE_F16)
         k_refine<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, o, rp, cands, refined_at, keep, cap, oc);
     else
         k_refine<DogF32><<<grid, 256, 0, st>>>(arena, pyr, o, rp, cands, refined_at, keep, cap, oc);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
-}
-
-int launch_compact(const uint32_t* keep, const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined,
-                   uint32_t cap, const OctCounters* oc, cudaStream_t st) {
-    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 2);
-    k_compact<<<grid, 256, 0, st>>>(keep, keep_off, refined_at, refined, cap, oc);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -280,24 +280,44 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
     }
     const sift::Keypoint* src = nullptr;
     uint64_t n = 0;
-    if (stage == SIFT_CUDA_STAGE_CANDIDATES || stage == SIFT_CUDA_STAGE_REFINED) {
+    if (stage == SIFT_CUDA_STAGE_CANDIDATES) {
         // per-octave regions, concatenated in octave order
-        const bool cand = stage == SIFT_CUDA_STAGE_CANDIDATES;
-        const sift::Keypoint* base = cand ? e.d_cands.as<sift::Keypoint>() : e.d_refined.as<sift::Keypoint>();
         uint64_t total = 0;
-        for (int o = 0; o < g.num_octaves; ++o)
-            total += std::min<uint64_t>(cand ? c.oct[o].n_cand : c.oct[o].n_ref, e.cap_c[o]);
+        for (int o = 0; o < g.num_octaves; ++o) total += std::min<uint64_t>(c.oct[o].n_cand, e.cap_c[o]);
         *count = total;
         if (!out) return 0;
         uint64_t pos = 0;
         for (int o = 0; o < g.num_octaves && pos < capacity; ++o) {
-            const uint64_t no = std::min<uint64_t>(cand ? c.oct[o].n_cand : c.oct[o].n_ref, e.cap_c[o]);
+            const uint64_t no = std::min<uint64_t>(c.oct[o].n_cand, e.cap_c[o]);
             const uint64_t m = std::min<uint64_t>(no, capacity - pos);
-            if (m && cudaMemcpy((sift::Keypoint*)out + pos, base + e.cb[o], m * sizeof(sift::Keypoint),
-                                cudaMemcpyDeviceToHost) != cudaSuccess)
+            if (m && cudaMemcpy((sift::Keypoint*)out + pos, e.d_cands.as<sift::Keypoint>() + e.cb[o],
+                                m * sizeof(sift::Keypoint), cudaMemcpyDeviceToHost) != cudaSuccess)
                 return sift::cuda_fail(cudaGetLastError(), "D2H stage");
             pos += m;
         }
+        return 0;
+    } else if (stage == SIFT_CUDA_STAGE_REFINED) {
+        // the refined keypoints stay in their candidate slots with keep
+        // flags; gathered here in slot order, octave after octave
+        std::vector<sift::Keypoint> slots;
+        std::vector<uint32_t> keep;
+        uint64_t pos = 0, total = 0;
+        for (int o = 0; o < g.num_octaves; ++o) {
+            const uint64_t no = std::min<uint64_t>(c.oct[o].n_cand, e.cap_c[o]);
+            slots.resize(no);
+            keep.resize(no);
+            if (no && (cudaMemcpy(slots.data(), e.d_refined_at.as<sift::Keypoint>() + e.cb[o],
+                                  no * sizeof(sift::Keypoint), cudaMemcpyDeviceToHost) != cudaSuccess ||
+                       cudaMemcpy(keep.data(), e.d_keep.as<uint32_t>() + e.cb[o], no * sizeof(uint32_t),
+                                  cudaMemcpyDeviceToHost) != cudaSuccess))
+                return sift::cuda_fail(cudaGetLastError(), "D2H stage");
+            for (uint64_t i = 0; i < no; ++i) {
+                if (!keep[i]) continue;
+                if (out && pos < capacity) ((sift::Keypoint*)out)[pos++] = slots[i];
+                ++total;
+            }
+        }
+        *count = total;
         return 0;
     } else if (stage == SIFT_CUDA_STAGE_KEYPOINTS) {
         src = e.d_oriented.as<sift::Keypoint>();

@@ -63,13 +63,12 @@ int launch_emit(int storage, const void* arena, const PyramidDev& pyr, int o, co
                 const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st);
 int launch_refine(int storage, const void* arena, const PyramidDev& pyr, int o, float sigma, float contrast,
                   float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
-                  const OctCounters* oc, cudaStream_t st);
-int launch_compact(const uint32_t* keep, const uint32_t* keep_off, const Keypoint* refined_at, Keypoint* refined,
-                   uint32_t cap, const OctCounters* oc, cudaStream_t st);
+                  OctCounters* oc, cudaStream_t st);
 template <typename TG>
-int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined, OctCounters* oc,
-                       float* ori_angle, uint32_t* ori_count, int grid, cudaStream_t st);
-int launch_orient_emit(const Keypoint* refined, int o, Counters* ctr, const float* ori_angle,
+int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
+                       uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,
+                       cudaStream_t st);
+int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counters* ctr, const float* ori_angle,
                        const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
                        cudaStream_t st);
 template <typename TG>
@@ -167,13 +166,14 @@ struct Engine {
     // scan scratch; the output lists (oriented keypoints, descriptors) are
     // shared, octave after octave.
     std::vector<uint32_t> cap_c, cb;
-    std::vector<size_t> pb, tb;  // scan-partials and horizontal-pass buffer offsets
+    std::vector<size_t> pb, tb;  // scan-state (64-bit words) and horizontal-pass buffer offsets
+    size_t scan_words = 0;       // scan state of the run, zeroed at its start
     uint32_t cap_cand = 0, cap_ori = 0;
 
     DevMem d_px;  // colour input before its luma conversion
     DevMem d_img, d_G, d_D, d_U, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
-    DevMem d_words, d_cand_off, d_keep, d_keep_off, d_partials;
-    DevMem d_cands, d_refined_at, d_refined, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
+    DevMem d_words, d_cand_off, d_keep, d_scan;
+    DevMem d_cands, d_refined_at, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
     HostPinned h_ctr, h_kps, h_desc;
     size_t img_pitch = 0;
     uint32_t launches = 0;
@@ -287,7 +287,7 @@ struct Engine {
     size_t device_bytes() const {
         size_t t = 0;
         for (const DevMem* m : {&d_img, &d_G, &d_D, &d_U, &d_tmp, &d_tmpo, &d_ltmp, &d_wts, &d_ltab, &d_lw, &d_words,
-                                &d_cand_off, &d_keep, &d_keep_off, &d_partials, &d_cands, &d_refined_at, &d_refined,
+                                &d_cand_off, &d_keep, &d_scan, &d_cands, &d_refined_at,
                                 &d_ori_angle, &d_ori_count, &d_ori_off, &d_oriented, &d_desc, &d_ctr})
             t += m->bytes;
         return t;
@@ -461,23 +461,23 @@ struct Engine {
         for (int o = 0; o < O; ++o) {
             cb[o] = (uint32_t)c;
             c += cap_c[o];
+            // two scans per octave: the candidate words, then the orientation counts
             pb[o] = pp;
-            pp += align_up(scan_partials_size(std::max<size_t>({(size_t)octave_words(o), (size_t)cap_c[o], 1})), 64);
+            pp += scan_state_words((size_t)octave_words(o)) + scan_state_words((size_t)cap_c[o]);
         }
+        scan_words = pp;
         if (c > (1u << 30)) return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint lists above 2^30");
         cap_cand = (uint32_t)c;
         const size_t kp = sizeof(Keypoint);
         CK(d_cands.ensure((size_t)cap_cand * kp), "cudaMalloc(cands)");
         CK(d_refined_at.ensure((size_t)cap_cand * kp), "cudaMalloc(refined_at)");
-        CK(d_refined.ensure((size_t)cap_cand * kp), "cudaMalloc(refined)");
         CK(d_ori_angle.ensure((size_t)cap_cand * kOriMaxPeaks * sizeof(float)), "cudaMalloc(ori_angle)");
         CK(d_ori_count.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(ori_count)");
         CK(d_ori_off.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(ori_off)");
         CK(d_keep.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(keep)");
-        CK(d_keep_off.ensure((size_t)cap_cand * sizeof(uint32_t)), "cudaMalloc(keep_off)");
         CK(d_oriented.ensure((size_t)cap_ori * kp), "cudaMalloc(oriented)");
         CK(d_desc.ensure((size_t)cap_ori * kDescLen * sizeof(float)), "cudaMalloc(desc)");
-        CK(d_partials.ensure(std::max<size_t>(pp, 1) * sizeof(uint32_t)), "cudaMalloc(partials)");
+        CK(d_scan.ensure(std::max<size_t>(pp, 1) * sizeof(unsigned long long)), "cudaMalloc(scan state)");
         return 0;
     }
 
@@ -509,6 +509,7 @@ struct Engine {
         std::vector<cudaEvent_t> run_ev;
         mark(&run_ev);
         CK(cudaMemsetAsync(d_ctr.p, 0, sizeof(Counters), st), "memset counters");
+        CK(cudaMemsetAsync(d_scan.p, 0, scan_words * sizeof(unsigned long long), st), "memset scan state");
         int O_used = 0;
         for (int o = 0; o < O && pyr.oct[o].W > 0 && pyr.oct[o].H > 0; ++o) O_used = o + 1;
 
@@ -550,16 +551,16 @@ struct Engine {
         auto detect = [&](int o, cudaStream_t q) -> int {
             const OctaveDev& od = pyr.oct[o];
             OctCounters* oc = &ctr->oct[o];
-            uint32_t* partials = d_partials.as<uint32_t>() + pb[o];
+            unsigned long long* sstate = d_scan.as<unsigned long long>() + pb[o];
             const long long nwo = octave_words(o);
             if (od.nw > 0 && ok(launch_extrema_mask(U, lut, pyr, o, (int)p.image_border_width, d_words.as<uint32_t>(),
                                                     q)))
                 return cuda_fail(cudaGetLastError(), "extrema mask");
             if (scan_exclusive(d_words.as<uint32_t>() + od.word_base, SCAN_POPC,
-                               d_cand_off.as<uint32_t>() + od.word_base, (size_t)nwo, nullptr, &oc->n_cand, partials,
-                               q))
+                               d_cand_off.as<uint32_t>() + od.word_base, (size_t)nwo, nullptr, &oc->n_cand, sstate,
+                               &ctr->overflow, q))
                 return cuda_fail(cudaGetLastError(), "scan candidates");
-            launches += nwo > 0 ? 3 : 0;
+            launches += nwo > 0 ? 1 : 0;
             if (ok(launch_emit(opt.storage, arena, pyr, o, d_words.as<uint32_t>() + od.word_base,
                                d_cand_off.as<uint32_t>() + od.word_base, d_cands.as<Keypoint>() + cb[o], cap_c[o], ctr,
                                q)))
@@ -568,34 +569,28 @@ struct Engine {
                                  d_cands.as<Keypoint>() + cb[o], d_refined_at.as<Keypoint>() + cb[o],
                                  d_keep.as<uint32_t>() + cb[o], cap_c[o], oc, q)))
                 return cuda_fail(cudaGetLastError(), "refine");
-            if (scan_exclusive(d_keep.as<uint32_t>() + cb[o], SCAN_U32, d_keep_off.as<uint32_t>() + cb[o],
-                               (size_t)cap_c[o], &oc->n_cand, &oc->n_ref, partials, q))
-                return cuda_fail(cudaGetLastError(), "scan refined");
-            launches += 3;
-            if (ok(launch_compact(d_keep.as<uint32_t>() + cb[o], d_keep_off.as<uint32_t>() + cb[o],
-                                  d_refined_at.as<Keypoint>() + cb[o], d_refined.as<Keypoint>() + cb[o], cap_c[o], oc,
-                                  q)))
-                return cuda_fail(cudaGetLastError(), "compact");
             return 0;
         };
-        // (d) orientation histograms and their scan
+        // (d) orientation histograms of the kept candidate slots and their scan
         auto orient = [&](int o, cudaStream_t q) -> int {
             OctCounters* oc = &ctr->oct[o];
             const int grid =
                 (int)std::min<uint32_t>(std::max<uint32_t>(cap_c[o] / 64, 32), 152u * (uint32_t)tune.ori_ctas_per_sm);
-            if (ok(launch_orientation<TG>(G, pyr, d_refined.as<Keypoint>() + cb[o], oc,
-                                          d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
+            if (ok(launch_orientation<TG>(G, pyr, d_refined_at.as<Keypoint>() + cb[o], d_keep.as<uint32_t>() + cb[o],
+                                          cap_c[o], oc, d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
                                           d_ori_count.as<uint32_t>() + cb[o], grid, q)))
                 return cuda_fail(cudaGetLastError(), "orientation");
+            unsigned long long* sstate =
+                d_scan.as<unsigned long long>() + pb[o] + scan_state_words((size_t)octave_words(o));
             if (scan_exclusive(d_ori_count.as<uint32_t>() + cb[o], SCAN_U32, d_ori_off.as<uint32_t>() + cb[o],
-                               (size_t)cap_c[o], &oc->n_ref, &oc->n_ori, d_partials.as<uint32_t>() + pb[o], q))
+                               (size_t)cap_c[o], &oc->n_cand, &oc->n_ori, sstate, &ctr->overflow, q))
                 return cuda_fail(cudaGetLastError(), "scan orientations");
-            launches += 3;
+            launches += 1;
             return 0;
         };
         // output slots of octave o (after octaves 0..o-1) and its descriptors
         auto emit_out = [&](int o, cudaStream_t q) -> int {
-            if (ok(launch_orient_emit(d_refined.as<Keypoint>() + cb[o], o, ctr,
+            if (ok(launch_orient_emit(d_refined_at.as<Keypoint>() + cb[o], cap_c[o], o, ctr,
                                       d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
                                       d_ori_count.as<uint32_t>() + cb[o], d_ori_off.as<uint32_t>() + cb[o],
                                       d_oriented.as<Keypoint>(), cap_ori, q)))
@@ -729,6 +724,7 @@ struct Engine {
     // *retry tells that the run must be repeated.
     int grow_from(const Counters& c, bool* retry) {
         *retry = false;
+        if (c.overflow & 8u) return fail(SIFT_CUDA_ERR_CUDA, "a prefix-scan wait ran out (the run was abandoned)");
         bool grow = false;
         for (int o = 0; o < pyr.num_octaves; ++o) {
             const uint32_t n = c.oct[o].n_cand;

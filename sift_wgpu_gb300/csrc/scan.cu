@@ -1,10 +1,22 @@
 // scan.cu — deterministic exclusive prefix sum used for ordered compaction.
 //
-// Three launches (tile reduce, scan of tile sums, tile scan) with a fixed
-// tile order, so every output position is a pure function of the inputs. The
-// element count may live in device memory (n_dev) so that a stage whose
+// One launch per scan (single pass with decoupled look-back): each CTA takes
+// the next tile ticket, reduces its tile, publishes the tile sum, then walks
+// back over its predecessors' published sums until it meets an inclusive
+// prefix, publishes its own inclusive prefix and writes its outputs. A CTA
+// waits only on tiles whose tickets were handed out before its own, to CTAs
+// already running, so every wait ends; each wait is bounded anyway, and a
+// wait that runs out sets bit 8 of the run's overflow word instead of
+// hanging. Every output is an exact integer sum, so the result does not
+// depend on scheduling.
+//
+// The element count may live in device memory (n_dev) so that a stage whose
 // length is only known on the GPU needs no host round trip; the grid is then
-// sized for the host bound and surplus tiles exit.
+// sized for the host bound and tiles past the end exit at once.
+//
+// State: scan_state_words(n) 64-bit words per scan — a ticket counter and one
+// status word per tile (flag << 32 | value; flag 1 = tile sum, 2 = inclusive
+// prefix), zero before the scan runs.
 #include "sift_internal.cuh"
 
 namespace sift {
@@ -13,20 +25,13 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kItems = 8;
 constexpr int kTile = kThreads * kItems;
+constexpr unsigned kMaxWaits = 1u << 20;  // x ~64 ns: a wait gives up after ~0.1 s
 
 template <int MODE>
 __device__ __forceinline__ uint32_t load_item(const uint32_t* in, size_t i, size_t n) {
     if (i >= n) return 0u;
     uint32_t v = in[i];
     return MODE == SCAN_POPC ? (uint32_t)__popc(v) : v;
-}
-
-__device__ __forceinline__ size_t eff_n(size_t n, const uint32_t* n_dev) {
-    if (n_dev) {
-        size_t d = *n_dev;
-        return d < n ? d : n;
-    }
-    return n;
 }
 
 // Block-wide exclusive scan of one value per thread; returns the exclusive
@@ -59,60 +64,28 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total)
     return r;
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_scan_reduce(const uint32_t* __restrict__ in, size_t n,
-                                                          const uint32_t* __restrict__ n_dev,
-                                                          uint32_t* __restrict__ partials) {
-    const size_t N = eff_n(n, n_dev);
-    const size_t base = (size_t)blockIdx.x * kTile;
-    if (base >= N) {
-        if (threadIdx.x == 0) partials[blockIdx.x] = 0u;
-        return;
-    }
-    uint32_t s = 0;
-#pragma unroll
-    for (int k = 0; k < kItems; ++k) s += load_item<MODE>(in, base + (size_t)k * kThreads + threadIdx.x, N);
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
-    __shared__ uint32_t ws[kThreads / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t t = 0;
-        for (int w = 0; w < kThreads / 32; ++w) t += ws[w];
-        partials[blockIdx.x] = t;
-    }
-}
-
-// One CTA scans the tile sums in place (exclusive) and writes the total.
-__global__ void __launch_bounds__(kThreads) k_scan_partials(uint32_t* __restrict__ partials, size_t nb,
-                                                            uint32_t* __restrict__ total_out) {
-    __shared__ uint32_t carry_s;
-    __shared__ uint32_t chunk_total;
-    if (threadIdx.x == 0) carry_s = 0u;
-    __syncthreads();
-    for (size_t base = 0; base < nb; base += kThreads) {
-        size_t i = base + threadIdx.x;
-        uint32_t v = i < nb ? partials[i] : 0u;
-        uint32_t ex = block_exclusive(v, &chunk_total);
-        uint32_t carry = carry_s;
-        if (i < nb) partials[i] = carry + ex;
-        __syncthreads();
-        if (threadIdx.x == 0) carry_s = carry + chunk_total;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0 && total_out) *total_out = carry_s;
+__device__ __forceinline__ void publish(unsigned long long* slot, unsigned long long flag, uint32_t v) {
+    __threadfence();
+    atomicExch(slot, (flag << 32) | v);
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_scan_down(const uint32_t* __restrict__ in,
-                                                        uint32_t* __restrict__ out, size_t n,
-                                                        const uint32_t* __restrict__ n_dev,
-                                                        const uint32_t* __restrict__ partials) {
-    const size_t N = eff_n(n, n_dev);
-    const size_t base = (size_t)blockIdx.x * kTile;
-    if (base >= N) return;
-    // Each thread owns kItems consecutive elements.
+__global__ void __launch_bounds__(kThreads) k_scan(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                   size_t n, const uint32_t* __restrict__ n_dev,
+                                                   uint32_t* __restrict__ total_out,
+                                                   unsigned long long* __restrict__ state, uint32_t* err) {
+    __shared__ uint32_t s_tile, s_excl, s_tot;
+    if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(state), 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    size_t N = n;
+    if (n_dev) {
+        const size_t d = *n_dev;
+        N = d < n ? d : n;
+    }
+    const size_t base = (size_t)tile * kTile;
+    if (base >= N && tile != 0) return;  // no later tile waits on this one
+    // each thread owns kItems consecutive elements
     const size_t mine = base + (size_t)threadIdx.x * kItems;
     uint32_t v[kItems];
     uint32_t s = 0;
@@ -121,8 +94,35 @@ __global__ void __launch_bounds__(kThreads) k_scan_down(const uint32_t* __restri
         v[k] = load_item<MODE>(in, mine + k, N);
         s += v[k];
     }
-    __shared__ uint32_t tot;
-    uint32_t ex = block_exclusive(s, &tot) + partials[blockIdx.x];
+    uint32_t ex = block_exclusive(s, &s_tot);
+    if (threadIdx.x == 0) {
+        unsigned long long* st = state + 1;
+        const uint32_t tot = s_tot;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            publish(st, 2ull, tot);
+        } else {
+            publish(st + tile, 1ull, tot);
+            for (int p = (int)tile - 1; p >= 0; --p) {
+                unsigned long long w = 0;
+                unsigned waits = 0;
+                while ((w = *reinterpret_cast<volatile unsigned long long*>(st + p)) >> 32 == 0ull &&
+                       ++waits < kMaxWaits)
+                    __nanosleep(64);
+                if (w >> 32 == 0ull) {
+                    atomicOr(err, 8u);  // gave up: the outputs of this scan are wrong, the run reports it
+                    break;
+                }
+                excl += (uint32_t)w;
+                if (w >> 32 == 2ull) break;
+            }
+            publish(st + tile, 2ull, excl + tot);
+        }
+        s_excl = excl;
+        if (total_out && base + kTile >= N) *total_out = excl + tot;  // the tile holding the last element
+    }
+    __syncthreads();
+    ex += s_excl;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         if (mine + k < N) out[mine + k] = ex;
@@ -132,28 +132,19 @@ __global__ void __launch_bounds__(kThreads) k_scan_down(const uint32_t* __restri
 
 }  // namespace
 
-size_t scan_partials_size(size_t n) { return (n + kTile - 1) / kTile + 1; }
-
-int scan_launches(size_t) { return 3; }
+size_t scan_state_words(size_t n) { return (n + kTile - 1) / kTile + 1; }
 
 int scan_exclusive(const uint32_t* in, ScanInput mode, uint32_t* out, size_t n, const uint32_t* n_dev,
-                   uint32_t* total_out, uint32_t* partials, cudaStream_t st) {
+                   uint32_t* total_out, unsigned long long* state, uint32_t* err, cudaStream_t st) {
     if (n == 0) {
         if (total_out) cudaMemsetAsync(total_out, 0, sizeof(uint32_t), st);
         return 0;
     }
-    const size_t nb = (n + kTile - 1) / kTile;
-    if (mode == SCAN_POPC) {
-        k_scan_reduce<SCAN_POPC><<<(unsigned)nb, kThreads, 0, st>>>(in, n, n_dev, partials);
-    } else {
-        k_scan_reduce<SCAN_U32><<<(unsigned)nb, kThreads, 0, st>>>(in, n, n_dev, partials);
-    }
-    k_scan_partials<<<1, kThreads, 0, st>>>(partials, nb, total_out);
-    if (mode == SCAN_POPC) {
-        k_scan_down<SCAN_POPC><<<(unsigned)nb, kThreads, 0, st>>>(in, out, n, n_dev, partials);
-    } else {
-        k_scan_down<SCAN_U32><<<(unsigned)nb, kThreads, 0, st>>>(in, out, n, n_dev, partials);
-    }
+    const unsigned nb = (unsigned)((n + kTile - 1) / kTile);
+    if (mode == SCAN_POPC)
+        k_scan<SCAN_POPC><<<nb, kThreads, 0, st>>>(in, out, n, n_dev, total_out, state, err);
+    else
+        k_scan<SCAN_U32><<<nb, kThreads, 0, st>>>(in, out, n, n_dev, total_out, state, err);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

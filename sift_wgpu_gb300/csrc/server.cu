@@ -90,7 +90,7 @@ uint64_t footprint_estimate(const SiftCudaParams& p, int storage, uint32_t w, ui
         ow /= 2;
         oh /= 2;
     }
-    const uint64_t per_cand = 3 * sizeof(Keypoint) + kOriMaxPeaks * 4 + 4 * 4;
+    const uint64_t per_cand = 2 * sizeof(Keypoint) + kOriMaxPeaks * 4 + 3 * 4;
     const uint64_t per_out = sizeof(Keypoint) + kDescLen * 4;
     return align_up(std::max<uint32_t>(w, 1), 128) * h + g + d + u + tmpb + tmpo + lt + words + caps * per_cand +
            caps * per_out + (1u << 20);

@@ -42,7 +42,7 @@ struct Counters {
     uint32_t n_candidates;  // totals (filled by the last octave's chain)
     uint32_t n_refined;
     uint32_t n_oriented;    // keypoints in the output
-    uint32_t overflow;      // bit 0 candidates, 2 oriented
+    uint32_t overflow;      // bit 0 candidates, 2 oriented, 8 a scan wait ran out
     uint32_t pad[4];
     OctCounters oct[kMaxOctaves];
 };
@@ -165,12 +165,12 @@ __device__ __forceinline__ int small_div(int k, float inv_d) { return (int)(((fl
 
 // Scan helpers (scan.cu).
 enum ScanInput { SCAN_U32 = 0, SCAN_POPC = 1 };
-// Exclusive scan of n values (n_dev, when not null, overrides n at run time
-// and must be <= n). total_out receives the sum. Needs scratch partials of
-// scan_partials_size(n) words.
-size_t scan_partials_size(size_t n);
+// Exclusive scan of n values in one launch (n_dev, when not null, overrides n
+// at run time and must be <= n). total_out receives the sum. state holds
+// scan_state_words(n) 64-bit words that must be zero when the scan starts;
+// a look-back wait that runs out sets bit 8 of *err.
+size_t scan_state_words(size_t n);
 int scan_exclusive(const uint32_t* in, ScanInput mode, uint32_t* out, size_t n, const uint32_t* n_dev,
-                   uint32_t* total_out, uint32_t* partials, cudaStream_t st);
-int scan_launches(size_t n);
+                   uint32_t* total_out, unsigned long long* state, uint32_t* err, cudaStream_t st);
 
 }  // namespace sift
