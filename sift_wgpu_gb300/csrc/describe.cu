@@ -26,12 +26,23 @@
 // libm by a few ulp. Histogram sums are not in the reference's sequential
 // order, so orientations and descriptors agree within rounding, not bit for
 // bit.
+#include <algorithm>
+
 #include "sift_internal.cuh"
 
 namespace sift {
 namespace {
 
 constexpr int kWarpsPerCta = 8;
+
+// Work-queue kernels launch more CTAs than fit on the device. A CTA (or an
+// orientation warp) below persist_from takes at most kBudget items and
+// retires, which frees its slot for kernels of more urgent streams (the
+// smaller octaves' chains) instead of holding it until the queue drains; the
+// CTAs from persist_from on, the last wave, loop until the queue is empty,
+// so every item is taken whatever the grid.
+constexpr int kOriBudget = 4;   // keypoints per warp
+constexpr int kDescBudget = 2;  // keypoints per CTA
 
 // A Gaussian level pixel as v/255 (get_gauss_pixel_value, src/sift.rs:218-223):
 // f32 levels store it directly, f16 levels store v and go through the table.
@@ -143,7 +154,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                                                                    const uint32_t* __restrict__ keep, uint32_t ncap,
                                                                    OctCounters* __restrict__ oc,
                                                                    float* __restrict__ ori_angle,
-                                                                   uint32_t* __restrict__ ori_count) {
+                                                                   uint32_t* __restrict__ ori_count,
+                                                                   int persist_from) {
     __shared__ float lut[sizeof(TG) == 2 ? 256 : 1];
     __shared__ float hist[kWarpsPerCta][kOriBins][32];
     __shared__ float hs[kWarpsPerCta][kOriBins];
@@ -153,7 +165,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
     const uint32_t n = min(oc->n_cand, ncap);  // candidate slots; rejected ones get 0 peaks
     const float two_pi = 2.0f * kPi;
     const float bin_w = 2.0f * kPi / (float)kOriBins;
-    for (;;) {
+    const bool persist = (int)blockIdx.x >= persist_from;
+    for (int taken = 0; persist || taken < kOriBudget; ++taken) {
         uint32_t i = 0;
         if (lane == 0) i = atomicAdd(&oc->next_ori, 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
@@ -296,7 +309,8 @@ template <typename TG>
 __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
                                                               const Keypoint* __restrict__ oriented,
                                                               OctCounters* __restrict__ oc,
-                                                              float* __restrict__ desc, uint32_t cap) {
+                                                              float* __restrict__ desc, uint32_t cap,
+                                                              int persist_from) {
     // v / 255 for f16 levels (f32 levels hold v / 255 already)
     __shared__ float lut[sizeof(TG) == 2 ? 256 : 1];
     __shared__ float grid[kDescGridSide * kDescGridSide];
@@ -316,7 +330,8 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     const float two_pi = 2.0f * kPi;
     const float sqrt2 = __fsqrt_rn(2.0f);
     __shared__ uint32_t next;
-    for (;;) {
+    const bool persist = (int)blockIdx.x >= persist_from;
+    for (int taken = 0; persist || taken < kDescBudget; ++taken) {
         // keypoints differ ~4x in window area: take them from a queue
         if (tid == 0) next = atomicAdd(&oc->next_desc, 1u);
         __syncthreads();
@@ -536,9 +551,9 @@ int describe_grid() { return 152 * 4; }
 template <typename TG>
 int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
                        uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,
-                       cudaStream_t st) {
+                       int persist_ctas, cudaStream_t st) {
     k_orientation<TG><<<grid, dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined_at, keep, ncap, oc, ori_angle,
-                                                               ori_count);
+                                                               ori_count, std::max(grid - persist_ctas, 0));
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -551,18 +566,19 @@ int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counter
 
 template <typename TG>
 int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
-                      uint32_t cap, int grid, cudaStream_t st) {
-    k_descriptor<TG><<<grid, kDescThreads, 0, st>>>(arena, pyr, oriented, oc, desc, cap);
+                      uint32_t cap, int grid, int persist_ctas, cudaStream_t st) {
+    k_descriptor<TG><<<grid, kDescThreads, 0, st>>>(arena, pyr, oriented, oc, desc, cap,
+                                                    std::max(grid - persist_ctas, 0));
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 template int launch_orientation<float>(const float*, const PyramidDev&, const Keypoint*, const uint32_t*, uint32_t,
-                                       OctCounters*, float*, uint32_t*, int, cudaStream_t);
+                                       OctCounters*, float*, uint32_t*, int, int, cudaStream_t);
 template int launch_orientation<__half>(const __half*, const PyramidDev&, const Keypoint*, const uint32_t*, uint32_t,
-                                        OctCounters*, float*, uint32_t*, int, cudaStream_t);
+                                        OctCounters*, float*, uint32_t*, int, int, cudaStream_t);
 template int launch_descriptor<float>(const float*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
-                                      uint32_t, int, cudaStream_t);
+                                      uint32_t, int, int, cudaStream_t);
 template int launch_descriptor<__half>(const __half*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
-                                       uint32_t, int, cudaStream_t);
+                                       uint32_t, int, int, cudaStream_t);
 
 }  // namespace sift

@@ -67,13 +67,13 @@ int launch_refine(int storage, const void* arena, const PyramidDev& pyr, int o, 
 template <typename TG>
 int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
                        uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,
-                       cudaStream_t st);
+                       int persist_ctas, cudaStream_t st);
 int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counters* ctr, const float* ori_angle,
                        const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
                        cudaStream_t st);
 template <typename TG>
 int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
-                      uint32_t cap, int grid, cudaStream_t st);
+                      uint32_t cap, int grid, int persist_ctas, cudaStream_t st);
 // Error reporting (engine.cu): the calling thread's sift_cuda_last_error.
 extern thread_local std::string g_last_error;
 int fail(int code, const std::string& msg);
@@ -277,8 +277,9 @@ struct Engine {
         return 0;
     }
 
-    // CUDA stream priority of the engine's streams (0 = default; lower is
-    // more urgent). A graph launched into st runs at st's priority.
+    // CUDA stream priority of the engine (0 = default; lower is more
+    // urgent): octave 0's stream runs at it, the other streams one step more
+    // urgent (see init).
     int priority = 0;
 
     bool f16() const { return opt.storage == SIFT_CUDA_STORAGE_F16; }
@@ -301,10 +302,20 @@ struct Engine {
 
     int init() {
         if (int rc = set_device()) return rc;
-        CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, priority), "cudaStreamCreate");
+        // Octave 0's stream runs at the engine's priority, the pyramid's main
+        // stream and the smaller octaves' streams one step more urgent: while
+        // octave 0's orientation and descriptors fill the device, the other
+        // octaves' levels and short latency-bound chains are scheduled first
+        // instead of being left as a tail after them.
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priority range");
+        const int base = std::min(std::max(priority, greatest), least);
+        const int urgent = std::max(base - 1, greatest);
+        CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, urgent), "cudaStreamCreate");
         st_oct.assign(kMaxOctaves, nullptr);
-        for (auto& q : st_oct)
-            CK(cudaStreamCreateWithPriority(&q, cudaStreamNonBlocking, priority), "cudaStreamCreate");
+        for (size_t o = 0; o < st_oct.size(); ++o)
+            CK(cudaStreamCreateWithPriority(&st_oct[o], cudaStreamNonBlocking, o == 0 ? base : urgent),
+               "cudaStreamCreate");
         for (auto* v : {&ev_level, &ev_ori, &ev_done}) {
             v->assign(kMaxOctaves, nullptr);
             for (auto& e : *v) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
@@ -574,11 +585,12 @@ struct Engine {
         // (d) orientation histograms of the kept candidate slots and their scan
         auto orient = [&](int o, cudaStream_t q) -> int {
             OctCounters* oc = &ctr->oct[o];
-            const int grid =
-                (int)std::min<uint32_t>(std::max<uint32_t>(cap_c[o] / 64, 32), 152u * (uint32_t)tune.ori_ctas_per_sm);
+            // one warp-item per 8 candidate slots, 4 per warp; the last
+            // 152 x ori_ctas_per_sm CTAs drain whatever is left
+            const int grid = (int)std::max<uint32_t>(cap_c[o] / 64, 32);
             if (ok(launch_orientation<TG>(G, pyr, d_refined_at.as<Keypoint>() + cb[o], d_keep.as<uint32_t>() + cb[o],
                                           cap_c[o], oc, d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
-                                          d_ori_count.as<uint32_t>() + cb[o], grid, q)))
+                                          d_ori_count.as<uint32_t>() + cb[o], grid, 152 * tune.ori_ctas_per_sm, q)))
                 return cuda_fail(cudaGetLastError(), "orientation");
             unsigned long long* sstate =
                 d_scan.as<unsigned long long>() + pb[o] + scan_state_words((size_t)octave_words(o));
@@ -599,10 +611,11 @@ struct Engine {
         };
         auto describe = [&](int o, cudaStream_t q) -> int {
             if (!with_desc) return 0;
-            const int grid =
-                (int)std::min<uint32_t>(std::max<uint32_t>(cap_c[o] / 16, 64), 152u * (uint32_t)tune.desc_ctas_per_sm);
+            // two keypoints per CTA for 1/8 of the candidate capacity; the
+            // last 152 x desc_ctas_per_sm CTAs drain whatever is left
+            const int grid = (int)std::max<uint32_t>(cap_c[o] / 16, 64);
             if (ok(launch_descriptor<TG>(G, pyr, d_oriented.as<Keypoint>(), &ctr->oct[o], d_desc.as<float>(), cap_ori,
-                                         grid, q)))
+                                         grid, 152 * tune.desc_ctas_per_sm, q)))
                 return cuda_fail(cudaGetLastError(), "descriptor");
             return 0;
         };
@@ -702,7 +715,8 @@ struct Engine {
             }
             if (e != cudaSuccess) return cuda_fail(e, "end capture");
             graph = g;
-            CK(cudaGraphInstantiate(&gexec, graph, 0), "graph instantiate");
+            // each kernel node keeps the priority of the stream it was captured on
+            CK(cudaGraphInstantiate(&gexec, graph, cudaGraphInstantiateFlagUseNodePriority), "graph instantiate");
             gkey = key;
             graph_launches = launches;
         }
