@@ -218,71 +218,86 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
 }
 
 // ---------------------------------------------------------------------------
-// Fused level kernel: both separable passes of one level in one launch. The
-// CTA stages the (64 + 2r) x (64 + 2r) clamp-to-edge neighbourhood of its
-// 64 x 64 output tile from the previous level's u8 plane, runs the horizontal
-// pass for all 64 + 2r rows into shared memory (u8-truncated like
+// Fused level kernel: both separable passes of one level in one launch, for
+// radii up to 8. The CTA stages the (64 + 2r)-row clamp-to-edge neighbourhood
+// of its 64 x 64 output tile from the previous level's u8 plane, runs the
+// horizontal pass for all 64 + 2r rows into shared memory (u8-truncated like
 // imageproc's intermediate image), then the vertical pass, and writes the
 // level, its u8 plane and the DoG below it; the previous level's value for the
 // DoG comes from the staged tile, so each scale is read once, as bytes.
+//
+// Staged row layout: shared column c holds global x = x0 - 16 - sh + c with
+// sh = r mod 4, so an interior row is the 96 bytes [x0 - 16, x0 + 80) written
+// without conditions, and the horizontal pass's first input (x0 - r, column
+// 16 + sh - r) is 16-byte aligned for its float4 window. Each vertical-pass
+// thread owns 4 columns x 4 rows: one float4 shared load per tap and vector
+// stores of level, u8 copy and DoG.
 constexpr int kFTX = 64, kFTY = 64, kFThreads = 256;
-constexpr int kFColRows = 16;  // vertical-pass outputs per thread
-
-__host__ __device__ constexpr int fused_row_stride(int r) { return ((kFTX + 2 * r + 4) + 3) & ~3; }
+constexpr int kFMaxR = 8;
+constexpr int kFSW = 100;  // staged row stride (floats): sh + 96 <= 99
 
 size_t blur_fused_smem(int r) {
     const int taps = 2 * r + 1;
     const size_t rows = (size_t)kFTY + 2 * r;
-    return sizeof(float) * ((size_t)((taps + 3) & ~3) + 256 + rows * fused_row_stride(r) + rows * kFTX);
+    return sizeof(float) * ((size_t)((taps + 3) & ~3) + 256 + rows * kFSW + rows * kFTX);
 }
 
-// R > 0: the radius is a compile-time constant and every tap loop unrolls
-// (the vertical window then slides by register renaming); R == 0: run time.
+template <typename TG>
+__device__ __forceinline__ void store_level4(TG* p, const int v[4], const float* lut);
+template <>
+__device__ __forceinline__ void store_level4<float>(float* p, const int v[4], const float* lut) {
+    *reinterpret_cast<float4*>(p) = make_float4(lut[v[0]], lut[v[1]], lut[v[2]], lut[v[3]]);
+}
+template <>
+__device__ __forceinline__ void store_level4<__half>(__half* p, const int v[4], const float*) {
+    const __half2 a = __halves2half2(__int2half_rn(v[0]), __int2half_rn(v[1]));
+    const __half2 b = __halves2half2(__int2half_rn(v[2]), __int2half_rn(v[3]));
+    uint2 u;
+    u.x = *reinterpret_cast<const unsigned*>(&a);
+    u.y = *reinterpret_cast<const unsigned*>(&b);
+    *reinterpret_cast<uint2*>(p) = u;
+}
+
 template <typename TG, int R>
 __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restrict__ in, int in_pitch,
                                                           TG* __restrict__ out, uint8_t* __restrict__ out_u8,
-                                                          float* __restrict__ dog, int pitch, int W, int H, int r_rt,
+                                                          float* __restrict__ dog, int pitch, int W, int H,
                                                           const float* __restrict__ wts,
                                                           const float* __restrict__ lut255, int round_mode) {
+    static_assert(R >= 1 && R <= kFMaxR, "fused radius");
     extern __shared__ __align__(16) float sm[];
-    const int r = R > 0 ? R : r_rt;
-    const int taps = 2 * r + 1;
-    const int wpad = (taps + 3) & ~3;
-    const int RW = fused_row_stride(r);
-    const int RH = kFTY + 2 * r;
+    constexpr int taps = 2 * R + 1;
+    constexpr int wpad = (taps + 3) & ~3;
+    constexpr int RH = kFTY + 2 * R;
+    constexpr int sh = R & 3;
     float* kw = sm;
     float* lut = kw + wpad;
-    float* src = lut + 256;             // [RH][RW] staged input (u8 values)
-    float* hb = src + (size_t)RH * RW;  // [RH][kFTX] horizontal pass
+    float* src = lut + 256;              // [RH][kFSW] staged input (u8 values)
+    float* hb = src + (size_t)RH * kFSW;  // [RH][kFTX] horizontal pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * kFTX, y0 = blockIdx.y * kFTY;
     for (int i = tid; i < wpad; i += kFThreads) kw[i] = i < taps ? wts[i] : 0.0f;
     for (int i = tid; i < 256; i += kFThreads) lut[i] = lut255[i];
-    // Stage rows y0-r .. y0+63+r, columns x0-r .. (RW columns). Interior tiles
-    // load the bytes [x0-16, x0+80) of every row as six 16-byte vectors, all
-    // issued before use; border tiles clamp per element.
-    const bool interior = R > 0 && r <= 16 && x0 >= 16 && x0 + 80 <= W && y0 >= r && y0 + kFTY + r <= H &&
-                          (in_pitch & 15) == 0;
+    const bool interior = x0 >= 16 && x0 + 80 <= W && y0 >= R && y0 + kFTY + R <= H && (in_pitch & 15) == 0;
     if (interior) {
         constexpr int Q = 6;
-        const uint8_t* org = in + (long long)(y0 - r) * in_pitch + (x0 - 16);
+        const uint8_t* org = in + (long long)(y0 - R) * in_pitch + (x0 - 16);
 #pragma unroll 2
         for (int q = tid; q < RH * Q; q += kFThreads) {
             const int yy = q / Q, k = q - yy * Q;
             float v[16];
             unpack16(*reinterpret_cast<const uint4*>(org + (long long)yy * in_pitch + 16 * k), v);
-            float* d = src + (size_t)yy * RW;
+            float* d = src + (size_t)yy * kFSW + sh + 16 * k;
 #pragma unroll
-            for (int e = 0; e < 16; ++e) {
-                const int xx = 16 * k + e - 16 + r;
-                if (xx >= 0 && xx < RW) d[xx] = v[e];
-            }
+            for (int e = 0; e < 16; ++e) d[e] = v[e];
         }
     } else {
+        // clamp-to-edge, only the columns the passes read: 16 + sh - R .. sh + 80 + R
         for (int yy = warp; yy < RH; yy += kFThreads / 32) {
-            const uint8_t* row = in + (long long)clampi(y0 - r + yy, 0, H - 1) * in_pitch;
-            float* d = src + (size_t)yy * RW;
-            for (int xx = lane; xx < RW; xx += 32) d[xx] = float_of_u8(row[clampi(x0 - r + xx, 0, W - 1)]);
+            const uint8_t* row = in + (long long)clampi(y0 - R + yy, 0, H - 1) * in_pitch;
+            float* d = src + (size_t)yy * kFSW;
+            for (int c = 16 + sh - R + lane; c <= sh + 80 + R; c += 32)
+                d[c] = float_of_u8(row[clampi(x0 - 16 - sh + c, 0, W - 1)]);
         }
     }
     __syncthreads();
@@ -290,7 +305,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
     {
         const int xq = (tid & 15) * 4;
         for (int yy = tid >> 4; yy < RH; yy += kFThreads / 16) {
-            const float* base = src + (size_t)yy * RW + xq;
+            const float* base = src + (size_t)yy * kFSW + (16 + sh - R) + xq;
             float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
             float4 A = *reinterpret_cast<const float4*>(base);
             int i = 0;
@@ -331,38 +346,56 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
         }
     }
     __syncthreads();
-    // vertical pass: 64 columns x 4 groups of 16 rows, sliding window
-    const int col = tid & (kFTX - 1);
-    const int ly = (tid >> 6) * kFColRows;
-    float acc[kFColRows];
-    float win[kFColRows];
+    // vertical pass: thread = 4 columns x 4 rows, a 4-row float4 window
+    // sliding down the taps
+    const int cg = tid & 15, rg = tid >> 4;
+    const float4* hb4 = reinterpret_cast<const float4*>(hb) + cg;  // row stride kFTX / 4
+    float4 acc[4];
 #pragma unroll
-    for (int j = 0; j < kFColRows; ++j) {
-        acc[j] = 0.0f;
-        win[j] = j < kFColRows - 1 ? hb[(size_t)(ly + j) * kFTX + col] : 0.0f;
-    }
+    for (int j = 0; j < 4; ++j) acc[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 w0 = hb4[(4 * rg + 0) * (kFTX / 4)], w1 = hb4[(4 * rg + 1) * (kFTX / 4)],
+           w2 = hb4[(4 * rg + 2) * (kFTX / 4)];
 #pragma unroll
     for (int i = 0; i < taps; ++i) {
-        win[kFColRows - 1] = hb[(size_t)(ly + i + kFColRows - 1) * kFTX + col];
+        const float4 w3 = hb4[(4 * rg + i + 3) * (kFTX / 4)];
         const float k = kw[i];
+        const float4 w[4] = {w0, w1, w2, w3};
 #pragma unroll
-        for (int j = 0; j < kFColRows; ++j) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], k));
-#pragma unroll
-        for (int j = 0; j < kFColRows - 1; ++j) win[j] = win[j + 1];
+        for (int j = 0; j < 4; ++j) {
+            acc[j].x = __fadd_rn(acc[j].x, __fmul_rn(w[j].x, k));
+            acc[j].y = __fadd_rn(acc[j].y, __fmul_rn(w[j].y, k));
+            acc[j].z = __fadd_rn(acc[j].z, __fmul_rn(w[j].z, k));
+            acc[j].w = __fadd_rn(acc[j].w, __fmul_rn(w[j].w, k));
+        }
+        w0 = w1;
+        w1 = w2;
+        w2 = w3;
     }
-    const int x = x0 + col;
-    if (x >= W) return;
+    const int xc = x0 + 4 * cg;
+    if (xc >= W) return;
+    const bool full = xc + 3 < W;
 #pragma unroll
-    for (int j = 0; j < kFColRows; ++j) {
-        const int y = y0 + ly + j;
-        if (y < H) {
-            const int v = clamp_u8_any(acc[j], round_mode);
-            const long long o = (long long)y * pitch + x;
-            store_level(out + o, v, lut[v]);
-            out_u8[o] = (uint8_t)v;
-            if (dog) {
-                const int pv = int_of(src[(size_t)(r + ly + j) * RW + r + col]);
-                dog[o] = __fsub_rn(lut[v], lut[pv]);
+    for (int j = 0; j < 4; ++j) {
+        const int y = y0 + 4 * rg + j;
+        if (y >= H) break;
+        const int v[4] = {clamp_u8_any(acc[j].x, round_mode), clamp_u8_any(acc[j].y, round_mode),
+                          clamp_u8_any(acc[j].z, round_mode), clamp_u8_any(acc[j].w, round_mode)};
+        const long long o = (long long)y * pitch + xc;
+        // previous level at these pixels: staged row R + 4 rg + j, column 16 + sh + 4 cg
+        const float* pv = src + (size_t)(R + 4 * rg + j) * kFSW + 16 + sh + 4 * cg;
+        if (full) {
+            store_level4(out + o, v, lut);
+            *reinterpret_cast<unsigned*>(out_u8 + o) =
+                (unsigned)v[0] | ((unsigned)v[1] << 8) | ((unsigned)v[2] << 16) | ((unsigned)v[3] << 24);
+            if (dog)
+                *reinterpret_cast<float4*>(dog + o) =
+                    make_float4(__fsub_rn(lut[v[0]], lut[int_of(pv[0])]), __fsub_rn(lut[v[1]], lut[int_of(pv[1])]),
+                                __fsub_rn(lut[v[2]], lut[int_of(pv[2])]), __fsub_rn(lut[v[3]], lut[int_of(pv[3])]));
+        } else {
+            for (int c = 0; c < 4 && xc + c < W; ++c) {
+                store_level(out + o + c, v[c], lut[v[c]]);
+                out_u8[o + c] = (uint8_t)v[c];
+                if (dog) dog[o + c] = __fsub_rn(lut[v[c]], lut[int_of(pv[c])]);
             }
         }
     }
@@ -517,18 +550,16 @@ static int set_smem(const void* k, size_t smem) {
     return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess ? 0 : -1;
 }
 
-// One level from the previous level's u8 plane: fused when r <=
-// fused_max_radius and its tile fits in shared memory (the horizontal pass
-// recomputes a 2r-row halo per 64-row tile; radii up to 8 are compiled in,
-// larger ones take the run-time-radius kernel), else the two separable
-// passes, which spread a large-radius level over many CTAs.
+// One level from the previous level's u8 plane: fused when r <= 8 and r <=
+// fused_max_radius (the horizontal pass recomputes a 2r-row halo per 64-row
+// tile, which stops paying beyond r = 8), else the two separable passes.
 template <typename TG>
 int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, float* dog, int pitch,
                       int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
                       int* launches, int fused_max_radius) {
     const size_t smem = blur_fused_smem(r);
-    if (r <= fused_max_radius && smem <= 160 * 1024) {
-        void (*kern)(const uint8_t*, int, TG*, uint8_t*, float*, int, int, int, int, const float*, const float*, int);
+    if (r <= kFMaxR && r <= fused_max_radius) {
+        void (*kern)(const uint8_t*, int, TG*, uint8_t*, float*, int, int, int, const float*, const float*, int);
         switch (r) {
             case 1: kern = k_blur_level<TG, 1>; break;
             case 2: kern = k_blur_level<TG, 2>; break;
@@ -537,12 +568,11 @@ int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, ui
             case 5: kern = k_blur_level<TG, 5>; break;
             case 6: kern = k_blur_level<TG, 6>; break;
             case 7: kern = k_blur_level<TG, 7>; break;
-            case 8: kern = k_blur_level<TG, 8>; break;
-            default: kern = k_blur_level<TG, 0>; break;
+            default: kern = k_blur_level<TG, 8>; break;
         }
         if (set_smem((const void*)kern, smem)) return -1;
         dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
-        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, out_u8, dog, pitch, W, H, r, wts, lut255, round_mode);
+        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, out_u8, dog, pitch, W, H, wts, lut255, round_mode);
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
