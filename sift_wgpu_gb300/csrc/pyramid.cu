@@ -124,51 +124,57 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __rest
         }
         const int v0 = clamp_u8_any(a0, round_mode), v1 = clamp_u8_any(a1, round_mode);
         const int v2 = clamp_u8_any(a2, round_mode), v3 = clamp_u8_any(a3, round_mode);
-        dst[x0] = (uint8_t)v0;
-        if (x0 + 1 < W) dst[x0 + 1] = (uint8_t)v1;
-        if (x0 + 2 < W) dst[x0 + 2] = (uint8_t)v2;
-        if (x0 + 3 < W) dst[x0 + 3] = (uint8_t)v3;
+        if (x0 + 3 < W) {  // out_pitch is a multiple of 32 and x0 of 4: one aligned word
+            *reinterpret_cast<unsigned*>(dst + x0) =
+                (unsigned)v0 | ((unsigned)v1 << 8) | ((unsigned)v2 << 16) | ((unsigned)v3 << 24);
+        } else {
+            dst[x0] = (uint8_t)v0;
+            if (x0 + 1 < W) dst[x0 + 1] = (uint8_t)v1;
+            if (x0 + 2 < W) dst[x0 + 2] = (uint8_t)v2;
+        }
     }
 }
 
-constexpr int kColTX = 32;
-constexpr int kColTY = 8;
-constexpr int kColRPT = 8;                 // output rows per thread
-constexpr int kColRows = kColTY * kColRPT;  // output rows per CTA
+constexpr int kColTX = 32;                 // output columns per CTA
+constexpr int kColRows = 64;               // output rows per CTA
+constexpr int kColThreads = 256;           // 8 column groups of 4 x 32 row groups of 2
 
 // Vertical pass over a 32 x 64 output tile. Shared layout: weights padded
 // with zeros to a multiple of 8, lut[256] (v / 255 in f32), then
 // (64 + taps8 - 1) rows x 32 floats of the u8 intermediate with
-// clamp-to-edge rows. Taps go in unrolled groups of 8 from a 15-row register
-// window; the zero taps at the end add +0 to a non-negative sum, which leaves
-// it unchanged. Writes level s (TG and u8) and, when dog != nullptr,
-// DoG(s-1) = G_s/255 - G_{s-1}/255 (src/sift.rs:92-124).
+// clamp-to-edge rows. Each thread owns 4 columns x 2 rows and slides a
+// two-row float4 window down the taps, in unrolled groups of 8; the zero taps
+// at the end add +0 to a non-negative sum, which leaves it unchanged. Writes
+// level s (TG and u8) and, when dog != nullptr, DoG(s-1) = G_s/255 -
+// G_{s-1}/255 (src/sift.rs:92-124), as vector stores.
 __host__ __device__ constexpr int taps8(int r) { return ((2 * r + 1) + 7) & ~7; }
 
 template <typename TG>
-__global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __restrict__ tmp, int tmp_pitch,
-                                                             const uint8_t* __restrict__ prev_u8,
-                                                             TG* __restrict__ out, uint8_t* __restrict__ out_u8,
-                                                             float* __restrict__ dog, int pitch, int W, int H, int r,
-                                                             const float* __restrict__ wts,
-                                                             const float* __restrict__ lut255, int round_mode) {
+__device__ __forceinline__ void store_level4(TG* p, const int v[4], const float* lut);
+
+template <typename TG>
+__global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __restrict__ tmp, int tmp_pitch,
+                                                          const uint8_t* __restrict__ prev_u8,
+                                                          TG* __restrict__ out, uint8_t* __restrict__ out_u8,
+                                                          float* __restrict__ dog, int pitch, int W, int H, int r,
+                                                          const float* __restrict__ wts,
+                                                          const float* __restrict__ lut255, int round_mode) {
     extern __shared__ __align__(16) float sm[];
     const int taps = 2 * r + 1;
     const int tp = taps8(r);
     float* kw = sm;
     float* lut = sm + tp;
     float* tile = lut + 256;
-    const int tid = threadIdx.y * kColTX + threadIdx.x;
-    const int nthreads = kColTX * kColTY;
+    const int tid = threadIdx.x;
     const int x0 = blockIdx.x * kColTX;
     const int y0 = blockIdx.y * kColRows;
-    for (int i = tid; i < tp; i += nthreads) kw[i] = i < taps ? wts[i] : 0.0f;
-    for (int i = tid; i < 256; i += nthreads) lut[i] = lut255[i];
+    for (int i = tid; i < tp; i += kColThreads) kw[i] = i < taps ? wts[i] : 0.0f;
+    for (int i = tid; i < 256; i += kColThreads) lut[i] = lut255[i];
     const int rows = kColRows + tp - 1;
     if (x0 + kColTX <= W && (tmp_pitch & 15) == 0) {
         // two 16-byte loads per row, all rows of the tile in flight
 #pragma unroll 4
-        for (int q = tid; q < rows * 2; q += nthreads) {
+        for (int q = tid; q < rows * 2; q += kColThreads) {
             const int k = q >> 1, h = q & 1;
             const int ys = clampi(y0 - r + k, 0, H - 1);
             float v[16];
@@ -178,41 +184,64 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_blur_cols(const uint8_t* __r
             for (int e = 0; e < 16; ++e) d[e] = v[e];
         }
     } else {
-        const int xg = min(x0 + (int)threadIdx.x, W - 1);
-        for (int k = threadIdx.y; k < rows; k += kColTY) {
-            int ys = clampi(y0 - r + k, 0, H - 1);
-            tile[k * kColTX + threadIdx.x] = float_of_u8(tmp[(long long)ys * tmp_pitch + xg]);
+        const int lx = tid & (kColTX - 1);
+        const int xg = min(x0 + lx, W - 1);
+        for (int k = tid / kColTX; k < rows; k += kColThreads / kColTX) {
+            const int ys = clampi(y0 - r + k, 0, H - 1);
+            tile[k * kColTX + lx] = float_of_u8(tmp[(long long)ys * tmp_pitch + xg]);
         }
     }
     __syncthreads();
-    const int x = x0 + threadIdx.x;
-    const int ly = threadIdx.y * kColRPT;  // first local output row
-    float acc[kColRPT];
-#pragma unroll
-    for (int j = 0; j < kColRPT; ++j) acc[j] = 0.0f;
-    const float* col = tile + ly * kColTX + threadIdx.x;
+    const int cg = tid & 7, rg = tid >> 3;
+    const float4* col = reinterpret_cast<const float4*>(tile) + (2 * rg) * (kColTX / 4) + cg;
+    float4 a0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), a1 = a0;
+    float4 w0 = col[0];
     for (int i0 = 0; i0 < tp; i0 += 8) {
-        float w[kColRPT + 7];
-#pragma unroll
-        for (int m = 0; m < kColRPT + 7; ++m) w[m] = col[(i0 + m) * kColTX];
         const float4 ka = *reinterpret_cast<const float4*>(kw + i0);
         const float4 kb = *reinterpret_cast<const float4*>(kw + i0 + 4);
         const float k8[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-#pragma unroll
-            for (int j = 0; j < kColRPT; ++j) acc[j] = __fadd_rn(acc[j], __fmul_rn(w[q + j], k8[q]));
+        for (int q = 0; q < 8; ++q) {
+            const float4 w1 = col[(i0 + q + 1) * (kColTX / 4)];
+            const float k = k8[q];
+            a0.x = __fadd_rn(a0.x, __fmul_rn(w0.x, k));
+            a0.y = __fadd_rn(a0.y, __fmul_rn(w0.y, k));
+            a0.z = __fadd_rn(a0.z, __fmul_rn(w0.z, k));
+            a0.w = __fadd_rn(a0.w, __fmul_rn(w0.w, k));
+            a1.x = __fadd_rn(a1.x, __fmul_rn(w1.x, k));
+            a1.y = __fadd_rn(a1.y, __fmul_rn(w1.y, k));
+            a1.z = __fadd_rn(a1.z, __fmul_rn(w1.z, k));
+            a1.w = __fadd_rn(a1.w, __fmul_rn(w1.w, k));
+            w0 = w1;
+        }
     }
-    if (x >= W) return;
+    const int xc = x0 + 4 * cg;
+    if (xc >= W) return;
+    const bool full = xc + 3 < W;
+    const float4 acc[2] = {a0, a1};
 #pragma unroll
-    for (int j = 0; j < kColRPT; ++j) {
-        const int y = y0 + ly + j;
-        if (y < H) {
-            const int v = clamp_u8_any(acc[j], round_mode);
-            const long long o = (long long)y * pitch + x;
-            store_level(out + o, v, lut[v]);
-            out_u8[o] = (uint8_t)v;
-            if (dog) dog[o] = __fsub_rn(lut[v], lut[prev_u8[o]]);
+    for (int j = 0; j < 2; ++j) {
+        const int y = y0 + 2 * rg + j;
+        if (y >= H) break;
+        const int v[4] = {clamp_u8_any(acc[j].x, round_mode), clamp_u8_any(acc[j].y, round_mode),
+                          clamp_u8_any(acc[j].z, round_mode), clamp_u8_any(acc[j].w, round_mode)};
+        const long long o = (long long)y * pitch + xc;
+        if (full) {
+            store_level4(out + o, v, lut);
+            *reinterpret_cast<unsigned*>(out_u8 + o) =
+                (unsigned)v[0] | ((unsigned)v[1] << 8) | ((unsigned)v[2] << 16) | ((unsigned)v[3] << 24);
+            if (dog) {
+                const unsigned pw = *reinterpret_cast<const unsigned*>(prev_u8 + o);
+                *reinterpret_cast<float4*>(dog + o) =
+                    make_float4(__fsub_rn(lut[v[0]], lut[pw & 0xffu]), __fsub_rn(lut[v[1]], lut[(pw >> 8) & 0xffu]),
+                                __fsub_rn(lut[v[2]], lut[(pw >> 16) & 0xffu]), __fsub_rn(lut[v[3]], lut[pw >> 24]));
+            }
+        } else {
+            for (int c = 0; c < 4 && xc + c < W; ++c) {
+                store_level(out + o + c, v[c], lut[v[c]]);
+                out_u8[o + c] = (uint8_t)v[c];
+                if (dog) dog[o + c] = __fsub_rn(lut[v[c]], lut[prev_u8[o + c]]);
+            }
         }
     }
 }
@@ -580,7 +609,7 @@ int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, ui
     if (set_smem((const void*)k_blur_rows, rs) || set_smem((const void*)k_blur_cols<TG>, cs)) return -1;
     k_blur_rows<<<H, kRowThreads, rs, st>>>(in, in_pitch, tmp, pitch, W, r, wts, round_mode);
     dim3 grid((W + kColTX - 1) / kColTX, (H + kColRows - 1) / kColRows);
-    k_blur_cols<TG><<<grid, dim3(kColTX, kColTY), cs, st>>>(tmp, pitch, in, out, out_u8, dog, pitch, W, H, r, wts,
+    k_blur_cols<TG><<<grid, kColThreads, cs, st>>>(tmp, pitch, in, out, out_u8, dog, pitch, W, H, r, wts,
                                                             lut255, round_mode);
     *launches += 2;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
