@@ -21,11 +21,14 @@
 //                   addition is associative, so the result does not depend on
 //                   scheduling), then L2 normalise, clip at 0.2, renormalise.
 //
-// The per-sample arithmetic follows the reference's f32 operation order
-// without FMA; atan2f/expf/sinf/cosf are CUDA's, which differ from the host
-// libm by a few ulp. Histogram sums are not in the reference's sequential
-// order, so orientations and descriptors agree within rounding, not bit for
-// bit.
+// The orientation histogram follows the reference's f32 operation order
+// without FMA, except the Gaussian weight (hardware exponential of a
+// reciprocal product) and the angle (polynomial atan2 away from bin edges,
+// atan2f and the IEEE division next to them, so every bin index is exact);
+// its column sums are in a fixed order. The descriptor loop trades exactness
+// for speed within the descriptor tolerance (see k_descriptor). Orientations
+// and descriptors therefore agree with the reference within rounding, not bit
+// for bit.
 #include <algorithm>
 
 #include "sift_internal.cuh"
@@ -105,6 +108,7 @@ __device__ __forceinline__ void fill_lut(float* lut) {
 template <typename TG, bool CHECK>
 __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, float yo, int r, float wd, float* hist,
                                            int lane) {
+    const float inv_wd = __frcp_rn(wd);
     const float two_pi = 2.0f * kPi;
     const int side = 2 * r + 1;
     const int total = side * side;
@@ -127,7 +131,10 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
         const float gx = __fsub_rn(g.px_in(xi + 1, yi), g.px_in(xi - 1, yi));
         const float gy = __fsub_rn(g.px_in(xi, yi + 1), g.px_in(xi, yi - 1));
         const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
-        const float wgt = expf(__fdiv_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), wd));
+        // exp(-(dx^2 + dy^2) / wd) with the quotient as a product by 1 / wd and
+        // the hardware exponential: a few ulp from expf of the IEEE quotient,
+        // the same order as expf's own distance from the host libm
+        const float wgt = __expf(__fmul_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), inv_wd));
         // Bin index: from the polynomial atan2 and a multiply by 36 / (2 pi)
         // (a few ulp from the exact value), unless that lands within 1e-4 of
         // a bin edge; then from atan2f and the IEEE division, the exact
