@@ -55,6 +55,8 @@ int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, 
 int lanczos_fused_span();
 int lanczos_fused_tile();
 int pixel_channels(int format);
+int launch_export(const Counters* ctr, const Keypoint* kps, const float* desc, Counters* hctr, Keypoint* hkps,
+                  float* hdesc, uint32_t cap, int with_desc, cudaStream_t st);
 int launch_to_luma(int format, const uint8_t* px, long long stride, int W, int H, uint8_t* out, long long out_pitch,
                    cudaStream_t st);
 int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
@@ -175,6 +177,19 @@ struct Engine {
     DevMem d_words, d_cand_off, d_keep, d_scan;
     DevMem d_cands, d_refined_at, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
     HostPinned h_ctr, h_kps, h_desc;
+    // Host calls: the run ends with an export kernel that writes counters,
+    // keypoints and descriptors into this mapped buffer (layout: Counters |
+    // keypoints[cap_x] | descriptors[cap_x]), sized from the last count.
+    HostPinned hx;
+    uint32_t cap_x = 0, last_n = 0;
+    Counters* hx_dctr = nullptr;  // device addresses of the three parts
+    Keypoint* hx_dkps = nullptr;
+    float* hx_ddesc = nullptr;
+    Counters* hx_ctr() const { return hx.as<Counters>(); }
+    Keypoint* hx_kps() const { return (Keypoint*)(hx.as<char>() + align_up(sizeof(Counters), 256)); }
+    float* hx_desc() const {
+        return (float*)(hx.as<char>() + align_up(sizeof(Counters), 256) + align_up((size_t)cap_x * sizeof(Keypoint), 256));
+    }
     size_t img_pitch = 0;
     uint32_t launches = 0;
     bool last_desc = true;
@@ -200,13 +215,13 @@ struct Engine {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     struct GraphKey {
-        uint32_t W = 0, H = 0, cap_ori = 0;
+        uint32_t W = 0, H = 0, cap_ori = 0, cap_x = 0;  // cap_x 0: no export node
         std::vector<uint32_t> cap_c;
         bool with_desc = false;
         Tuning tune{};
         bool operator==(const GraphKey& o) const {
             return W == o.W && H == o.H && cap_ori == o.cap_ori && cap_c == o.cap_c && with_desc == o.with_desc &&
-                   tune == o.tune;
+                   tune == o.tune && cap_x == o.cap_x;
         }
     } gkey{};
     uint32_t graph_launches = 0;
@@ -503,7 +518,7 @@ struct Engine {
     // Octave 0's descriptors (most of the work) overlap the smaller octaves'
     // pyramid. Levels on st_oct[o] use their own horizontal-pass buffer.
     template <typename TG>
-    int enqueue_t(const uint8_t* img, long long stride, bool with_desc, bool dag) {
+    int enqueue_t(const uint8_t* img, long long stride, bool with_desc, bool dag, bool exp) {
         const int O = pyr.num_octaves, S = pyr.S;
         TG* G = d_G.as<TG>();
         float* D = f16() ? nullptr : d_D.as<float>();
@@ -682,20 +697,47 @@ struct Engine {
         }
         mark(&run_ev);
         if (prof) ev_runs.push_back(std::move(run_ev));
+        if (exp) {
+            if (ok(launch_export(ctr, d_oriented.as<Keypoint>(), d_desc.as<float>(), hx_dctr, hx_dkps, hx_ddesc, cap_x,
+                                 with_desc ? 1 : 0, st)))
+                return cuda_fail(cudaGetLastError(), "export");
+        }
         last_desc = with_desc;
         return 0;
     }
 
-    int enqueue(const uint8_t* img, long long stride, bool with_desc, bool dag) {
-        return f16() ? enqueue_t<__half>(img, stride, with_desc, dag) : enqueue_t<float>(img, stride, with_desc, dag);
+    int enqueue(const uint8_t* img, long long stride, bool with_desc, bool dag, bool exp) {
+        return f16() ? enqueue_t<__half>(img, stride, with_desc, dag, exp)
+                     : enqueue_t<float>(img, stride, with_desc, dag, exp);
+    }
+
+    // Mapped export buffer for at least n keypoints (host calls). It grows
+    // with twice the headroom so that images of one size with more keypoints
+    // than the last seldom force a reallocation (and a graph re-capture).
+    int ensure_export(uint32_t n) {
+        if (hx.p && n <= cap_x) return 0;
+        const uint32_t cap = std::max<uint32_t>(2 * n + 4096, 2 * cap_x);
+        hx.release();
+        void* ptr = nullptr;
+        const size_t bytes = align_up(sizeof(Counters), 256) + align_up((size_t)cap * sizeof(Keypoint), 256) +
+                             (size_t)cap * kDescLen * sizeof(float);
+        CK(cudaHostAlloc(&ptr, bytes, cudaHostAllocMapped), "cudaHostAlloc(export)");
+        hx.p = ptr;
+        hx.bytes = bytes;
+        cap_x = cap;
+        CK(cudaHostGetDevicePointer((void**)&hx_dctr, hx_ctr(), 0), "cudaHostGetDevicePointer");
+        CK(cudaHostGetDevicePointer((void**)&hx_dkps, hx_kps(), 0), "cudaHostGetDevicePointer");
+        CK(cudaHostGetDevicePointer((void**)&hx_ddesc, hx_desc(), 0), "cudaHostGetDevicePointer");
+        return 0;
     }
 
     // One run on the image in d_img: replayed from the CUDA graph of this
     // size (captured on first use), or launched in order with stage events
     // when profiling.
-    int run(bool with_desc) {
+    // exp: end the run with the export into the mapped buffer (host calls).
+    int run(bool with_desc, bool exp = false) {
         const long long stride = (long long)img_pitch;
-        if (prof) return enqueue(d_img.as<uint8_t>(), stride, with_desc, false);
+        if (prof) return enqueue(d_img.as<uint8_t>(), stride, with_desc, false, exp);
         GraphKey key;
         key.W = W;
         key.H = H;
@@ -703,10 +745,11 @@ struct Engine {
         key.cap_c = cap_c;
         key.with_desc = with_desc;
         key.tune = tune;
+        key.cap_x = exp ? cap_x : 0;
         if (!gexec || !(key == gkey)) {
             drop_graph();
             CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
-            int rc = enqueue(d_img.as<uint8_t>(), stride, with_desc, true);
+            int rc = enqueue(d_img.as<uint8_t>(), stride, with_desc, true, exp);
             cudaGraph_t g = nullptr;
             cudaError_t e = cudaStreamEndCapture(st, &g);
             if (rc) {
@@ -790,30 +833,38 @@ struct Engine {
                     return cuda_fail(cudaGetLastError(), "luma conversion");
             }
         }
+        if (int rc = ensure_export(last_n ? last_n : 4096)) return rc;
         for (int attempt = 0; attempt < 8; ++attempt) {
-            if (int rc = run(with_desc)) return rc;
+            if (int rc = run(with_desc, true)) return rc;
+            CK(cudaStreamSynchronize(st), "run");
+            const Counters c = *hx_ctr();
+            *h_ctr.as<Counters>() = c;
             bool retry = false;
-            if (int rc = check_counters(&retry)) return rc;
-            if (!retry) return view ? fetch_view(with_desc, out) : fetch(with_desc, out);
+            if (int rc = grow_from(c, &retry)) return rc;
+            if (retry) continue;
+            const uint32_t n = c.n_oriented;
+            if (n > cap_x) {
+                // more keypoints than the export buffer holds: grow it (the
+                // next run exports them all) and copy this run's results
+                if (int rc = ensure_export(n)) return rc;
+                *hx_ctr() = c;
+                CK(cudaMemcpy(hx_kps(), d_oriented.p, sizeof(Keypoint) * n, cudaMemcpyDeviceToHost), "D2H kps");
+                if (with_desc)
+                    CK(cudaMemcpy(hx_desc(), d_desc.p, sizeof(float) * kDescLen * n, cudaMemcpyDeviceToHost),
+                       "D2H desc");
+            }
+            last_n = n;
+            return view ? fetch_view(with_desc, out) : fetch(with_desc, out);
         }
         return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint lists kept overflowing");
     }
 
-    // Results copied into the engine's pinned buffers; out points at them.
+    // Results of a host call, already in the mapped export buffer; out points
+    // at them (valid until the next call).
     int fetch_view(bool with_desc, SiftCudaResult* out) {
-        const uint32_t n = h_ctr.as<Counters>()->n_oriented;
-        CK(h_kps.ensure(sizeof(Keypoint) * std::max<uint32_t>(n, 1)), "cudaHostAlloc(kps)");
-        if (with_desc) CK(h_desc.ensure(sizeof(float) * kDescLen * std::max<uint32_t>(n, 1)), "cudaHostAlloc(desc)");
-        if (n) {
-            CK(cudaMemcpyAsync(h_kps.p, d_oriented.p, sizeof(Keypoint) * n, cudaMemcpyDeviceToHost, st), "D2H kps");
-            if (with_desc)
-                CK(cudaMemcpyAsync(h_desc.p, d_desc.p, sizeof(float) * kDescLen * n, cudaMemcpyDeviceToHost, st),
-                   "D2H desc");
-            CK(cudaStreamSynchronize(st), "D2H results");
-        }
-        out->n = n;
-        out->kps = h_kps.as<SiftCudaKeypoint>();
-        out->desc = with_desc ? h_desc.as<float>() : nullptr;
+        out->n = h_ctr.as<Counters>()->n_oriented;
+        out->kps = (SiftCudaKeypoint*)hx_kps();
+        out->desc = with_desc ? hx_desc() : nullptr;
         return 0;
     }
 
@@ -831,16 +882,8 @@ struct Engine {
             return fail(SIFT_CUDA_ERR_OUT_OF_MEMORY, "host allocation of the result");
         }
         if (n == 0) return 0;
-        CK(h_kps.ensure(sizeof(Keypoint) * n), "cudaHostAlloc(kps)");
-        CK(cudaMemcpyAsync(h_kps.p, d_oriented.p, sizeof(Keypoint) * n, cudaMemcpyDeviceToHost, st), "D2H kps");
-        if (with_desc) {
-            CK(h_desc.ensure(sizeof(float) * kDescLen * n), "cudaHostAlloc(desc)");
-            CK(cudaMemcpyAsync(h_desc.p, d_desc.p, sizeof(float) * kDescLen * n, cudaMemcpyDeviceToHost, st),
-               "D2H desc");
-        }
-        CK(cudaStreamSynchronize(st), "D2H results");
-        std::memcpy(out->kps, h_kps.p, sizeof(Keypoint) * n);
-        if (with_desc) std::memcpy(out->desc, h_desc.p, sizeof(float) * kDescLen * n);
+        std::memcpy(out->kps, hx_kps(), sizeof(Keypoint) * n);
+        if (with_desc) std::memcpy(out->desc, hx_desc(), sizeof(float) * kDescLen * n);
         return 0;
     }
 };

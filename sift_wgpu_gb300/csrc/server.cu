@@ -16,8 +16,8 @@
 //              max_inflight requests run at once.
 //   service    One host thread owns every CUDA call of the server: it
 //              launches admitted requests (H2D copy of the image, the slot's
-//              graph, one export kernel that writes the counters, keypoints
-//              and descriptors straight into the slot's mapped host buffer,
+//              graph, one export kernel (export.cu) that writes the counters,
+//              keypoints and descriptors into the slot's mapped host buffer,
 //              an event) and polls the events of running requests. A request
 //              whose lists overflowed is re-run with grown lists; results stay
 //              in the slot until the caller releases them.
@@ -48,24 +48,6 @@ namespace {
 
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
-}
-
-// Counters, keypoints and descriptors of one finished run copied into mapped
-// host memory by the device (no host-known size needed).
-__global__ void __launch_bounds__(256) k_export(const Counters* __restrict__ ctr, const Keypoint* __restrict__ kps,
-                                                const float* __restrict__ desc, Counters* hctr, Keypoint* hkps,
-                                                float* hdesc, uint32_t cap, int with_desc) {
-    const uint32_t n = min(ctr->n_oriented, cap);
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-    constexpr uint32_t kCtrWords = sizeof(Counters) / 4;
-    if (tid < kCtrWords) reinterpret_cast<uint32_t*>(hctr)[tid] = reinterpret_cast<const uint32_t*>(ctr)[tid];
-    const uint32_t kw = n * (uint32_t)(sizeof(Keypoint) / 4);
-    for (uint32_t i = tid; i < kw; i += stride)
-        reinterpret_cast<uint32_t*>(hkps)[i] = reinterpret_cast<const uint32_t*>(kps)[i];
-    if (!with_desc) return;
-    const uint32_t dv = n * (kDescLen / 4);
-    for (uint32_t i = tid; i < dv; i += stride)
-        reinterpret_cast<float4*>(hdesc)[i] = reinterpret_cast<const float4*>(desc)[i];
 }
 
 // Device bytes an engine of size w x h holds after its first run (the arena
@@ -341,9 +323,9 @@ struct Server {
         CK(cudaHostGetDevicePointer((void**)&hc, s->hctr(), 0), "cudaHostGetDevicePointer");
         CK(cudaHostGetDevicePointer((void**)&hk, s->hkps(), 0), "cudaHostGetDevicePointer");
         CK(cudaHostGetDevicePointer((void**)&hd, s->hdesc(), 0), "cudaHostGetDevicePointer");
-        k_export<<<152 * 2, 256, 0, e.st>>>(e.d_ctr.as<Counters>(), e.d_oriented.as<Keypoint>(), e.d_desc.as<float>(),
-                                            hc, hk, hd, s->cap_x, 1);
-        CK(cudaGetLastError(), "export kernel");
+        if (sift::launch_export(e.d_ctr.as<Counters>(), e.d_oriented.as<Keypoint>(), e.d_desc.as<float>(), hc, hk,
+                                hd, s->cap_x, 1, e.st))
+            return cuda_fail(cudaGetLastError(), "export kernel");
         CK(cudaEventRecord(s->done, e.st), "event record");
         return 0;
     }
