@@ -127,12 +127,16 @@ constexpr int kExTX = 64, kExTY = 16, kExRows = 4, kExMaxLayers = 18;
 constexpr int kExSW = kExTX + 8;  // staged width: x0-4 .. x0+68 (word aligned)
 constexpr int kExSH = kExTY + 2;
 
-__global__ void __launch_bounds__(256) k_extrema_mask(const uint8_t* __restrict__ u8arena,
+// NL > 0: the number of DoG layers (S + 2) is compiled in and the layer loop
+// unrolls, so the sliding window renames registers instead of moving them;
+// NL == 0: any S.
+template <int NL>
+__global__ void __launch_bounds__(256, 4) k_extrema_mask(const uint8_t* __restrict__ u8arena,
                                                       const float* __restrict__ lut255, PyramidDev pyr, int o,
                                                       int border, uint32_t* __restrict__ words) {
     extern __shared__ __align__(16) float tile[];  // [layers][kExSH][kExSW], then lut[256]
     const OctaveDev& od = pyr.oct[o];
-    const int W = od.W, H = od.H, nw = od.nw, S = pyr.S, L = S + 2;
+    const int W = od.W, H = od.H, nw = od.nw, L = NL > 0 ? NL : pyr.S + 2;
     const int tid = threadIdx.x, lane = tid & 31;
     const int x0 = blockIdx.x * kExTX, y0 = blockIdx.y * kExTY;
     float* lut = tile + L * kExSH * kExSW;
@@ -145,11 +149,16 @@ __global__ void __launch_bounds__(256) k_extrema_mask(const uint8_t* __restrict_
     const int x = x0 + col;
     const int tx = col + 4;                     // staged column of x
     const int word = (x0 >> 5) + ((tid >> 5) & 1);  // this warp's 32 columns
+    const bool xin = x >= border && x < W - border;
+    bool yin[kExRows];
+#pragma unroll
+    for (int j = 0; j < kExRows; ++j) yin[j] = xin && y0 + r0 + j >= border && y0 + r0 + j < H - border;
     // Sliding window over the layers: p = l-2, c = l-1, n = l.
     float BMp[kExRows], Bmp[kExRows], BMc[kExRows], Bmc[kExRows], RMc[kExRows], Rmc[kExRows], Vc[kExRows];
 #pragma unroll
     for (int j = 0; j < kExRows; ++j) BMp[j] = Bmp[j] = BMc[j] = Bmc[j] = RMc[j] = Rmc[j] = Vc[j] = 0.0f;
-    for (int l = 0; l < L; ++l) {
+#pragma unroll
+    for (int l = 0; l < (NL > 0 ? NL : L); ++l) {
         const float* t = tile + (l * kExSH + r0) * kExSW + tx;  // staged row y0 + r0 - 1
         float left[kExRows + 2], mid[kExRows + 2], right[kExRows + 2], hM[kExRows + 2], hm[kExRows + 2];
 #pragma unroll
@@ -174,8 +183,7 @@ __global__ void __launch_bounds__(256) k_extrema_mask(const uint8_t* __restrict_
             for (int j = 0; j < kExRows; ++j) {
                 const int y = y0 + r0 + j;
                 const float v = Vc[j];
-                const bool inside = y >= border && y < H - border && x >= border && x < W - border;
-                const bool ext = inside && ((v > fmaxf(fmaxf(BMp[j], BMn[j]), RMc[j])) ||
+                const bool ext = yin[j] && ((v > fmaxf(fmaxf(BMp[j], BMn[j]), RMc[j])) ||
                                             (v < fminf(fminf(Bmp[j], Bmn[j]), Rmc[j])));
                 const uint32_t wv = __ballot_sync(0xffffffffu, ext);
                 if (lane == 0 && y < H && word < nw) words[od.word_base + ((long long)(s - 1) * H + y) * nw + word] = wv;
@@ -376,10 +384,11 @@ int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const Pyram
     if (pyr.S + 2 > kExMaxLayers) return -1;
     dim3 grid((od.W + kExTX - 1) / kExTX, (od.H + kExTY - 1) / kExTY);
     const size_t smem = sizeof(float) * ((size_t)(pyr.S + 2) * kExSH * kExSW + 256);
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_extrema_mask, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    void (*k)(const uint8_t*, const float*, PyramidDev, int, int, uint32_t*) =
+        pyr.S == 3 ? k_extrema_mask<5> : (pyr.S == 4 ? k_extrema_mask<6> : k_extrema_mask<0>);
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return -1;
-    k_extrema_mask<<<grid, 256, smem, st>>>(u8arena, lut255, pyr, o, border, words);
+    k<<<grid, 256, smem, st>>>(u8arena, lut255, pyr, o, border, words);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
