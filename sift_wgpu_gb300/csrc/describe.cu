@@ -317,6 +317,7 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                                                               const Keypoint* __restrict__ oriented,
                                                               OctCounters* __restrict__ oc,
                                                               float* __restrict__ desc, uint32_t cap,
+                                                              float* __restrict__ hdesc, uint32_t hcap,
                                                               int persist_from) {
     // v / 255 for f16 levels (f32 levels hold v / 255 already)
     __shared__ float lut[sizeof(TG) == 2 ? 256 : 1];
@@ -544,8 +545,10 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                     for (int q = 0; q < 4; ++q) d[q] = __fmul_rn(d[q], inv2);
                 }
             }
+            // keypoints below hcap straight into the host call's mapped buffer
+            float* dst = (i < hcap ? hdesc : desc) + (size_t)i * kDescLen;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) desc[(size_t)i * kDescLen + tid + 32 * q] = d[q];
+            for (int q = 0; q < 4; ++q) dst[tid + 32 * q] = d[q];
         }
         __syncthreads();
     }
@@ -573,8 +576,9 @@ int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counter
 
 template <typename TG>
 int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
-                      uint32_t cap, int grid, int persist_ctas, cudaStream_t st) {
-    k_descriptor<TG><<<grid, kDescThreads, 0, st>>>(arena, pyr, oriented, oc, desc, cap,
+                      uint32_t cap, float* hdesc, uint32_t hcap, int grid, int persist_ctas, cudaStream_t st) {
+    if (!hdesc) hcap = 0;
+    k_descriptor<TG><<<grid, kDescThreads, 0, st>>>(arena, pyr, oriented, oc, desc, cap, hdesc, hcap,
                                                     std::max(grid - persist_ctas, 0));
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -584,8 +588,8 @@ template int launch_orientation<float>(const float*, const PyramidDev&, const Ke
 template int launch_orientation<__half>(const __half*, const PyramidDev&, const Keypoint*, const uint32_t*, uint32_t,
                                         OctCounters*, float*, uint32_t*, int, int, cudaStream_t);
 template int launch_descriptor<float>(const float*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
-                                      uint32_t, int, int, cudaStream_t);
+                                      uint32_t, float*, uint32_t, int, int, cudaStream_t);
 template int launch_descriptor<__half>(const __half*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
-                                       uint32_t, int, int, cudaStream_t);
+                                      uint32_t, float*, uint32_t, int, int, cudaStream_t);
 
 }  // namespace sift

@@ -326,8 +326,12 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
         const uint64_t nd = std::min<uint64_t>(c.n_oriented, e.cap_ori) * sift::kDescLen;
         *count = nd;
         if (out && nd) {
-            if (cudaMemcpy(out, e.d_desc.p, std::min<uint64_t>(nd, capacity) * sizeof(float), cudaMemcpyDeviceToHost) !=
-                cudaSuccess)
+            // after a host call the first descriptors are in the export buffer only
+            const uint64_t m = std::min<uint64_t>(nd, capacity);
+            const uint64_t on_host = std::min<uint64_t>((uint64_t)e.desc_on_host * sift::kDescLen, m);
+            if (on_host) std::memcpy(out, e.hx_desc(), on_host * sizeof(float));
+            if (m > on_host && cudaMemcpy((float*)out + on_host, e.d_desc.as<float>() + on_host,
+                                          (m - on_host) * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
                 return sift::cuda_fail(cudaGetLastError(), "D2H stage");
         }
         return 0;

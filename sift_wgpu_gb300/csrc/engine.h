@@ -55,8 +55,8 @@ int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, 
 int lanczos_fused_span();
 int lanczos_fused_tile();
 int pixel_channels(int format);
-int launch_export(const Counters* ctr, const Keypoint* kps, const float* desc, Counters* hctr, Keypoint* hkps,
-                  float* hdesc, uint32_t cap, int with_desc, cudaStream_t st);
+int launch_export(const Counters* ctr, const Keypoint* kps, Counters* hctr, Keypoint* hkps, uint32_t cap,
+                  cudaStream_t st);
 int launch_to_luma(int format, const uint8_t* px, long long stride, int W, int H, uint8_t* out, long long out_pitch,
                    cudaStream_t st);
 int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
@@ -75,7 +75,7 @@ int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counter
                        cudaStream_t st);
 template <typename TG>
 int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
-                      uint32_t cap, int grid, int persist_ctas, cudaStream_t st);
+                      uint32_t cap, float* hdesc, uint32_t hcap, int grid, int persist_ctas, cudaStream_t st);
 // Error reporting (engine.cu): the calling thread's sift_cuda_last_error.
 extern thread_local std::string g_last_error;
 int fail(int code, const std::string& msg);
@@ -182,6 +182,9 @@ struct Engine {
     // keypoints[cap_x] | descriptors[cap_x]), sized from the last count.
     HostPinned hx;
     uint32_t cap_x = 0, last_n = 0;
+    // descriptors [0, desc_on_host) of the last run live only in the export
+    // buffer (a host call writes them there from the descriptor stage)
+    uint32_t desc_on_host = 0;
     Counters* hx_dctr = nullptr;  // device addresses of the three parts
     Keypoint* hx_dkps = nullptr;
     float* hx_ddesc = nullptr;
@@ -629,8 +632,11 @@ struct Engine {
             // two keypoints per CTA for 1/8 of the candidate capacity; the
             // last 152 x desc_ctas_per_sm CTAs drain whatever is left
             const int grid = (int)std::max<uint32_t>(cap_c[o] / 16, 64);
+            // host calls: descriptors below cap_x go straight into the mapped
+            // export buffer while the stage runs, the rest to d_desc
             if (ok(launch_descriptor<TG>(G, pyr, d_oriented.as<Keypoint>(), &ctr->oct[o], d_desc.as<float>(), cap_ori,
-                                         grid, 152 * tune.desc_ctas_per_sm, q)))
+                                         exp ? hx_ddesc : nullptr, exp ? cap_x : 0u, grid,
+                                         152 * tune.desc_ctas_per_sm, q)))
                 return cuda_fail(cudaGetLastError(), "descriptor");
             return 0;
         };
@@ -698,8 +704,8 @@ struct Engine {
         mark(&run_ev);
         if (prof) ev_runs.push_back(std::move(run_ev));
         if (exp) {
-            if (ok(launch_export(ctr, d_oriented.as<Keypoint>(), d_desc.as<float>(), hx_dctr, hx_dkps, hx_ddesc, cap_x,
-                                 with_desc ? 1 : 0, st)))
+            // counters and keypoints; the descriptors are there already
+            if (ok(launch_export(ctr, d_oriented.as<Keypoint>(), hx_dctr, hx_dkps, cap_x, st)))
                 return cuda_fail(cudaGetLastError(), "export");
         }
         last_desc = with_desc;
@@ -731,12 +737,39 @@ struct Engine {
         return 0;
     }
 
+    // After a run that ended with the export (its counters c read from the
+    // buffer): a run with more keypoints than the buffer holds grows it and
+    // moves its results there — keypoints from d_oriented, descriptors below
+    // the old capacity from the old buffer, the rest from d_desc. Records
+    // what the buffer holds.
+    int settle_export(const Counters& c, bool with_desc) {
+        const uint32_t n = c.n_oriented;
+        if (n > cap_x) {
+            const uint32_t head = cap_x;
+            std::vector<float> d_head;
+            if (with_desc) d_head.assign(hx_desc(), hx_desc() + (size_t)head * kDescLen);
+            if (int rc = ensure_export(n)) return rc;
+            *hx_ctr() = c;
+            CK(cudaMemcpy(hx_kps(), d_oriented.p, sizeof(Keypoint) * n, cudaMemcpyDeviceToHost), "D2H kps");
+            if (with_desc) {
+                std::memcpy(hx_desc(), d_head.data(), sizeof(float) * d_head.size());
+                CK(cudaMemcpy(hx_desc() + (size_t)head * kDescLen, d_desc.as<float>() + (size_t)head * kDescLen,
+                              sizeof(float) * kDescLen * (n - head), cudaMemcpyDeviceToHost),
+                   "D2H desc");
+            }
+        }
+        last_n = n;
+        desc_on_host = with_desc ? n : 0;
+        return 0;
+    }
+
     // One run on the image in d_img: replayed from the CUDA graph of this
     // size (captured on first use), or launched in order with stage events
     // when profiling.
     // exp: end the run with the export into the mapped buffer (host calls).
     int run(bool with_desc, bool exp = false) {
         const long long stride = (long long)img_pitch;
+        desc_on_host = 0;
         if (prof) return enqueue(d_img.as<uint8_t>(), stride, with_desc, false, exp);
         GraphKey key;
         key.W = W;
@@ -842,18 +875,7 @@ struct Engine {
             bool retry = false;
             if (int rc = grow_from(c, &retry)) return rc;
             if (retry) continue;
-            const uint32_t n = c.n_oriented;
-            if (n > cap_x) {
-                // more keypoints than the export buffer holds: grow it (the
-                // next run exports them all) and copy this run's results
-                if (int rc = ensure_export(n)) return rc;
-                *hx_ctr() = c;
-                CK(cudaMemcpy(hx_kps(), d_oriented.p, sizeof(Keypoint) * n, cudaMemcpyDeviceToHost), "D2H kps");
-                if (with_desc)
-                    CK(cudaMemcpy(hx_desc(), d_desc.p, sizeof(float) * kDescLen * n, cudaMemcpyDeviceToHost),
-                       "D2H desc");
-            }
-            last_n = n;
+            if (int rc = settle_export(c, with_desc)) return rc;
             return view ? fetch_view(with_desc, out) : fetch(with_desc, out);
         }
         return fail(SIFT_CUDA_ERR_CAPACITY, "keypoint lists kept overflowing");

@@ -6,8 +6,9 @@
 //
 //   slots      Each slot is a complete engine (engine.h) bound to one image
 //              size: its pyramid, DoG, u8 and list arenas stay resident and
-//              its CUDA graph for that size is captured once. A slot also owns
-//              a mapped pinned export buffer and a completion event.
+//              its CUDA graph for that size is captured once, together with
+//              the engine's mapped pinned export buffer. A slot also owns a
+//              completion event.
 //   admission  A request waits in FIFO order until an idle slot of its size
 //              exists, or a new slot fits the device-memory budget
 //              (arena_bytes, counted as the slots' device bytes; a new slot
@@ -16,9 +17,10 @@
 //              max_inflight requests run at once.
 //   service    One host thread owns every CUDA call of the server: it
 //              launches admitted requests (H2D copy of the image, the slot's
-//              graph, one export kernel (export.cu) that writes the counters,
-//              keypoints and descriptors into the slot's mapped host buffer,
-//              an event) and polls the events of running requests. A request
+//              graph — whose descriptor stage writes into the mapped host
+//              buffer and whose last kernel (export.cu) writes the counters
+//              and keypoints there — then an event) and polls the events of
+//              running requests. A request
 //              whose lists overflowed is re-run with grown lists; results stay
 //              in the slot until the caller releases them.
 //   overlap    Running requests are on different slots, hence different
@@ -86,23 +88,12 @@ struct Slot {
     std::unique_ptr<Engine> eng;
     uint32_t w = 0, h = 0;
     uint64_t bytes = 0;  // device bytes of the engine
-    cudaEvent_t done = nullptr;
-    HostPinned hx;       // mapped: Counters | keypoints[cap_x] | descriptors[cap_x]
-    uint32_t cap_x = 0;
+    cudaEvent_t done = nullptr;  // results are in the engine's mapped export buffer
     enum State { Idle, Running, Holding } state = Idle;
     Request* req = nullptr;
     uint64_t last_use = 0;
     int reruns = 0;
 
-    Counters* hctr() const { return hx.as<Counters>(); }
-    Keypoint* hkps() const { return (Keypoint*)(hx.as<char>() + align_up(sizeof(Counters), 256)); }
-    float* hdesc() const {
-        return (float*)(hx.as<char>() + align_up(sizeof(Counters), 256) + align_up((size_t)cap_x * sizeof(Keypoint), 256));
-    }
-    static size_t export_bytes(uint32_t cap) {
-        return align_up(sizeof(Counters), 256) + align_up((size_t)cap * sizeof(Keypoint), 256) +
-               (size_t)cap * kDescLen * sizeof(float);
-    }
     ~Slot() {
         if (done) cudaEventDestroy(done);
     }
@@ -200,18 +191,6 @@ struct Server {
         return 0;
     }
 
-    int ensure_export(Slot* s, uint32_t n) {
-        if (s->hx.p && n <= s->cap_x) return 0;
-        const uint32_t cap = std::max<uint32_t>(n + n / 4 + 1024, s->cap_x);
-        s->hx.release();
-        void* ptr = nullptr;
-        CK(cudaHostAlloc(&ptr, Slot::export_bytes(cap), cudaHostAllocMapped), "cudaHostAlloc(export)");
-        s->hx.p = ptr;
-        s->hx.bytes = Slot::export_bytes(cap);
-        s->cap_x = cap;
-        return 0;
-    }
-
     // Admission of r (lock held). Returns 0 and either *out (an idle slot of
     // r's size), or *create (a new slot of r's size fits: its estimated
     // footprint is reserved in device_bytes; idle slots of other sizes may
@@ -261,13 +240,15 @@ struct Server {
         cudaEvent_t a = nullptr, b = nullptr;
         CK(cudaEventCreate(&a), "cudaEventCreate");
         CK(cudaEventCreate(&b), "cudaEventCreate");
+        // the graph timed is the one served: ending with the export
+        if (int rc = e.ensure_export(e.last_n ? e.last_n : 4096)) return rc;
         auto time_cfg = [&](const Engine::Tuning& t, float* ms) -> int {
             e.tune = t;
             for (int k = 0; k < 2; ++k)
-                if (int rc = e.run(true)) return rc;
+                if (int rc = e.run(true, true)) return rc;
             CK(cudaEventRecord(a, e.st), "event");
             for (int k = 0; k < 3; ++k)
-                if (int rc = e.run(true)) return rc;
+                if (int rc = e.run(true, true)) return rc;
             CK(cudaEventRecord(b, e.st), "event");
             CK(cudaEventSynchronize(b), "event sync");
             CK(cudaEventElapsedTime(ms, a, b), "elapsed");
@@ -310,43 +291,34 @@ struct Server {
         }
         if (tune)
             if (int rc = autotune(s)) return rc;
-        if (int rc = e.run(true)) return rc;
-        return launch_export(s);
+        return run_exported(s);
     }
 
-    int launch_export(Slot* s) {
+    // One run of the slot's graph that ends with the export into the
+    // engine's mapped buffer (descriptors written there by the descriptor
+    // stage), then the completion event.
+    int run_exported(Slot* s) {
         Engine& e = *s->eng;
-        if (int rc = ensure_export(s, s->cap_x ? s->cap_x : 4096)) return rc;
-        Counters* hc = nullptr;
-        Keypoint* hk = nullptr;
-        float* hd = nullptr;
-        CK(cudaHostGetDevicePointer((void**)&hc, s->hctr(), 0), "cudaHostGetDevicePointer");
-        CK(cudaHostGetDevicePointer((void**)&hk, s->hkps(), 0), "cudaHostGetDevicePointer");
-        CK(cudaHostGetDevicePointer((void**)&hd, s->hdesc(), 0), "cudaHostGetDevicePointer");
-        if (sift::launch_export(e.d_ctr.as<Counters>(), e.d_oriented.as<Keypoint>(), e.d_desc.as<float>(), hc, hk,
-                                hd, s->cap_x, 1, e.st))
-            return cuda_fail(cudaGetLastError(), "export kernel");
+        if (int rc = e.ensure_export(e.last_n ? e.last_n : 4096)) return rc;
+        if (int rc = e.run(true, true)) return rc;
         CK(cudaEventRecord(s->done, e.st), "event record");
         return 0;
     }
 
     // A running slot whose event completed (lock held): re-run on overflow,
-    // re-export when the export buffer was short, else finish the request.
+    // grow the export buffer when it was short, finish the request.
     // Returns 0 or a status; on 0 the slot is either running again or done.
     int complete(Slot* s) {
         Request* r = s->req;
-        const Counters c = *s->hctr();
+        const Counters c = *s->eng->hx_ctr();
         bool retry = false;
         if (int rc = s->eng->grow_from(c, &retry)) return rc;
         if (retry) {
             ++n_reruns;
-            if (int rc = s->eng->run(true)) return rc;
-            return launch_export(s);
+            return run_exported(s);
         }
-        if (c.n_oriented > s->cap_x) {
-            if (int rc = ensure_export(s, c.n_oriented)) return rc;
-            return launch_export(s);
-        }
+        // more keypoints than the buffer held: grown, results moved (rare)
+        if (int rc = s->eng->settle_export(c, true)) return rc;
         r->t_done = now_s();
         s->state = Slot::Holding;
         --running;
@@ -636,10 +608,10 @@ int sift_cuda_server_poll(SiftCudaServer* server, SiftCudaServed* out, int64_t t
     out->start_s = r->t_start;
     out->done_s = r->t_done;
     if (r->status == 0 && r->slot) {
-        const sift::Counters* c = r->slot->hctr();
-        out->n = c->n_oriented;
-        out->kps = (const SiftCudaKeypoint*)r->slot->hkps();
-        out->desc = r->slot->hdesc();
+        const sift::Engine& e = *r->slot->eng;
+        out->n = e.hx_ctr()->n_oriented;
+        out->kps = (const SiftCudaKeypoint*)e.hx_kps();
+        out->desc = e.hx_desc();
     }
     return 1;
 }

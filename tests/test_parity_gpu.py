@@ -234,3 +234,29 @@ def test_all_call_forms_agree(sgb):
     k4, d4 = eng.detect_and_compute(img)
     assert k4.tobytes() == k1.tobytes() and d4.tobytes() == d1.tobytes()
     eng.close()
+
+
+def test_export_buffer_growth(sgb):
+    """A host call writes descriptors below the export buffer's capacity into
+    it from the descriptor stage and the rest to device memory. The first
+    call of an engine on a 1080p frame has more keypoints than the initial
+    buffer holds (the buffer grows, the head moves over from the old buffer,
+    the tail comes from the device); later calls fit. Every form agrees, and
+    the descriptor stage read back after a host call is the host result."""
+    import torch
+    w, h = 1920, 1080
+    img = image(sgb, w, h, 1)
+    eng = sgb.Engine(sgb.Sift.default())
+    k1, d1 = eng.detect_and_compute(img)
+    assert len(k1) > 3 * 4096
+    assert eng.debug_stage(sgb.STAGE_DESCRIPTORS).tobytes() == d1.tobytes()
+    k2, d2 = eng.detect_and_compute(img)
+    assert k2.tobytes() == k1.tobytes() and d2.tobytes() == d1.tobytes()
+    assert eng.debug_stage(sgb.STAGE_DESCRIPTORS).tobytes() == d1.tobytes()
+    dimg = torch.from_numpy(img).cuda()
+    torch.cuda.synchronize()
+    eng.run_device(dimg.data_ptr(), w, h, w)
+    eng.synchronize()
+    assert eng.debug_stage(sgb.STAGE_KEYPOINTS).tobytes() == k1.tobytes()
+    assert eng.debug_stage(sgb.STAGE_DESCRIPTORS).tobytes() == d1.tobytes()
+    eng.close()
