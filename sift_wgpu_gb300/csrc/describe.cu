@@ -30,6 +30,7 @@
 // and descriptors therefore agree with the reference within rounding, not bit
 // for bit.
 #include <algorithm>
+#include <type_traits>
 
 #include "sift_internal.cuh"
 
@@ -335,7 +336,6 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     uint32_t n = oc->n_ori;
     if (base >= cap) n = 0;
     else if (n > cap - base) n = cap - base;
-    const float two_pi = 2.0f * kPi;
     const float sqrt2 = __fsqrt_rn(2.0f);
     __shared__ uint32_t next;
     const bool persist = (int)blockIdx.x >= persist_from;
@@ -436,74 +436,91 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
             // Descriptor samples are interpolated linearly into their bins, so
             // this loop is written for speed within the descriptor tolerance:
             // fused multiply-adds, reciprocal products instead of divisions,
-            // exp2 with the scale folded in, and the relative angle binned
-            // directly from (pa - angle) * 8 / (2 pi) (floor and & 7 give the
-            // rem_euclid bins). Each changes a descriptor value by ~1e-7.
-            const float inv_bw = 1.0f / bw, inv_side = 1.0f / (float)side;
-            const float to_bins = 8.0f / two_pi;
+            // the hardware's approximate square root and exp2 (scale folded
+            // in), an arctangent polynomial in units of angle bins (error
+            // 1.5e-5 bin) from which the relative angle is binned directly
+            // (floor and & 7 give the rem_euclid bins), and the fixed-point
+            // rounding fused into the weight product. Each changes a
+            // descriptor value by ~1e-5 or less.
+            const float inv_bw = 1.0f / bw;
+            const float angb = ang * (4.0f / kPi);  // keypoint angle in 45-degree bins
             const float wexp = -1.4426950408889634f / wd;  // exp(-d2/wd) = exp2(d2 * wexp)
+            // |rx|, |ry| below lim keep xb, yb inside (-1, 4) after rounding, so
+            // every cell index lies in the padded grid (samples within 1e-6
+            // of the window edge, whose shares there are ~0, are left out)
+            const float lim = __fmul_rn(2.5f, bw) * 0.99999905f;
             unsigned int* hcopy = hist + ((tid & 31) >> 2) * kHistStride;
-            // Branch-free: samples outside the rotated 4x4 window or the level
-            // carry weight 0 and their adds are predicated off, so the lanes of
-            // a warp never split.
-            // Loop indices without int<->float conversions: k is mirrored in an
-            // exact float counter; q = k / side by the floor add, px and py are
-            // exact small integers in f32, and the grid index of (px, py) is
-            // (py + rad + 1) * gs + px + rad + 1 = k + 2 q + gs + 1.
             const float side_f = (float)side, rad_f = (float)rad;
-            float kf = (float)tid;
-            for (int k = tid; k < total; k += kDescThreads, kf += (float)kDescThreads) {
-                int q;
-                const float qf = floor_fi((kf + 0.5f) * inv_side, &q);
-                const float py = qf - rad_f;
-                const float px = kf - qf * side_f - rad_f;
-                const float rx = fmaf(ca, px, sa * py);
-                const float ry = fmaf(-sa, px, ca * py);
-                const float xb = fmaf(rx, inv_bw, 1.5f);
-                const float yb = fmaf(ry, inv_bw, 1.5f);
-                const float xs = xo + px, ys = yo + py;
-                const bool in = (xb > -1.0f && xb < 4.0f && yb > -1.0f && yb < 4.0f) &&
-                                !(xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1);
-                // warps whose 32 samples all fall outside skip the rest
-                if (!__any_sync(__activemask(), in)) continue;
-                float gx, gy;
-                if (use_grid) {
-                    const int c = k + 2 * q + gs + 1;
-                    gx = grid[c + 1] - grid[c - 1];
-                    gy = grid[c + gs] - grid[c - gs];
-                } else {
-                    gx = __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
-                    gy = __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
-                }
-                const float m2 = fmaf(gx, gx, gy * gy);
-                const float mag = m2 > 0.0f ? m2 * rsqrtf(m2) : 0.0f;
-                const float pa = atan2_poly(gy, gx);
-                const float wgt = exp2f(fmaf(px, px, py * py) * wexp);
-                const float wm = in ? mag * wgt : 0.0f;
-                const float ab = (pa - ang) * to_bins;  // in [-8, 8]
-                int xbi, ybi, abi;
-                const float xbf = floor_fi(xb, &xbi), ybf = floor_fi(yb, &ybi), abf = floor_fi(ab, &abi);
-                const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
-                const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
-                // cells (xbi + i, ybi + j), i, j in {0, 1}: xbi, ybi in -1..3 for
-                // samples inside, so all four lie in the padded 6 x 6 grid.
-                // Samples outside add nothing; inside, the eight adds are
-                // unconditional (a zero share adds 0): one branch per sample
-                // instead of one per add.
-                if (in) {
-                    const float wx0 = 1.0f - fx, wx1 = fx;
-                    const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
-                    unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
+            // windows that stay inside the level need no per-sample border test
+            const bool edge = !(__fadd_rn(xo, -rad_f) >= 0.0f && __fadd_rn(xo, rad_f) < wm1 &&
+                                __fadd_rn(yo, -rad_f) >= 0.0f && __fadd_rn(yo, rad_f) < hm1);
+            // Sample k of the window (row-major) is (px, py) = (k % side - rad,
+            // k / side - rad), grid index c = (py + rad + 1) * gs + px + rad + 1.
+            // A thread steps k by the block size: px, py (exact small integers
+            // in f32) and c advance by fixed amounts, with one wrap per step.
+            const int q0 = tid / side, dq = kDescThreads / side;
+            const float dr_f = (float)(kDescThreads - dq * side), dq_f = (float)dq;
+            const int dc = dq * gs + (kDescThreads - dq * side);
+            auto samples = [&](auto edge_tag) {
+                constexpr bool kEdge = decltype(edge_tag)::value;
+                float px = (float)(tid - q0 * side) - rad_f, py = (float)q0 - rad_f;
+                int c = (q0 + 1) * gs + (tid - q0 * side) + 1;
+                for (;; px += dr_f, py += dq_f, c += dc) {
+                    // the wrap to the next row as selects: a branch here would
+                    // split the warp for the rest of the step
+                    const bool wrap = px > rad_f;
+                    px = wrap ? px - side_f : px;
+                    py = wrap ? py + 1.0f : py;
+                    c = wrap ? c + 2 : c;
+                    if (py > rad_f) break;
+                    const float rx = fmaf(ca, px, sa * py);
+                    const float ry = fmaf(-sa, px, ca * py);
+                    bool in = fabsf(rx) < lim && fabsf(ry) < lim;
+                    if constexpr (kEdge) {
+                        const float xs = xo + px, ys = yo + py;
+                        in = in && !(xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1);
+                    }
+                    // warps whose 32 samples all fall outside skip the rest
+                    if (!__any_sync(__activemask(), in)) continue;
+                    float gx, gy;
+                    if (use_grid) {
+                        gx = grid[c + 1] - grid[c - 1];
+                        gy = grid[c + gs] - grid[c - gs];
+                    } else {
+                        const float xs = xo + px, ys = yo + py;
+                        gx = __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
+                        gy = __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
+                    }
+                    if (in) {
+                        const float mag = sqrt_approx(fmaf(gx, gx, gy * gy));
+                        const float wm = mag * ex2_approx(fmaf(px, px, py * py) * wexp);
+                        const float ab = atan2_bins(gy, gx) - angb;  // in [-12, 4]
+                        const float xb = fmaf(rx, inv_bw, 1.5f), yb = fmaf(ry, inv_bw, 1.5f);
+                        int xbi, ybi, abi;
+                        const float xbf = floor_fi(xb, &xbi), ybf = floor_fi(yb, &ybi), abf = floor_fi(ab, &abi);
+                        const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
+                        const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
+                        // cells (xbi + i, ybi + j), i, j in {0, 1}: xbi, ybi in
+                        // -1..3, so all four lie in the padded 6 x 6 grid; the
+                        // eight adds are unconditional (a zero share adds 0)
+                        const float wx0 = 1.0f - fx, wx1 = fx;
+                        const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
+                        unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) {
-                        const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
-                        unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
-                        // round to the nearest integer (< 2^23 by the scale choice)
-                        atomicAdd(hc, __float_as_uint(__fadd_rn(wxy * wa0, kMagic)) - 0x4B000000u);
-                        atomicAdd(hc + 1, __float_as_uint(__fadd_rn(wxy * wa1, kMagic)) - 0x4B000000u);
+                        for (int cc = 0; cc < 4; ++cc) {
+                            const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
+                            unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
+                            // the product rounded to the nearest integer (< 2^23 by the scale choice)
+                            atomicAdd(hc, __float_as_uint(__fmaf_rn(wxy, wa0, kMagic)) - 0x4B000000u);
+                            atomicAdd(hc + 1, __float_as_uint(__fmaf_rn(wxy, wa1, kMagic)) - 0x4B000000u);
+                        }
                     }
                 }
-            }
+            };
+            if (edge)
+                samples(std::true_type{});
+            else
+                samples(std::false_type{});
         }
         __syncthreads();
         // normalize_and_clip_descriptor (src/sift.rs:889-913)

@@ -158,6 +158,40 @@ __device__ __forceinline__ float atan2_poly(float y, float x) {
     return copysignf(r, y);
 }
 
+// atan2(y, x) in units of 45-degree bins (pi/4 = 1), in [-4, 4]: a = min/max
+// of |x|, |y| and an odd degree-9 polynomial in a fitted here to
+// atan(a) * 4/pi on [0, 1] (least squares reweighted towards the minimax
+// error, max error 1.5e-5 bin), then the octant fix-ups. For sums that are
+// interpolated linearly into bins (the descriptor), not for exact angles.
+__device__ __forceinline__ float atan2_bins(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    const float a = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
+    const float t = a * a;
+    float p = 0.02654077112674713f;
+    p = fmaf(p, t, -0.10842433571815491f);
+    p = fmaf(p, t, 0.2293858826160431f);
+    p = fmaf(p, t, -0.4205571115016937f);
+    p = fmaf(p, t, 1.2730693817138672f);
+    float r = p * a;
+    if (ay > ax) r = 2.0f - r;
+    if (x < 0.0f) r = 4.0f - r;
+    return copysignf(r, y);
+}
+
+// The hardware's approximate square root and base-2 exponential (one
+// instruction each; subnormal inputs and results flush to zero).
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // k / d and k % d for 0 <= k < 2^20, 0 < d < 2^10 without an integer divide:
 // (k + 0.5) / d is at least 0.5/d away from the next integer and the f32
 // product errs by far less.
