@@ -112,15 +112,18 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
     const float inv_wd = __frcp_rn(wd);
     const float two_pi = 2.0f * kPi;
     const int side = 2 * r + 1;
-    const int total = side * side;
-    const float inv_side = 1.0f / (float)side;
     const float side_f = (float)side, r_f = (float)r;
-    float kf = (float)lane;
-    for (int k = lane; k < total; k += 32, kf += 32.0f) {
-        int q;
-        const float qf = floor_fi((kf + 0.5f) * inv_side, &q);
-        const float fdy = qf - r_f;
-        const float fdx = kf - qf * side_f - r_f;
+    // Sample k = lane + 32 j of the window (row-major) is (fdx, fdy) =
+    // (k % side - r, k / side - r): exact small integers in f32 that advance
+    // by fixed amounts per step, with one row wrap (as selects) at most.
+    const int q0 = lane / side, dq = 32 / side;
+    const float dr_f = (float)(32 - dq * side), dq_f = (float)dq;
+    float fdx = (float)(lane - q0 * side) - r_f, fdy = (float)q0 - r_f;
+    for (;; fdx += dr_f, fdy += dq_f) {
+        const bool wrap = fdx > r_f;
+        fdx = wrap ? fdx - side_f : fdx;
+        fdy = wrap ? fdy + 1.0f : fdy;
+        if (fdy > r_f) break;
         int xi = round_away_i(__fadd_rn(xo, fdx));
         int yi = round_away_i(__fadd_rn(yo, fdy));
         bool in = true;
@@ -131,7 +134,9 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
         }
         const float gx = __fsub_rn(g.px_in(xi + 1, yi), g.px_in(xi - 1, yi));
         const float gy = __fsub_rn(g.px_in(xi, yi + 1), g.px_in(xi, yi - 1));
-        const float mag = __fsqrt_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
+        // the hardware square root (within an ulp; the bins are sums whose
+        // order differs from the reference's anyway)
+        const float mag = sqrt_approx(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
         // exp(-(dx^2 + dy^2) / wd) with the quotient as a product by 1 / wd and
         // the hardware exponential: a few ulp from expf of the IEEE quotient,
         // the same order as expf's own distance from the host libm
@@ -157,7 +162,7 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
 }
 
 template <typename TG>
-__global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
+__global__ void __launch_bounds__(32 * kWarpsPerCta, 5) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
                                                                    const Keypoint* __restrict__ refined_at,
                                                                    const uint32_t* __restrict__ keep, uint32_t ncap,
                                                                    OctCounters* __restrict__ oc,
@@ -208,11 +213,28 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                 else
                     ori_window<TG, true>(g, xo, yo, r, wd, &hist[wid][0][0], lane);
                 __syncwarp();
-                // Column sums, bins lane and lane+32.
-                for (int b = lane; b < kOriBins; b += 32) {
-                    float s = 0.0f;
-                    for (int l = 0; l < 32; ++l) s = __fadd_rn(s, hist[wid][b][(l + b) & 31]);
-                    hs[wid][b] = s;
+                // Column sums: bin `lane` in four interleaved partial sums (the
+                // column index rotated by the bin keeps the 32 lanes in 32
+                // banks), bins 32..35 by eight lanes each and a shuffle tree.
+                {
+                    const float* hb = &hist[wid][lane][0];
+                    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll
+                    for (int l = 0; l < 32; l += 4) {
+                        s0 = __fadd_rn(s0, hb[(l + lane) & 31]);
+                        s1 = __fadd_rn(s1, hb[(l + 1 + lane) & 31]);
+                        s2 = __fadd_rn(s2, hb[(l + 2 + lane) & 31]);
+                        s3 = __fadd_rn(s3, hb[(l + 3 + lane) & 31]);
+                    }
+                    hs[wid][lane] = __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
+                    const int bb = 32 + (lane >> 3), c0 = (lane & 7) * 4;
+                    const float* ht = &hist[wid][bb][0];
+                    float t = __fadd_rn(__fadd_rn(ht[(c0 + bb) & 31], ht[(c0 + 1 + bb) & 31]),
+                                        __fadd_rn(ht[(c0 + 2 + bb) & 31], ht[(c0 + 3 + bb) & 31]));
+                    t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 1));
+                    t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 2));
+                    t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 4));
+                    if ((lane & 7) == 0) hs[wid][bb] = t;
                 }
                 __syncwarp();
                 for (int it = 0; it < 2; ++it) {
@@ -228,8 +250,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_orientation(const TG* __r
                     for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) hs[wid][b] = q == 0 ? nv0 : nv1;
                     __syncwarp();
                 }
-                float mx = 0.0f;
-                for (int b = 0; b < kOriBins; ++b) mx = fmaxf(mx, hs[wid][b]);
+                float mx = fmaxf(hs[wid][lane], lane + 32 < kOriBins ? hs[wid][lane + 32] : 0.0f);
+#pragma unroll
+                for (int m = 16; m > 0; m >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, m));
                 const float thr = __fmul_rn(mx, 0.8f);
                 bool pk[2] = {false, false};
                 float pa[2] = {0.0f, 0.0f};
