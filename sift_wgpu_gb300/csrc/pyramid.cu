@@ -247,6 +247,31 @@ __global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __rest
 }
 
 // ---------------------------------------------------------------------------
+// Packed pairs of f32: mul.rn.f32x2 rounds each of the two products like a
+// scalar multiply. The products are added to scalar accumulators: a packed
+// multiply followed by a packed add was measured to come out fused (one
+// rounding: a third of the sums differed from the reference's), a packed
+// multiply followed by scalar adds matched the scalar sequence on 2^20 sums.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 pack2(float lo, float hi) {
+    return ((f32x2)__float_as_uint(hi) << 32) | __float_as_uint(lo);
+}
+__device__ __forceinline__ float lo2(f32x2 v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float hi2(f32x2 v) { return __uint_as_float((unsigned)(v >> 32)); }
+// tap sum step for two accumulators: a + v * k, rounded after the products
+// and after the sums
+__device__ __forceinline__ void tap2(float& a_lo, float& a_hi, f32x2 v, f32x2 k) {
+    const f32x2 p = mul2(v, k);
+    a_lo = __fadd_rn(a_lo, lo2(p));
+    a_hi = __fadd_rn(a_hi, hi2(p));
+}
+
+// ---------------------------------------------------------------------------
 // Fused level kernel: both separable passes of one level in one launch, for
 // radii up to 8. The CTA stages the (64 + 2r)-row clamp-to-edge neighbourhood
 // of its 64 x 64 output tile from the previous level's u8 plane, runs the
@@ -259,8 +284,8 @@ __global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __rest
 // sh = r mod 4, so an interior row is the 96 bytes [x0 - 16, x0 + 80) written
 // without conditions, and the horizontal pass's first input (x0 - r, column
 // 16 + sh - r) is 16-byte aligned for its float4 window. Each vertical-pass
-// thread owns 4 columns x 4 rows: one float4 shared load per tap and vector
-// stores of level, u8 copy and DoG.
+// thread owns 4 columns x 4 rows: one float4 shared load per tap, two packed
+// multiplies per row and tap, and vector stores of level, u8 copy and DoG.
 constexpr int kFTX = 64, kFTY = 64, kFThreads = 256;
 constexpr int kFMaxR = 8;
 constexpr int kFSW = 100;  // staged row stride (floats): sh + 96 <= 99
@@ -268,7 +293,7 @@ constexpr int kFSW = 100;  // staged row stride (floats): sh + 96 <= 99
 size_t blur_fused_smem(int r) {
     const int taps = 2 * r + 1;
     const size_t rows = (size_t)kFTY + 2 * r;
-    return sizeof(float) * ((size_t)((taps + 3) & ~3) + 256 + rows * kFSW + rows * kFTX);
+    return sizeof(float) * ((size_t)3 * ((taps + 3) & ~3) + 256 + rows * kFSW + rows * kFTX);
 }
 
 template <typename TG>
@@ -299,13 +324,18 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
     constexpr int wpad = (taps + 3) & ~3;
     constexpr int RH = kFTY + 2 * R;
     constexpr int sh = R & 3;
-    float* kw = sm;
+    f32x2* kw2 = reinterpret_cast<f32x2*>(sm);  // [wpad] (k, k), vertical pass
+    float* kw = sm + 2 * wpad;                  // [wpad] k, horizontal pass
     float* lut = kw + wpad;
     float* src = lut + 256;              // [RH][kFSW] staged input (u8 values)
     float* hb = src + (size_t)RH * kFSW;  // [RH][kFTX] horizontal pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int x0 = blockIdx.x * kFTX, y0 = blockIdx.y * kFTY;
-    for (int i = tid; i < wpad; i += kFThreads) kw[i] = i < taps ? wts[i] : 0.0f;
+    for (int i = tid; i < wpad; i += kFThreads) {
+        const float k = i < taps ? wts[i] : 0.0f;
+        kw2[i] = pack2(k, k);
+        kw[i] = k;
+    }
     for (int i = tid; i < 256; i += kFThreads) lut[i] = lut255[i];
     const bool interior = x0 >= 16 && x0 + 80 <= W && y0 >= R && y0 + kFTY + R <= H && (in_pitch & 15) == 0;
     if (interior) {
@@ -378,23 +408,21 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
     // vertical pass: thread = 4 columns x 4 rows, a 4-row float4 window
     // sliding down the taps
     const int cg = tid & 15, rg = tid >> 4;
-    const float4* hb4 = reinterpret_cast<const float4*>(hb) + cg;  // row stride kFTX / 4
+    const ulonglong2* hb2 = reinterpret_cast<const ulonglong2*>(hb) + cg;  // row stride kFTX / 4
     float4 acc[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float4 w0 = hb4[(4 * rg + 0) * (kFTX / 4)], w1 = hb4[(4 * rg + 1) * (kFTX / 4)],
-           w2 = hb4[(4 * rg + 2) * (kFTX / 4)];
+    ulonglong2 w0 = hb2[(4 * rg + 0) * (kFTX / 4)], w1 = hb2[(4 * rg + 1) * (kFTX / 4)],
+               w2 = hb2[(4 * rg + 2) * (kFTX / 4)];
 #pragma unroll
     for (int i = 0; i < taps; ++i) {
-        const float4 w3 = hb4[(4 * rg + i + 3) * (kFTX / 4)];
-        const float k = kw[i];
-        const float4 w[4] = {w0, w1, w2, w3};
+        const ulonglong2 w3 = hb2[(4 * rg + i + 3) * (kFTX / 4)];
+        const f32x2 k = kw2[i];
+        const ulonglong2 w[4] = {w0, w1, w2, w3};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            acc[j].x = __fadd_rn(acc[j].x, __fmul_rn(w[j].x, k));
-            acc[j].y = __fadd_rn(acc[j].y, __fmul_rn(w[j].y, k));
-            acc[j].z = __fadd_rn(acc[j].z, __fmul_rn(w[j].z, k));
-            acc[j].w = __fadd_rn(acc[j].w, __fmul_rn(w[j].w, k));
+            tap2(acc[j].x, acc[j].y, w[j].x, k);
+            tap2(acc[j].z, acc[j].w, w[j].y, k);
         }
         w0 = w1;
         w1 = w2;
