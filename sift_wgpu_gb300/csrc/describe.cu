@@ -103,12 +103,32 @@ __device__ __forceinline__ void fill_lut(float* lut) {
         lut[i] = __fdiv_rn((float)i, 255.0f);
 }
 
+// The exact orientation bin position of a gradient angle (src/sift.rs:652-656):
+// atan2 in (-pi, pi] to [0, 2 pi), times 36, divided by 2 pi.
+__device__ __forceinline__ float exact_bin_pos(float ang) {
+    const float two_pi = 2.0f * kPi;
+    const float an = ang < 0.0f ? __fadd_rn(ang, two_pi) : ang;
+    return __fdiv_rn(__fmul_rn(an, (float)kOriBins), two_pi);  // in [0, 36]
+}
+
+// Bin positions of the four axis directions. The levels are quantised, so
+// many gradients have gx or gy exactly 0; their angles (0, pi/2, pi, -pi/2)
+// fall exactly on bin edges, where only the exact sequence decides the bin.
+// They are computed once with that sequence instead of per sample.
+struct AxisBins {
+    float right, up, left, down;  // angle 0, pi/2, pi, -pi/2
+};
+__device__ __forceinline__ AxisBins axis_bins() {
+    return AxisBins{exact_bin_pos(atan2f(0.0f, 1.0f)), exact_bin_pos(atan2f(1.0f, 0.0f)),
+                    exact_bin_pos(atan2f(0.0f, -1.0f)), exact_bin_pos(atan2f(-1.0f, 0.0f))};
+}
+
 // The orientation window of one keypoint (src/sift.rs:640-662), lane-strided:
 // each lane adds into its own column of the bin-major histogram hist[bin][32].
 // Index and rounding arithmetic stays on the FMA pipe and is exact.
 template <typename TG, bool CHECK>
 __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, float yo, int r, float wd, float* hist,
-                                           int lane) {
+                                           int lane, const AxisBins& ab) {
     const float inv_wd = __frcp_rn(wd);
     const float two_pi = 2.0f * kPi;
     const int side = 2 * r + 1;
@@ -142,17 +162,18 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
         // the same order as expf's own distance from the host libm
         const float wgt = __expf(__fmul_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), inv_wd));
         // Bin index: from the polynomial atan2 and a multiply by 36 / (2 pi)
-        // (a few ulp from the exact value), unless that lands within 1e-4 of
-        // a bin edge; then from atan2f and the IEEE division, the exact
-        // sequence. Away from the edges both floor to the same bin.
+        // (a few ulp from the exact value); axis directions take their exact
+        // position from the table; any other angle within 1e-4 of a bin edge
+        // takes atan2f and the IEEE division, the exact sequence (rare: the
+        // branch no longer splits warps on every flat patch). Away from the
+        // edges all three floor to the same bin.
         const float pa = atan2_poly(gy, gx);
         const float pn = pa < 0.0f ? __fadd_rn(pa, two_pi) : pa;
         float bf = __fmul_rn(pn, (float)kOriBins / two_pi);
-        if (fabsf(__fsub_rn(bf, rintf(bf))) < 1e-4f) {
-            const float ang = atan2f(gy, gx);
-            const float an = ang < 0.0f ? __fadd_rn(ang, two_pi) : ang;
-            bf = __fdiv_rn(__fmul_rn(an, (float)kOriBins), two_pi);  // in [0, 36]
-        }
+        const bool axis = gx == 0.0f || gy == 0.0f;  // (0, 0): atan2 0, angle 0
+        const float bax = gy == 0.0f ? (gx < 0.0f ? ab.left : ab.right) : (gy > 0.0f ? ab.up : ab.down);
+        bf = axis ? bax : bf;
+        if (!axis && fabsf(__fsub_rn(bf, rintf(bf))) < 1e-4f) bf = exact_bin_pos(atan2f(gy, gx));
         const int fl = floor_i(bf);
         const int bin = fl >= kOriBins ? fl - kOriBins : fl;
         const float v = __fmul_rn(mag, wgt);
@@ -178,6 +199,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, 5) k_orientation(const TG* 
     const uint32_t n = min(oc->n_cand, ncap);  // candidate slots; rejected ones get 0 peaks
     const float two_pi = 2.0f * kPi;
     const float bin_w = 2.0f * kPi / (float)kOriBins;
+    const AxisBins ab = axis_bins();
     const bool persist = (int)blockIdx.x >= persist_from;
     for (int taken = 0; persist || taken < kOriBudget; ++taken) {
         uint32_t i = 0;
@@ -209,9 +231,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, 5) k_orientation(const TG* 
                 const bool interior = xo - (float)r >= 2.5f && xo + (float)r <= (float)(g.W - 3) - 0.5f &&
                                       yo - (float)r >= 2.5f && yo + (float)r <= (float)(g.H - 3) - 0.5f;
                 if (interior)
-                    ori_window<TG, false>(g, xo, yo, r, wd, &hist[wid][0][0], lane);
+                    ori_window<TG, false>(g, xo, yo, r, wd, &hist[wid][0][0], lane, ab);
                 else
-                    ori_window<TG, true>(g, xo, yo, r, wd, &hist[wid][0][0], lane);
+                    ori_window<TG, true>(g, xo, yo, r, wd, &hist[wid][0][0], lane, ab);
                 __syncwarp();
                 // Column sums: bin `lane` in four interleaved partial sums (the
                 // column index rotated by the bin keeps the 32 lanes in 32
