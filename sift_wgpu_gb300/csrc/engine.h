@@ -51,7 +51,7 @@ int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, uint8_t* o
 template <typename TG>
 int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst,
                    uint8_t* dst_u8, int dst_pitch, int nW, int nH, const int* vtab, const float* vw, const int* htab,
-                   const float* hw, cudaStream_t st, bool fused, int* launches);
+                   const float* hw, const LanczosUniform& uni, cudaStream_t st, bool fused, int* launches);
 int lanczos_fused_span();
 int lanczos_fused_tile();
 int pixel_channels(int format);
@@ -160,7 +160,28 @@ struct Engine {
     struct LTab {
         size_t vtab, vw, htab, hw;  // element offsets in d_ltab / d_lw
         bool fused;                 // every output tile's source window fits the fused kernel
+        LanczosUniform uni;         // the interior of a 2x resize (empty otherwise)
     };
+    // Outputs [*lo, *hi) of a resize axis whose taps start at 2 o - 5, number
+    // kLz2xTaps and equal the middle output's bit for bit (a 2x resize away
+    // from the borders); w receives those taps. Empty unless src = 2 dst.
+    static void uniform_2x(const AxisTaps& t, uint32_t src, int* lo, int* hi, float* w) {
+        *lo = *hi = 0;
+        const int n = (int)t.left.size();
+        if (n < 8 || src != 2u * (uint32_t)n) return;
+        const int m = n / 2;
+        auto same = [&](int o) {
+            if (t.count[o] != kLz2xTaps || t.left[o] != 2 * o - 5) return false;
+            return std::memcmp(&t.w[t.woff[o]], &t.w[t.woff[m]], sizeof(float) * kLz2xTaps) == 0;
+        };
+        if (!same(m)) return;
+        int a = m, b = m + 1;
+        while (a > 0 && same(a - 1)) --a;
+        while (b < n && same(b)) ++b;
+        *lo = a;
+        *hi = b;
+        std::memcpy(w, &t.w[t.woff[m]], sizeof(float) * kLz2xTaps);
+    }
     std::vector<LTab> ltab;  // [o] for o -> o+1
 
     // Lists. Octave o owns [cb[o], cb[o] + cap_c[o]) of the candidate-sized
@@ -403,7 +424,7 @@ struct Engine {
         // Lanczos tables
         std::vector<int> itab;
         std::vector<float> ftab;
-        ltab.assign(O, LTab{0, 0, 0, 0, false});
+        ltab.assign(O, LTab{0, 0, 0, 0, false, LanczosUniform{}});
         auto max_span = [](const AxisTaps& t) {
             const int T = lanczos_fused_tile(), n = (int)t.left.size();
             int m = 0;
@@ -433,6 +454,10 @@ struct Engine {
             t.hw = ftab.size();
             ftab.insert(ftab.end(), th.w.begin(), th.w.end());
             t.fused = max_span(tv) <= lanczos_fused_span() && max_span(th) <= lanczos_fused_span();
+            t.uni = LanczosUniform{};
+            uniform_2x(th, (uint32_t)a.W, &t.uni.x0, &t.uni.x1, t.uni.wh);
+            uniform_2x(tv, (uint32_t)a.H, &t.uni.y0, &t.uni.y1, t.uni.wv);
+            if (t.uni.x0 >= t.uni.x1 || t.uni.y0 >= t.uni.y1) t.uni.x0 = t.uni.x1 = t.uni.y0 = t.uni.y1 = 0;
             ltab[o] = t;
         }
         // allocate
@@ -571,7 +596,7 @@ struct Engine {
             int nl = 0;
             if (launch_lanczos<TG>(U + od.u_off + (long long)S * od.plane, od.pitch, od.W, od.H, d_ltmp.as<float>(),
                                    od.pitch, G + nx.g_off, U + nx.u_off, nx.pitch, nx.W, nx.H, it + t.vtab, ft + t.vw,
-                                   it + t.htab, ft + t.hw, st, t.fused, &nl))
+                                   it + t.htab, ft + t.hw, t.uni, st, t.fused, &nl))
                 return cuda_fail(cudaGetLastError(), "lanczos");
             launches += nl;
             return 0;

@@ -490,16 +490,20 @@ __global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride,
 // source window (at most kLzSpan x kLzSpan, checked on the host), runs the
 // vertical pass for the columns the horizontal pass reads, then the
 // horizontal pass; every value is formed exactly as in the two-kernel form.
-constexpr int kLzT = 32, kLzSpan = 80;
+// Tiles inside the uniform interior of a 2x resize (LanczosUniform) run both
+// passes with the 12 taps as constants: each thread sums 4 outputs from 18
+// shared loads, the tap loops unrolled; the sums are the same, in the same
+// order.
+constexpr int kLzT = 32, kLzSpan = 80, kLzMid = 81;  // odd mid stride: lanes on rows hit 32 banks
 
 template <typename TG>
 __global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict__ src, int src_pitch,
                                                        TG* __restrict__ dst, uint8_t* __restrict__ dst_u8,
                                                        int dst_pitch, int nW, int nH, const int* __restrict__ vtab,
                                                        const float* __restrict__ vw, const int* __restrict__ htab,
-                                                       const float* __restrict__ hw) {
+                                                       const float* __restrict__ hw, const LanczosUniform uni) {
     __shared__ float in[kLzSpan][kLzSpan];
-    __shared__ float mid[kLzT][kLzSpan];
+    __shared__ float mid[kLzT][kLzMid];
     const int* vleft = vtab;
     const int* vcount = vtab + nH;
     const int* voff = vtab + 2 * nH;
@@ -526,6 +530,44 @@ __global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict
         }
     }
     __syncthreads();
+    if (ox0 >= uni.x0 && ox0 + kLzT <= uni.x1 && oy0 >= uni.y0 && oy0 + kLzT <= uni.y1) {
+        // vertical pass: warp w makes mid rows 4w .. 4w+3 from source rows
+        // 8w .. 8w+17 (output row r reads from 2r, tap i at j = 2r + i)
+        for (int xx = lane; xx < sw; xx += 32) {
+            float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int j = 0; j < 18; ++j) {
+                const float v = in[8 * warp + j][xx];
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (j - 2 * r >= 0 && j - 2 * r < kLz2xTaps) a[r] = __fadd_rn(a[r], __fmul_rn(v, uni.wv[j - 2 * r]));
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r) mid[4 * warp + r][xx] = a[r];
+        }
+        __syncthreads();
+        // horizontal pass: lane = output row, warp w = outputs 4w .. 4w+3 of
+        // it, from mid columns 8w .. 8w+17
+        float b[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int j = 0; j < 18; ++j) {
+            const float v = mid[lane][8 * warp + j];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (j - 2 * r >= 0 && j - 2 * r < kLz2xTaps) b[r] = __fadd_rn(b[r], __fmul_rn(v, uni.wh[j - 2 * r]));
+        }
+        const long long od = (long long)(oy0 + lane) * dst_pitch + ox0 + 4 * warp;
+        unsigned packed = 0u;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const float t = b[r] < 0.0f ? 0.0f : (b[r] > 255.0f ? 255.0f : b[r]);
+            const int v = (int)roundf(t);
+            store_level(dst + od + r, v, norm255(v));
+            packed |= (unsigned)v << (8 * r);
+        }
+        *reinterpret_cast<unsigned*>(dst_u8 + od) = packed;
+        return;
+    }
     // vertical pass: rows oy0..oy1-1 (one warp per row), columns x_lo..x_hi-1
     for (int oyl = warp; oyl < oy1 - oy0; oyl += 8) {
         const int oy = oy0 + oyl;
@@ -662,10 +704,11 @@ int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, uint8_t* o
 template <typename TG>
 int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst,
                    uint8_t* dst_u8, int dst_pitch, int nW, int nH, const int* vtab, const float* vw, const int* htab,
-                   const float* hw, cudaStream_t st, bool fused, int* launches) {
+                   const float* hw, const LanczosUniform& uni, cudaStream_t st, bool fused, int* launches) {
     if (fused) {
         dim3 g((nW + kLzT - 1) / kLzT, (nH + kLzT - 1) / kLzT);
-        k_lanczos_fused<TG><<<g, 256, 0, st>>>(src, src_pitch, dst, dst_u8, dst_pitch, nW, nH, vtab, vw, htab, hw);
+        k_lanczos_fused<TG><<<g, 256, 0, st>>>(src, src_pitch, dst, dst_u8, dst_pitch, nW, nH, vtab, vw, htab, hw,
+                                               uni);
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
@@ -689,7 +732,8 @@ int lanczos_fused_tile() { return kLzT; }
                                        cudaStream_t);                                                              \
     template int launch_u8_to_level<TG>(const uint8_t*, long long, TG*, uint8_t*, int, int, int, cudaStream_t);    \
     template int launch_lanczos<TG>(const uint8_t*, int, int, int, float*, int, TG*, uint8_t*, int, int, int,      \
-                                    const int*, const float*, const int*, const float*, cudaStream_t, bool, int*);
+                                    const int*, const float*, const int*, const float*, const LanczosUniform&,      \
+                                    cudaStream_t, bool, int*);
 SIFT_INST(float)
 SIFT_INST(__half)
 #undef SIFT_INST

@@ -65,6 +65,16 @@ struct PyramidDev {
     OctaveDev oct[kMaxOctaves];
 };
 
+// The interior of a 2x Lanczos3 resize: output columns [x0, x1) and rows
+// [y0, y1) read the source from 2 o - 5 with the same kLz2xTaps taps (bit for
+// bit the table's), so a tile inside both ranges can take them as constants.
+// An empty range disables it.
+constexpr int kLz2xTaps = 12;
+struct LanczosUniform {
+    int x0, x1, y0, y1;
+    float wv[kLz2xTaps], wh[kLz2xTaps];
+};
+
 // Exact integer rounding on the FMA pipe. Conversions (F2I/I2F/FRND) run on
 // the quarter-rate XU pipe; for |x| < 2^22 adding a power of two of the right
 // size in a directed rounding mode leaves the rounded value in the low
