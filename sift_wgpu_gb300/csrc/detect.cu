@@ -28,43 +28,23 @@ namespace sift {
 namespace {
 
 // DoG access for one octave (src/sift.rs:208-214 get_pixel_value, clamped).
-struct DogF32 {
-    const float* base;  // DoG level 0 of the octave
+// DoG of one octave recomputed from the u8 copies of its Gaussian levels:
+// D_l = lut[G_{l+1}] - lut[G_l] with lut[v] = v/255 in f32 — the stored f32 DoG
+// bit for bit (src/sift.rs:92-124) in either storage mode, at one byte per
+// level value instead of four (the refinement's scattered 3 x 3 x 3 reads
+// then mostly hit L2).
+struct DogFromU8 {
+    const uint8_t* base;  // u8 level 0 of the octave
+    const float* lut;     // v / 255, shared or global
     long long plane;
     int pitch, W, H;
     __device__ __forceinline__ float at(int l, int x, int y) const {
         x = clampi(x, 0, W - 1);
         y = clampi(y, 0, H - 1);
-        return base[(long long)l * plane + (long long)y * pitch + x];
+        const uint8_t* p = base + (long long)l * plane + (long long)y * pitch + x;
+        return __fsub_rn(lut[p[plane]], lut[p[0]]);
     }
 };
-
-// DoG recomputed in f32 from f16-stored Gaussian levels:
-// D_l = G_{l+1}/255 - G_l/255, exactly as stored DoG would hold it.
-struct DogFromG16 {
-    const __half* base;  // G level 0 of the octave
-    long long plane;
-    int pitch, W, H;
-    __device__ __forceinline__ float at(int l, int x, int y) const {
-        x = clampi(x, 0, W - 1);
-        y = clampi(y, 0, H - 1);
-        const long long o = (long long)y * pitch + x;
-        float a = __half2float(base[(long long)(l + 1) * plane + o]);
-        float b = __half2float(base[(long long)l * plane + o]);
-        return __fsub_rn(__fdiv_rn(a, 255.0f), __fdiv_rn(b, 255.0f));
-    }
-};
-
-template <class Dog>
-__device__ __forceinline__ Dog make_dog(const void* arena, const OctaveDev& od);
-template <>
-__device__ __forceinline__ DogF32 make_dog<DogF32>(const void* arena, const OctaveDev& od) {
-    return DogF32{(const float*)arena + od.d_off, od.plane, od.pitch, od.W, od.H};
-}
-template <>
-__device__ __forceinline__ DogFromG16 make_dog<DogFromG16>(const void* arena, const OctaveDev& od) {
-    return DogFromG16{(const __half*)arena + od.g_off, od.plane, od.pitch, od.W, od.H};
-}
 
 // DoG staged from the u8 copies of the Gaussian levels of one octave:
 // D_l = lut[G_{l+1}] - lut[G_l] with lut[v] = v/255 in f32, which is the
@@ -307,8 +287,8 @@ __device__ bool refine_one(const Dog& dog, int o, int x, int y, int s, const Ref
 // One thread per mask word of octave o: the candidates of the word go to
 // their scanned slots in the octave's list, in x order within the word, i.e.
 // (layer, y, x) within the octave.
-template <class Dog>
-__global__ void __launch_bounds__(256) k_emit(const void* arena, PyramidDev pyr, int o,
+__global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ u8arena, const float* __restrict__ lut255,
+                                              PyramidDev pyr, int o,
                                               const uint32_t* __restrict__ words,
                                               const uint32_t* __restrict__ cand_off,
                                               Keypoint* __restrict__ cands, uint32_t cap,
@@ -319,7 +299,7 @@ __global__ void __launch_bounds__(256) k_emit(const void* arena, PyramidDev pyr,
     if (w >= nwo) return;
     uint32_t word = words[w];
     if (word == 0u) return;
-    const Dog dog = make_dog<Dog>(arena, od);
+    const DogFromU8 dog{u8arena + od.u_off, lut255, od.plane, od.pitch, od.W, od.H};
     const int c = (int)(w % od.nw);
     const long long rowid = w / od.nw;
     const int y = (int)(rowid % od.H);
@@ -348,13 +328,17 @@ __global__ void __launch_bounds__(256) k_emit(const void* arena, PyramidDev pyr,
 
 // One thread per candidate of octave o (persistent grid over its count); the
 // survivors are counted per warp into oc->n_ref (a count, order-free).
-template <class Dog>
-__global__ void __launch_bounds__(256) k_refine(const void* arena, PyramidDev pyr, int o, RefineParams rp,
-                                                const Keypoint* __restrict__ cands,
+__global__ void __launch_bounds__(256) k_refine(const uint8_t* __restrict__ u8arena,
+                                                const float* __restrict__ lut255, PyramidDev pyr, int o,
+                                                RefineParams rp, const Keypoint* __restrict__ cands,
                                                 Keypoint* __restrict__ refined_at, uint32_t* __restrict__ keep,
                                                 uint32_t cap, OctCounters* __restrict__ oc) {
+    __shared__ float lut[256];
+    lut[threadIdx.x] = lut255[threadIdx.x];
+    __syncthreads();
     const uint32_t n = min(oc->n_cand, cap);
-    const Dog dog = make_dog<Dog>(arena, pyr.oct[o]);
+    const OctaveDev& od = pyr.oct[o];
+    const DogFromU8 dog{u8arena + od.u_off, lut, od.plane, od.pitch, od.W, od.H};
     const float scale = __int_as_float((127 + o) << 23);
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -392,28 +376,24 @@ int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const Pyram
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_emit(int storage, const void* arena, const PyramidDev& pyr, int o, const uint32_t* words,
+int launch_emit(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, const uint32_t* words,
                 const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st) {
     const OctaveDev& od = pyr.oct[o];
     const long long nwo = (long long)pyr.S * od.H * od.nw;
     if (nwo <= 0) return 0;
     unsigned grid = (unsigned)((nwo + 255) / 256);
-    if (storage == SIFT_CUDA_STORAGE_F16)
-        k_emit<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, o, words, cand_off, cands, cap, ctr);
-    else
-        k_emit<DogF32><<<grid, 256, 0, st>>>(arena, pyr, o, words, cand_off, cands, cap, ctr);
+    k_emit<<<grid, 256, 0, st>>>(u8arena, lut255, pyr, o, words, cand_off, cands, cap, ctr);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_refine(int storage, const void* arena, const PyramidDev& pyr, int o, float sigma, float contrast,
-                  float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
-                  OctCounters* oc, cudaStream_t st) {
+// Refinement is a chain of dependent scattered reads per candidate: up to
+// 5 CTAs of 8 warps per SM keep enough of them in flight.
+int launch_refine(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, float sigma,
+                  float contrast, float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep,
+                  uint32_t cap, OctCounters* oc, cudaStream_t st) {
     RefineParams rp{sigma, contrast, edge, pyr.S, pyr.S + 2};
-    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 2);
-    if (storage == SIFT_CUDA_STORAGE_F16)
-        k_refine<DogFromG16><<<grid, 256, 0, st>>>(arena, pyr, o, rp, cands, refined_at, keep, cap, oc);
-    else
-        k_refine<DogF32><<<grid, 256, 0, st>>>(arena, pyr, o, rp, cands, refined_at, keep, cap, oc);
+    const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 5);
+    k_refine<<<grid, 256, 0, st>>>(u8arena, lut255, pyr, o, rp, cands, refined_at, keep, cap, oc);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -61,11 +61,11 @@ int launch_to_luma(int format, const uint8_t* px, long long stride, int W, int H
                    cudaStream_t st);
 int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
                         uint32_t* words, cudaStream_t st);
-int launch_emit(int storage, const void* arena, const PyramidDev& pyr, int o, const uint32_t* words,
+int launch_emit(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, const uint32_t* words,
                 const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st);
-int launch_refine(int storage, const void* arena, const PyramidDev& pyr, int o, float sigma, float contrast,
-                  float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
-                  OctCounters* oc, cudaStream_t st);
+int launch_refine(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, float sigma,
+                  float contrast, float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep,
+                  uint32_t cap, OctCounters* oc, cudaStream_t st);
 template <typename TG>
 int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
                        uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,
@@ -554,7 +554,6 @@ struct Engine {
         const float* lut = wts + lut_off;
         uint8_t* U = d_U.as<uint8_t>();
         Counters* ctr = d_ctr.as<Counters>();
-        const void* arena = f16() ? (const void*)d_G.p : (const void*)d_D.p;
         launches = 0;
         auto ok = [&](int rc) {
             ++launches;
@@ -615,11 +614,11 @@ struct Engine {
                                &ctr->overflow, q))
                 return cuda_fail(cudaGetLastError(), "scan candidates");
             launches += nwo > 0 ? 1 : 0;
-            if (ok(launch_emit(opt.storage, arena, pyr, o, d_words.as<uint32_t>() + od.word_base,
+            if (ok(launch_emit(U, lut, pyr, o, d_words.as<uint32_t>() + od.word_base,
                                d_cand_off.as<uint32_t>() + od.word_base, d_cands.as<Keypoint>() + cb[o], cap_c[o], ctr,
                                q)))
                 return cuda_fail(cudaGetLastError(), "emit");
-            if (ok(launch_refine(opt.storage, arena, pyr, o, p.sigma, p.contrast_threshold, p.edge_threshold,
+            if (ok(launch_refine(U, lut, pyr, o, p.sigma, p.contrast_threshold, p.edge_threshold,
                                  d_cands.as<Keypoint>() + cb[o], d_refined_at.as<Keypoint>() + cb[o],
                                  d_keep.as<uint32_t>() + cb[o], cap_c[o], oc, q)))
                 return cuda_fail(cudaGetLastError(), "refine");
