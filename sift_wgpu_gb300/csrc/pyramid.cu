@@ -74,18 +74,25 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __rest
     const uint8_t* src = in + (long long)y * in_pitch;
     for (int i = threadIdx.x; i < wpad; i += blockDim.x) kw[i] = i < taps ? wts[i] : 0.0f;
     const int padded = W + 2 * r;
-    const int nv = (in_pitch & 15) == 0 ? (W >> 4) : 0;  // 16-byte vectors of the interior
-#pragma unroll 2
-    for (int k = threadIdx.x; k < nv; k += blockDim.x) {
-        float v[16];
-        unpack16(*reinterpret_cast<const uint4*>(src + 16 * k), v);
-#pragma unroll
-        for (int e = 0; e < 16; ++e) row[r + 16 * k + e] = v[e];
+    // Interior as 4-byte words, consecutive lanes on consecutive words: the
+    // four stores of a lane land 4 floats apart from its neighbour's (4-way
+    // bank sharing; 16-byte words per lane would put a warp's stores in two
+    // banks).
+    const int nw4 = (in_pitch & 3) == 0 ? (W >> 2) : 0;
+#pragma unroll 4
+    for (int k = threadIdx.x; k < nw4; k += blockDim.x) {
+        const unsigned b = *reinterpret_cast<const unsigned*>(src + 4 * k);
+        float* d = row + r + 4 * k;
+        d[0] = float_of_u8(b & 0xffu);
+        d[1] = float_of_u8((b >> 8) & 0xffu);
+        d[2] = float_of_u8((b >> 16) & 0xffu);
+        d[3] = float_of_u8(b >> 24);
     }
-    for (int j = threadIdx.x; j < padded + 8; j += blockDim.x) {
-        const int xs = j - r;
-        if (xs >= 0 && xs < 16 * nv) continue;
-        row[j] = float_of_u8(src[clampi(xs, 0, W - 1)]);
+    // clamp-to-edge borders, the tail after the whole words and the slack
+    const int hi0 = r + 4 * nw4, nb = r + (padded + 8 - hi0);
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        const int jj = j < r ? j : hi0 + (j - r);
+        row[jj] = float_of_u8(src[clampi(jj - r, 0, W - 1)]);
     }
     __syncthreads();
     uint8_t* dst = out + (long long)y * out_pitch;
