@@ -429,30 +429,52 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                 const int px0 = (int)xf - (rad + 1), py0 = (int)yf - (rad + 1);
                 const bool inner = px0 >= 0 && py0 >= 0 && px0 + gs < g.W && py0 + gs < g.H;
                 const float inv_gs = 1.0f / (float)gs;
-                float qf = (float)tid;
-                for (int q = tid; q < gs * gs; q += kDescThreads, qf += (float)kDescThreads) {
-                    const int qy = floor_i((qf + 0.5f) * inv_gs);
-                    const int qx = q - qy * gs;
-                    float q11, q21, q12, q22;
-                    if (inner) {
-                        const TG* pp = g.base + (py0 + qy) * g.pitch + (px0 + qx);
-                        q11 = gnorm(pp, lut);
-                        q21 = gnorm(pp + 1, lut);
-                        q12 = gnorm(pp + g.pitch, lut);
-                        q22 = gnorm(pp + g.pitch + 1, lut);
-                    } else {
-                        q11 = g.px(px0 + qx, py0 + qy);
-                        q21 = g.px(px0 + qx + 1, py0 + qy);
-                        q12 = g.px(px0 + qx, py0 + qy + 1);
-                        q22 = g.px(px0 + qx + 1, py0 + qy + 1);
+                if (inner) {
+                    // A thread makes a column strip of 4 grid points from 5
+                    // pixel rows: each row's horizontal lerp serves two points
+                    // (10 loads for 4 points); consecutive lanes take
+                    // consecutive columns. The same two lerps per point as
+                    // below, so the same values.
+                    const int strips = (gs + 3) >> 2;
+                    const TG* org = g.base + py0 * g.pitch + px0;
+                    float tf = (float)tid;
+                    for (int t = tid; t < strips * gs; t += kDescThreads, tf += (float)kDescThreads) {
+                        const int sy = floor_i((tf + 0.5f) * inv_gs);
+                        const int qx = t - sy * gs, qy0 = 4 * sy;
+                        const int nr = min(4, gs - qy0);
+                        const TG* pp = org + qy0 * g.pitch + qx;
+                        float a0 = gnorm(pp, lut), a1 = gnorm(pp + 1, lut);
+                        float rp = fmaf(fdx, a1 - a0, a0);
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            if (j < nr) {
+                                pp += g.pitch;
+                                a0 = gnorm(pp, lut);
+                                a1 = gnorm(pp + 1, lut);
+                                const float rn = fmaf(fdx, a1 - a0, a0);
+                                const float b = fmaf(fdy, rn - rp, rp);
+                                grid[(qy0 + j) * gs + qx] = b;
+                                lo = fminf(lo, b);
+                                hi = fmaxf(hi, b);
+                                rp = rn;
+                            }
+                        }
                     }
-                    // the reference's bilinear blend as two lerps (within the
-                    // descriptor tolerance)
-                    const float r0 = fmaf(fdx, q21 - q11, q11), r1 = fmaf(fdx, q22 - q12, q12);
-                    const float b = fmaf(fdy, r1 - r0, r0);
-                    grid[q] = b;
-                    lo = fminf(lo, b);
-                    hi = fmaxf(hi, b);
+                } else {
+                    float qf = (float)tid;
+                    for (int q = tid; q < gs * gs; q += kDescThreads, qf += (float)kDescThreads) {
+                        const int qy = floor_i((qf + 0.5f) * inv_gs);
+                        const int qx = q - qy * gs;
+                        const float q11 = g.px(px0 + qx, py0 + qy), q21 = g.px(px0 + qx + 1, py0 + qy);
+                        const float q12 = g.px(px0 + qx, py0 + qy + 1), q22 = g.px(px0 + qx + 1, py0 + qy + 1);
+                        // the reference's bilinear blend as two lerps (within the
+                        // descriptor tolerance)
+                        const float r0 = fmaf(fdx, q21 - q11, q11), r1 = fmaf(fdx, q22 - q12, q12);
+                        const float b = fmaf(fdy, r1 - r0, r0);
+                        grid[q] = b;
+                        lo = fminf(lo, b);
+                        hi = fmaxf(hi, b);
+                    }
                 }
             } else {
                 lo = 0.0f;
