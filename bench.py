@@ -303,6 +303,61 @@ def run_batch64(args, world, rank, local):
         }), flush=True)
 
 
+def run_match(args, world, rank, local):
+    """Descriptor matching (sift_cuda_match_device on resident descriptors;
+    the host form for e2e): the 1080p frame's descriptors as train set, those
+    of the same scene shifted by (5, 3) pixels as queries; pairs/s = queries x
+    train descriptors compared per second."""
+    import ctypes as C
+    import torch
+    import sift_wgpu_gb300 as sg
+    img = sg.synth_image(1, 1920, 1080)
+    shifted = np.zeros_like(img)
+    shifted[3:, 5:] = img[:-3, :-5]
+    torch.cuda.set_device(local)
+    with sg.Engine(sg.Sift.default(), device=local) as eng:
+        _, dt = eng.detect_and_compute(img)
+        _, dq = eng.detect_and_compute(shifted)
+        nq, nt = len(dq), len(dt)
+        lib = sg._capi.lib()
+        q, t = torch.from_numpy(dq).cuda(), torch.from_numpy(dt).cuda()
+        out = torch.empty(nq * 4, dtype=torch.int32, device="cuda")
+        scratch = torch.empty(lib.sift_cuda_match_scratch_bytes(nq, nt), dtype=torch.uint8, device="cuda")
+        stream = torch.cuda.current_stream()
+        launch = lambda: lib.sift_cuda_match_device(C.c_void_p(q.data_ptr()), nq, C.c_void_p(t.data_ptr()), nt,
+                                                    C.c_void_p(out.data_ptr()), C.c_void_p(scratch.data_ptr()),
+                                                    C.c_void_p(stream.cuda_stream))
+        for _ in range(args.warmup):
+            assert launch() == 0, lib.sift_cuda_last_error()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            launch()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / args.steps
+        for _ in range(max(1, args.warmup)):
+            eng.match(dq, dt)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            m = eng.match(dq, dt)
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        good = int((m["distance"] < 0.8 * m["second_distance"]).sum())
+    pairs = float(nq) * nt
+    if rank == 0:
+        print(json.dumps({
+            "metric": "descriptor pairs/s", "value": pairs / (ms / 1e3), "unit": "pairs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "match: 1080p frame seed 1 (train) vs the same scene shifted by (5, 3) px (queries)",
+                       "queries": nq, "train": nt, "ratio_test_0.8_matches": good},
+            "tflops_f32": 2.0 * pairs * 128 / (ms / 1e3) / 1e12,
+            "e2e": {"value": pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": (nq + nt) * 512,
+                    "d2h_bytes_per_step": nq * 16},
+        }), flush=True)
+
+
 def run_serve(args, world, rank, local):
     rep = serving_report(args.requests, [500, 1000, 2000, 4000, 8000], max_inflight=args.inflight,
                          autotune=args.autotune, device=local)
@@ -522,7 +577,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64", "serve"], default="1080p")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64", "serve", "match"], default="1080p")
     ap.add_argument("--storage", choices=["f32", "f16"], default="f32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -540,6 +595,8 @@ def main():
         run_batch64(args, world, rank, local)
     elif args.workload == "serve":
         run_serve(args, world, rank, local)
+    elif args.workload == "match":
+        run_match(args, world, rank, local)
     else:
         run_cuda(args, world, rank, local)
     if world > 1:

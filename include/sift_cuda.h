@@ -313,6 +313,30 @@ int sift_cuda_replay(SiftCudaServer* server, const SiftCudaParams* params, const
                      const SiftCudaReplayImage* images, uint32_t n_images, const SiftCudaReplayRequest* reqs,
                      uint32_t n_reqs, SiftCudaReplayResult* results, double* wall_s);
 
+/* ---- descriptor matching ------------------------------------------------ */
+
+/* The nearest and second-nearest train descriptor of each query descriptor
+ * by Euclidean distance (brute force, f32): the input of Lowe's ratio test.
+ * Not in the reference crate; it consumes the 128-float descriptors that
+ * detect_and_compute returns. Ties go to the lower train index. */
+typedef struct {
+    int32_t train_idx;      /* nearest train descriptor, -1 if n_train == 0 */
+    float distance;         /* its Euclidean distance (INFINITY if none) */
+    int32_t second_idx;     /* second nearest, -1 if n_train < 2 */
+    float second_distance;
+} SiftCudaMatch;
+
+/* Host arrays: query n_query x 128 floats, train n_train x 128 floats, out
+ * n_query entries; runs on the engine's stream and synchronises. */
+int sift_cuda_match(SiftCudaEngine* engine, const float* query, uint32_t n_query, const float* train,
+                    uint32_t n_train, SiftCudaMatch* out);
+/* Device form, asynchronous on `stream` (a cudaStream_t; NULL = default):
+ * d_query and d_train 16-byte aligned, d_scratch at least
+ * sift_cuda_match_scratch_bytes(n_query, n_train) bytes of device memory. */
+size_t sift_cuda_match_scratch_bytes(uint32_t n_query, uint32_t n_train);
+int sift_cuda_match_device(const float* d_query, uint32_t n_query, const float* d_train, uint32_t n_train,
+                           SiftCudaMatch* d_out, void* d_scratch, void* stream);
+
 /* ---- blur without allocation ---------------------------------------------- */
 
 /* Gaussian blur of a u8 image in device memory into a caller-owned device

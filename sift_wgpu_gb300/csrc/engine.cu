@@ -212,6 +212,50 @@ int sift_cuda_device_outputs(SiftCudaEngine* engine, const uint32_t** d_count, c
     return 0;
 }
 
+size_t sift_cuda_match_scratch_bytes(uint32_t n_query, uint32_t n_train) {
+    return sift::match_scratch_bytes(n_query, n_train);
+}
+
+int sift_cuda_match_device(const float* d_query, uint32_t n_query, const float* d_train, uint32_t n_train,
+                           SiftCudaMatch* d_out, void* d_scratch, void* stream) {
+    sift::g_last_error.clear();
+    if (n_query == 0) return 0;
+    if (!d_query || !d_out || !d_scratch || (n_train && !d_train))
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "a matching buffer is NULL");
+    if (((uintptr_t)d_query | (uintptr_t)d_train) & 15)
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "descriptor arrays must be 16-byte aligned");
+    if (sift::launch_match(d_query, n_query, d_train, n_train, d_out, d_scratch, (cudaStream_t)stream))
+        return sift::cuda_fail(cudaGetLastError(), "match");
+    return 0;
+}
+
+int sift_cuda_match(SiftCudaEngine* engine, const float* query, uint32_t n_query, const float* train,
+                    uint32_t n_train, SiftCudaMatch* out) {
+    sift::g_last_error.clear();
+    if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
+    if (n_query == 0) return 0;
+    if (!query || !out || (n_train && !train)) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "a matching buffer is NULL");
+    Engine& e = engine->e;
+    if (int rc = e.set_device()) return rc;
+    const size_t qb = (size_t)n_query * sift::kDescLen * sizeof(float), tb = (size_t)n_train * sift::kDescLen * sizeof(float);
+    if (e.d_mq.ensure(qb) != cudaSuccess || e.d_mt.ensure(std::max<size_t>(tb, 16)) != cudaSuccess ||
+        e.d_mo.ensure((size_t)n_query * sizeof(SiftCudaMatch)) != cudaSuccess ||
+        e.d_ms.ensure(sift::match_scratch_bytes(n_query, n_train)) != cudaSuccess)
+        return sift::cuda_fail(cudaGetLastError(), "cudaMalloc(match)");
+    cudaStream_t st = e.st;
+    if (cudaMemcpyAsync(e.d_mq.p, query, qb, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        (tb && cudaMemcpyAsync(e.d_mt.p, train, tb, cudaMemcpyHostToDevice, st) != cudaSuccess))
+        return sift::cuda_fail(cudaGetLastError(), "H2D descriptors");
+    if (sift::launch_match(e.d_mq.as<float>(), n_query, e.d_mt.as<float>(), n_train, e.d_mo.as<SiftCudaMatch>(),
+                           e.d_ms.p, st))
+        return sift::cuda_fail(cudaGetLastError(), "match");
+    if (cudaMemcpyAsync(out, e.d_mo.p, (size_t)n_query * sizeof(SiftCudaMatch), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return sift::cuda_fail(cudaGetLastError(), "match results");
+    return 0;
+}
+
 int sift_cuda_synchronize(SiftCudaEngine* engine) {
     if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
     cudaError_t e = cudaStreamSynchronize(engine->e.st);

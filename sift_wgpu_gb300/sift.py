@@ -215,6 +215,21 @@ class Engine:
         return (np.frombuffer(kbuf, dtype=KEYPOINT_DTYPE, count=n),
                 np.frombuffer(dbuf, dtype=np.float32, count=n * DESC_LEN).reshape(n, DESC_LEN))
 
+    # descriptor matching ----------------------------------------------------
+    def match(self, query, train) -> np.ndarray:
+        """Nearest and second-nearest train descriptor of every query
+        descriptor by Euclidean distance (brute force on the GPU, ties to the
+        lower index): a MATCH_DTYPE array of len(query) entries. Not in the
+        reference crate; the consumer of detect_and_compute's descriptors."""
+        q = np.ascontiguousarray(query, dtype=np.float32).reshape(-1, DESC_LEN)
+        t = np.ascontiguousarray(train, dtype=np.float32).reshape(-1, DESC_LEN)
+        out = np.empty(len(q), dtype=_capi.MATCH_DTYPE)
+        if len(q) == 0:
+            return out
+        _capi.check(_capi.lib().sift_cuda_match(self.handle, q.ctypes.data, len(q), t.ctypes.data if len(t) else None,
+                                                len(t), out.ctypes.data))
+        return out
+
     # device-resident form -------------------------------------------------
     def run_device(self, d_img: int, width: int, height: int, stride: int, with_descriptors: bool = True) -> None:
         _capi.check(_capi.lib().sift_cuda_run_device(self.handle, C.c_void_p(d_img), width, height, stride,

@@ -208,3 +208,27 @@ def test_luma_restatements(oracle_mod):
     want = [int(np.trunc((f(0.299) * f(r) + f(0.587) * f(g)) + f(0.114) * f(b))) for r, g, b, _ in px[0]]
     assert oracle_mod.luma_u8(px, 3).tolist() == [want]
     assert oracle_mod.luma_u8(px[..., :3], 1).tolist() == oracle_mod.luma_u8(px, 2).tolist()
+
+
+def test_match_oracle_against_a_plain_loop():
+    """oracle/match.py (the checker of sift_cuda_match) against a plain loop
+    over every pair, with duplicate train rows (ties go to the lower index),
+    a single train row and an empty train set."""
+    import numpy as np
+    from oracle.match import match
+    rng = np.random.default_rng(3)
+    q = rng.random((20, 128)).astype(np.float32)
+    t = rng.random((30, 128)).astype(np.float32)
+    t[7] = t[3]
+    q[0] = t[3]
+    i1, d1, i2, d2, third, _ = match(q, t)
+    for a in range(len(q)):
+        d = [float(((q[a].astype(np.float64) - t[b]) ** 2).sum()) for b in range(len(t))]
+        order = sorted(range(len(t)), key=lambda b: (d[b], b))
+        assert i1[a] == order[0] and i2[a] == order[1]
+        assert abs(d1[a] ** 2 - d[order[0]]) < 1e-9 and abs(d2[a] ** 2 - d[order[1]]) < 1e-9
+    assert i1[0] == 3 and i2[0] == 7
+    i1, d1, i2, d2, third, _ = match(q[:2], t[:1])
+    assert list(i1) == [0, 0] and list(i2) == [-1, -1] and np.all(np.isinf(d2))
+    i1, d1, i2, d2, third, _ = match(q[:2], t[:0])
+    assert list(i1) == [-1, -1] and np.all(np.isinf(d1))
