@@ -337,6 +337,19 @@ size_t sift_cuda_match_scratch_bytes(uint32_t n_query, uint32_t n_train);
 int sift_cuda_match_device(const float* d_query, uint32_t n_query, const float* d_train, uint32_t n_train,
                            SiftCudaMatch* d_out, void* d_scratch, void* stream);
 
+/* ---- drawing ---------------------------------------------------------------- */
+
+/* draw_keypoints_to_image (src/lib.rs:69-116): the grey image as RGB with,
+ * for every keypoint, a filled circle of radius 6 at (x as i32, y as i32), the
+ * orientation line from (x, y) to (x + 6 cos angle, y + 6 sin angle) and a
+ * filled circle of radius 1, in colour (r, g, b) (imageproc 0.25.0
+ * draw_filled_circle_mut / draw_line_segment_mut, restated). Host buffers:
+ * gray width x height with `stride` bytes per row, rgb_out width x height x 3
+ * with out_stride >= 3 * width bytes per row. Synchronous. */
+int sift_cuda_draw_keypoints(SiftCudaEngine* engine, const uint8_t* gray, uint32_t width, uint32_t height,
+                             uint32_t stride, const SiftCudaKeypoint* kps, uint32_t n, uint8_t r, uint8_t g,
+                             uint8_t b, uint8_t* rgb_out, uint32_t out_stride);
+
 /* ---- blur without allocation ---------------------------------------------- */
 
 /* Gaussian blur of a u8 image in device memory into a caller-owned device

@@ -173,6 +173,8 @@ def lib() -> C.CDLL:
         "sift_cuda_footprint_bytes": (u64, [P(Params), i32, u32, u32]),
         "sift_cuda_replay": (C.c_int, [C.c_void_p, P(Params), P(Options), P(ReplayImage), u32, P(ReplayRequest),
                                        u32, P(ReplayResult), P(C.c_double)]),
+        "sift_cuda_draw_keypoints": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, C.c_void_p, u32, C.c_uint8,
+                                               C.c_uint8, C.c_uint8, C.c_void_p, u32]),
         "sift_cuda_match": (C.c_int, [C.c_void_p, C.c_void_p, u32, C.c_void_p, u32, C.c_void_p]),
         "sift_cuda_match_scratch_bytes": (C.c_size_t, [u32, u32]),
         "sift_cuda_match_device": (C.c_int, [C.c_void_p, u32, C.c_void_p, u32, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -199,7 +201,8 @@ def exported_symbols() -> list[str]:
         "sift_cuda_profile_read", "sift_cuda_server_options_default", "sift_cuda_server_create",
         "sift_cuda_server_destroy", "sift_cuda_server_submit", "sift_cuda_server_poll", "sift_cuda_server_release",
         "sift_cuda_server_warm", "sift_cuda_server_stats", "sift_cuda_server_tuning", "sift_cuda_footprint_bytes",
-        "sift_cuda_replay", "sift_cuda_gaussian_blur_u8_noalloc", "sift_cuda_match", "sift_cuda_match_scratch_bytes",
+        "sift_cuda_replay", "sift_cuda_gaussian_blur_u8_noalloc", "sift_cuda_draw_keypoints", "sift_cuda_match",
+        "sift_cuda_match_scratch_bytes",
         "sift_cuda_match_device", "sift_synth_image",
         "sift_synth_density",
     ]

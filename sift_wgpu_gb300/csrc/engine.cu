@@ -256,6 +256,36 @@ int sift_cuda_match(SiftCudaEngine* engine, const float* query, uint32_t n_query
     return 0;
 }
 
+int sift_cuda_draw_keypoints(SiftCudaEngine* engine, const uint8_t* gray, uint32_t width, uint32_t height,
+                             uint32_t stride, const SiftCudaKeypoint* kps, uint32_t n, uint8_t r, uint8_t g,
+                             uint8_t b, uint8_t* rgb_out, uint32_t out_stride) {
+    sift::g_last_error.clear();
+    if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
+    if (width == 0 || height == 0) return 0;
+    if (!gray || !rgb_out || (n && !kps)) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "a drawing buffer is NULL");
+    if (stride < width || out_stride < 3ull * width || width > (1u << 30) / 3)
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "stride below the row size");
+    Engine& e = engine->e;
+    if (int rc = e.set_device()) return rc;
+    const size_t pitch = ((size_t)width * 3 + 127) & ~(size_t)127;
+    if (e.d_dg.ensure((size_t)width * height) != cudaSuccess || e.d_drgb.ensure(pitch * height) != cudaSuccess ||
+        e.d_dk.ensure(std::max<size_t>((size_t)n * sizeof(SiftCudaKeypoint), 16)) != cudaSuccess)
+        return sift::cuda_fail(cudaGetLastError(), "cudaMalloc(draw)");
+    cudaStream_t st = e.st;
+    if (cudaMemcpy2DAsync(e.d_dg.p, width, gray, stride, width, height, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        (n && cudaMemcpyAsync(e.d_dk.p, kps, (size_t)n * sizeof(SiftCudaKeypoint), cudaMemcpyHostToDevice, st) !=
+                  cudaSuccess))
+        return sift::cuda_fail(cudaGetLastError(), "H2D draw");
+    if (sift::launch_draw_keypoints(e.d_dg.as<uint8_t>(), (int)width, e.d_dk.as<sift::Keypoint>(), n,
+                                    e.d_drgb.as<uint8_t>(), (int)pitch, (int)width, (int)height, r, g, b, st))
+        return sift::cuda_fail(cudaGetLastError(), "draw");
+    if (cudaMemcpy2DAsync(rgb_out, out_stride, e.d_drgb.p, pitch, (size_t)width * 3, height, cudaMemcpyDeviceToHost,
+                          st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return sift::cuda_fail(cudaGetLastError(), "D2H draw");
+    return 0;
+}
+
 int sift_cuda_synchronize(SiftCudaEngine* engine) {
     if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
     cudaError_t e = cudaStreamSynchronize(engine->e.st);

@@ -57,6 +57,8 @@ int lanczos_fused_tile();
 int pixel_channels(int format);
 int launch_export(const Counters* ctr, const Keypoint* kps, Counters* hctr, Keypoint* hkps, uint32_t cap,
                   cudaStream_t st);
+int launch_draw_keypoints(const uint8_t* d_gray, int stride, const Keypoint* d_kps, uint32_t n, uint8_t* d_rgb,
+                          int pitch, int W, int H, uint8_t r, uint8_t g, uint8_t b, cudaStream_t st);
 size_t match_scratch_bytes(uint32_t nq, uint32_t nt);
 int launch_match(const float* d_q, uint32_t nq, const float* d_t, uint32_t nt, SiftCudaMatch* d_out, void* scratch,
                  cudaStream_t st);
@@ -198,6 +200,7 @@ struct Engine {
 
     DevMem d_px;  // colour input before its luma conversion
     DevMem d_mq, d_mt, d_mo, d_ms;  // descriptor matching: query, train, result, scratch
+    DevMem d_dg, d_dk, d_drgb;       // drawing: grey input, keypoints, RGB output
     DevMem d_img, d_G, d_D, d_U, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
     DevMem d_words, d_cand_off, d_keep, d_scan;
     DevMem d_cands, d_refined_at, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;

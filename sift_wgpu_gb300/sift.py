@@ -95,6 +95,15 @@ def _as_gray(img) -> np.ndarray:
     return a
 
 
+def _keypoint_array(keypoints) -> np.ndarray:
+    if isinstance(keypoints, np.ndarray) and keypoints.dtype == KEYPOINT_DTYPE:
+        return np.ascontiguousarray(keypoints)
+    a = np.zeros(len(keypoints), dtype=KEYPOINT_DTYPE)
+    for i, k in enumerate(keypoints):
+        a[i] = (k.x, k.y, k.size, k.angle, k.response, k.octave, k.layer)
+    return a
+
+
 class Engine:
     """One libsiftcuda engine: a CUDA stream plus resident device arenas."""
 
@@ -214,6 +223,25 @@ class Engine:
         dbuf = (C.c_char * (n * DESC_LEN * 4)).from_address(C.cast(res.desc, C.c_void_p).value)
         return (np.frombuffer(kbuf, dtype=KEYPOINT_DTYPE, count=n),
                 np.frombuffer(dbuf, dtype=np.float32, count=n * DESC_LEN).reshape(n, DESC_LEN))
+
+    # drawing -----------------------------------------------------------------
+    def draw_keypoints(self, img, keypoints, color=(255, 0, 0)) -> np.ndarray:
+        """draw_keypoints_to_image (src/lib.rs:69-116) on the GPU: an
+        (h, w, 3) uint8 RGB image. keypoints: a KEYPOINT_DTYPE array or a
+        sequence of KeyPoint."""
+        g = _as_gray(img)
+        if g.strides[1] != 1:
+            g = np.ascontiguousarray(g)
+        h, w = g.shape
+        kps = _keypoint_array(keypoints)
+        out = np.empty((h, w, 3), dtype=np.uint8)
+        if h == 0 or w == 0:
+            return out
+        r, gr, b = (int(c) for c in color)
+        _capi.check(_capi.lib().sift_cuda_draw_keypoints(
+            self.handle, g.ctypes.data, w, h, g.strides[0], kps.ctypes.data if len(kps) else None, len(kps), r, gr, b,
+            out.ctypes.data, 3 * w))
+        return out
 
     # descriptor matching ----------------------------------------------------
     def match(self, query, train) -> np.ndarray:
@@ -360,3 +388,11 @@ class Sift:
                 return keypoints_from_array(self._engine().detect(img))
         except SiftCudaError as e:
             raise SiftError(f"CUDA detection failed: {e}") from e
+
+
+def draw_keypoints_to_image(img, keypoints, color=(255, 0, 0)) -> np.ndarray:
+    """draw_keypoints_to_image (src/lib.rs:69-116): the image as RGB with each
+    keypoint's circle, orientation line and centre dot in `color`, drawn on
+    the GPU by the default engine."""
+    with Sift._lock:
+        return Sift.default()._engine().draw_keypoints(img, keypoints, color)

@@ -232,3 +232,24 @@ def test_match_oracle_against_a_plain_loop():
     assert list(i1) == [0, 0] and list(i2) == [-1, -1] and np.all(np.isinf(d2))
     i1, d1, i2, d2, third, _ = match(q[:2], t[:0])
     assert list(i1) == [-1, -1] and np.all(np.isinf(d1))
+
+
+def test_draw_oracle_shapes():
+    """oracle/draw.py (the checker of sift_cuda_draw_keypoints): one keypoint
+    gives the midpoint-circle disc of radius 6 (symmetric, 13 rows and columns
+    wide), its orientation line and the centre dot, clipped at the border."""
+    import numpy as np
+    from oracle.draw import draw_keypoints_to_image
+    from sift_wgpu_gb300._capi import KEYPOINT_DTYPE
+    kp = np.zeros(1, KEYPOINT_DTYPE)
+    kp["x"], kp["y"], kp["angle"] = 20.7, 20.2, 0.0
+    img = draw_keypoints_to_image(np.zeros((41, 41), np.uint8), kp, (255, 0, 0))
+    red = img[:, :, 0] == 255
+    assert np.array_equal(red, red[::-1, :]) and np.array_equal(red, red[:, ::-1])
+    ys, xs = np.nonzero(red)
+    assert (ys.min(), ys.max(), xs.min(), xs.max()) == (14, 26, 14, 26)
+    assert red[20, 14:27].all() and not red[20, 27]
+    assert np.all(img[:, :, 1][red] == 0) and np.all(img[~red] == 0)
+    kp["x"], kp["y"] = 1.5, 1.5
+    img = draw_keypoints_to_image(np.full((10, 10), 7, np.uint8), kp, (0, 255, 0))
+    assert (img[:, :, 1] == 255).sum() > 0 and img[9, 9, 1] == 7
