@@ -352,7 +352,7 @@ def run_match(args, world, rank, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "match: 1080p frame seed 1 (train) vs the same scene shifted by (5, 3) px (queries)",
                        "queries": nq, "train": nt, "ratio_test_0.8_matches": good},
-            "tflops_f32": 2.0 * pairs * 128 / (ms / 1e3) / 1e12,
+            "tflops_dot": 2.0 * pairs * 128 / (ms / 1e3) / 1e12,
             "e2e": {"value": pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": (nq + nt) * 512,
                     "d2h_bytes_per_step": nq * 16},
         }), flush=True)
