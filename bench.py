@@ -61,29 +61,17 @@ FLUSH_BYTES = 256 << 20
 
 
 def pyramid_bytes(w: int, h: int, octaves: int, S: int, b: int) -> int:
-    """Algorithmic bytes of pyramid + DoG: the u8 input read once, every
-    octave base read once, S+3 Gaussian and S+2 DoG levels written once, b
-    bytes per stored value."""
+    """Algorithmic bytes of the pyramid stage as stored here: the u8 input
+    read once, every octave base read once, S+3 Gaussian levels written once
+    at b bytes per value (4 f32, 2 f16) plus their u8 planes (1 byte). No DoG
+    plane is written: extrema and refinement form DoG from the u8 planes."""
     total = w * h  # u8 input
     ow, oh = w, h
     for o in range(octaves):
         n = ow * oh
         if o > 0:
             total += n * b
-        total += n * ((S + 3) + (S + 2)) * b
-        ow, oh = ow // 2, oh // 2
-    return total
-
-
-def pyramid_bytes_f16(w: int, h: int, octaves: int, S: int) -> int:
-    """f16 storage: Gaussian levels in 2 bytes, no stored DoG."""
-    total = w * h
-    ow, oh = w, h
-    for o in range(octaves):
-        n = ow * oh
-        if o > 0:
-            total += n * 2
-        total += n * (S + 3) * 2
+        total += n * (S + 3) * (b + 1)
         ow, oh = ow // 2, oh // 2
     return total
 
@@ -519,7 +507,7 @@ def run_cuda(args, world, rank, local):
     dominant = max(per_run, key=per_run.get)
     peak, peak_kind = measured_peaks()
     octs, S = sargs[1], sargs[2]
-    b_pyr = pyramid_bytes(w, h, octs, S, 4) if args.storage == "f32" else pyramid_bytes_f16(w, h, octs, S)
+    b_pyr = pyramid_bytes(w, h, octs, S, 4 if args.storage == "f32" else 2)
     pyr_gbs = b_pyr / (per_run["pyramid_dog"] / 1e3) / 1e9
     roof_pyr = {"stage": "pyramid_dog", "bound": "hbm", "achieved": pyr_gbs, "peak": peak, "unit": "GB/s",
                 "frac": pyr_gbs / peak, "traffic": traffic_from_profiles(args.workload, "pyramid_dog"),

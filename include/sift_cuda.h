@@ -76,11 +76,12 @@ typedef struct {
 
 /* Pyramid storage of the Gaussian levels in device memory. Levels of the
  * reference-compatible pyramid hold u8 integers, so both modes are exact; F16
- * halves the Gaussian bytes and recomputes DoG in f32 from the stored
- * Gaussians instead of storing it. */
+ * halves the Gaussian bytes. In both modes each level also has a u8 plane,
+ * from which the detection forms DoG in f32 where it reads it (no DoG plane
+ * is stored). */
 typedef enum {
-    SIFT_CUDA_STORAGE_F32 = 0, /* Gaussian + DoG levels stored as f32 */
-    SIFT_CUDA_STORAGE_F16 = 1  /* Gaussian levels stored as f16, DoG recomputed */
+    SIFT_CUDA_STORAGE_F32 = 0, /* Gaussian levels stored as f32 (v / 255) */
+    SIFT_CUDA_STORAGE_F16 = 1  /* Gaussian levels stored as f16 (v) */
 } SiftCudaStorage;
 
 typedef struct {
@@ -196,7 +197,8 @@ void* sift_cuda_stream(SiftCudaEngine* engine);
  *  SIFT_CUDA_STAGE_REFINED:    refine_and_filter_extrema output
  *                              (src/sift.rs:299-474), SiftCudaKeypoint each.
  *  SIFT_CUDA_STAGE_DOG:        all DoG levels as f32, octave-major, level,
- *                              row-major (F32 storage only).
+ *                              row-major, formed from the level planes as
+ *                              the detection forms them.
  *  SIFT_CUDA_STAGE_KEYPOINTS:  the final keypoints, SiftCudaKeypoint each.
  *  SIFT_CUDA_STAGE_DESCRIPTORS: the final descriptors, 128 floats each
  *                              (count = keypoints x 128).

@@ -317,10 +317,41 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
     if (cudaMemcpy(&c, e.d_ctr.p, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess)
         return sift::cuda_fail(cudaGetLastError(), "D2H counters");
     const sift::PyramidDev& g = e.pyr;
-    if (stage == SIFT_CUDA_STAGE_PYRAMID || stage == SIFT_CUDA_STAGE_DOG) {
-        const bool dog = stage == SIFT_CUDA_STAGE_DOG;
-        if (dog && e.f16()) return sift::fail(SIFT_CUDA_ERR_UNSUPPORTED, "no stored DoG in f16 storage");
-        const int L = dog ? g.S + 2 : g.S + 3;
+    if (stage == SIFT_CUDA_STAGE_DOG) {
+        // No DoG plane is stored: extrema and refinement form DoG(l) =
+        // G_{l+1}/255 - G_l/255 (src/sift.rs:92-124) from the u8 level planes
+        // through the v / 255 table, and so does this read-back, with the same
+        // IEEE f32 division and subtraction.
+        const int L = g.S + 2;
+        uint64_t total = 0;
+        for (int o = 0; o < g.num_octaves; ++o) total += (uint64_t)g.oct[o].W * g.oct[o].H * L;
+        *count = total;
+        if (!out) return 0;
+        float lut[256];
+        for (int v = 0; v < 256; ++v) lut[v] = (float)v / 255.0f;
+        uint64_t pos = 0;
+        std::vector<uint8_t> lo, hi;
+        for (int o = 0; o < g.num_octaves; ++o) {
+            const sift::OctaveDev& od = g.oct[o];
+            if (od.W == 0 || od.H == 0) continue;
+            const size_t npx = (size_t)od.W * od.H;
+            auto plane = [&](int l, std::vector<uint8_t>& dst) {
+                dst.resize(npx);
+                return cudaMemcpy2D(dst.data(), (size_t)od.W, e.d_U.as<uint8_t>() + od.u_off + (long long)l * od.plane,
+                                    (size_t)od.pitch, (size_t)od.W, od.H, cudaMemcpyDeviceToHost);
+            };
+            if (plane(0, lo) != cudaSuccess) return sift::cuda_fail(cudaGetLastError(), "D2H stage");
+            for (int l = 0; l < L; ++l) {
+                if (plane(l + 1, hi) != cudaSuccess) return sift::cuda_fail(cudaGetLastError(), "D2H stage");
+                for (size_t q = 0; q < npx && pos < capacity; ++q, ++pos)
+                    ((float*)out)[pos] = lut[hi[q]] - lut[lo[q]];
+                lo.swap(hi);
+            }
+        }
+        return 0;
+    }
+    if (stage == SIFT_CUDA_STAGE_PYRAMID) {
+        const int L = g.S + 3;
         uint64_t total = 0;
         for (int o = 0; o < g.num_octaves; ++o) total += (uint64_t)g.oct[o].W * g.oct[o].H * L;
         *count = total;
@@ -331,18 +362,15 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
             const sift::OctaveDev& od = g.oct[o];
             if (od.W == 0 || od.H == 0) continue;
             for (int l = 0; l < L; ++l) {
-                const size_t es = dog ? 4 : e.g_elem_size();
-                const char* src = dog ? (const char*)e.d_D.p + (size_t)(od.d_off + (long long)l * od.plane) * 4
-                                      : (const char*)e.d_G.p + (size_t)(od.g_off + (long long)l * od.plane) * es;
+                const size_t es = e.g_elem_size();
+                const char* src = (const char*)e.d_G.p + (size_t)(od.g_off + (long long)l * od.plane) * es;
                 buf.resize((size_t)od.W * od.H * es);
                 if (cudaMemcpy2D(buf.data(), (size_t)od.W * es, src, (size_t)od.pitch * es, (size_t)od.W * es, od.H,
                                  cudaMemcpyDeviceToHost) != cudaSuccess)
                     return sift::cuda_fail(cudaGetLastError(), "D2H stage");
                 const size_t npx = (size_t)od.W * od.H;
                 for (size_t q = 0; q < npx && pos < capacity; ++q, ++pos) {
-                    if (dog) {
-                        ((float*)out)[pos] = ((const float*)buf.data())[q];
-                    } else if (es == 4) {
+                    if (es == 4) {
                         ((uint8_t*)out)[pos] = (uint8_t)std::lrint(((const float*)buf.data())[q] * 255.0f);
                     } else {
                         ((uint8_t*)out)[pos] = (uint8_t)__half2float(((const __half*)buf.data())[q]);

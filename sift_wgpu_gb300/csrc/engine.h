@@ -39,11 +39,10 @@ namespace sift {
 
 // launchers (pyramid.cu, detect.cu, describe.cu)
 template <typename TG>
-int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, float* dog, int pitch,
-                      int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
+int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
                       int* launches, int fused_max_radius);
 template <typename TG>
-int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, float* dog, int pitch, int W,
+int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, cudaStream_t st);
 template <typename TG>
 int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, uint8_t* out_u8, int pitch, int W, int H,
@@ -158,7 +157,7 @@ struct Engine {
     bool have_geom = false;
     PyramidDev pyr{};
     long long n_words = 0;
-    size_t g_elems = 0, d_elems = 0, u_bytes = 0, tmp_bytes = 0, ltmp_elems = 0;
+    size_t g_elems = 0, u_bytes = 0, tmp_bytes = 0, ltmp_elems = 0;
     size_t lut_off = 0;  // v / 255 table (256 floats) in d_wts
     LevelBlur base{};
     std::vector<std::vector<LevelBlur>> lv;  // [o][s-1]
@@ -201,7 +200,7 @@ struct Engine {
     DevMem d_px;  // colour input before its luma conversion
     DevMem d_mq, d_mt, d_mo, d_ms;  // descriptor matching: query, train, result, scratch
     DevMem d_dg, d_dk, d_drgb;       // drawing: grey input, keypoints, RGB output
-    DevMem d_img, d_G, d_D, d_U, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
+    DevMem d_img, d_G, d_U, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
     DevMem d_words, d_cand_off, d_keep, d_scan;
     DevMem d_cands, d_refined_at, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
     HostPinned h_ctr, h_kps, h_desc;
@@ -333,7 +332,7 @@ struct Engine {
     // Device bytes held by the engine's arenas and lists.
     size_t device_bytes() const {
         size_t t = 0;
-        for (const DevMem* m : {&d_img, &d_G, &d_D, &d_U, &d_tmp, &d_tmpo, &d_ltmp, &d_wts, &d_ltab, &d_lw, &d_words,
+        for (const DevMem* m : {&d_img, &d_G, &d_U, &d_tmp, &d_tmpo, &d_ltmp, &d_wts, &d_ltab, &d_lw, &d_words,
                                 &d_cand_off, &d_keep, &d_scan, &d_cands, &d_refined_at,
                                 &d_ori_angle, &d_ori_count, &d_ori_off, &d_oriented, &d_desc, &d_ctr})
             t += m->bytes;
@@ -382,7 +381,7 @@ struct Engine {
         g.num_octaves = O;
         g.S = S;
         g.levels = S + 3;
-        size_t goff = 0, doff = 0, uoff = 0, wbase = 0, tmpb = 0, lt = 0, tmpo = 0;
+        size_t goff = 0, uoff = 0, wbase = 0, tmpb = 0, lt = 0, tmpo = 0;
         std::vector<size_t> tbo(O, 0);
         uint32_t ow = w, oh = h;
         for (int o = 0; o < O; ++o) {
@@ -393,12 +392,10 @@ struct Engine {
             od.nw = (int)((ow + 31) / 32);
             od.plane = (long long)od.pitch * oh;
             od.g_off = (long long)goff;
-            od.d_off = (long long)doff;
             od.word_base = (long long)wbase;
             od.u_off = (long long)uoff;
             goff += (size_t)od.plane * (S + 3);
             uoff += (size_t)od.plane * (S + 3);
-            doff += f16() ? 0 : (size_t)od.plane * (S + 2);
             wbase += (size_t)S * oh * od.nw;
             tmpb = std::max(tmpb, (size_t)od.pitch * oh);
             tbo[o] = tmpo;
@@ -471,7 +468,6 @@ struct Engine {
         drop_graph();
         n_words = (long long)wbase;
         CK(d_G.ensure(goff * g_elem_size()), "cudaMalloc(G)");
-        if (!f16()) CK(d_D.ensure(doff * sizeof(float)), "cudaMalloc(DoG)");
         CK(d_U.ensure(uoff + 64), "cudaMalloc(u8 levels)");
         CK(d_tmp.ensure(std::max<size_t>(tmpb, 16)), "cudaMalloc(tmp)");
         CK(d_tmpo.ensure(std::max<size_t>(tmpo, 16)), "cudaMalloc(tmp per octave)");
@@ -492,7 +488,6 @@ struct Engine {
         CK(cudaStreamSynchronize(st), "table upload");
         pyr = g;
         g_elems = goff;
-        d_elems = doff;
         u_bytes = uoff;
         lut_off = lutw;
         tmp_bytes = tmpb;
@@ -556,7 +551,6 @@ struct Engine {
     int enqueue_t(const uint8_t* img, long long stride, bool with_desc, bool dag, bool exp) {
         const int O = pyr.num_octaves, S = pyr.S;
         TG* G = d_G.as<TG>();
-        float* D = f16() ? nullptr : d_D.as<float>();
         const float* wts = d_wts.as<float>();
         const float* lut = wts + lut_off;
         uint8_t* U = d_U.as<uint8_t>();
@@ -580,14 +574,13 @@ struct Engine {
             TG* out = G + od.g_off + (long long)s * od.plane;
             const uint8_t* prev_u8 = U + od.u_off + (long long)(s - 1) * od.plane;
             uint8_t* out_u8 = U + od.u_off + (long long)s * od.plane;
-            float* dog = D ? D + od.d_off + (long long)(s - 1) * od.plane : nullptr;
             if (b.sigma <= 0.0f) {
-                if (ok(launch_copy_level<TG>(prev, prev_u8, out, out_u8, dog, od.pitch, od.W, od.H, q)))
+                if (ok(launch_copy_level<TG>(prev, prev_u8, out, out_u8, od.pitch, od.W, od.H, q)))
                     return cuda_fail(cudaGetLastError(), "copy level");
                 return 0;
             }
             int nl = 0;
-            if (launch_blur_level<TG>(prev_u8, od.pitch, tmp, out, out_u8, dog, od.pitch, od.W, od.H, b.radius,
+            if (launch_blur_level<TG>(prev_u8, od.pitch, tmp, out, out_u8, od.pitch, od.W, od.H, b.radius,
                                       wts + b.woff, lut, round_mode, q, &nl, tune.fused_max_radius))
                 return cuda_fail(cudaGetLastError(), "blur level");
             launches += nl;
@@ -677,7 +670,7 @@ struct Engine {
             // base image (src/sift.rs:1204-1214)
             if (base.sigma > 0.0f) {
                 int nl = 0;
-                if (launch_blur_level<TG>(img, (int)stride, d_tmp.as<uint8_t>(), G + o0.g_off, U + o0.u_off, nullptr,
+                if (launch_blur_level<TG>(img, (int)stride, d_tmp.as<uint8_t>(), G + o0.g_off, U + o0.u_off,
                                           o0.pitch, o0.W, o0.H, base.radius, wts + base.woff, lut, round_mode, st,
                                           &nl, tune.fused_max_radius))
                     return cuda_fail(cudaGetLastError(), "blur (base)");

@@ -152,8 +152,9 @@ constexpr int kColThreads = 256;           // 8 column groups of 4 x 32 row grou
 // clamp-to-edge rows. Each thread owns 4 columns x 2 rows and slides a
 // two-row float4 window down the taps, in unrolled groups of 8; the zero taps
 // at the end add +0 to a non-negative sum, which leaves it unchanged. Writes
-// level s (TG and u8) and, when dog != nullptr, DoG(s-1) = G_s/255 -
-// G_{s-1}/255 (src/sift.rs:92-124), as vector stores.
+// level s (TG and u8) as vector stores. No DoG plane is stored: the detection
+// stages form DoG(s-1) = G_s/255 - G_{s-1}/255 (src/sift.rs:92-124) from the
+// u8 planes through the v / 255 table where they read it.
 __host__ __device__ constexpr int taps8(int r) { return ((2 * r + 1) + 7) & ~7; }
 
 template <typename TG>
@@ -161,9 +162,8 @@ __device__ __forceinline__ void store_level4(TG* p, const int v[4], const float*
 
 template <typename TG>
 __global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __restrict__ tmp, int tmp_pitch,
-                                                          const uint8_t* __restrict__ prev_u8,
                                                           TG* __restrict__ out, uint8_t* __restrict__ out_u8,
-                                                          float* __restrict__ dog, int pitch, int W, int H, int r,
+                                                          int pitch, int W, int H, int r,
                                                           const float* __restrict__ wts,
                                                           const float* __restrict__ lut255, int round_mode) {
     extern __shared__ __align__(16) float sm[];
@@ -237,17 +237,10 @@ __global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __rest
             store_level4(out + o, v, lut);
             *reinterpret_cast<unsigned*>(out_u8 + o) =
                 (unsigned)v[0] | ((unsigned)v[1] << 8) | ((unsigned)v[2] << 16) | ((unsigned)v[3] << 24);
-            if (dog) {
-                const unsigned pw = *reinterpret_cast<const unsigned*>(prev_u8 + o);
-                *reinterpret_cast<float4*>(dog + o) =
-                    make_float4(__fsub_rn(lut[v[0]], lut[pw & 0xffu]), __fsub_rn(lut[v[1]], lut[(pw >> 8) & 0xffu]),
-                                __fsub_rn(lut[v[2]], lut[(pw >> 16) & 0xffu]), __fsub_rn(lut[v[3]], lut[pw >> 24]));
-            }
         } else {
             for (int c = 0; c < 4 && xc + c < W; ++c) {
                 store_level(out + o + c, v[c], lut[v[c]]);
                 out_u8[o + c] = (uint8_t)v[c];
-                if (dog) dog[o + c] = __fsub_rn(lut[v[c]], lut[prev_u8[o + c]]);
             }
         }
     }
@@ -322,7 +315,7 @@ __device__ __forceinline__ void store_level4<__half>(__half* p, const int v[4], 
 template <typename TG, int R>
 __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restrict__ in, int in_pitch,
                                                           TG* __restrict__ out, uint8_t* __restrict__ out_u8,
-                                                          float* __restrict__ dog, int pitch, int W, int H,
+                                                          int pitch, int W, int H,
                                                           const float* __restrict__ wts,
                                                           const float* __restrict__ lut255, int round_mode) {
     static_assert(R >= 1 && R <= kFMaxR, "fused radius");
@@ -445,38 +438,30 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
         const int v[4] = {clamp_u8_any(acc[j].x, round_mode), clamp_u8_any(acc[j].y, round_mode),
                           clamp_u8_any(acc[j].z, round_mode), clamp_u8_any(acc[j].w, round_mode)};
         const long long o = (long long)y * pitch + xc;
-        // previous level at these pixels: staged row R + 4 rg + j, column 16 + sh + 4 cg
-        const float* pv = src + (size_t)(R + 4 * rg + j) * kFSW + 16 + sh + 4 * cg;
         if (full) {
             store_level4(out + o, v, lut);
             *reinterpret_cast<unsigned*>(out_u8 + o) =
                 (unsigned)v[0] | ((unsigned)v[1] << 8) | ((unsigned)v[2] << 16) | ((unsigned)v[3] << 24);
-            if (dog)
-                *reinterpret_cast<float4*>(dog + o) =
-                    make_float4(__fsub_rn(lut[v[0]], lut[int_of(pv[0])]), __fsub_rn(lut[v[1]], lut[int_of(pv[1])]),
-                                __fsub_rn(lut[v[2]], lut[int_of(pv[2])]), __fsub_rn(lut[v[3]], lut[int_of(pv[3])]));
         } else {
             for (int c = 0; c < 4 && xc + c < W; ++c) {
                 store_level(out + o + c, v[c], lut[v[c]]);
                 out_u8[o + c] = (uint8_t)v[c];
-                if (dog) dog[o + c] = __fsub_rn(lut[v[c]], lut[int_of(pv[c])]);
             }
         }
     }
 }
 
 // A level whose blur increment is below 1e-4 is a copy of the previous one
-// (src/sift.rs:152-154); its DoG is then exactly zero.
+// (src/sift.rs:152-154).
 template <typename TG>
 __global__ void k_copy_level(const TG* __restrict__ prev, const uint8_t* __restrict__ prev_u8, TG* __restrict__ out,
-                             uint8_t* __restrict__ out_u8, float* __restrict__ dog, int pitch, int W, int H) {
+                             uint8_t* __restrict__ out_u8, int pitch, int W, int H) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x >= W) return;
     long long o = (long long)y * pitch + x;
     out[o] = prev[o];
     out_u8[o] = prev_u8[o];
-    if (dog) dog[o] = 0.0f;
 }
 
 // Base level without a blur (sigma <= assumed_blur, src/sift.rs:1204-1214).
@@ -660,12 +645,11 @@ static int set_smem(const void* k, size_t smem) {
 // fused_max_radius (the horizontal pass recomputes a 2r-row halo per 64-row
 // tile, which stops paying beyond r = 8), else the two separable passes.
 template <typename TG>
-int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, float* dog, int pitch,
-                      int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
+int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
                       int* launches, int fused_max_radius) {
     const size_t smem = blur_fused_smem(r);
     if (r <= kFMaxR && r <= fused_max_radius) {
-        void (*kern)(const uint8_t*, int, TG*, uint8_t*, float*, int, int, int, const float*, const float*, int);
+        void (*kern)(const uint8_t*, int, TG*, uint8_t*, int, int, int, const float*, const float*, int);
         switch (r) {
             case 1: kern = k_blur_level<TG, 1>; break;
             case 2: kern = k_blur_level<TG, 2>; break;
@@ -678,7 +662,7 @@ int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, ui
         }
         if (set_smem((const void*)kern, smem)) return -1;
         dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
-        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, out_u8, dog, pitch, W, H, wts, lut255, round_mode);
+        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, out_u8, pitch, W, H, wts, lut255, round_mode);
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
@@ -686,17 +670,17 @@ int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, ui
     if (set_smem((const void*)k_blur_rows, rs) || set_smem((const void*)k_blur_cols<TG>, cs)) return -1;
     k_blur_rows<<<H, kRowThreads, rs, st>>>(in, in_pitch, tmp, pitch, W, r, wts, round_mode);
     dim3 grid((W + kColTX - 1) / kColTX, (H + kColRows - 1) / kColRows);
-    k_blur_cols<TG><<<grid, kColThreads, cs, st>>>(tmp, pitch, in, out, out_u8, dog, pitch, W, H, r, wts,
+    k_blur_cols<TG><<<grid, kColThreads, cs, st>>>(tmp, pitch, out, out_u8, pitch, W, H, r, wts,
                                                             lut255, round_mode);
     *launches += 2;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 template <typename TG>
-int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, float* dog, int pitch, int W,
+int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, cudaStream_t st) {
     dim3 grid((W + 255) / 256, H);
-    k_copy_level<TG><<<grid, 256, 0, st>>>(prev, prev_u8, out, out_u8, dog, pitch, W, H);
+    k_copy_level<TG><<<grid, 256, 0, st>>>(prev, prev_u8, out, out_u8, pitch, W, H);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -733,9 +717,9 @@ int lanczos_fused_span() { return kLzSpan; }
 int lanczos_fused_tile() { return kLzT; }
 
 #define SIFT_INST(TG)                                                                                              \
-    template int launch_blur_level<TG>(const uint8_t*, int, uint8_t*, TG*, uint8_t*, float*, int, int, int, int,   \
+    template int launch_blur_level<TG>(const uint8_t*, int, uint8_t*, TG*, uint8_t*, int, int, int, int,           \
                                        const float*, const float*, int, cudaStream_t, int*, int);                  \
-    template int launch_copy_level<TG>(const TG*, const uint8_t*, TG*, uint8_t*, float*, int, int, int,            \
+    template int launch_copy_level<TG>(const TG*, const uint8_t*, TG*, uint8_t*, int, int, int,                    \
                                        cudaStream_t);                                                              \
     template int launch_u8_to_level<TG>(const uint8_t*, long long, TG*, uint8_t*, int, int, int, cudaStream_t);    \
     template int launch_lanczos<TG>(const uint8_t*, int, int, int, float*, int, TG*, uint8_t*, int, int, int,      \

@@ -52,7 +52,6 @@ struct OctaveDev {
     int W, H, pitch;          // pitch in elements (G and DoG planes)
     int nw;                   // 32-pixel words per row of the extrema mask
     long long g_off;          // element offset of level 0 in the G arena
-    long long d_off;          // element offset of DoG level 0 in the DoG arena
     long long plane;          // elements per plane (pitch * H)
     long long word_base;      // first word of this octave in the mask arena
     long long u_off;          // byte offset of level 0 in the u8 level arena

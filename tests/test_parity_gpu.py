@@ -149,8 +149,8 @@ def test_strided_input_and_determinism(sgb):
 
 
 def test_f16_storage_is_exact(sgb):
-    """u8-valued levels are exact in f16, and DoG recomputed in f32 from them
-    equals the stored f32 DoG, so the f16 pyramid gives identical output."""
+    """u8-valued levels are exact in f16 and both storage modes form DoG from
+    the same u8 planes, so the f16 pyramid gives identical output."""
     args = (1.6, 4, 3, 0.5, 0.04, 10.0)
     img = image(sgb, 1920, 1080, 1)
     k32, d32 = engine_for(sgb, args).detect_and_compute(img)
