@@ -29,9 +29,9 @@ namespace {
 
 // DoG access for one octave (src/sift.rs:208-214 get_pixel_value, clamped).
 // DoG of one octave recomputed from the u8 copies of its Gaussian levels:
-// D_l = lut[G_{l+1}] - lut[G_l] with lut[v] = v/255 in f32 — the stored f32 DoG
-// bit for bit (src/sift.rs:92-124) in either storage mode, at one byte per
-// level value instead of four (the refinement's scattered 3 x 3 x 3 reads
+// D_l = lut[G_{l+1}] - lut[G_l] with lut[v] = v/255 in f32 — the reference's
+// f32 DoG bit for bit (src/sift.rs:92-124) in either storage mode, at one byte
+// per level value instead of four (the refinement's scattered 3 x 3 x 3 reads
 // then mostly hit L2).
 struct DogFromU8 {
     const uint8_t* base;  // u8 level 0 of the octave
@@ -48,7 +48,8 @@ struct DogFromU8 {
 
 // DoG staged from the u8 copies of the Gaussian levels of one octave:
 // D_l = lut[G_{l+1}] - lut[G_l] with lut[v] = v/255 in f32, which is the
-// stored f32 DoG bit for bit (src/sift.rs:92-124) at a quarter of the bytes.
+// reference's f32 DoG bit for bit (src/sift.rs:92-124) at a quarter of the
+// bytes.
 // Stages layers 0..L-1 of the clamped window [x0, x0+TW) x [y0, y0+TH) into
 // tile[L][TH][TW]; windows inside the plane go as aligned 4-byte words, all
 // L+1 levels of a word per thread.

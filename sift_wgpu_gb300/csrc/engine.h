@@ -5,7 +5,6 @@
 //   G arena    octave-major Gaussian levels, (S+3) planes per octave, each
 //              plane pitch x H (pitch = width rounded up to 32 elements), f32
 //              or f16 (u8-valued either way)
-//   DoG arena  (S+2) f32 planes per octave (f32 storage only)
 //   U arena    (S+3) u8 planes per octave: every level as bytes, the input
 //              of the next level, of the resize and of the extrema scan
 //   tmp        one u8 plane for the horizontal blur pass (largest octave)

@@ -1,24 +1,25 @@
-// pyramid.cu — Gaussian pyramid + DoG kernels (sm_103a).
+// pyramid.cu — Gaussian pyramid kernels (sm_103a).
 //
 // Stage (a) of the hot path: generate_gaussian_pyramid and
 // generate_dog_pyramid (src/sift.rs:129-204), with the base blur of
 // detect_and_compute_cpu (src/sift.rs:1200-1214). The levels are
 // reference-compatible: each separable blur pass and the Lanczos3 resize end
 // in u8 values exactly as the reference's GrayImage levels do, so every level
-// and every DoG value is bit-identical to the CPU path. Products and sums are
-// rounded one by one (__fmul_rn/__fadd_rn) in the reference's tap order.
+// is bit-identical to the CPU path, and so is every DoG value the detection
+// forms from them. Products and sums are rounded one by one
+// (__fmul_rn/__fadd_rn) in the reference's tap order.
 //
-// Every level is written three ways: the u8 plane (1 byte/pixel, what the next
-// level, the resize and the extrema scan read), the stored level in the
-// storage type (f32 v/255 or f16 v, read by the orientation and descriptor
-// stages) and, for f32 storage, the DoG level below it. Nothing in the chain
-// re-reads a 4-byte plane.
+// Every level is written two ways: the u8 plane (1 byte/pixel, what the next
+// level, the resize and the extrema and refinement stages read; DoG is formed
+// from it there, never stored) and the stored level in the storage type (f32
+// v/255 or f16 v, read by the orientation and descriptor stages). Nothing in
+// the chain re-reads a 4-byte plane.
 //
 // Kernels
 //   k_blur_level   both separable passes of a level for r <= 8 (the first two
 //                  octaves at the default sigma): a 64 x 64 tile stages its
 //                  u8 window with 16-byte loads, the horizontal pass goes to
-//                  shared memory, the vertical pass writes level, DoG and u8.
+//                  shared memory, the vertical pass writes level and u8.
 //   k_blur_rows    horizontal pass for larger radii, one row per CTA. u8 out.
 //   k_blur_cols    vertical pass for larger radii on a 32 x 64 tile.
 //   k_lanczos_fused  the 2x Lanczos3 resize between octaves, both passes.
@@ -277,15 +278,14 @@ __device__ __forceinline__ void tap2(float& a_lo, float& a_hi, f32x2 v, f32x2 k)
 // of its 64 x 64 output tile from the previous level's u8 plane, runs the
 // horizontal pass for all 64 + 2r rows into shared memory (u8-truncated like
 // imageproc's intermediate image), then the vertical pass, and writes the
-// level, its u8 plane and the DoG below it; the previous level's value for the
-// DoG comes from the staged tile, so each scale is read once, as bytes.
+// level and its u8 plane; each scale is read once, as bytes.
 //
 // Staged row layout: shared column c holds global x = x0 - 16 - sh + c with
 // sh = r mod 4, so an interior row is the 96 bytes [x0 - 16, x0 + 80) written
 // without conditions, and the horizontal pass's first input (x0 - r, column
 // 16 + sh - r) is 16-byte aligned for its float4 window. Each vertical-pass
 // thread owns 4 columns x 4 rows: one float4 shared load per tap, two packed
-// multiplies per row and tap, and vector stores of level, u8 copy and DoG.
+// multiplies per row and tap, and vector stores of level and u8 copy.
 constexpr int kFTX = 64, kFTY = 64, kFThreads = 256;
 constexpr int kFMaxR = 8;
 constexpr int kFSW = 100;  // staged row stride (floats): sh + 96 <= 99

@@ -49,7 +49,7 @@ struct Counters {
 
 // Geometry of one octave in the device arena.
 struct OctaveDev {
-    int W, H, pitch;          // pitch in elements (G and DoG planes)
+    int W, H, pitch;          // pitch in elements (G and u8 planes)
     int nw;                   // 32-pixel words per row of the extrema mask
     long long g_off;          // element offset of level 0 in the G arena
     long long plane;          // elements per plane (pitch * H)

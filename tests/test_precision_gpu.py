@@ -1,8 +1,7 @@
 """Precision statement: both storage modes against the FP64 ideal model (GPU).
 
-F32 storage keeps Gaussian levels as f32 (v/255) with a stored f32 DoG; F16
-storage keeps them as f16 (v) and recomputes every DoG value in f32 from the
-stored levels. Both hold the reference's u8-quantised levels exactly, so their
+F32 storage keeps Gaussian levels as f32 (v/255), F16 storage as f16 (v);
+both form every DoG value in f32 from the u8 level planes. Both hold the reference's u8-quantised levels exactly, so their
 outputs are bit-identical and their errors against the FP64 model (no u8
 rounding; oracle/ideal64.py) are the reference CPU path's own. The test
 prints the statement and checks that both modes give the same numbers.
