@@ -287,6 +287,7 @@ def run_batch64(args, world, rank, local):
                        "max_inflight": args.inflight, "autotune": bool(args.autotune)},
             "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": int(px),
                     "d2h_bytes_per_step": int(nk * (28 + 512))},
+            "keypoints_per_s": value * int(nk) / 64,
             "plain_images_s": plain, "batched_over_plain": value / plain, "server_stats": stats,
         }), flush=True)
 
@@ -540,6 +541,7 @@ def run_cuda(args, world, rank, local):
                        "storage": args.storage, "parallelism": f"replicas x{world}",
                        "l2": "256 MiB flush before every step", "keypoints": int(nk)},
             "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": w * h, "d2h_bytes_per_step": d2h},
+            "keypoints_per_s": {"device": value * int(nk), "e2e": e2e_value * int(nk)},
             "roofline": roof,
             "roofline_pyramid_dog": roof_pyr,
             "stages_ms": per_run,
