@@ -49,31 +49,31 @@ constexpr int kOriBudget = 4;   // keypoints per warp
 constexpr int kDescBudget = 2;  // keypoints per CTA
 
 // A Gaussian level pixel as v/255 (get_gauss_pixel_value, src/sift.rs:218-223):
-// f32 levels store it directly, f16 levels store v and go through the table.
+// f32 levels store it directly, f16 levels store v, divided here (div255: the
+// IEEE quotient, so both storage modes give the same values).
 template <typename T>
-__device__ __forceinline__ float gnorm(const T* p, const float* lut);
+__device__ __forceinline__ float gnorm(const T* p);
 template <>
-__device__ __forceinline__ float gnorm<float>(const float* p, const float*) {
+__device__ __forceinline__ float gnorm<float>(const float* p) {
     return *p;
 }
 template <>
-__device__ __forceinline__ float gnorm<__half>(const __half* p, const float* lut) {
-    return lut[(int)__half2float(*p)];
+__device__ __forceinline__ float gnorm<__half>(const __half* p) {
+    return div255(__half2float(*p));
 }
 
 template <typename TG>
 struct GaussPlane {
     const TG* base;
     int pitch, W, H;
-    const float* lut;  // v / 255 in shared memory
     // get_gauss_pixel_value (src/sift.rs:218-223)
     __device__ __forceinline__ float px(int x, int y) const {
         x = clampi(x, 0, W - 1);
         y = clampi(y, 0, H - 1);
-        return gnorm(base + (long long)y * pitch + x, lut);
+        return gnorm(base + (long long)y * pitch + x);
     }
     // the same for coordinates already inside the level
-    __device__ __forceinline__ float px_in(int x, int y) const { return gnorm(base + y * pitch + x, lut); }
+    __device__ __forceinline__ float px_in(int x, int y) const { return gnorm(base + y * pitch + x); }
     // get_gauss_pixel_bilinear (src/sift.rs:238-266)
     __device__ __forceinline__ float bilinear(float x, float y) const {
         const float xf = floorf(x), yf = floorf(y);
@@ -91,17 +91,12 @@ struct GaussPlane {
 };
 
 template <typename TG>
-__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const PyramidDev& pyr, int o, int layer,
-                                                    const float* lut) {
+__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const PyramidDev& pyr, int o, int layer) {
     const int li = clampi(layer, 0, pyr.S + 2);
     const OctaveDev& od = pyr.oct[o];
-    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H, lut};
+    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H};
 }
 
-__device__ __forceinline__ void fill_lut(float* lut) {
-    for (int i = threadIdx.x + threadIdx.y * blockDim.x; i < 256; i += blockDim.x * blockDim.y)
-        lut[i] = __fdiv_rn((float)i, 255.0f);
-}
 
 // The exact orientation bin position of a gradient angle (src/sift.rs:652-656):
 // atan2 in (-pi, pi] to [0, 2 pi), times 36, divided by 2 pi.
@@ -190,11 +185,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, 5) k_orientation(const TG* 
                                                                    float* __restrict__ ori_angle,
                                                                    uint32_t* __restrict__ ori_count,
                                                                    int persist_from) {
-    __shared__ float lut[sizeof(TG) == 2 ? 256 : 1];
     __shared__ float hist[kWarpsPerCta][kOriBins][32];
     __shared__ float hs[kWarpsPerCta][kOriBins];
-    if constexpr (sizeof(TG) == 2) fill_lut(lut);
-    __syncthreads();
     const int lane = threadIdx.x, wid = threadIdx.y;
     const uint32_t n = min(oc->n_cand, ncap);  // candidate slots; rejected ones get 0 peaks
     const float two_pi = 2.0f * kPi;
@@ -214,7 +206,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, 5) k_orientation(const TG* 
         const int o = kp.octave;
         uint32_t cnt = 0;
         if (o >= 0 && o < pyr.num_octaves) {
-            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
+            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer);
             const float scale = __int_as_float((127 + o) << 23);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float so = __fdiv_rn(kp.size, scale);
@@ -365,8 +357,6 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                                                               float* __restrict__ desc, uint32_t cap,
                                                               float* __restrict__ hdesc, uint32_t hcap,
                                                               int persist_from) {
-    // v / 255 for f16 levels (f32 levels hold v / 255 already)
-    __shared__ float lut[sizeof(TG) == 2 ? 256 : 1];
     __shared__ float grid[kDescGridSide * kDescGridSide];
     // Neighbouring samples land in the same bins, so the lanes of a warp add
     // into kHistCopies copies of the histogram: adds to one address
@@ -378,8 +368,6 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     // integer sums make the order irrelevant.
     __shared__ unsigned int hist[kHistCopies * kHistStride];
     __shared__ float red_lo[kDescThreads / 32], red_hi[kDescThreads / 32];
-    if constexpr (sizeof(TG) == 2) fill_lut(lut);
-    __syncthreads();
     const int tid = threadIdx.x;
     const uint32_t base = oc->out_base;
     uint32_t n = oc->n_ori;
@@ -403,7 +391,7 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
         const bool valid = valid_oct && so > 0.0f;
         float inv_fix = 0.0f;
         if (valid) {
-            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
+            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float ang = kp.angle;
             const float ca = cosf(ang), sa = sinf(ang);
@@ -443,14 +431,14 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                         const int qx = t - sy * gs, qy0 = 4 * sy;
                         const int nr = min(4, gs - qy0);
                         const TG* pp = org + qy0 * g.pitch + qx;
-                        float a0 = gnorm(pp, lut), a1 = gnorm(pp + 1, lut);
+                        float a0 = gnorm(pp), a1 = gnorm(pp + 1);
                         float rp = fmaf(fdx, a1 - a0, a0);
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             if (j < nr) {
                                 pp += g.pitch;
-                                a0 = gnorm(pp, lut);
-                                a1 = gnorm(pp + 1, lut);
+                                a0 = gnorm(pp);
+                                a1 = gnorm(pp + 1);
                                 const float rn = fmaf(fdx, a1 - a0, a0);
                                 const float b = fmaf(fdy, rn - rp, rp);
                                 grid[(qy0 + j) * gs + qx] = b;
