@@ -25,7 +25,8 @@ quoted on. Prints one JSON line.
           images/s of both (all requests due at once).
 
 --workload batch64 prints the batched form (64 images of uneven sizes in
-flight at once) against the plain path; --workload serve prints the full
+flight at once, results as views of the host buffers the GPU wrote; the
+owned-copy form beside it) against the plain path; --workload serve prints the full
 serving sweep (20000 requests per offered rate, 500-8000 req/s).
 
 --impl reference times that CPU path alone (the reference crate itself cannot
@@ -260,12 +261,19 @@ def run_batch64(args, world, rank, local):
         srv.detect_batch(images, borrow=True)  # creates and captures a slot per size
         for _ in range(max(0, args.warmup - 1)):
             srv.detect_batch(images, borrow=True)
-        t = []
+        # results as views of the slots' host buffers (the GPU writes them
+        # there), and as arrays the caller owns (copied by a thread pool while
+        # the rest of the batch runs)
+        t, tc = [], []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            out = srv.detect_batch(images, borrow=True)
+            out = srv.detect_batch(images, borrow=True, copy=False)
             t.append(time.perf_counter() - t0)
         nk = sum(len(k) for k, _ in out)
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            srv.detect_batch(images, borrow=True, copy=True)
+            tc.append(time.perf_counter() - t0)
         stats = srv.stats()
     zero = np.zeros(len(images))
     idx = np.arange(len(images))
@@ -288,6 +296,7 @@ def run_batch64(args, world, rank, local):
             "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": int(px),
                     "d2h_bytes_per_step": int(nk * (28 + 512))},
             "keypoints_per_s": value * int(nk) / 64,
+            "owned_copy_images_s": len(images) / statistics.median(tc),
             "plain_images_s": plain, "batched_over_plain": value / plain, "server_stats": stats,
         }), flush=True)
 

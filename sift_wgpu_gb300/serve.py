@@ -12,6 +12,8 @@ Results are bit-identical to ``Engine.detect_and_compute`` on the same image.
 from __future__ import annotations
 
 import ctypes as C
+import os
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass
 
 import numpy as np
@@ -45,6 +47,13 @@ def footprint_bytes(sift: Sift, width: int, height: int, storage: str = "f32") -
     return int(_capi.lib().sift_cuda_footprint_bytes(C.byref(p), _STORAGE[storage], width, height))
 
 
+def _host_view(addr: int, nbytes: int) -> np.ndarray:
+    """A uint8 view of library-owned host memory (no copy, no ownership)."""
+    if not nbytes:
+        return np.empty(0, np.uint8)
+    return np.ctypeslib.as_array((C.c_uint8 * nbytes).from_address(addr))
+
+
 def _c_image(img: np.ndarray):
     img = _as_gray(img)
     if img.strides[1] != 1:
@@ -67,13 +76,20 @@ class Server:
         h = C.c_void_p()
         _capi.check(L.sift_cuda_server_create(C.byref(p), C.byref(o), C.byref(h)))
         self._h = h
+        self._storage, self._arena = storage, arena_bytes
         self._borrowed = {}  # ticket -> array kept alive while borrowed
+        self._held = []      # tickets whose results detect_batch(copy=False) returned as views
+        self._pool = None    # copy threads of detect_batch(copy=True)
 
     def close(self) -> None:
         if getattr(self, "_h", None):
+            if self._pool is not None:
+                self._pool.shutdown(wait=True)
+                self._pool = None
             _capi.lib().sift_cuda_server_destroy(self._h)
             self._h = C.c_void_p()
             self._borrowed.clear()
+            self._held.clear()
 
     def __del__(self):
         try:
@@ -90,6 +106,8 @@ class Server:
     def submit(self, img, tag: int = 0, borrow: bool = False) -> int:
         """Queues one image; returns its ticket. borrow=True skips the copy:
         the array must stay unchanged until its result is polled."""
+        if self._held:
+            self._release_held()
         img, w, h, stride = _c_image(img)
         t = C.c_uint64()
         _capi.check(_capi.lib().sift_cuda_server_submit(self._h, img.ctypes.data, w, h, stride, tag,
@@ -98,17 +116,30 @@ class Server:
             self._borrowed[t.value] = img
         return t.value
 
-    def poll(self, timeout_s: float | None = None, release: bool = True) -> Served | None:
-        """The next finished request (copied out), or None on timeout."""
+    def poll(self, timeout_s: float | None = None, release: bool | None = None,
+             copy: bool = True) -> Served | None:
+        """The next finished request, or None on timeout. copy=True copies the
+        keypoints and descriptors out and (by default) releases the request's
+        slot; copy=False returns views of the slot's host buffers, which stay
+        valid until release(ticket) (the default then is not to release)."""
+        if release is None:
+            release = copy
+        if release and not copy:
+            raise ValueError("views of a released request would dangle: pass copy=True or release=False")
         sv = _capi.Served()
         us = -1 if timeout_s is None else int(timeout_s * 1e6)
         if _capi.lib().sift_cuda_server_poll(self._h, C.byref(sv), us) != 1:
             return None
-        kps = np.empty(sv.n, dtype=KEYPOINT_DTYPE)
-        desc = np.empty((sv.n, DESC_LEN), dtype=np.float32)
-        if sv.status == 0 and sv.n:
-            C.memmove(kps.ctypes.data, sv.kps, sv.n * KEYPOINT_DTYPE.itemsize)
-            C.memmove(desc.ctypes.data, sv.desc, sv.n * DESC_LEN * 4)
+        n = sv.n if sv.status == 0 else 0
+        if copy:
+            kps = np.empty(n, dtype=KEYPOINT_DTYPE)
+            desc = np.empty((n, DESC_LEN), dtype=np.float32)
+            if n:
+                C.memmove(kps.ctypes.data, sv.kps, n * KEYPOINT_DTYPE.itemsize)
+                C.memmove(desc.ctypes.data, sv.desc, n * DESC_LEN * 4)
+        else:
+            kps = _host_view(sv.kps or 0, n * KEYPOINT_DTYPE.itemsize).view(KEYPOINT_DTYPE)
+            desc = _host_view(sv.desc or 0, n * DESC_LEN * 4).view(np.float32).reshape(n, DESC_LEN)
         out = Served(sv.ticket, sv.tag, sv.status, kps, desc, sv.submit_s, sv.start_s, sv.done_s)
         self._borrowed.pop(sv.ticket, None)
         if release:
@@ -133,18 +164,67 @@ class Server:
         tuned = _capi.lib().sift_cuda_server_tuning(self._h, width, height, k) == 1
         return tuned, {"fused_max_radius": k[0], "ori_ctas_per_sm": k[1], "desc_ctas_per_sm": k[2]}
 
-    def detect_batch(self, images, borrow: bool = False) -> list[tuple[np.ndarray, np.ndarray]]:
+    def _copy_out(self, r: Served):
+        kps, desc = r.keypoints.copy(), r.descriptors.copy()
+        self.release(r.ticket)
+        return r.tag, kps, desc
+
+    def _release_held(self) -> None:
+        held, self._held = self._held, []
+        for t in held:
+            self.release(t)
+
+    def detect_batch(self, images, borrow: bool = False, copy: bool = True) -> list[tuple[np.ndarray, np.ndarray]]:
         """The batched form: all images in flight at once; results in input
         order. borrow=True skips the copy into pinned memory (pass pinned
-        arrays for the fastest host-to-device copies)."""
+        arrays for the fastest host-to-device copies).
+
+        copy=True returns arrays the caller owns; they are copied out of the
+        slots' host buffers by a pool of threads while the GPU runs the rest
+        of the batch. copy=False returns views of those buffers (the GPU
+        writes its results there): valid until the next detect_batch, submit
+        or close on this server. Held views keep their slots busy, so a batch
+        whose slots together exceed the server's arena (where requests would
+        wait for slots that only the next call frees) is copied instead."""
+        self._release_held()
+        if not copy:
+            need = 0
+            for img in images:
+                g = _as_gray(img)
+                need += footprint_bytes(self.sift, g.shape[1], g.shape[0], self._storage)
+            copy = need > self._arena
         for i, img in enumerate(images):
             self.submit(img, tag=i, borrow=borrow)
         out = [None] * len(images)
+        if copy:
+            if self._pool is None:
+                self._pool = ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1))
+            futs = []
+            failed = None
+            for _ in range(len(images)):
+                r = self.poll(copy=False)
+                if r.status:
+                    self.release(r.ticket)
+                    failed = failed or r
+                    continue
+                futs.append(self._pool.submit(self._copy_out, r))
+            for f in futs:
+                tag, kps, desc = f.result()
+                out[tag] = (kps, desc)
+            if failed is not None:
+                raise _capi.SiftCudaError(failed.status, f"request {failed.tag} failed")
+            return out
+        failed = None
         for _ in range(len(images)):
-            r = self.poll()
+            r = self.poll(copy=False)
             if r.status:
-                raise _capi.SiftCudaError(r.status, f"request {r.tag} failed")
+                self.release(r.ticket)
+                failed = failed or r
+                continue
+            self._held.append(r.ticket)
             out[r.tag] = (r.keypoints, r.descriptors)
+        if failed is not None:
+            raise _capi.SiftCudaError(failed.status, f"request {failed.tag} failed")
         return out
 
 

@@ -64,6 +64,23 @@ def test_batch_matches_per_image(sgb, images, alone):
         assert same(res, alone[len(images) - 1 - i])
 
 
+def test_batch_views_match_per_image(sgb, images, alone):
+    """detect_batch(copy=False): views of the slots' host buffers, the same
+    values; a second batch of the same sizes reuses the released slots."""
+    with sgb.Server(max_inflight=4) as srv:
+        batch = images + images[::-1]
+        out = srv.detect_batch(batch, copy=False)
+        for i, res in enumerate(out):
+            assert not res[1].flags.owndata
+            assert same(res, alone[i if i < len(images) else len(batch) - 1 - i])
+        slots = srv.stats()["slots"]
+        out = srv.detect_batch(batch, copy=False)
+        assert same(out[0], alone[0])
+        assert srv.stats()["slots"] == slots
+        with pytest.raises(ValueError):  # views of a released request
+            srv.poll(timeout_s=0, copy=False, release=True)
+
+
 def test_small_arena_evicts_and_still_matches(sgb, images, alone):
     """A budget that holds about one 1080p slot: requests wait for memory,
     idle slots of other sizes are evicted, results unchanged."""
