@@ -145,7 +145,9 @@ class Engine:
     def __exit__(self, *exc):
         self.close()
 
-    def _call(self, fn, img: np.ndarray, with_desc: bool):
+    def _call(self, fn, img: np.ndarray, with_desc: bool, view: bool = False):
+        """Runs fn and copies its result into owned arrays. view=True: fn is
+        a view entry (results in the engine's host buffers, not freed)."""
         img = _as_gray(img)
         h, w = img.shape
         stride = img.strides[0]
@@ -165,7 +167,8 @@ class Engine:
                 if n:
                     C.memmove(desc.ctypes.data, res.desc, n * DESC_LEN * 4)
         finally:
-            _capi.lib().sift_cuda_result_free(C.byref(res))
+            if not view:
+                _capi.lib().sift_cuda_result_free(C.byref(res))
         return kps, desc
 
     def detect_and_compute(self, img) -> tuple[np.ndarray, np.ndarray]:
@@ -175,7 +178,8 @@ class Engine:
         a = np.asarray(img)
         if a.ndim == 3 and a.dtype == np.uint8 and a.shape[2] in (3, 4):
             return self.detect_and_compute_pixels(a, _capi.PIXELS_RGB8 if a.shape[2] == 3 else _capi.PIXELS_RGBA8)
-        return self._call(_capi.lib().sift_cuda_detect_and_compute, img, True)
+        # the view entry and one copy out of the buffers the GPU wrote
+        return self._call(_capi.lib().sift_cuda_detect_and_compute_view, img, True, view=True)
 
     def detect_and_compute_pixels(self, img, fmt: int) -> tuple[np.ndarray, np.ndarray]:
         """A colour image (H x W x 3 for PIXELS_RGB8, H x W x 4 for PIXELS_RGBA8
