@@ -38,7 +38,7 @@ namespace sift {
 
 // launchers (pyramid.cu, detect.cu, describe.cu)
 template <typename TG>
-int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
+int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W, int H, int r, const float* wts, const float* lut255, cudaStream_t st,
                       int* launches, int fused_max_radius);
 template <typename TG>
 int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, int pitch, int W,
@@ -149,7 +149,6 @@ struct Engine {
     SiftCudaParams p{};
     SiftCudaOptions opt{};
     cudaStream_t st = nullptr;
-    int round_mode = 0;
 
     // geometry of the current arena
     uint32_t W = 0, H = 0;
@@ -580,7 +579,7 @@ struct Engine {
             }
             int nl = 0;
             if (launch_blur_level<TG>(prev_u8, od.pitch, tmp, out, out_u8, od.pitch, od.W, od.H, b.radius,
-                                      wts + b.woff, lut, round_mode, q, &nl, tune.fused_max_radius))
+                                      wts + b.woff, lut, q, &nl, tune.fused_max_radius))
                 return cuda_fail(cudaGetLastError(), "blur level");
             launches += nl;
             return 0;
@@ -670,7 +669,7 @@ struct Engine {
             if (base.sigma > 0.0f) {
                 int nl = 0;
                 if (launch_blur_level<TG>(img, (int)stride, d_tmp.as<uint8_t>(), G + o0.g_off, U + o0.u_off,
-                                          o0.pitch, o0.W, o0.H, base.radius, wts + base.woff, lut, round_mode, st,
+                                          o0.pitch, o0.W, o0.H, base.radius, wts + base.woff, lut, st,
                                           &nl, tune.fused_max_radius))
                     return cuda_fail(cudaGetLastError(), "blur (base)");
                 launches += nl;

@@ -91,10 +91,10 @@ __global__ void __launch_bounds__(kRowThreads) k_rows_to_scratch(const uint8_t* 
             a2 = __fadd_rn(a2, __fmul_rn(b[i + 2], k));
             a3 = __fadd_rn(a3, __fmul_rn(b[i + 3], k));
         }
-        d[x0] = (uint8_t)clamp_u8(a0, 0);
-        if (x0 + 1 < W) d[x0 + 1] = (uint8_t)clamp_u8(a1, 0);
-        if (x0 + 2 < W) d[x0 + 2] = (uint8_t)clamp_u8(a2, 0);
-        if (x0 + 3 < W) d[x0 + 3] = (uint8_t)clamp_u8(a3, 0);
+        d[x0] = (uint8_t)clamp_u8(a0);
+        if (x0 + 1 < W) d[x0 + 1] = (uint8_t)clamp_u8(a1);
+        if (x0 + 2 < W) d[x0 + 2] = (uint8_t)clamp_u8(a2);
+        if (x0 + 3 < W) d[x0 + 3] = (uint8_t)clamp_u8(a3);
     }
 }
 
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_cols_from_scratch(const uint
 #pragma unroll
     for (int j = 0; j < kColRPT; ++j) {
         const int y = y0 + ly + j;
-        if (y < H) dst[(long long)y * dst_stride + x] = (uint8_t)clamp_u8(acc[j], 0);
+        if (y < H) dst[(long long)y * dst_stride + x] = (uint8_t)clamp_u8(acc[j]);
     }
 }
 

@@ -48,16 +48,15 @@ __device__ __forceinline__ void unpack16(const uint4 b, float* v) {
     const unsigned w[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-        v[4 * e + 0] = float_of_u8(w[e] & 0xffu);
-        v[4 * e + 1] = float_of_u8((w[e] >> 8) & 0xffu);
-        v[4 * e + 2] = float_of_u8((w[e] >> 16) & 0xffu);
-        v[4 * e + 3] = float_of_u8(w[e] >> 24);
+        v[4 * e + 0] = float_of_byte<0>(w[e]);
+        v[4 * e + 1] = float_of_byte<1>(w[e]);
+        v[4 * e + 2] = float_of_byte<2>(w[e]);
+        v[4 * e + 3] = float_of_byte<3>(w[e]);
     }
 }
 
-__device__ __forceinline__ int clamp_u8_any(float a, int round_mode) {
-    return round_mode ? clamp_u8(a, 1) : int_of(clamp_u8f(a));
-}
+// imageproc's f32 -> u8 clamp (truncation) as an int
+__device__ __forceinline__ int to_u8(float a) { return int_of(clamp_u8f(a)); }
 
 constexpr int kRowThreads = 128;
 
@@ -65,7 +64,7 @@ constexpr int kRowThreads = 128;
 // then the row with r clamp-to-edge pixels on each side and 8 floats of slack.
 __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __restrict__ in, int in_pitch,
                                                            uint8_t* __restrict__ out, int out_pitch, int W, int r,
-                                                           const float* __restrict__ wts, int round_mode) {
+                                                           const float* __restrict__ wts) {
     extern __shared__ __align__(16) float sm[];
     const int taps = 2 * r + 1;
     const int wpad = (taps + 3) & ~3;
@@ -84,10 +83,10 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __rest
     for (int k = threadIdx.x; k < nw4; k += blockDim.x) {
         const unsigned b = *reinterpret_cast<const unsigned*>(src + 4 * k);
         float* d = row + r + 4 * k;
-        d[0] = float_of_u8(b & 0xffu);
-        d[1] = float_of_u8((b >> 8) & 0xffu);
-        d[2] = float_of_u8((b >> 16) & 0xffu);
-        d[3] = float_of_u8(b >> 24);
+        d[0] = float_of_byte<0>(b);
+        d[1] = float_of_byte<1>(b);
+        d[2] = float_of_byte<2>(b);
+        d[3] = float_of_byte<3>(b);
     }
     // clamp-to-edge borders, the tail after the whole words and the slack
     const int hi0 = r + 4 * nw4, nb = r + (padded + 8 - hi0);
@@ -130,8 +129,7 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __rest
             a2 = __fadd_rn(a2, __fmul_rn(base[i + 2], k));
             a3 = __fadd_rn(a3, __fmul_rn(base[i + 3], k));
         }
-        const int v0 = clamp_u8_any(a0, round_mode), v1 = clamp_u8_any(a1, round_mode);
-        const int v2 = clamp_u8_any(a2, round_mode), v3 = clamp_u8_any(a3, round_mode);
+        const int v0 = to_u8(a0), v1 = to_u8(a1), v2 = to_u8(a2), v3 = to_u8(a3);
         if (x0 + 3 < W) {  // out_pitch is a multiple of 32 and x0 of 4: one aligned word
             *reinterpret_cast<unsigned*>(dst + x0) =
                 (unsigned)v0 | ((unsigned)v1 << 8) | ((unsigned)v2 << 16) | ((unsigned)v3 << 24);
@@ -166,7 +164,7 @@ __global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __rest
                                                           TG* __restrict__ out, uint8_t* __restrict__ out_u8,
                                                           int pitch, int W, int H, int r,
                                                           const float* __restrict__ wts,
-                                                          const float* __restrict__ lut255, int round_mode) {
+                                                          const float* __restrict__ lut255) {
     extern __shared__ __align__(16) float sm[];
     const int taps = 2 * r + 1;
     const int tp = taps8(r);
@@ -231,8 +229,7 @@ __global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __rest
     for (int j = 0; j < 2; ++j) {
         const int y = y0 + 2 * rg + j;
         if (y >= H) break;
-        const int v[4] = {clamp_u8_any(acc[j].x, round_mode), clamp_u8_any(acc[j].y, round_mode),
-                          clamp_u8_any(acc[j].z, round_mode), clamp_u8_any(acc[j].w, round_mode)};
+        const int v[4] = {to_u8(acc[j].x), to_u8(acc[j].y), to_u8(acc[j].z), to_u8(acc[j].w)};
         const long long o = (long long)y * pitch + xc;
         if (full) {
             store_level4(out + o, v, lut);
@@ -317,7 +314,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
                                                           TG* __restrict__ out, uint8_t* __restrict__ out_u8,
                                                           int pitch, int W, int H,
                                                           const float* __restrict__ wts,
-                                                          const float* __restrict__ lut255, int round_mode) {
+                                                          const float* __restrict__ lut255) {
     static_assert(R >= 1 && R <= kFMaxR, "fused radius");
     extern __shared__ __align__(16) float sm[];
     constexpr int taps = 2 * R + 1;
@@ -398,9 +395,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
                 a2 = __fadd_rn(a2, __fmul_rn(base[i + 2], k));
                 a3 = __fadd_rn(a3, __fmul_rn(base[i + 3], k));
             }
-            float4 o4 = round_mode ? make_float4((float)clamp_u8(a0, 1), (float)clamp_u8(a1, 1),
-                                                 (float)clamp_u8(a2, 1), (float)clamp_u8(a3, 1))
-                                   : make_float4(clamp_u8f(a0), clamp_u8f(a1), clamp_u8f(a2), clamp_u8f(a3));
+            const float4 o4 = make_float4(clamp_u8f(a0), clamp_u8f(a1), clamp_u8f(a2), clamp_u8f(a3));
             *reinterpret_cast<float4*>(hb + (size_t)yy * kFTX + xq) = o4;
         }
     }
@@ -435,8 +430,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
     for (int j = 0; j < 4; ++j) {
         const int y = y0 + 4 * rg + j;
         if (y >= H) break;
-        const int v[4] = {clamp_u8_any(acc[j].x, round_mode), clamp_u8_any(acc[j].y, round_mode),
-                          clamp_u8_any(acc[j].z, round_mode), clamp_u8_any(acc[j].w, round_mode)};
+        const int v[4] = {to_u8(acc[j].x), to_u8(acc[j].y), to_u8(acc[j].z), to_u8(acc[j].w)};
         const long long o = (long long)y * pitch + xc;
         if (full) {
             store_level4(out + o, v, lut);
@@ -645,11 +639,11 @@ static int set_smem(const void* k, size_t smem) {
 // fused_max_radius (the horizontal pass recomputes a 2r-row halo per 64-row
 // tile, which stops paying beyond r = 8), else the two separable passes.
 template <typename TG>
-int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W, int H, int r, const float* wts, const float* lut255, int round_mode, cudaStream_t st,
+int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W, int H, int r, const float* wts, const float* lut255, cudaStream_t st,
                       int* launches, int fused_max_radius) {
     const size_t smem = blur_fused_smem(r);
     if (r <= kFMaxR && r <= fused_max_radius) {
-        void (*kern)(const uint8_t*, int, TG*, uint8_t*, int, int, int, const float*, const float*, int);
+        void (*kern)(const uint8_t*, int, TG*, uint8_t*, int, int, int, const float*, const float*);
         switch (r) {
             case 1: kern = k_blur_level<TG, 1>; break;
             case 2: kern = k_blur_level<TG, 2>; break;
@@ -662,16 +656,16 @@ int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, ui
         }
         if (set_smem((const void*)kern, smem)) return -1;
         dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
-        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, out_u8, pitch, W, H, wts, lut255, round_mode);
+        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, out_u8, pitch, W, H, wts, lut255);
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
     const size_t rs = blur_rows_smem(W, r), cs = blur_cols_smem(r);
     if (set_smem((const void*)k_blur_rows, rs) || set_smem((const void*)k_blur_cols<TG>, cs)) return -1;
-    k_blur_rows<<<H, kRowThreads, rs, st>>>(in, in_pitch, tmp, pitch, W, r, wts, round_mode);
+    k_blur_rows<<<H, kRowThreads, rs, st>>>(in, in_pitch, tmp, pitch, W, r, wts);
     dim3 grid((W + kColTX - 1) / kColTX, (H + kColRows - 1) / kColRows);
     k_blur_cols<TG><<<grid, kColThreads, cs, st>>>(tmp, pitch, out, out_u8, pitch, W, H, r, wts,
-                                                            lut255, round_mode);
+                                                            lut255);
     *launches += 2;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -718,7 +712,7 @@ int lanczos_fused_tile() { return kLzT; }
 
 #define SIFT_INST(TG)                                                                                              \
     template int launch_blur_level<TG>(const uint8_t*, int, uint8_t*, TG*, uint8_t*, int, int, int, int,           \
-                                       const float*, const float*, int, cudaStream_t, int*, int);                  \
+                                       const float*, const float*, cudaStream_t, int*, int);                       \
     template int launch_copy_level<TG>(const TG*, const uint8_t*, TG*, uint8_t*, int, int, int,                    \
                                        cudaStream_t);                                                              \
     template int launch_u8_to_level<TG>(const uint8_t*, long long, TG*, uint8_t*, int, int, int, cudaStream_t);    \

@@ -95,6 +95,13 @@ __device__ __forceinline__ float rint_pos(float x) { return __fsub_rn(__fadd_rn(
 __device__ __forceinline__ int int_of(float v) { return __float_as_int(__fadd_rn(v, kMagic)) - 0x4B000000; }
 // u8 -> float without a conversion
 __device__ __forceinline__ float float_of_u8(unsigned b) { return __fsub_rn(__uint_as_float(0x4B000000u | b), kMagic); }
+// byte K of w -> float: one byte permute assembles the bits 0x4B0000bb (2^23
+// + b), one subtraction removes 2^23
+template <int K>
+__device__ __forceinline__ float float_of_byte(unsigned w) {
+    static_assert(K >= 0 && K < 4, "byte index");
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4Bu, 0x4550u | K)), kMagic);
+}
 // round half away from zero (f32::round) to int, |x| < 2^22
 __device__ __forceinline__ int round_away_i(float x) {
     const int m = floor_i(__fadd_rn(fabsf(x), 0.5f));
@@ -117,10 +124,8 @@ __device__ __forceinline__ float div255(float v) {
 __device__ __forceinline__ float clamp_u8f(float a) { return fminf(fmaxf(trunc_pos(a), 0.0f), 255.0f); }
 
 // f32 -> u8 the way imageproc's Clamp<f32> for u8 does it: truncation of
-// values strictly inside (0, 255), saturation outside. round_mode 1 rounds
-// half away from zero first (the alternative rule, selectable for study).
-__device__ __forceinline__ int clamp_u8(float a, int round_mode) {
-    if (round_mode) a = roundf(a);
+// values strictly inside (0, 255), saturation outside.
+__device__ __forceinline__ int clamp_u8(float a) {
     if (a < 255.0f) {
         if (a > 0.0f) return (int)a;
         return 0;
