@@ -537,7 +537,9 @@ def run_cuda(args, world, rank, local):
         roof = {"stage": dominant, "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
                 "frac": gbs / peak, "traffic": traffic_from_profiles(args.workload, dominant),
                 "algorithmic_bytes": alg, "ms": per_run[dominant], "peak_kind": peak_kind,
-                "note": "gather/SFU-bound stage; its DRAM bytes are small, see stages_ms"}
+                "note": ("issue-bound gather stage (ncu: k_descriptor 86 % issue-active, k_orientation "
+                         "latency-bound, profiles/); its DRAM bytes are small, so the HBM fraction is low by "
+                         "nature; roofline_pyramid_dog is the HBM roofline of the pyramid stage")}
 
     out = None
     if rank == 0:

@@ -36,6 +36,7 @@ __device__ __forceinline__ uint32_t luma_canvas(uint32_t r, uint32_t g, uint32_t
 template <int FMT>
 __global__ void __launch_bounds__(256) k_to_luma(const uint8_t* __restrict__ px, long long stride, int W, int H,
                                                  uint8_t* __restrict__ out, long long out_pitch) {
+    chain_wait();
     const int y = blockIdx.y;
     const uint8_t* row = px + (long long)y * stride;
     uint8_t* o = out + (long long)y * out_pitch;
@@ -91,13 +92,19 @@ int launch_to_luma(int format, const uint8_t* px, long long stride, int W, int H
     dim3 grid((unsigned)std::min<long long>(((long long)W + 256 * per - 1) / (256 * per), 64), (unsigned)H);
     switch (format) {
         case SIFT_CUDA_PIXELS_RGB8:
-            k_to_luma<SIFT_CUDA_PIXELS_RGB8><<<grid, 256, 0, st>>>(px, stride, W, H, out, out_pitch);
+            if (launch_chained(k_to_luma<SIFT_CUDA_PIXELS_RGB8>, grid, 256, 0, st, px, stride, W, H, out,
+                               out_pitch) != cudaSuccess)
+                return -1;
             break;
         case SIFT_CUDA_PIXELS_RGBA8:
-            k_to_luma<SIFT_CUDA_PIXELS_RGBA8><<<grid, 256, 0, st>>>(px, stride, W, H, out, out_pitch);
+            if (launch_chained(k_to_luma<SIFT_CUDA_PIXELS_RGBA8>, grid, 256, 0, st, px, stride, W, H, out,
+                               out_pitch) != cudaSuccess)
+                return -1;
             break;
         case SIFT_CUDA_PIXELS_RGBA8_CANVAS:
-            k_to_luma<SIFT_CUDA_PIXELS_RGBA8_CANVAS><<<grid, 256, 0, st>>>(px, stride, W, H, out, out_pitch);
+            if (launch_chained(k_to_luma<SIFT_CUDA_PIXELS_RGBA8_CANVAS>, grid, 256, 0, st, px, stride, W, H, out,
+                               out_pitch) != cudaSuccess)
+                return -1;
             break;
         default: return -1;
     }

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, 5) k_orientation(const TG* 
                                                                    float* __restrict__ ori_angle,
                                                                    uint32_t* __restrict__ ori_count,
                                                                    int persist_from) {
+    chain_wait();
     __shared__ float hist[kWarpsPerCta][kOriBins][32];
     __shared__ float hs[kWarpsPerCta][kOriBins];
     const int lane = threadIdx.x, wid = threadIdx.y;
@@ -307,6 +308,7 @@ __global__ void k_orient_emit(const Keypoint* __restrict__ refined_at, uint32_t 
                               Counters* __restrict__ ctr, const float* __restrict__ ori_angle,
                               const uint32_t* __restrict__ ori_count, const uint32_t* __restrict__ ori_off,
                               Keypoint* __restrict__ oriented, uint32_t cap) {
+    chain_wait();
     OctCounters* oc = &ctr->oct[o];
     uint32_t base = 0;
     for (int q = 0; q < o; ++q) base += ctr->oct[q].n_ori;
@@ -357,6 +359,7 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                                                               float* __restrict__ desc, uint32_t cap,
                                                               float* __restrict__ hdesc, uint32_t hcap,
                                                               int persist_from) {
+    chain_wait();
     __shared__ float grid[kDescGridSide * kDescGridSide];
     // Neighbouring samples land in the same bins, so the lanes of a warp add
     // into kHistCopies copies of the histogram: adds to one address
@@ -638,15 +641,18 @@ template <typename TG>
 int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
                        uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,
                        int persist_ctas, cudaStream_t st) {
-    k_orientation<TG><<<grid, dim3(32, kWarpsPerCta), 0, st>>>(arena, pyr, refined_at, keep, ncap, oc, ori_angle,
-                                                               ori_count, std::max(grid - persist_ctas, 0));
+    if (launch_chained(k_orientation<TG>, grid, dim3(32, kWarpsPerCta), 0, st, arena, pyr, refined_at, keep, ncap, oc,
+                       ori_angle, ori_count, std::max(grid - persist_ctas, 0)) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counters* ctr, const float* ori_angle,
                        const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
                        cudaStream_t st) {
-    k_orient_emit<<<152, 256, 0, st>>>(refined_at, ncap, o, ctr, ori_angle, ori_count, ori_off, oriented, cap);
+    if (launch_chained(k_orient_emit, 152, 256, 0, st, refined_at, ncap, o, ctr, ori_angle, ori_count, ori_off,
+                       oriented, cap) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -654,8 +660,9 @@ template <typename TG>
 int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
                       uint32_t cap, float* hdesc, uint32_t hcap, int grid, int persist_ctas, cudaStream_t st) {
     if (!hdesc) hcap = 0;
-    k_descriptor<TG><<<grid, kDescThreads, 0, st>>>(arena, pyr, oriented, oc, desc, cap, hdesc, hcap,
-                                                    std::max(grid - persist_ctas, 0));
+    if (launch_chained(k_descriptor<TG>, grid, kDescThreads, 0, st, arena, pyr, oriented, oc, desc, cap, hdesc, hcap,
+                       std::max(grid - persist_ctas, 0)) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

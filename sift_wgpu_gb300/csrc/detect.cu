@@ -115,6 +115,7 @@ template <int NL>
 __global__ void __launch_bounds__(256, 4) k_extrema_mask(const uint8_t* __restrict__ u8arena,
                                                       const float* __restrict__ lut255, PyramidDev pyr, int o,
                                                       int border, uint32_t* __restrict__ words) {
+    chain_wait();
     extern __shared__ __align__(16) float tile[];  // [layers][kExSH][kExSW], then lut[256]
     const OctaveDev& od = pyr.oct[o];
     const int W = od.W, H = od.H, nw = od.nw, L = NL > 0 ? NL : pyr.S + 2;
@@ -294,6 +295,7 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ u8aren
                                               const uint32_t* __restrict__ cand_off,
                                               Keypoint* __restrict__ cands, uint32_t cap,
                                               Counters* __restrict__ ctr) {
+    chain_wait();
     const OctaveDev& od = pyr.oct[o];
     const long long nwo = (long long)pyr.S * od.H * od.nw;
     const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -334,6 +336,7 @@ __global__ void __launch_bounds__(256) k_refine(const uint8_t* __restrict__ u8ar
                                                 RefineParams rp, const Keypoint* __restrict__ cands,
                                                 Keypoint* __restrict__ refined_at, uint32_t* __restrict__ keep,
                                                 uint32_t cap, OctCounters* __restrict__ oc) {
+    chain_wait();
     __shared__ float lut[256];
     lut[threadIdx.x] = lut255[threadIdx.x];
     __syncthreads();
@@ -371,9 +374,11 @@ int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const Pyram
     const size_t smem = sizeof(float) * ((size_t)(pyr.S + 2) * kExSH * kExSW + 256);
     void (*k)(const uint8_t*, const float*, PyramidDev, int, int, uint32_t*) =
         pyr.S == 3 ? k_extrema_mask<5> : (pyr.S == 4 ? k_extrema_mask<6> : k_extrema_mask<0>);
-    if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return -1;
-    k<<<grid, 256, smem, st>>>(u8arena, lut255, pyr, o, border, words);
+    if (launch_chained(k, grid, 256, smem, st, u8arena, lut255, pyr, o, border, words) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -383,7 +388,9 @@ int launch_emit(const uint8_t* u8arena, const float* lut255, const PyramidDev& p
     const long long nwo = (long long)pyr.S * od.H * od.nw;
     if (nwo <= 0) return 0;
     unsigned grid = (unsigned)((nwo + 255) / 256);
-    k_emit<<<grid, 256, 0, st>>>(u8arena, lut255, pyr, o, words, cand_off, cands, cap, ctr);
+    if (launch_chained(k_emit, grid, 256, 0, st, u8arena, lut255, pyr, o, words, cand_off, cands, cap,
+                       ctr) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -394,7 +401,9 @@ int launch_refine(const uint8_t* u8arena, const float* lut255, const PyramidDev&
                   uint32_t cap, OctCounters* oc, cudaStream_t st) {
     RefineParams rp{sigma, contrast, edge, pyr.S, pyr.S + 2};
     const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 5);
-    k_refine<<<grid, 256, 0, st>>>(u8arena, lut255, pyr, o, rp, cands, refined_at, keep, cap, oc);
+    if (launch_chained(k_refine, grid, 256, 0, st, u8arena, lut255, pyr, o, rp, cands, refined_at, keep, cap,
+                       oc) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -38,8 +38,9 @@ namespace sift {
 
 // launchers (pyramid.cu, detect.cu, describe.cu)
 template <typename TG>
-int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W, int H, int r, const float* wts, const float* lut255, cudaStream_t st,
-                      int* launches, int fused_max_radius);
+int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W,
+                      int H, int r, const float* wts, const float* lut255, cudaStream_t st, int* launches,
+                      int fused_max_radius);
 template <typename TG>
 int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, cudaStream_t st);

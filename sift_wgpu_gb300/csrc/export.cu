@@ -15,6 +15,7 @@ namespace {
 
 __global__ void __launch_bounds__(256) k_export(const Counters* __restrict__ ctr, const Keypoint* __restrict__ kps,
                                                 Counters* hctr, Keypoint* hkps, uint32_t cap) {
+    chain_wait();
     const uint32_t n = min(ctr->n_oriented, cap);
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     constexpr uint32_t kCtrWords = sizeof(Counters) / 4;
@@ -28,7 +29,8 @@ __global__ void __launch_bounds__(256) k_export(const Counters* __restrict__ ctr
 
 int launch_export(const Counters* ctr, const Keypoint* kps, Counters* hctr, Keypoint* hkps, uint32_t cap,
                   cudaStream_t st) {
-    k_export<<<152, 256, 0, st>>>(ctr, kps, hctr, hkps, cap);
+    if (launch_chained(k_export, 152, 256, 0, st, ctr, kps, hctr, hkps, cap) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

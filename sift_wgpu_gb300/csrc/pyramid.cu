@@ -65,6 +65,7 @@ constexpr int kRowThreads = 128;
 __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __restrict__ in, int in_pitch,
                                                            uint8_t* __restrict__ out, int out_pitch, int W, int r,
                                                            const float* __restrict__ wts) {
+    chain_wait();
     extern __shared__ __align__(16) float sm[];
     const int taps = 2 * r + 1;
     const int wpad = (taps + 3) & ~3;
@@ -165,6 +166,7 @@ __global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __rest
                                                           int pitch, int W, int H, int r,
                                                           const float* __restrict__ wts,
                                                           const float* __restrict__ lut255) {
+    chain_wait();
     extern __shared__ __align__(16) float sm[];
     const int taps = 2 * r + 1;
     const int tp = taps8(r);
@@ -315,6 +317,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
                                                           int pitch, int W, int H,
                                                           const float* __restrict__ wts,
                                                           const float* __restrict__ lut255) {
+    chain_wait();
     static_assert(R >= 1 && R <= kFMaxR, "fused radius");
     extern __shared__ __align__(16) float sm[];
     constexpr int taps = 2 * R + 1;
@@ -450,6 +453,7 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
 template <typename TG>
 __global__ void k_copy_level(const TG* __restrict__ prev, const uint8_t* __restrict__ prev_u8, TG* __restrict__ out,
                              uint8_t* __restrict__ out_u8, int pitch, int W, int H) {
+    chain_wait();
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x >= W) return;
@@ -462,6 +466,7 @@ __global__ void k_copy_level(const TG* __restrict__ prev, const uint8_t* __restr
 template <typename TG>
 __global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride, TG* __restrict__ out,
                               uint8_t* __restrict__ out_u8, int pitch, int W, int H) {
+    chain_wait();
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x >= W) return;
@@ -488,6 +493,7 @@ __global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict
                                                        int dst_pitch, int nW, int nH, const int* __restrict__ vtab,
                                                        const float* __restrict__ vw, const int* __restrict__ htab,
                                                        const float* __restrict__ hw, const LanczosUniform uni) {
+    chain_wait();
     __shared__ float in[kLzSpan][kLzSpan];
     __shared__ float mid[kLzT][kLzMid];
     const int* vleft = vtab;
@@ -587,6 +593,7 @@ __global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict
 __global__ void k_lanczos_v(const uint8_t* __restrict__ src, int src_pitch, float* __restrict__ dst, int dst_pitch,
                             int W, int nH, const int* __restrict__ left, const int* __restrict__ count,
                             const int* __restrict__ woff, const float* __restrict__ w) {
+    chain_wait();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int oy = blockIdx.y;
     if (x >= W || oy >= nH) return;
@@ -604,6 +611,7 @@ __global__ void k_lanczos_h(const float* __restrict__ src, int src_pitch, TG* __
                             uint8_t* __restrict__ dst_u8, int dst_pitch, int nW, int nH, const int* __restrict__ left,
                             const int* __restrict__ count, const int* __restrict__ woff,
                             const float* __restrict__ w) {
+    chain_wait();
     const int ox = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
     if (ox >= nW || y >= nH) return;
@@ -639,8 +647,9 @@ static int set_smem(const void* k, size_t smem) {
 // fused_max_radius (the horizontal pass recomputes a 2r-row halo per 64-row
 // tile, which stops paying beyond r = 8), else the two separable passes.
 template <typename TG>
-int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W, int H, int r, const float* wts, const float* lut255, cudaStream_t st,
-                      int* launches, int fused_max_radius) {
+int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W,
+                      int H, int r, const float* wts, const float* lut255, cudaStream_t st, int* launches,
+                      int fused_max_radius) {
     const size_t smem = blur_fused_smem(r);
     if (r <= kFMaxR && r <= fused_max_radius) {
         void (*kern)(const uint8_t*, int, TG*, uint8_t*, int, int, int, const float*, const float*);
@@ -656,16 +665,20 @@ int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, ui
         }
         if (set_smem((const void*)kern, smem)) return -1;
         dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
-        kern<<<grid, kFThreads, smem, st>>>(in, in_pitch, out, out_u8, pitch, W, H, wts, lut255);
+        if (launch_chained(kern, grid, kFThreads, smem, st, in, in_pitch, out, out_u8, pitch, W, H, wts,
+                           lut255) != cudaSuccess)
+            return -1;
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
     const size_t rs = blur_rows_smem(W, r), cs = blur_cols_smem(r);
     if (set_smem((const void*)k_blur_rows, rs) || set_smem((const void*)k_blur_cols<TG>, cs)) return -1;
-    k_blur_rows<<<H, kRowThreads, rs, st>>>(in, in_pitch, tmp, pitch, W, r, wts);
+    if (launch_chained(k_blur_rows, H, kRowThreads, rs, st, in, in_pitch, tmp, pitch, W, r, wts) != cudaSuccess)
+        return -1;
     dim3 grid((W + kColTX - 1) / kColTX, (H + kColRows - 1) / kColRows);
-    k_blur_cols<TG><<<grid, kColThreads, cs, st>>>(tmp, pitch, out, out_u8, pitch, W, H, r, wts,
-                                                            lut255);
+    if (launch_chained(k_blur_cols<TG>, grid, kColThreads, cs, st, tmp, pitch, out, out_u8, pitch, W, H, r, wts,
+                       lut255) != cudaSuccess)
+        return -1;
     *launches += 2;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -674,7 +687,8 @@ template <typename TG>
 int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, cudaStream_t st) {
     dim3 grid((W + 255) / 256, H);
-    k_copy_level<TG><<<grid, 256, 0, st>>>(prev, prev_u8, out, out_u8, pitch, W, H);
+    if (launch_chained(k_copy_level<TG>, grid, 256, 0, st, prev, prev_u8, out, out_u8, pitch, W, H) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -682,7 +696,8 @@ template <typename TG>
 int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, uint8_t* out_u8, int pitch, int W, int H,
                        cudaStream_t st) {
     dim3 grid((W + 255) / 256, H);
-    k_u8_to_level<TG><<<grid, 256, 0, st>>>(img, stride, out, out_u8, pitch, W, H);
+    if (launch_chained(k_u8_to_level<TG>, grid, 256, 0, st, img, stride, out, out_u8, pitch, W, H) != cudaSuccess)
+        return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -692,16 +707,20 @@ int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, 
                    const float* hw, const LanczosUniform& uni, cudaStream_t st, bool fused, int* launches) {
     if (fused) {
         dim3 g((nW + kLzT - 1) / kLzT, (nH + kLzT - 1) / kLzT);
-        k_lanczos_fused<TG><<<g, 256, 0, st>>>(src, src_pitch, dst, dst_u8, dst_pitch, nW, nH, vtab, vw, htab, hw,
-                                               uni);
+        if (launch_chained(k_lanczos_fused<TG>, g, 256, 0, st, src, src_pitch, dst, dst_u8, dst_pitch, nW, nH, vtab,
+                           vw, htab, hw, uni) != cudaSuccess)
+            return -1;
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
     dim3 gv((W + 127) / 128, nH);
-    k_lanczos_v<<<gv, 128, 0, st>>>(src, src_pitch, tmp, tmp_pitch, W, nH, vtab, vtab + nH, vtab + 2 * nH, vw);
+    if (launch_chained(k_lanczos_v, gv, 128, 0, st, src, src_pitch, tmp, tmp_pitch, W, nH, vtab, vtab + nH,
+                       vtab + 2 * nH, vw) != cudaSuccess)
+        return -1;
     dim3 gh((nW + 127) / 128, nH);
-    k_lanczos_h<TG><<<gh, 128, 0, st>>>(tmp, tmp_pitch, dst, dst_u8, dst_pitch, nW, nH, htab, htab + nW,
-                                        htab + 2 * nW, hw);
+    if (launch_chained(k_lanczos_h<TG>, gh, 128, 0, st, tmp, tmp_pitch, dst, dst_u8, dst_pitch, nW, nH, htab,
+                       htab + nW, htab + 2 * nW, hw) != cudaSuccess)
+        return -1;
     (void)H;
     *launches += 2;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;

@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(kThreads) k_scan(const uint32_t* __restrict__ 
                                                    size_t n, const uint32_t* __restrict__ n_dev,
                                                    uint32_t* __restrict__ total_out,
                                                    unsigned long long* __restrict__ state, uint32_t* err) {
+    chain_wait();
     __shared__ uint32_t s_tile, s_excl, s_tot;
     if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(state), 1u);
     __syncthreads();
@@ -141,10 +142,11 @@ int scan_exclusive(const uint32_t* in, ScanInput mode, uint32_t* out, size_t n, 
         return 0;
     }
     const unsigned nb = (unsigned)((n + kTile - 1) / kTile);
-    if (mode == SCAN_POPC)
-        k_scan<SCAN_POPC><<<nb, kThreads, 0, st>>>(in, out, n, n_dev, total_out, state, err);
-    else
-        k_scan<SCAN_U32><<<nb, kThreads, 0, st>>>(in, out, n, n_dev, total_out, state, err);
+    const cudaError_t e =
+        mode == SCAN_POPC
+            ? launch_chained(k_scan<SCAN_POPC>, nb, kThreads, 0, st, in, out, n, n_dev, total_out, state, err)
+            : launch_chained(k_scan<SCAN_U32>, nb, kThreads, 0, st, in, out, n, n_dev, total_out, state, err);
+    if (e != cudaSuccess) return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
