@@ -58,12 +58,11 @@ double now_s() {
 uint64_t footprint_estimate(const SiftCudaParams& p, int storage, uint32_t w, uint32_t h) {
     const int O = (int)p.num_octaves, S = (int)p.num_intervals;
     const size_t es = storage == SIFT_CUDA_STORAGE_F16 ? 2 : 4;
-    uint64_t g = 0, d = 0, u = 0, tmpb = 0, tmpo = 0, lt = 0, words = 0, caps = 0;
+    uint64_t g = 0, u = 0, tmpb = 0, tmpo = 0, lt = 0, words = 0, caps = 0;
     uint32_t ow = w, oh = h;
     for (int o = 0; o < O; ++o) {
         const uint64_t pitch = align_up(std::max<uint32_t>(ow, 1), 32), plane = pitch * oh, nw = (ow + 31) / 32;
         g += plane * (S + 3) * es;
-        if (es == 4) d += plane * (S + 2) * 4;
         u += plane * (S + 3);
         tmpb = std::max<uint64_t>(tmpb, plane);
         tmpo += align_up(plane, 256);
@@ -76,7 +75,7 @@ uint64_t footprint_estimate(const SiftCudaParams& p, int storage, uint32_t w, ui
     }
     const uint64_t per_cand = 2 * sizeof(Keypoint) + kOriMaxPeaks * 4 + 3 * 4;
     const uint64_t per_out = sizeof(Keypoint) + kDescLen * 4;
-    return align_up(std::max<uint32_t>(w, 1), 128) * h + g + d + u + tmpb + tmpo + lt + words + caps * per_cand +
+    return align_up(std::max<uint32_t>(w, 1), 128) * h + g + u + tmpb + tmpo + lt + words + caps * per_cand +
            caps * per_out + (1u << 20);
 }
 

@@ -91,19 +91,18 @@ def test_engine_errors_are_reported(built_lib):
 
 def footprint_restated(S, O, w, h, es):
     """The admission estimate of a server slot, restated: the arena layout
-    (pitch = width rounded to 32; S+3 Gaussian, S+2 DoG (f32 only) and S+3 u8
-    planes per octave; horizontal-pass and resize scratch; two mask-word
+    (pitch = width rounded to 32; S+3 Gaussian and S+3 u8 planes per octave,
+    no DoG planes; horizontal-pass and resize scratch; two mask-word
     arrays) plus list capacities of 1/64 of the scanned positions (>= 1024)
     at 140 candidate-list bytes and 540 output bytes each, plus the padded
     image and 1 MiB of tables."""
     al = lambda v, a: (v + a - 1) // a * a
-    g = d = u = tmpb = tmpo = lt = words = caps = 0
+    g = u = tmpb = tmpo = lt = words = caps = 0
     ow, oh = w, h
     for o in range(O):
         pitch = al(max(ow, 1), 32)
         plane, nw = pitch * oh, (ow + 31) // 32
         g += plane * (S + 3) * es
-        d += plane * (S + 2) * 4 if es == 4 else 0
         u += plane * (S + 3)
         tmpb = max(tmpb, plane)
         tmpo += al(plane, 256)
@@ -113,7 +112,7 @@ def footprint_restated(S, O, w, h, es):
         words += wo * 8
         caps += min(max(wo * 32 // 64, 1024), 1 << 28)
         ow, oh = ow // 2, oh // 2
-    return al(max(w, 1), 128) * h + g + d + u + tmpb + tmpo + lt + words + caps * 140 + caps * 540 + (1 << 20)
+    return al(max(w, 1), 128) * h + g + u + tmpb + tmpo + lt + words + caps * 140 + caps * 540 + (1 << 20)
 
 
 @pytest.mark.parametrize("shape", [(640, 480), (1920, 1080), (3840, 2160), (333, 217), (1, 1)])
