@@ -14,7 +14,8 @@ quoted on. Prints one JSON line.
           and the device->host copy of keypoints and descriptors into host
           memory inside the timed region (wall clock).
   roofline  the dominant stage, timed live with CUDA events in the timed
-          region; algorithmic bytes per run are stated in the design doc.
+          region; algorithmic bytes per run: pyramid_bytes() below for the
+          pyramid stage, keypoint and descriptor bytes for the gather stages.
   cpu_baseline  the C++ restatement of the reference CPU path (oracle/) on the
           host cores, bounded sample of the same frame.
 
