@@ -80,7 +80,6 @@ struct LanczosUniform {
 // mantissa bits, exactly.
 //   floor:  RD(x + 1.5*2^23) - 1.5*2^23   (1.5*2^23 keeps negatives in the binade)
 //   trunc:  RZ(x + 2^23) - 2^23           (x >= 0)
-//   rint:   RN(x + 2^23) - 2^23           (x >= 0, ties to even)
 constexpr float kMagic = 8388608.0f;         // 2^23
 constexpr float kMagic15 = 12582912.0f;      // 1.5 * 2^23
 __device__ __forceinline__ float floor_fi(float x, int* xi) {
@@ -90,7 +89,6 @@ __device__ __forceinline__ float floor_fi(float x, int* xi) {
 }
 __device__ __forceinline__ int floor_i(float x) { return __float_as_int(__fadd_rd(x, kMagic15)) - 0x4B400000; }
 __device__ __forceinline__ float trunc_pos(float x) { return __fsub_rn(__fadd_rz(x, kMagic), kMagic); }
-__device__ __forceinline__ float rint_pos(float x) { return __fsub_rn(__fadd_rn(x, kMagic), kMagic); }
 // integer value of a float holding an integer in [0, 2^23)
 __device__ __forceinline__ int int_of(float v) { return __float_as_int(__fadd_rn(v, kMagic)) - 0x4B000000; }
 // u8 -> float without a conversion
@@ -216,11 +214,6 @@ __device__ __forceinline__ float ex2_approx(float x) {
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
-
-// k / d and k % d for 0 <= k < 2^20, 0 < d < 2^10 without an integer divide:
-// (k + 0.5) / d is at least 0.5/d away from the next integer and the f32
-// product errs by far less.
-__device__ __forceinline__ int small_div(int k, float inv_d) { return (int)(((float)k + 0.5f) * inv_d); }
 
 // Chained launches (programmatic dependent launch). The pipeline's kernels
 // go out with launch_chained, and every one of them starts with chain_wait:
