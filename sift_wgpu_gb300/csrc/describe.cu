@@ -635,8 +635,6 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
 
 }  // namespace
 
-int describe_grid() { return 152 * 4; }
-
 template <typename TG>
 int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
                        uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,

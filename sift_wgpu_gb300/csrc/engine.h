@@ -824,15 +824,6 @@ struct Engine {
         return 0;
     }
 
-    // Reads the counters; grows the lists and reports a retry when one
-    // overflowed.
-    int check_counters(bool* retry) {
-        *retry = false;
-        CK(cudaMemcpyAsync(h_ctr.p, d_ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, st), "D2H counters");
-        CK(cudaStreamSynchronize(st), "run");
-        return grow_from(*h_ctr.as<Counters>(), retry);
-    }
-
     // Grows the lists that the counters c of a finished run overflowed;
     // *retry tells that the run must be repeated.
     int grow_from(const Counters& c, bool* retry) {
