@@ -78,6 +78,57 @@ def pyramid_bytes(w: int, h: int, octaves: int, S: int, b: int) -> int:
     return total
 
 
+def blur_radii(octaves: int, S: int, sigma: float = 1.6, assumed_blur: float = 0.5):
+    """(base radius, [[radius of level s = 1..S+2] per octave]) of the
+    pyramid's Gaussian blurs: the increments of generate_gaussian_pyramid
+    (src/sift.rs:141-147) in f32 and imageproc's radius ceil(2 sigma)."""
+    f = np.float32
+    sg, ab = f(sigma), f(assumed_blur)
+    base = np.sqrt(sg * sg - ab * ab) if sg > ab else f(0)
+    k = f(2.0) ** (f(1.0) / f(S))
+    target = [sg * f(k) ** s for s in range(S + 3)]
+    out = []
+    for o in range(octaves):
+        scale = f(2.0 ** o)
+        prev = sg * scale
+        row = []
+        for s in range(1, S + 3):
+            t = f(target[s] * scale)
+            b = np.sqrt(t * t - prev * prev)
+            row.append(int(np.ceil(f(2.0) * b)) if b >= f(1e-4) else 0)
+            prev = t
+        out.append(row)
+    return (int(np.ceil(f(2.0) * base)) if base > f(1e-4) else 0), out
+
+
+def pyramid_fp32_ops(w: int, h: int, octaves: int, S: int, sigma: float = 1.6, assumed_blur: float = 0.5) -> int:
+    """Separately rounded f32 multiplies and adds the pyramid stage needs (the
+    reference's tap order forbids fusing them): two passes of 2r + 1 taps per
+    pixel for every Gaussian level, and the 2x Lanczos3 resize between octaves
+    (12 taps per output in each pass: the vertical pass over the source width,
+    the horizontal over the destination). Halo recomputation is not counted."""
+    r0, radii = blur_radii(octaves, S, sigma, assumed_blur)
+    taps = 0
+    ow, oh = w, h
+    for o in range(octaves):
+        n = ow * oh
+        if n == 0:
+            break
+        if o == 0 and r0:
+            taps += n * 2 * (2 * r0 + 1)
+        for r in radii[o]:
+            if r:
+                taps += n * 2 * (2 * r + 1)
+        if o + 1 < octaves and ow // 2 and oh // 2:
+            taps += 12 * ow * (oh // 2) + 12 * (ow // 2) * (oh // 2)
+        ow, oh = ow // 2, oh // 2
+    return 2 * taps
+
+
+FP32_LANES_PER_SM = 128
+N_SMS = 152
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -175,7 +226,7 @@ SERVE_MIX = [((640, 480), 0.4), ((1280, 720), 0.3), ((1920, 1080), 0.2), ((3840,
 def serve_pool(per_size: int = 4):
     """Images of the serving mix: per_size distinct seeded frames per
     resolution (seeds 4000000 + k), at the 512x512 density."""
-    from sift_wgpu_gb300 import synth_image
+    from synthetic import synth_image
     images, size_of = [], []
     for si, ((w, h), _) in enumerate(SERVE_MIX):
         for j in range(per_size):
@@ -244,10 +295,8 @@ def serving_report(n_req: int, rates, max_inflight: int = 8, autotune: bool = Fa
 def batch64_images():
     """64 images, width and height uniform over the multiples of 16 in
     [320, 2560] (seed 2), image i made with seed 1000 + i."""
-    from sift_wgpu_gb300 import synth_image
-    rng = np.random.default_rng(2)
-    dims = rng.integers(20, 161, size=(64, 2)) * 16
-    return [synth_image(1000 + i, int(w), int(h)) for i, (w, h) in enumerate(dims)]
+    from synthetic import batch64_images as make
+    return make()
 
 
 def run_batch64(args, world, rank, local):
@@ -310,7 +359,8 @@ def run_match(args, world, rank, local):
     import ctypes as C
     import torch
     import sift_wgpu_gb300 as sg
-    img = sg.synth_image(1, 1920, 1080)
+    from synthetic import synth_image
+    img = synth_image(1, 1920, 1080)
     shifted = np.zeros_like(img)
     shifted[3:, 5:] = img[:-3, :-5]
     torch.cuda.set_device(local)
@@ -401,7 +451,7 @@ def run_reference(args, world, rank):
     """The reference CPU path (its C++ restatement) on the host cores."""
     if rank != 0:
         return
-    from sift_wgpu_gb300 import synth_image
+    from synthetic import synth_image
     from oracle import oracle
     w, h, seed, sargs = WORKLOADS.get(args.workload, WORKLOADS["1080p"])
     img = synth_image(seed, w, h)
@@ -435,6 +485,60 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def fp32_roofline(ops: int, ms: float, sm_mhz) -> dict:
+    """The pyramid stage against the FP32 pipe: its separately rounded
+    multiplies and adds over the stage time, as a fraction of 152 SMs x 128
+    f32 lanes x the SM clock sampled during the timed region."""
+    mhz = float(sm_mhz) if sm_mhz else 2070.0
+    peak = N_SMS * FP32_LANES_PER_SM * mhz * 1e6
+    ach = ops / (ms / 1e3)
+    return {"bound": "fp32", "ops": int(ops), "achieved_tops": ach / 1e12, "peak_tops": peak / 1e12,
+            "unit": "Tops/s", "frac": ach / peak, "sm_mhz": mhz,
+            "peak_kind": "152 SMs x 128 f32 lanes x sampled SM clock"}
+
+
+def pyramid_section(workload: str, local: int, storage: str, steps: int, warmup: int, sm_mhz) -> dict:
+    """The pyramid stage of one workload, launched in stage order with CUDA
+    events at the stage boundaries (no overlap with the other stages), after
+    an L2 flush: HBM and FP32-pipe rooflines."""
+    import torch
+    import sift_wgpu_gb300 as sg
+    from synthetic import synth_image
+    w, h, seed, sargs = WORKLOADS[workload]
+    img = synth_image(seed, w, h)
+    d_img = torch.from_numpy(img).to(f"cuda:{local}")
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    with sg.Engine(sg.Sift.new(*sargs), device=local, storage=storage) as eng:
+        stream = torch.cuda.ExternalStream(eng.stream, device=torch.device("cuda", local))
+        torch.cuda.synchronize()
+        eng.profile(True)
+        with torch.cuda.stream(stream):
+            for _ in range(max(1, warmup)):
+                eng.run_device(d_img.data_ptr(), w, h, w)
+        torch.cuda.synchronize()
+        eng.profile_read()
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                flush.zero_()
+                eng.run_device(d_img.data_ptr(), w, h, w)
+        torch.cuda.synchronize()
+        stage_ms, runs = eng.profile_read()
+        eng.profile(False)
+        nk = len(eng.debug_stage(sg.STAGE_KEYPOINTS))
+    per_run = {k: v / max(runs, 1) for k, v in stage_ms.items()}
+    peak, peak_kind = measured_peaks()
+    octs, S = sargs[1], sargs[2]
+    b = pyramid_bytes(w, h, octs, S, 4 if storage == "f32" else 2)
+    ms = per_run["pyramid_dog"]
+    gbs = b / (ms / 1e3) / 1e9
+    return {"workload": f"{w}x{h} u8 synthetic frame, seed {seed}, Sift::new{sargs}", "storage": storage,
+            "runs": runs, "stages_ms": per_run, "keypoints": nk,
+            "hbm": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                    "algorithmic_bytes": b, "ms": ms, "peak_kind": peak_kind,
+                    "traffic": traffic_from_profiles(workload, "pyramid_dog")},
+            "fp32_pipe": fp32_roofline(pyramid_fp32_ops(w, h, octs, S, sargs[0], sargs[3]), ms, sm_mhz)}
+
+
 def run_cuda(args, world, rank, local):
     import torch
 
@@ -442,7 +546,8 @@ def run_cuda(args, world, rank, local):
 
     w, h, seed, sargs = WORKLOADS[args.workload]
     torch.cuda.set_device(local)
-    img = sg.synth_image(seed, w, h)
+    from synthetic import synth_image
+    img = synth_image(seed, w, h)
     eng = sg.Engine(sg.Sift.new(*sargs), device=local, storage=args.storage)
     stream = torch.cuda.ExternalStream(eng.stream, device=torch.device("cuda", local))
     d_img = torch.from_numpy(img).to(f"cuda:{local}")
@@ -513,6 +618,18 @@ def run_cuda(args, world, rank, local):
     e2e_value = world * e2e_n / e2e_s
     d2h = 16 + nk * (28 + 512)
 
+    # the drop-in call as the documented Rust arm makes it: a pageable image,
+    # results copied out of the engine's buffers into arrays the caller owns
+    pageable = np.array(img, copy=True)
+    for _ in range(max(1, args.warmup)):
+        eng.detect_and_compute(pageable)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_n):
+        kk, dd = eng.detect_and_compute(pageable)
+    dropin_s = allreduce_max(world, time.perf_counter() - t0)
+    dropin_value = world * e2e_n / dropin_s
+
     # roofline of the dominant stage
     per_run = {k: v / max(runs, 1) for k, v in stage_ms.items()}
     dominant = max(per_run, key=per_run.get)
@@ -522,7 +639,9 @@ def run_cuda(args, world, rank, local):
     pyr_gbs = b_pyr / (per_run["pyramid_dog"] / 1e3) / 1e9
     roof_pyr = {"stage": "pyramid_dog", "bound": "hbm", "achieved": pyr_gbs, "peak": peak, "unit": "GB/s",
                 "frac": pyr_gbs / peak, "traffic": traffic_from_profiles(args.workload, "pyramid_dog"),
-                "algorithmic_bytes": b_pyr, "ms": per_run["pyramid_dog"], "peak_kind": peak_kind}
+                "algorithmic_bytes": b_pyr, "ms": per_run["pyramid_dog"], "peak_kind": peak_kind,
+                "fp32_pipe": fp32_roofline(pyramid_fp32_ops(w, h, octs, S, sargs[0], sargs[3]), per_run["pyramid_dog"],
+                                           clocks.get("sm_mhz"))}
     if dominant == "pyramid_dog":
         roof = dict(roof_pyr)
     else:
@@ -552,7 +671,12 @@ def run_cuda(args, world, rank, local):
             "config": {"workload": f"{w}x{h} u8 synthetic frame, seed {seed}, Sift::new{sargs}",
                        "storage": args.storage, "parallelism": f"replicas x{world}",
                        "l2": "256 MiB flush before every step", "keypoints": int(nk)},
-            "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": w * h, "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": w * h, "d2h_bytes_per_step": d2h,
+                    "form": "sift_cuda_detect_and_compute_view, pinned host image, results read in place"},
+            "e2e_dropin": {"value": dropin_value, "unit": "images/s", "h2d_bytes_per_step": w * h,
+                           "d2h_bytes_per_step": d2h,
+                           "form": "pageable host image through sift_cuda_detect_and_compute_view, keypoints and "
+                                   "descriptors copied into caller-owned arrays (the Rust arm's copy)"},
             "keypoints_per_s": {"device": value * int(nk), "e2e": e2e_value * int(nk)},
             "roofline": roof,
             "roofline_pyramid_dog": roof_pyr,
@@ -564,6 +688,10 @@ def run_cuda(args, world, rank, local):
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(img, sargs, args.cpu_budget)
     eng.close()
+    if args.workload == "1080p" and not args.no_4096:
+        sec = pyramid_section("4096", local, args.storage, 2, 1, clocks.get("sm_mhz"))
+        if rank == 0:
+            out["pyramid_4096"] = sec
     if not args.no_serving:
         srv = serving_report(args.serve_requests, [1000, 2000, 4000], max_inflight=args.inflight, device=local)
         if rank == 0:
@@ -584,6 +712,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain section")
+    ap.add_argument("--no-4096", action="store_true", help="skip the 4096x4096 pyramid section")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--requests", type=int, default=20000, help="requests per rate (--workload serve)")
     ap.add_argument("--inflight", type=int, default=8, help="server: requests on the device at once")

@@ -197,8 +197,9 @@ void* sift_cuda_stream(SiftCudaEngine* engine);
  *  SIFT_CUDA_STAGE_REFINED:    refine_and_filter_extrema output
  *                              (src/sift.rs:299-474), SiftCudaKeypoint each.
  *  SIFT_CUDA_STAGE_DOG:        all DoG levels as f32, octave-major, level,
- *                              row-major, formed from the level planes as
- *                              the detection forms them.
+ *                              row-major, formed on the device from the u8
+ *                              level planes by the function the candidate
+ *                              emission and refinement read DoG through.
  *  SIFT_CUDA_STAGE_KEYPOINTS:  the final keypoints, SiftCudaKeypoint each.
  *  SIFT_CUDA_STAGE_DESCRIPTORS: the final descriptors, 128 floats each
  *                              (count = keypoints x 128).
@@ -368,25 +369,15 @@ int sift_cuda_draw_keypoints(SiftCudaEngine* engine, const uint8_t* gray, uint32
  *    nothing runs. d_dst may equal d_src.
  *  - The first call on a device looks the array's address up (and may make
  *    the runtime load this library's device code there): make it before any
- *    stream capture begins.
+ *    stream capture begins. The address is kept for the life of the process:
+ *    do not use this entry point after a cudaDeviceReset of that device (the
+ *    module may reload elsewhere).
  *  - Calls share the array: calls that can overlap on the device (different
  *    streams, unordered threads) race and corrupt each other's output.
  *  - Asynchronous on `stream` (a cudaStream_t; NULL = the default stream). */
 int sift_cuda_gaussian_blur_u8_noalloc(const uint8_t* d_src, uint32_t width, uint32_t height,
                                        uint32_t src_stride, uint8_t* d_dst, uint32_t dst_stride,
                                        float sigma, void* stream);
-
-/* ---- synthetic input -------------------------------------------------------- */
-
-/* Seeded synthetic image: background 128, n_blobs isotropic Gaussian blobs
- * (centre uniform, sigma U(2,20), amplitude U(-90,90)), n_rects filled
- * axis-aligned rectangles (sides U{8..96}, intensity U{0..255}), i.i.d.
- * N(0, 3^2) noise, clamped and rounded to u8. RNG: splitmix64-seeded
- * xoshiro256**. Writes width*height bytes (stride = width). Host-only. */
-void sift_synth_image(uint64_t seed, uint32_t width, uint32_t height, uint32_t n_blobs,
-                      uint32_t n_rects, uint8_t* out);
-/* Blob and rectangle counts at the 512x512 density (200 blobs, 40 rects). */
-void sift_synth_density(uint32_t width, uint32_t height, uint32_t* n_blobs, uint32_t* n_rects);
 
 #ifdef __cplusplus
 }

@@ -178,8 +178,6 @@ def lib() -> C.CDLL:
         "sift_cuda_match": (C.c_int, [C.c_void_p, C.c_void_p, u32, C.c_void_p, u32, C.c_void_p]),
         "sift_cuda_match_scratch_bytes": (C.c_size_t, [u32, u32]),
         "sift_cuda_match_device": (C.c_int, [C.c_void_p, u32, C.c_void_p, u32, C.c_void_p, C.c_void_p, C.c_void_p]),
-        "sift_synth_image": (None, [u64, u32, u32, u32, u32, C.c_void_p]),
-        "sift_synth_density": (None, [u32, u32, P(u32), P(u32)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -203,25 +201,10 @@ def exported_symbols() -> list[str]:
         "sift_cuda_server_warm", "sift_cuda_server_stats", "sift_cuda_server_tuning", "sift_cuda_footprint_bytes",
         "sift_cuda_replay", "sift_cuda_gaussian_blur_u8_noalloc", "sift_cuda_draw_keypoints", "sift_cuda_match",
         "sift_cuda_match_scratch_bytes",
-        "sift_cuda_match_device", "sift_synth_image",
-        "sift_synth_density",
+        "sift_cuda_match_device",
     ]
 
 
 def check(rc: int) -> None:
     if rc != 0:
         raise SiftCudaError(rc, lib().sift_cuda_last_error().decode(errors="replace"))
-
-
-def synth_image(seed: int, width: int, height: int, n_blobs: int | None = None,
-                n_rects: int | None = None) -> np.ndarray:
-    """Seeded synthetic u8 image (sift_synth_image), default 512x512 density."""
-    L = lib()
-    if n_blobs is None or n_rects is None:
-        b, r = C.c_uint32(), C.c_uint32()
-        L.sift_synth_density(width, height, C.byref(b), C.byref(r))
-        n_blobs = b.value if n_blobs is None else n_blobs
-        n_rects = r.value if n_rects is None else n_rects
-    out = np.empty((height, width), dtype=np.uint8)
-    L.sift_synth_image(seed, width, height, n_blobs, n_rects, out.ctypes.data)
-    return out

@@ -23,7 +23,7 @@ LIB = PKG / "libsiftcuda.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["scan.cu", "pyramid.cu", "detect.cu", "describe.cu", "engine.cu", "server.cu", "convert.cu", "export.cu", "noalloc.cu", "match.cu", "draw.cu"]
-CPP_SOURCES = ["tables.cpp", "synth.cpp"]
+CPP_SOURCES = ["tables.cpp"]
 HEADERS = ["sift_internal.cuh", "tables.h", "engine.h"]
 
 

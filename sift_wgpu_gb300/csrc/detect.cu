@@ -361,9 +361,31 @@ __global__ void __launch_bounds__(256) k_refine(const uint8_t* __restrict__ u8ar
     }
 }
 
+// Debug read-back of DoG layer l of octave o as a dense W x H f32 plane, each
+// value formed by DogFromU8::at, the function the candidate emission and the
+// refinement read DoG through (u8 planes and the v / 255 table in device
+// memory). Not part of a run.
+__global__ void k_dog_dense(const uint8_t* __restrict__ u8arena, const float* __restrict__ lut255, PyramidDev pyr,
+                            int o, int l, float* __restrict__ out) {
+    chain_wait();
+    const OctaveDev& od = pyr.oct[o];
+    const DogFromU8 dog{u8arena + od.u_off, lut255, od.plane, od.pitch, od.W, od.H};
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x < od.W && y < od.H) out[(long long)y * od.W + x] = dog.at(l, x, y);
+}
+
 }  // namespace
 
 // ---- launchers -------------------------------------------------------------
+
+int launch_dog_dense(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int l, float* out,
+                     cudaStream_t st) {
+    const OctaveDev& od = pyr.oct[o];
+    if (od.W <= 0 || od.H <= 0) return 0;
+    dim3 grid((od.W + 127) / 128, od.H);
+    if (launch_chained(k_dog_dense, grid, 128, 0, st, u8arena, lut255, pyr, o, l, out) != cudaSuccess) return -1;
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
 
 int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
                         uint32_t* words, cudaStream_t st) {

@@ -318,34 +318,36 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
         return sift::cuda_fail(cudaGetLastError(), "D2H counters");
     const sift::PyramidDev& g = e.pyr;
     if (stage == SIFT_CUDA_STAGE_DOG) {
-        // No DoG plane is stored: extrema and refinement form DoG(l) =
+        // No DoG plane is stored: the detection forms DoG(l) =
         // G_{l+1}/255 - G_l/255 (src/sift.rs:92-124) from the u8 level planes
-        // through the v / 255 table, and so does this read-back, with the same
-        // IEEE f32 division and subtraction.
+        // where it reads it. This read-back runs the device function the
+        // candidate emission and the refinement use (DogFromU8) over every
+        // pixel of every layer.
         const int L = g.S + 2;
         uint64_t total = 0;
         for (int o = 0; o < g.num_octaves; ++o) total += (uint64_t)g.oct[o].W * g.oct[o].H * L;
         *count = total;
         if (!out) return 0;
-        float lut[256];
-        for (int v = 0; v < 256; ++v) lut[v] = (float)v / 255.0f;
+        size_t most = 0;
+        for (int o = 0; o < g.num_octaves; ++o) most = std::max(most, (size_t)g.oct[o].W * g.oct[o].H);
+        sift::DevMem tmp;
+        if (tmp.ensure(std::max<size_t>(most, 1) * sizeof(float)) != cudaSuccess)
+            return sift::cuda_fail(cudaGetLastError(), "cudaMalloc(DoG read-back)");
+        const float* lut = e.d_wts.as<float>() + e.lut_off;
         uint64_t pos = 0;
-        std::vector<uint8_t> lo, hi;
-        for (int o = 0; o < g.num_octaves; ++o) {
+        for (int o = 0; o < g.num_octaves && pos < capacity; ++o) {
             const sift::OctaveDev& od = g.oct[o];
             if (od.W == 0 || od.H == 0) continue;
-            const size_t npx = (size_t)od.W * od.H;
-            auto plane = [&](int l, std::vector<uint8_t>& dst) {
-                dst.resize(npx);
-                return cudaMemcpy2D(dst.data(), (size_t)od.W, e.d_U.as<uint8_t>() + od.u_off + (long long)l * od.plane,
-                                    (size_t)od.pitch, (size_t)od.W, od.H, cudaMemcpyDeviceToHost);
-            };
-            if (plane(0, lo) != cudaSuccess) return sift::cuda_fail(cudaGetLastError(), "D2H stage");
-            for (int l = 0; l < L; ++l) {
-                if (plane(l + 1, hi) != cudaSuccess) return sift::cuda_fail(cudaGetLastError(), "D2H stage");
-                for (size_t q = 0; q < npx && pos < capacity; ++q, ++pos)
-                    ((float*)out)[pos] = lut[hi[q]] - lut[lo[q]];
-                lo.swap(hi);
+            const uint64_t npx = (uint64_t)od.W * od.H;
+            for (int l = 0; l < L && pos < capacity; ++l) {
+                if (sift::launch_dog_dense(e.d_U.as<uint8_t>(), lut, g, o, l, tmp.as<float>(), e.st))
+                    return sift::cuda_fail(cudaGetLastError(), "DoG read-back");
+                const uint64_t n = std::min<uint64_t>(npx, capacity - pos);
+                if (cudaMemcpyAsync((float*)out + pos, tmp.p, n * sizeof(float), cudaMemcpyDeviceToHost, e.st) !=
+                        cudaSuccess ||
+                    cudaStreamSynchronize(e.st) != cudaSuccess)
+                    return sift::cuda_fail(cudaGetLastError(), "D2H stage");
+                pos += n;
             }
         }
         return 0;

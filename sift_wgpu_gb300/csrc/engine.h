@@ -65,6 +65,8 @@ int launch_to_luma(int format, const uint8_t* px, long long stride, int W, int H
                    cudaStream_t st);
 int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
                         uint32_t* words, cudaStream_t st);
+int launch_dog_dense(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int l, float* out,
+                     cudaStream_t st);
 int launch_emit(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, const uint32_t* words,
                 const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st);
 int launch_refine(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, float sigma,

@@ -140,8 +140,9 @@ __global__ void __launch_bounds__(kColTX* kColTY) k_cols_from_scratch(const uint
 // same values as the engine's blur tables.
 int gaussian_taps(float sigma, BlurTaps* t) {
     const float fr = std::ceil(2.0f * sigma);
+    // compared as a float first: a radius beyond int range must not reach the cast
+    if (!(fr <= (float)kMaxRadius)) return -1;
     const int r = fr > 0.0f ? (int)fr : 0;
-    if (r > kMaxRadius) return -1;
     const float c = 1.0f / (std::sqrt(2.0f * 3.14159265358979323846f) * sigma);
     t->r = r;
     for (int i = 0; i < kTapSlots; ++i) t->w[i] = 0.0f;

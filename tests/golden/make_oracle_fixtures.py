@@ -1,5 +1,5 @@
 """Writes tests/golden/oracle_256_seed0.npz: a 256 x 256 synthetic image
-(sift_synth_image, seed 0, the 512 x 512 density) and the oracle's keypoints
+(synthetic.synth_image, seed 0, the 512 x 512 density) and the oracle's keypoints
 and descriptors for it under Sift::default().
 
     python tests/golden/make_oracle_fixtures.py
@@ -20,10 +20,8 @@ OUT = Path(__file__).resolve().parent / "oracle_256_seed0.npz"
 
 def main() -> None:
     from oracle import oracle
-    from sift_wgpu_gb300 import build_ext
-    build_ext.build()
-    import sift_wgpu_gb300 as sgb
-    img = sgb.synth_image(0, 256, 256)
+    from synthetic import synth_image
+    img = synth_image(0, 256, 256)
     kps, desc = oracle.detect_and_compute(img)
     np.savez_compressed(OUT, image=img, keypoints=kps, descriptors=desc.astype(np.float32))
     print(f"{OUT.name}: {len(kps)} keypoints")

@@ -60,18 +60,24 @@ def test_other_backends_are_not_served_here(built_lib):
             Sift.default().detect_and_compute_with_backend(img, b)
 
 
-def test_synth_is_seeded_and_dense(built_lib):
-    from sift_wgpu_gb300 import synth_image
-    a = synth_image(0, 512, 512)
-    b = synth_image(0, 512, 512)
-    c = synth_image(1, 512, 512)
+def test_synth_is_seeded_and_dense():
+    """The workload generator is seeded, dense, and loads no native code."""
+    import synthetic
+    a = synthetic.synth_image(0, 512, 512)
+    b = synthetic.synth_image(0, 512, 512)
+    c = synthetic.synth_image(1, 512, 512)
     assert a.dtype == np.uint8 and a.shape == (512, 512)
     assert np.array_equal(a, b) and not np.array_equal(a, c)
     assert 100 < a.mean() < 160 and a.std() > 10
-    from sift_wgpu_gb300 import _capi
-    nb, nr = C.c_uint32(), C.c_uint32()
-    _capi.lib().sift_synth_density(1920, 1080, C.byref(nb), C.byref(nr))
-    assert (nb.value, nr.value) == (1582, 316)
+    assert synthetic.density(1920, 1080) == (1582, 316)
+    assert synthetic.density(4096, 4096) == (12800, 2560)
+    assert synthetic.synth_image(3, 0, 0).shape == (0, 0)
+    # draws of one stream do not depend on how they are split
+    u = synthetic.uniforms(5, 3, 0, 1000)
+    assert np.array_equal(u[400:], synthetic.uniforms(5, 3, 400, 600))
+    assert 0.45 < u.mean() < 0.55 and u.min() >= 0.0 and u.max() < 1.0
+    imports = re.findall(r"^\s*(?:import|from)\s+(\S+)", (ROOT / "synthetic.py").read_text(), flags=re.M)
+    assert set(imports) <= {"numpy", "__future__"}, imports
 
 
 def test_engine_errors_are_reported(built_lib):

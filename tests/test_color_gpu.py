@@ -5,6 +5,7 @@ import ctypes as C
 
 import numpy as np
 import pytest
+from synthetic import synth_image
 
 pytestmark = pytest.mark.gpu
 
@@ -41,7 +42,7 @@ def test_to_luma_kernel_matches_oracle(sgb, oracle_mod, fmt, ch, shape):
 
 @pytest.mark.parametrize("fmt,ch", FORMATS)
 def test_colour_pipeline_equals_luma_pipeline(sgb, oracle_mod, fmt, ch):
-    gray = sgb.synth_image(11, 640, 480)
+    gray = synth_image(11, 640, 480)
     rng = np.random.default_rng(fmt)
     # a colour image whose channels differ, alpha random
     px = np.stack([gray, np.roll(gray, 3, axis=1), np.roll(gray, 5, axis=0)]

@@ -3,6 +3,7 @@
 (oracle/draw.py), through the C ABI: bit-exact RGB images."""
 import numpy as np
 import pytest
+from synthetic import synth_image
 
 pytestmark = pytest.mark.gpu
 
@@ -15,7 +16,7 @@ def sgb(built_lib):
 
 def test_detected_keypoints_bit_exact(sgb):
     from oracle.draw import draw_keypoints_to_image
-    img = sgb.synth_image(0, 512, 512)
+    img = synth_image(0, 512, 512)
     with sgb.Engine(sgb.Sift.default()) as eng:
         kps, _ = eng.detect_and_compute(img)
         got = eng.draw_keypoints(img, kps, (255, 0, 0))

@@ -10,6 +10,7 @@ import ctypes as C
 
 import numpy as np
 import pytest
+from synthetic import synth_image
 
 pytestmark = pytest.mark.gpu
 
@@ -55,7 +56,7 @@ def unit_rows(rng, n):
 def test_real_descriptors_two_frames(sgb, eng):
     """Descriptors of a 1080p frame against those of the same scene shifted by
     a few pixels: the shifted keypoints find their originals."""
-    img = sgb.synth_image(1, 1920, 1080)
+    img = synth_image(1, 1920, 1080)
     k1, d1 = eng.detect_and_compute(img)
     shifted = np.zeros_like(img)
     shifted[3:, 5:] = img[:-3, :-5]

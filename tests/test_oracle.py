@@ -13,6 +13,7 @@ from pathlib import Path
 
 import numpy as np
 import pytest
+from synthetic import synth_image
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 KAT = json.loads((GOLDEN / "reference_kat.json").read_text())
@@ -62,8 +63,7 @@ def test_small_gradient_properties(oracle_mod):
         check_properties(kps, 20, 15)
 
 
-def test_synthetic_properties_and_determinism(oracle_mod, built_lib):
-    from sift_wgpu_gb300 import synth_image
+def test_synthetic_properties_and_determinism(oracle_mod):
     img = synth_image(0, 512, 512)
     k1, d1 = oracle_mod.detect_and_compute(img, threads=4)
     k2, d2 = oracle_mod.detect_and_compute(img, threads=1)
@@ -76,8 +76,7 @@ def test_synthetic_properties_and_determinism(oracle_mod, built_lib):
     assert np.all((np.abs(norms - 1.0) < 1e-4) | (norms == 0.0))
 
 
-def test_high_contrast_threshold(oracle_mod, built_lib):
-    from sift_wgpu_gb300 import synth_image
+def test_high_contrast_threshold(oracle_mod):
     img = synth_image(0, 512, 512)
     k_def, _ = oracle_mod.detect_and_compute(img)
     k_hi, d_hi = oracle_mod.detect_and_compute(img, oracle_mod.params(contrast_threshold=1.0))
@@ -130,10 +129,9 @@ def test_lanczos_uniform_and_shape(oracle_mod):
     assert out.shape == (18, 25) and np.all(out == 77)
 
 
-def test_extrema_match_numpy_restatement(oracle_mod, built_lib):
+def test_extrema_match_numpy_restatement(oracle_mod):
     """find_scale_space_extrema restated in numpy on the oracle's own pyramid:
     same candidates, same (octave, layer, y, x) order."""
-    from sift_wgpu_gb300 import synth_image
     img = synth_image(11, 96, 80)
     st = oracle_mod.stages(img)
     rows = []
@@ -171,9 +169,8 @@ def test_fp64_model_is_the_reference_algorithm(oracle_mod):
     to the few pixels where float64 and f32 accumulation truncate differently),
     so the FP64 model of the precision statement differs from the reference
     path only by those roundings."""
-    import sift_wgpu_gb300 as sg
     from oracle.ideal64 import Ideal64
-    img = sg.synth_image(0, 512, 512)
+    img = synth_image(0, 512, 512)
     m = Ideal64(quantize=True, dog_f32=True)
     pyr = m.pyramid(img)
     dog = m.dog(pyr)

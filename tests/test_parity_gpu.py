@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from parity import DESC_RTOL, MATCH_RATE, match
+from synthetic import synth_image
 
 pytestmark = pytest.mark.gpu
 
@@ -19,6 +20,9 @@ CASES = [
     ("odd_333x217", 333, 217, 5, (1.6, 4, 3, 0.5, 0.04, 10.0)),
     ("1024_6oct", 1024, 1024, 3, (1.6, 6, 3, 0.5, 0.04, 10.0)),
     ("640x480_s4", 640, 480, 9, (1.6, 5, 4, 0.5, 0.04, 10.0)),
+    # the large-image workload: blur radii of octaves 4-5 (sigma ~49-99 px)
+    # exceed the 256 x 256 and 128 x 128 octave sizes
+    ("4096_6oct", 4096, 4096, 3, (1.6, 6, 3, 0.5, 0.04, 10.0)),
 ]
 
 
@@ -48,7 +52,7 @@ def oracle_stages(oracle_mod, img, args, key):
 
 
 def image(sgb, w, h, seed):
-    return sgb.synth_image(seed, w, h)
+    return synth_image(seed, w, h)
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
@@ -63,7 +67,12 @@ def test_stages_bit_exact(sgb, oracle_mod, case):
     if not np.array_equal(pyr, st.pyramid):
         bad = np.nonzero(pyr != st.pyramid)[0]
         pytest.fail(f"pyramid differs at {len(bad)} of {pyr.size} values, first at {bad[:5]}")
-    # DoG = G_{s+1}/255 - G_s/255 in f32 (src/sift.rs:92-124)
+    # DoG = G_{s+1}/255 - G_s/255 in f32 (src/sift.rs:92-124). No DoG plane
+    # is stored; this read-back runs, on the device, the function through
+    # which candidate emission and refinement read DoG (the u8 planes and the
+    # v / 255 table in device memory), over every pixel. The extrema scan
+    # stages DoG through its own tile loader, which the bit-identical
+    # candidate list below checks.
     dog = eng.debug_stage(sgb.STAGE_DOG)
     off_g = off_d = 0
     L = st.levels

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from precision import dog_errors, keypoint_errors
+from synthetic import synth_image
 
 pytestmark = pytest.mark.gpu
 
@@ -19,7 +20,7 @@ pytestmark = pytest.mark.gpu
 def test_precision_statement(built_lib, oracle_mod):
     import sift_wgpu_gb300 as sg
     from oracle.ideal64 import Ideal64
-    img = sg.synth_image(0, 512, 512)
+    img = synth_image(0, 512, 512)
     k64, d64, pyr64, dog64 = Ideal64().detect_and_compute(img)
     dims = [(lv[0].shape[1], lv[0].shape[0]) for lv in pyr64]
     report = {"image": "512x512 synthetic, seed 0, Sift::default()"}

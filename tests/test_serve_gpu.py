@@ -8,6 +8,7 @@ import time
 
 import numpy as np
 import pytest
+from synthetic import synth_image
 
 pytestmark = pytest.mark.gpu
 
@@ -22,7 +23,7 @@ def sgb(built_lib):
 
 @pytest.fixture(scope="module")
 def images(sgb):
-    return [sgb.synth_image(4_000_000 + i, w, h) for i, (w, h) in enumerate(SIZES)]
+    return [synth_image(4_000_000 + i, w, h) for i, (w, h) in enumerate(SIZES)]
 
 
 @pytest.fixture(scope="module")
@@ -145,7 +146,7 @@ def test_replay_served_and_plain(sgb, images, alone):
 def test_requests_submitted_while_others_run_start_early(sgb, images):
     """Continuous batching: a small request submitted while a large one runs
     finishes before the large one (it is not queued behind it)."""
-    big = sgb.synth_image(77, 4096, 4096)
+    big = synth_image(77, 4096, 4096)
     with sgb.Server(max_inflight=4) as srv:
         srv.warm(big, 1)
         srv.warm(images[3], 1)
@@ -157,3 +158,28 @@ def test_requests_submitted_while_others_run_start_early(sgb, images):
         assert first.status == 0 and second.status == 0
         assert first.tag == 1 and second.tag == 0
         assert first.start_s < second.done_s
+
+
+def test_batch64_sample_matches_oracle(sgb, oracle_mod):
+    """Six images of the uneven 64-image batch (the smallest, the largest, the
+    most elongated and three more) run together through detect_batch, each
+    compared with the CPU oracle on its own: the same keypoints in the
+    reference order within the tolerance bar, descriptors within 1e-3
+    relative L2."""
+    from parity import DESC_RTOL, MATCH_RATE, match
+    import synthetic
+    shapes = synthetic.batch64_shapes()
+    area = [w * h for w, h in shapes]
+    elong = [max(w / h, h / w) for w, h in shapes]
+    pick = []
+    for i in (int(np.argmin(area)), int(np.argmax(area)), int(np.argmax(elong)), 0, 1, 2):
+        if i not in pick:
+            pick.append(i)
+    imgs = [synthetic.synth_image(1000 + i, *shapes[i]) for i in pick]
+    with sgb.Server(max_inflight=8) as srv:
+        out = srv.detect_batch(imgs)
+    for i, img, (k, d) in zip(pick, imgs, out):
+        rk, rd = oracle_mod.detect_and_compute(img)
+        m = match(rk, rd, k, d)
+        assert len(rk) > 0 and m.rate >= MATCH_RATE and m.same_order, f"image {i} {shapes[i]}: {m.summary()}"
+        assert float(m.desc_err.max()) <= DESC_RTOL, f"image {i}: {m.summary()}"

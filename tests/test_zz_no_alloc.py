@@ -11,6 +11,7 @@ import ctypes as C
 
 import numpy as np
 import pytest
+from synthetic import synth_image
 
 pytestmark = pytest.mark.gpu
 
@@ -44,7 +45,7 @@ def test_base_level_matches_engine_twice(sgb, oracle_mod):
     import torch
     lib = sgb._capi.lib()
     w, h = 1920, 1080
-    img = sgb.synth_image(1, w, h)
+    img = synth_image(1, w, h)
     eng = sgb.Engine(sgb.Sift.default())
     eng.detect_and_compute(img)
     level0 = eng.debug_stage(sgb.STAGE_PYRAMID)[: w * h].reshape(h, w)
@@ -67,7 +68,7 @@ def test_level_blurs_match_engine(sgb, oracle_mod):
     import torch
     lib = sgb._capi.lib()
     w, h, O, S = 1024, 768, 3, 3
-    img = sgb.synth_image(7, w, h)
+    img = synth_image(7, w, h)
     eng = sgb.Engine(sgb.Sift.new(1.6, O, S, 0.5, 0.04, 10.0))
     eng.detect_and_compute(img)
     pyr = octave_levels(eng.debug_stage(sgb.STAGE_PYRAMID), w, h, O, S + 3)
@@ -115,7 +116,8 @@ def test_rejects_requests_beyond_the_scratch(sgb):
     lib = sgb._capi.lib()
     src = torch.zeros(16, dtype=torch.uint8, device="cuda")
     dst = torch.full((16,), 9, dtype=torch.uint8, device="cuda")
-    for (w, h, sigma) in [(8193, 1, 1.0), (4096, 4097, 1.0), (4, 4, 40.0)]:
+    # 3e9: a radius beyond int range, rejected on the host like any other
+    for (w, h, sigma) in [(8193, 1, 1.0), (4096, 4097, 1.0), (4, 4, 40.0), (4, 4, 3e9)]:
         rc = blur_noalloc(lib, src, dst, w, h, sigma)
         assert rc == ERR_UNSUPPORTED
         msg = lib.sift_cuda_last_error().decode()
