@@ -59,20 +59,22 @@ WORKLOADS = {
     "4096": (4096, 4096, 3, (1.6, 6, 3, 0.5, 0.04, 10.0)),
 }
 METRIC = "1080p images/s"
+STORED_BYTES = {"f32": 4, "f16": 2, "u8": 0}  # per pixel of a stored level, beside its u8 plane
 FLUSH_BYTES = 256 << 20
 
 
 def pyramid_bytes(w: int, h: int, octaves: int, S: int, b: int) -> int:
     """Algorithmic bytes of the pyramid stage as stored here: the u8 input
-    read once, every octave base read once, S+3 Gaussian levels written once
-    at b bytes per value (4 f32, 2 f16) plus their u8 planes (1 byte). No DoG
-    plane is written: extrema and refinement form DoG from the u8 planes."""
+    read once, every octave base read once (as its u8 plane), S+3 Gaussian
+    levels written once as u8 planes (1 byte) plus, in the f32 and f16 modes,
+    the stored level (b = 4 or 2 bytes; 0 in u8 storage). No DoG plane is
+    written: extrema and refinement form DoG from the u8 planes."""
     total = w * h  # u8 input
     ow, oh = w, h
     for o in range(octaves):
         n = ow * oh
         if o > 0:
-            total += n * b
+            total += n
         total += n * (S + 3) * (b + 1)
         ow, oh = ow // 2, oh // 2
     return total
@@ -528,7 +530,7 @@ def pyramid_section(workload: str, local: int, storage: str, steps: int, warmup:
     per_run = {k: v / max(runs, 1) for k, v in stage_ms.items()}
     peak, peak_kind = measured_peaks()
     octs, S = sargs[1], sargs[2]
-    b = pyramid_bytes(w, h, octs, S, 4 if storage == "f32" else 2)
+    b = pyramid_bytes(w, h, octs, S, STORED_BYTES[storage])
     ms = per_run["pyramid_dog"]
     gbs = b / (ms / 1e3) / 1e9
     return {"workload": f"{w}x{h} u8 synthetic frame, seed {seed}, Sift::new{sargs}", "storage": storage,
@@ -635,7 +637,7 @@ def run_cuda(args, world, rank, local):
     dominant = max(per_run, key=per_run.get)
     peak, peak_kind = measured_peaks()
     octs, S = sargs[1], sargs[2]
-    b_pyr = pyramid_bytes(w, h, octs, S, 4 if args.storage == "f32" else 2)
+    b_pyr = pyramid_bytes(w, h, octs, S, STORED_BYTES[args.storage])
     pyr_gbs = b_pyr / (per_run["pyramid_dog"] / 1e3) / 1e9
     roof_pyr = {"stage": "pyramid_dog", "bound": "hbm", "achieved": pyr_gbs, "peak": peak, "unit": "GB/s",
                 "frac": pyr_gbs / peak, "traffic": traffic_from_profiles(args.workload, "pyramid_dog"),
@@ -708,7 +710,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64", "serve", "match"], default="1080p")
-    ap.add_argument("--storage", choices=["f32", "f16"], default="f32")
+    ap.add_argument("--storage", choices=["f32", "f16", "u8"], default="f32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain section")

@@ -75,13 +75,16 @@ typedef struct {
 } SiftCudaResult;
 
 /* Pyramid storage of the Gaussian levels in device memory. Levels of the
- * reference-compatible pyramid hold u8 integers, so both modes are exact; F16
- * halves the Gaussian bytes. In both modes each level also has a u8 plane,
- * from which the detection forms DoG in f32 where it reads it (no DoG plane
- * is stored). */
+ * reference-compatible pyramid hold u8 integers, so every mode is exact.
+ * Each level has a u8 plane, from which the detection forms DoG in f32 where
+ * it reads it (no DoG plane is stored). U8 stores nothing else: orientation
+ * and descriptors read v / 255 from the u8 planes through the IEEE quotient
+ * table. F32 and F16 also store every level in that type (4 and 2 more bytes
+ * per pixel), which orientation and descriptors then read. */
 typedef enum {
-    SIFT_CUDA_STORAGE_F32 = 0, /* Gaussian levels stored as f32 (v / 255) */
-    SIFT_CUDA_STORAGE_F16 = 1  /* Gaussian levels stored as f16 (v) */
+    SIFT_CUDA_STORAGE_F32 = 0, /* u8 planes + levels stored as f32 (v / 255) */
+    SIFT_CUDA_STORAGE_F16 = 1, /* u8 planes + levels stored as f16 (v) */
+    SIFT_CUDA_STORAGE_U8 = 2   /* u8 planes only */
 } SiftCudaStorage;
 
 typedef struct {

@@ -26,6 +26,7 @@ STATUS = {
 
 STORAGE_F32 = 0
 STORAGE_F16 = 1
+STORAGE_U8 = 2
 
 PIXELS_GRAY8 = 0
 PIXELS_RGB8 = 1

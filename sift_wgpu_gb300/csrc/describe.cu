@@ -37,7 +37,7 @@
 namespace sift {
 namespace {
 
-constexpr int kWarpsPerCta = 8;
+constexpr int kOriWarps = 8;  // orientation: one keypoint per warp
 
 // Work-queue kernels launch more CTAs than fit on the device. A CTA (or an
 // orientation warp) below persist_from takes at most kBudget items and
@@ -49,31 +49,63 @@ constexpr int kOriBudget = 4;   // keypoints per warp
 constexpr int kDescBudget = 2;  // keypoints per CTA
 
 // A Gaussian level pixel as v/255 (get_gauss_pixel_value, src/sift.rs:218-223):
-// f32 levels store it directly, f16 levels store v, divided here (div255: the
-// IEEE quotient, so both storage modes give the same values).
+// f32 levels store it directly, f16 and u8 levels store v, divided here
+// (div255 is the IEEE quotient for every u8 value), so every storage mode
+// reads the same values.
 template <typename T>
-__device__ __forceinline__ float gnorm(const T* p);
+__device__ __forceinline__ float gnorm(const T* p, const float* lut);
 template <>
-__device__ __forceinline__ float gnorm<float>(const float* p) {
+__device__ __forceinline__ float gnorm<float>(const float* p, const float*) {
     return *p;
 }
 template <>
-__device__ __forceinline__ float gnorm<__half>(const __half* p) {
+__device__ __forceinline__ float gnorm<__half>(const __half* p, const float*) {
     return div255(__half2float(*p));
+}
+template <>
+__device__ __forceinline__ float gnorm<uint8_t>(const uint8_t* p, const float*) {
+    return div255(float_of_u8(*p));
+}
+
+// The same pixel as v itself (0..255): f32 levels give it back exactly as
+// fl(fl(v / 255) * 255) (true for every u8 value), f16 and u8 levels store it.
+// The descriptor works in these units: its histogram is L2-normalised, so the
+// factor 255 cancels, and the three storage modes give the same values.
+template <typename T>
+__device__ __forceinline__ float graw(const T* p);
+template <>
+__device__ __forceinline__ float graw<float>(const float* p) {
+    return __fmul_rn(*p, 255.0f);
+}
+template <>
+__device__ __forceinline__ float graw<__half>(const __half* p) {
+    return __half2float(*p);
+}
+template <>
+__device__ __forceinline__ float graw<uint8_t>(const uint8_t* p) {
+    return float_of_u8(*p);
 }
 
 template <typename TG>
 struct GaussPlane {
     const TG* base;
     int pitch, W, H;
+    const float* lut;  // v / 255 (read by the u8 storage mode only)
+    __device__ __forceinline__ float at(const TG* p) const { return gnorm(p, lut); }
     // get_gauss_pixel_value (src/sift.rs:218-223)
     __device__ __forceinline__ float px(int x, int y) const {
         x = clampi(x, 0, W - 1);
         y = clampi(y, 0, H - 1);
-        return gnorm(base + (long long)y * pitch + x);
+        return at(base + (long long)y * pitch + x);
     }
     // the same for coordinates already inside the level
-    __device__ __forceinline__ float px_in(int x, int y) const { return gnorm(base + y * pitch + x); }
+    __device__ __forceinline__ float px_in(int x, int y) const { return at(base + y * pitch + x); }
+    // get_gauss_pixel_value in v units (graw)
+    __device__ __forceinline__ float px_raw(int x, int y) const {
+        x = clampi(x, 0, W - 1);
+        y = clampi(y, 0, H - 1);
+        return graw(base + (long long)y * pitch + x);
+    }
     // get_gauss_pixel_bilinear (src/sift.rs:238-266)
     __device__ __forceinline__ float bilinear(float x, float y) const {
         const float xf = floorf(x), yf = floorf(y);
@@ -91,10 +123,11 @@ struct GaussPlane {
 };
 
 template <typename TG>
-__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const PyramidDev& pyr, int o, int layer) {
+__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const PyramidDev& pyr, int o, int layer,
+                                                    const float* lut) {
     const int li = clampi(layer, 0, pyr.S + 2);
     const OctaveDev& od = pyr.oct[o];
-    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H};
+    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H, lut};
 }
 
 
@@ -118,14 +151,47 @@ __device__ __forceinline__ AxisBins axis_bins() {
                     exact_bin_pos(atan2f(0.0f, -1.0f)), exact_bin_pos(atan2f(-1.0f, 0.0f))};
 }
 
+// One orientation sample (src/sift.rs:640-662) into the lane's column of the
+// bin-major histogram hist[bin][32]: the gradient (gx, gy) at window offset
+// (fdx, fdy), added as +0.0 when the sample lies outside the level (`in`
+// false), which leaves a bin bit-identical.
+__device__ __forceinline__ void ori_add(float gx, float gy, float fdx, float fdy, float inv_wd, bool in,
+                                        float* hist, int lane, const AxisBins& ab) {
+    const float two_pi = 2.0f * kPi;
+    // the hardware square root (within an ulp; the bins are sums whose
+    // order differs from the reference's anyway)
+    const float mag = sqrt_approx(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
+    // exp(-(dx^2 + dy^2) / wd) with the quotient as a product by 1 / wd and
+    // the hardware exponential: a few ulp from expf of the IEEE quotient,
+    // the same order as expf's own distance from the host libm
+    const float wgt = __expf(__fmul_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), inv_wd));
+    // Bin index: from the polynomial atan2 and a multiply by 36 / (2 pi)
+    // (a few ulp from the exact value); axis directions take their exact
+    // position from the table; any other angle within 1e-4 of a bin edge
+    // takes atan2f and the IEEE division, the exact sequence (rare: the
+    // branch no longer splits warps on every flat patch). Away from the
+    // edges all three floor to the same bin.
+    const float pa = atan2_poly(gy, gx);
+    const float pn = pa < 0.0f ? __fadd_rn(pa, two_pi) : pa;
+    float bf = __fmul_rn(pn, (float)kOriBins / two_pi);
+    const bool axis = gx == 0.0f || gy == 0.0f;  // (0, 0): atan2 0, angle 0
+    const float bax = gy == 0.0f ? (gx < 0.0f ? ab.left : ab.right) : (gy > 0.0f ? ab.up : ab.down);
+    bf = axis ? bax : bf;
+    if (!axis && fabsf(__fsub_rn(bf, rintf(bf))) < 1e-4f) bf = exact_bin_pos(atan2f(gy, gx));
+    const int fl = floor_i(bf);
+    const int bin = fl >= kOriBins ? fl - kOriBins : fl;
+    const float v = __fmul_rn(mag, wgt);
+    float* h = hist + bin * 32 + lane;
+    *h = __fadd_rn(*h, in ? v : 0.0f);
+}
+
 // The orientation window of one keypoint (src/sift.rs:640-662), lane-strided:
-// each lane adds into its own column of the bin-major histogram hist[bin][32].
-// Index and rounding arithmetic stays on the FMA pipe and is exact.
+// sample k = lane + 32 j of the (2r+1)^2 window, read from the level (the
+// reads mostly hit L1). Windows at the level's border take the CHECK form.
 template <typename TG, bool CHECK>
 __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, float yo, int r, float wd, float* hist,
                                            int lane, const AxisBins& ab) {
     const float inv_wd = __frcp_rn(wd);
-    const float two_pi = 2.0f * kPi;
     const int side = 2 * r + 1;
     const float side_f = (float)side, r_f = (float)r;
     // Sample k = lane + 32 j of the window (row-major) is (fdx, fdy) =
@@ -149,46 +215,26 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
         }
         const float gx = __fsub_rn(g.px_in(xi + 1, yi), g.px_in(xi - 1, yi));
         const float gy = __fsub_rn(g.px_in(xi, yi + 1), g.px_in(xi, yi - 1));
-        // the hardware square root (within an ulp; the bins are sums whose
-        // order differs from the reference's anyway)
-        const float mag = sqrt_approx(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
-        // exp(-(dx^2 + dy^2) / wd) with the quotient as a product by 1 / wd and
-        // the hardware exponential: a few ulp from expf of the IEEE quotient,
-        // the same order as expf's own distance from the host libm
-        const float wgt = __expf(__fmul_rn(-__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), inv_wd));
-        // Bin index: from the polynomial atan2 and a multiply by 36 / (2 pi)
-        // (a few ulp from the exact value); axis directions take their exact
-        // position from the table; any other angle within 1e-4 of a bin edge
-        // takes atan2f and the IEEE division, the exact sequence (rare: the
-        // branch no longer splits warps on every flat patch). Away from the
-        // edges all three floor to the same bin.
-        const float pa = atan2_poly(gy, gx);
-        const float pn = pa < 0.0f ? __fadd_rn(pa, two_pi) : pa;
-        float bf = __fmul_rn(pn, (float)kOriBins / two_pi);
-        const bool axis = gx == 0.0f || gy == 0.0f;  // (0, 0): atan2 0, angle 0
-        const float bax = gy == 0.0f ? (gx < 0.0f ? ab.left : ab.right) : (gy > 0.0f ? ab.up : ab.down);
-        bf = axis ? bax : bf;
-        if (!axis && fabsf(__fsub_rn(bf, rintf(bf))) < 1e-4f) bf = exact_bin_pos(atan2f(gy, gx));
-        const int fl = floor_i(bf);
-        const int bin = fl >= kOriBins ? fl - kOriBins : fl;
-        const float v = __fmul_rn(mag, wgt);
-        float* h = hist + bin * 32 + lane;
-        *h = __fadd_rn(*h, in ? v : 0.0f);
+        ori_add(gx, gy, fdx, fdy, inv_wd, in, hist, lane, ab);
     }
 }
 
 template <typename TG>
-__global__ void __launch_bounds__(32 * kWarpsPerCta, 5) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
-                                                                   const Keypoint* __restrict__ refined_at,
-                                                                   const uint32_t* __restrict__ keep, uint32_t ncap,
-                                                                   OctCounters* __restrict__ oc,
-                                                                   float* __restrict__ ori_angle,
-                                                                   uint32_t* __restrict__ ori_count,
-                                                                   int persist_from) {
+__global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
+                                                                const float* __restrict__ lut255,
+                                                                const Keypoint* __restrict__ refined_at,
+                                                                const uint32_t* __restrict__ keep, uint32_t ncap,
+                                                                OctCounters* __restrict__ oc,
+                                                                float* __restrict__ ori_angle,
+                                                                uint32_t* __restrict__ ori_count,
+                                                                int persist_from) {
     chain_wait();
-    __shared__ float hist[kWarpsPerCta][kOriBins][32];
-    __shared__ float hs[kWarpsPerCta][kOriBins];
+    __shared__ float hist[kOriWarps][kOriBins][32];
+    __shared__ float hs[kOriWarps][kOriBins];
+    __shared__ float lut[256];
     const int lane = threadIdx.x, wid = threadIdx.y;
+    for (int v = threadIdx.y * 32 + lane; v < 256; v += 32 * kOriWarps) lut[v] = lut255[v];
+    __syncthreads();
     const uint32_t n = min(oc->n_cand, ncap);  // candidate slots; rejected ones get 0 peaks
     const float two_pi = 2.0f * kPi;
     const float bin_w = 2.0f * kPi / (float)kOriBins;
@@ -207,7 +253,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta, 5) k_orientation(const TG* 
         const int o = kp.octave;
         uint32_t cnt = 0;
         if (o >= 0 && o < pyr.num_octaves) {
-            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer);
+            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
             const float scale = __int_as_float((127 + o) << 23);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float so = __fdiv_rn(kp.size, scale);
@@ -354,6 +400,7 @@ constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad
 // per-sample bilinears from the level itself.
 template <typename TG>
 __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
+                                                              const float* __restrict__ lut255,
                                                               const Keypoint* __restrict__ oriented,
                                                               OctCounters* __restrict__ oc,
                                                               float* __restrict__ desc, uint32_t cap,
@@ -371,7 +418,9 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     // integer sums make the order irrelevant.
     __shared__ unsigned int hist[kHistCopies * kHistStride];
     __shared__ float red_lo[kDescThreads / 32], red_hi[kDescThreads / 32];
+    __shared__ float lut[256];
     const int tid = threadIdx.x;
+    for (int v = tid; v < 256; v += kDescThreads) lut[v] = lut255[v];
     const uint32_t base = oc->out_base;
     uint32_t n = oc->n_ori;
     if (base >= cap) n = 0;
@@ -394,7 +443,7 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
         const bool valid = valid_oct && so > 0.0f;
         float inv_fix = 0.0f;
         if (valid) {
-            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer);
+            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float ang = kp.angle;
             const float ca = cosf(ang), sa = sinf(ang);
@@ -408,10 +457,11 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
             const int total = side * side;
             const bool use_grid = rad <= kDescRadGrid;
             const int gs = side + 2;
-            float lo = 1.0f, hi = 0.0f;
+            float lo = 3.0e38f, hi = 0.0f;
             if (use_grid) {
-                // Bilinear samples at the window's integer offsets, straight
-                // from the level (the patch stays in L1). All of them share the
+                // Bilinear samples at the window's integer offsets, in v units
+                // (graw), straight from the level (the patch stays in L1). All
+                // of them share the
                 // fraction of (xo, yo): the reference's sample positions xo + i
                 // differ from it only by the rounding of that sum. Clamped
                 // reads (get_gauss_pixel_value) only for windows at the border.
@@ -434,14 +484,14 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                         const int qx = t - sy * gs, qy0 = 4 * sy;
                         const int nr = min(4, gs - qy0);
                         const TG* pp = org + qy0 * g.pitch + qx;
-                        float a0 = gnorm(pp), a1 = gnorm(pp + 1);
+                        float a0 = graw(pp), a1 = graw(pp + 1);
                         float rp = fmaf(fdx, a1 - a0, a0);
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             if (j < nr) {
                                 pp += g.pitch;
-                                a0 = gnorm(pp);
-                                a1 = gnorm(pp + 1);
+                                a0 = graw(pp);
+                                a1 = graw(pp + 1);
                                 const float rn = fmaf(fdx, a1 - a0, a0);
                                 const float b = fmaf(fdy, rn - rp, rp);
                                 grid[(qy0 + j) * gs + qx] = b;
@@ -456,8 +506,8 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                     for (int q = tid; q < gs * gs; q += kDescThreads, qf += (float)kDescThreads) {
                         const int qy = floor_i((qf + 0.5f) * inv_gs);
                         const int qx = q - qy * gs;
-                        const float q11 = g.px(px0 + qx, py0 + qy), q21 = g.px(px0 + qx + 1, py0 + qy);
-                        const float q12 = g.px(px0 + qx, py0 + qy + 1), q22 = g.px(px0 + qx + 1, py0 + qy + 1);
+                        const float q11 = g.px_raw(px0 + qx, py0 + qy), q21 = g.px_raw(px0 + qx + 1, py0 + qy);
+                        const float q12 = g.px_raw(px0 + qx, py0 + qy + 1), q22 = g.px_raw(px0 + qx + 1, py0 + qy + 1);
                         // the reference's bilinear blend as two lerps (within the
                         // descriptor tolerance)
                         const float r0 = fmaf(fdx, q21 - q11, q11), r1 = fmaf(fdx, q22 - q12, q12);
@@ -636,11 +686,11 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
 }  // namespace
 
 template <typename TG>
-int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
-                       uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,
-                       int persist_ctas, cudaStream_t st) {
-    if (launch_chained(k_orientation<TG>, grid, dim3(32, kWarpsPerCta), 0, st, arena, pyr, refined_at, keep, ncap, oc,
-                       ori_angle, ori_count, std::max(grid - persist_ctas, 0)) != cudaSuccess)
+int launch_orientation(const TG* arena, const PyramidDev& pyr, const float* lut255, const Keypoint* refined_at,
+                       const uint32_t* keep, uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count,
+                       int grid, int persist_ctas, cudaStream_t st) {
+    if (launch_chained(k_orientation<TG>, grid, dim3(32, kOriWarps), 0, st, arena, pyr, lut255, refined_at, keep, ncap,
+                       oc, ori_angle, ori_count, std::max(grid - persist_ctas, 0)) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -655,22 +705,24 @@ int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counter
 }
 
 template <typename TG>
-int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
-                      uint32_t cap, float* hdesc, uint32_t hcap, int grid, int persist_ctas, cudaStream_t st) {
+int launch_descriptor(const TG* arena, const PyramidDev& pyr, const float* lut255, const Keypoint* oriented,
+                      OctCounters* oc, float* desc, uint32_t cap, float* hdesc, uint32_t hcap, int grid,
+                      int persist_ctas, cudaStream_t st) {
     if (!hdesc) hcap = 0;
-    if (launch_chained(k_descriptor<TG>, grid, kDescThreads, 0, st, arena, pyr, oriented, oc, desc, cap, hdesc, hcap,
-                       std::max(grid - persist_ctas, 0)) != cudaSuccess)
+    if (launch_chained(k_descriptor<TG>, grid, kDescThreads, 0, st, arena, pyr, lut255, oriented, oc, desc, cap, hdesc,
+                       hcap, std::max(grid - persist_ctas, 0)) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-template int launch_orientation<float>(const float*, const PyramidDev&, const Keypoint*, const uint32_t*, uint32_t,
-                                       OctCounters*, float*, uint32_t*, int, int, cudaStream_t);
-template int launch_orientation<__half>(const __half*, const PyramidDev&, const Keypoint*, const uint32_t*, uint32_t,
-                                        OctCounters*, float*, uint32_t*, int, int, cudaStream_t);
-template int launch_descriptor<float>(const float*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
-                                      uint32_t, float*, uint32_t, int, int, cudaStream_t);
-template int launch_descriptor<__half>(const __half*, const PyramidDev&, const Keypoint*, OctCounters*, float*,
-                                      uint32_t, float*, uint32_t, int, int, cudaStream_t);
+#define SIFT_INST(TG)                                                                                              \
+    template int launch_orientation<TG>(const TG*, const PyramidDev&, const float*, const Keypoint*, const uint32_t*, \
+                                        uint32_t, OctCounters*, float*, uint32_t*, int, int, cudaStream_t);        \
+    template int launch_descriptor<TG>(const TG*, const PyramidDev&, const float*, const Keypoint*, OctCounters*,  \
+                                       float*, uint32_t, float*, uint32_t, int, int, cudaStream_t);
+SIFT_INST(float)
+SIFT_INST(__half)
+SIFT_INST(uint8_t)
+#undef SIFT_INST
 
 }  // namespace sift

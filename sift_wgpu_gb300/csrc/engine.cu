@@ -92,7 +92,7 @@ int sift_cuda_create(const SiftCudaParams* params, const SiftCudaOptions* opts, 
     SiftCudaOptions o;
     sift_cuda_options_default(&o);
     if (opts) o = *opts;
-    if (o.storage != SIFT_CUDA_STORAGE_F32 && o.storage != SIFT_CUDA_STORAGE_F16)
+    if (o.storage != SIFT_CUDA_STORAGE_F32 && o.storage != SIFT_CUDA_STORAGE_F16 && o.storage != SIFT_CUDA_STORAGE_U8)
         return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "unknown storage mode");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -364,15 +364,19 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
             const sift::OctaveDev& od = g.oct[o];
             if (od.W == 0 || od.H == 0) continue;
             for (int l = 0; l < L; ++l) {
-                const size_t es = e.g_elem_size();
-                const char* src = (const char*)e.d_G.p + (size_t)(od.g_off + (long long)l * od.plane) * es;
+                // the stored levels (the u8 planes themselves in u8 storage)
+                const size_t es = e.u8() ? 1 : e.g_elem_size();
+                const char* src = e.u8() ? (const char*)e.d_U.p + (size_t)(od.u_off + (long long)l * od.plane)
+                                         : (const char*)e.d_G.p + (size_t)(od.g_off + (long long)l * od.plane) * es;
                 buf.resize((size_t)od.W * od.H * es);
                 if (cudaMemcpy2D(buf.data(), (size_t)od.W * es, src, (size_t)od.pitch * es, (size_t)od.W * es, od.H,
                                  cudaMemcpyDeviceToHost) != cudaSuccess)
                     return sift::cuda_fail(cudaGetLastError(), "D2H stage");
                 const size_t npx = (size_t)od.W * od.H;
                 for (size_t q = 0; q < npx && pos < capacity; ++q, ++pos) {
-                    if (es == 4) {
+                    if (es == 1) {
+                        ((uint8_t*)out)[pos] = buf[q];
+                    } else if (es == 4) {
                         ((uint8_t*)out)[pos] = (uint8_t)std::lrint(((const float*)buf.data())[q] * 255.0f);
                     } else {
                         ((uint8_t*)out)[pos] = (uint8_t)__half2float(((const __half*)buf.data())[q]);

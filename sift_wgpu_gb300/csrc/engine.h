@@ -73,15 +73,16 @@ int launch_refine(const uint8_t* u8arena, const float* lut255, const PyramidDev&
                   float contrast, float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep,
                   uint32_t cap, OctCounters* oc, cudaStream_t st);
 template <typename TG>
-int launch_orientation(const TG* arena, const PyramidDev& pyr, const Keypoint* refined_at, const uint32_t* keep,
-                       uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count, int grid,
-                       int persist_ctas, cudaStream_t st);
+int launch_orientation(const TG* arena, const PyramidDev& pyr, const float* lut255, const Keypoint* refined_at,
+                       const uint32_t* keep, uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count,
+                       int grid, int persist_ctas, cudaStream_t st);
 int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counters* ctr, const float* ori_angle,
                        const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
                        cudaStream_t st);
 template <typename TG>
-int launch_descriptor(const TG* arena, const PyramidDev& pyr, const Keypoint* oriented, OctCounters* oc, float* desc,
-                      uint32_t cap, float* hdesc, uint32_t hcap, int grid, int persist_ctas, cudaStream_t st);
+int launch_descriptor(const TG* arena, const PyramidDev& pyr, const float* lut255, const Keypoint* oriented,
+                      OctCounters* oc, float* desc, uint32_t cap, float* hdesc, uint32_t hcap, int grid,
+                      int persist_ctas, cudaStream_t st);
 // Error reporting (engine.cu): the calling thread's sift_cuda_last_error.
 extern thread_local std::string g_last_error;
 int fail(int code, const std::string& msg);
@@ -329,6 +330,7 @@ struct Engine {
     int priority = 0;
 
     bool f16() const { return opt.storage == SIFT_CUDA_STORAGE_F16; }
+    bool u8() const { return opt.storage == SIFT_CUDA_STORAGE_U8; }
 
     // Device bytes held by the engine's arenas and lists.
     size_t device_bytes() const {
@@ -339,7 +341,8 @@ struct Engine {
             t += m->bytes;
         return t;
     }
-    size_t g_elem_size() const { return f16() ? 2 : 4; }
+    // bytes of a stored level value; u8 storage stores nothing beyond the u8 planes
+    size_t g_elem_size() const { return u8() ? 0 : (f16() ? 2 : 4); }
 
     int set_device() {
         CK(cudaSetDevice(opt.device), "cudaSetDevice");
@@ -551,7 +554,7 @@ struct Engine {
     template <typename TG>
     int enqueue_t(const uint8_t* img, long long stride, bool with_desc, bool dag, bool exp) {
         const int O = pyr.num_octaves, S = pyr.S;
-        TG* G = d_G.as<TG>();
+        TG* G = u8() ? (TG*)d_U.p : d_G.as<TG>();  // u8 storage: the levels are the u8 planes
         const float* wts = d_wts.as<float>();
         const float* lut = wts + lut_off;
         uint8_t* U = d_U.as<uint8_t>();
@@ -631,7 +634,7 @@ struct Engine {
             // one warp-item per 8 candidate slots, 4 per warp; the last
             // 152 x ori_ctas_per_sm CTAs drain whatever is left
             const int grid = (int)std::max<uint32_t>(cap_c[o] / 64, 32);
-            if (ok(launch_orientation<TG>(G, pyr, d_refined_at.as<Keypoint>() + cb[o], d_keep.as<uint32_t>() + cb[o],
+            if (ok(launch_orientation<TG>(G, pyr, lut, d_refined_at.as<Keypoint>() + cb[o], d_keep.as<uint32_t>() + cb[o],
                                           cap_c[o], oc, d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
                                           d_ori_count.as<uint32_t>() + cb[o], grid, 152 * tune.ori_ctas_per_sm, q)))
                 return cuda_fail(cudaGetLastError(), "orientation");
@@ -659,7 +662,7 @@ struct Engine {
             const int grid = (int)std::max<uint32_t>(cap_c[o] / 16, 64);
             // host calls: descriptors below cap_x go straight into the mapped
             // export buffer while the stage runs, the rest to d_desc
-            if (ok(launch_descriptor<TG>(G, pyr, d_oriented.as<Keypoint>(), &ctr->oct[o], d_desc.as<float>(), cap_ori,
+            if (ok(launch_descriptor<TG>(G, pyr, lut, d_oriented.as<Keypoint>(), &ctr->oct[o], d_desc.as<float>(), cap_ori,
                                          exp ? hx_ddesc : nullptr, exp ? cap_x : 0u, grid,
                                          152 * tune.desc_ctas_per_sm, q)))
                 return cuda_fail(cudaGetLastError(), "descriptor");
@@ -703,12 +706,22 @@ struct Engine {
             }
             for (int o = 0; o < O_used; ++o) CK(cudaStreamWaitEvent(st, ev_done[o], 0), "stream wait");
         } else {
+            // Stage by stage. Inside the pyramid stage, as in the graph, the
+            // levels above S of octave o (which the next octave does not
+            // need) run on the octave's stream beside the next octave's
+            // chain; the stage ends when every level exists.
             for (int o = 0; o < O_used; ++o) {
-                for (int s = 1; s < S + 3; ++s)
+                for (int s = 1; s <= S; ++s)
                     if (int rc = level(o, s, st, d_tmp.as<uint8_t>())) return rc;
+                CK(cudaEventRecord(ev_level[o], st), "event record");
+                CK(cudaStreamWaitEvent(st_oct[o], ev_level[o], 0), "stream wait");
+                for (int s = S + 1; s < S + 3; ++s)
+                    if (int rc = level(o, s, st_oct[o], d_tmpo.as<uint8_t>() + tb[o])) return rc;
+                CK(cudaEventRecord(ev_done[o], st_oct[o]), "event record");
                 if (o + 1 < O_used)
                     if (int rc = lanczos(o)) return rc;
             }
+            for (int o = 0; o < O_used; ++o) CK(cudaStreamWaitEvent(st, ev_done[o], 0), "stream wait");
             mark(&run_ev);
             for (int o = 0; o < O_used; ++o)
                 if (int rc = detect(o, st)) return rc;
@@ -738,6 +751,7 @@ struct Engine {
     }
 
     int enqueue(const uint8_t* img, long long stride, bool with_desc, bool dag, bool exp) {
+        if (u8()) return enqueue_t<uint8_t>(img, stride, with_desc, dag, exp);
         return f16() ? enqueue_t<__half>(img, stride, with_desc, dag, exp)
                      : enqueue_t<float>(img, stride, with_desc, dag, exp);
     }

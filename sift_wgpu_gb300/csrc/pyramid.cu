@@ -23,6 +23,8 @@
 //   k_blur_rows    horizontal pass for larger radii, one row per CTA. u8 out.
 //   k_blur_cols    vertical pass for larger radii on a 32 x 64 tile.
 //   k_lanczos_fused  the 2x Lanczos3 resize between octaves, both passes.
+#include <type_traits>
+
 #include "sift_internal.cuh"
 
 namespace sift {
@@ -32,7 +34,8 @@ namespace {
 __device__ __forceinline__ float norm255(int v) { return __fdiv_rn((float)v, 255.0f); }
 
 // Level storage: f32 holds v/255 (the reference's convert_u8_to_f32_gray
-// value, src/sift.rs:92-101), f16 holds v (v/255 is not exact in f16).
+// value, src/sift.rs:92-101), f16 holds v (v/255 is not exact in f16), u8
+// storage stores nothing beyond the u8 plane.
 template <typename T>
 __device__ __forceinline__ void store_level(T* p, int v, float vn);
 template <>
@@ -43,6 +46,9 @@ template <>
 __device__ __forceinline__ void store_level<__half>(__half* p, int v, float) {
     *p = __int2half_rn(v);
 }
+// u8 storage: the level is its u8 plane, which every kernel writes anyway
+template <>
+__device__ __forceinline__ void store_level<uint8_t>(uint8_t*, int, float) {}
 
 __device__ __forceinline__ void unpack16(const uint4 b, float* v) {
     const unsigned w[4] = {b.x, b.y, b.z, b.w};
@@ -302,6 +308,8 @@ __device__ __forceinline__ void store_level4<float>(float* p, const int v[4], co
     *reinterpret_cast<float4*>(p) = make_float4(lut[v[0]], lut[v[1]], lut[v[2]], lut[v[3]]);
 }
 template <>
+__device__ __forceinline__ void store_level4<uint8_t>(uint8_t*, const int*, const float*) {}
+template <>
 __device__ __forceinline__ void store_level4<__half>(__half* p, const int v[4], const float*) {
     const __half2 a = __halves2half2(__int2half_rn(v[0]), __int2half_rn(v[1]));
     const __half2 b = __halves2half2(__int2half_rn(v[2]), __int2half_rn(v[3]));
@@ -458,7 +466,7 @@ __global__ void k_copy_level(const TG* __restrict__ prev, const uint8_t* __restr
     int y = blockIdx.y;
     if (x >= W) return;
     long long o = (long long)y * pitch + x;
-    out[o] = prev[o];
+    if constexpr (!std::is_same<TG, uint8_t>::value) out[o] = prev[o];  // u8 storage: out is out_u8
     out_u8[o] = prev_u8[o];
 }
 
@@ -740,6 +748,7 @@ int lanczos_fused_tile() { return kLzT; }
                                     cudaStream_t, bool, int*);
 SIFT_INST(float)
 SIFT_INST(__half)
+SIFT_INST(uint8_t)
 #undef SIFT_INST
 
 }  // namespace sift

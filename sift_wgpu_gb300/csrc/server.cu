@@ -57,7 +57,7 @@ double now_s() {
 // Engine::ensure_lists), used to admit a new slot before it exists.
 uint64_t footprint_estimate(const SiftCudaParams& p, int storage, uint32_t w, uint32_t h) {
     const int O = (int)p.num_octaves, S = (int)p.num_intervals;
-    const size_t es = storage == SIFT_CUDA_STORAGE_F16 ? 2 : 4;
+    const size_t es = storage == SIFT_CUDA_STORAGE_U8 ? 0 : (storage == SIFT_CUDA_STORAGE_F16 ? 2 : 4);
     uint64_t g = 0, u = 0, tmpb = 0, tmpo = 0, lt = 0, words = 0, caps = 0;
     uint32_t ow = w, oh = h;
     for (int o = 0; o < O; ++o) {

@@ -22,7 +22,7 @@ from . import _capi
 from ._capi import DESC_LEN, KEYPOINT_DTYPE
 from .sift import Sift, _as_gray
 
-_STORAGE = {"f32": _capi.STORAGE_F32, "f16": _capi.STORAGE_F16}
+_STORAGE = {"f32": _capi.STORAGE_F32, "f16": _capi.STORAGE_F16, "u8": _capi.STORAGE_U8}
 
 
 @dataclass

@@ -115,7 +115,7 @@ class Engine:
         opts = _capi.Options()
         L.sift_cuda_options_default(C.byref(opts))
         opts.device = device
-        opts.storage = {"f32": _capi.STORAGE_F32, "f16": _capi.STORAGE_F16}[storage]
+        opts.storage = {"f32": _capi.STORAGE_F32, "f16": _capi.STORAGE_F16, "u8": _capi.STORAGE_U8}[storage]
         h = C.c_void_p()
         _capi.check(L.sift_cuda_create(C.byref(p), C.byref(opts), C.byref(h)))
         self._h = h

@@ -14,25 +14,37 @@ import bench  # noqa: E402
 
 
 def pyramid_bytes_restated(w, h, octaves, S, b):
-    """u8 input once; octave o >= 1 reads its base (b bytes per value); every
-    octave writes S+3 levels at b bytes plus their u8 planes."""
+    """u8 input once; octave o >= 1 reads its base as its u8 plane; every
+    octave writes S+3 levels as u8 planes plus b bytes each (f32 4, f16 2,
+    u8 storage 0)."""
     total, ow, oh = w * h, w, h
     for o in range(octaves):
         n = ow * oh
-        total += (n * b if o else 0) + n * (S + 3) * b + n * (S + 3)
+        total += (n if o else 0) + n * (S + 3) * b + n * (S + 3)
         ow, oh = ow // 2, oh // 2
     return total
 
 
 @pytest.mark.parametrize("w,h,octs,b", [(1920, 1080, 4, 4), (4096, 4096, 6, 4), (4096, 4096, 6, 2), (512, 512, 4, 4),
-                                        (333, 217, 4, 4)])
+                                        (333, 217, 4, 4), (4096, 4096, 6, 0)])
 def test_pyramid_bytes(w, h, octs, b):
     assert bench.pyramid_bytes(w, h, octs, 3, b) == pyramid_bytes_restated(w, h, octs, 3, b)
 
 
 def test_pyramid_bytes_headline_values():
-    assert bench.pyramid_bytes(1920, 1080, 4, 3, 4) == 87_415_200
-    assert bench.pyramid_bytes(4096, 4096, 6, 3, 4) == 710_049_792
+    assert bench.pyramid_bytes(1920, 1080, 4, 3, 4) == 85_374_000
+    assert bench.pyramid_bytes(4096, 4096, 6, 3, 4) == 693_288_960
+    assert bench.pyramid_bytes(4096, 4096, 6, 3, 0) == 156_549_120
+
+
+def test_fp32_ops_and_radii():
+    """The blur radii follow the reference's 2^o-scaled increments, and the
+    operation count is two per tap."""
+    r0, radii = bench.blur_radii(6, 3)
+    assert r0 == 4 and radii[0] == [3, 4, 4, 5, 7] and radii[5] == [79, 99, 125, 157, 198]
+    n = 512 * 512
+    taps = n * 2 * (9 + 7 + 9 + 9 + 11 + 15)
+    assert bench.pyramid_fp32_ops(512, 512, 1, 3) == 2 * taps
 
 
 class _DoneProc:

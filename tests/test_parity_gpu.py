@@ -157,16 +157,22 @@ def test_strided_input_and_determinism(sgb):
     assert d1.tobytes() == d2.tobytes() == d3.tobytes()
 
 
-def test_f16_storage_is_exact(sgb):
-    """u8-valued levels are exact in f16 and both storage modes form DoG from
-    the same u8 planes, so the f16 pyramid gives identical output."""
+@pytest.mark.parametrize("storage", ["f16", "u8"])
+def test_other_storage_modes_are_exact(sgb, storage):
+    """u8-valued levels are exact in f16 and in u8 (read as v / 255 through
+    the IEEE quotient table), and every mode forms DoG from the same u8
+    planes, so f16 and u8 storage give the f32 mode's output bit for bit,
+    pyramid included."""
     args = (1.6, 4, 3, 0.5, 0.04, 10.0)
     img = image(sgb, 1920, 1080, 1)
-    k32, d32 = engine_for(sgb, args).detect_and_compute(img)
-    e16 = engine_for(sgb, args, "f16")
-    k16, d16 = e16.detect_and_compute(img)
-    assert k16.tobytes() == k32.tobytes()
-    assert d16.tobytes() == d32.tobytes()
+    e32 = engine_for(sgb, args)
+    k32, d32 = e32.detect_and_compute(img)
+    p32 = e32.debug_stage(sgb.STAGE_PYRAMID)
+    e = engine_for(sgb, args, storage)
+    k, d = e.detect_and_compute(img)
+    assert k.tobytes() == k32.tobytes()
+    assert d.tobytes() == d32.tobytes()
+    assert np.array_equal(e.debug_stage(sgb.STAGE_PYRAMID), p32)
 
 
 def test_high_contrast_threshold(sgb):
@@ -199,7 +205,7 @@ def test_sift_api_drop_in(sgb):
 
 def test_large_6_octave_properties(sgb):
     """4096 x 4096, Sift::new(1.6, 6, 3, 0.5, 0.04, 10.0): size-independent
-    properties at the full size (determinism, f16 == f32, unit-norm
+    properties at the full size (determinism, f16 == u8 == f32, unit-norm
     descriptors, keypoints inside the image)."""
     args = (1.6, 6, 3, 0.5, 0.04, 10.0)
     img = image(sgb, 4096, 4096, 3)
@@ -211,8 +217,9 @@ def test_large_6_octave_properties(sgb):
     n = np.linalg.norm(d1, axis=1)
     assert np.all((np.abs(n - 1) < 1e-4) | (n == 0))
     assert np.all((k1["x"] >= -1) & (k1["x"] <= 4097) & (k1["y"] >= -1) & (k1["y"] <= 4097))
-    k16, d16 = engine_for(sgb, args, "f16").detect_and_compute(img)
-    assert k16.tobytes() == k1.tobytes() and d16.tobytes() == d1.tobytes()
+    for storage in ("f16", "u8"):
+        ks, ds = engine_for(sgb, args, storage).detect_and_compute(img)
+        assert ks.tobytes() == k1.tobytes() and ds.tobytes() == d1.tobytes(), storage
 
 
 def test_all_call_forms_agree(sgb):
