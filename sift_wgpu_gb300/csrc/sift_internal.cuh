@@ -157,9 +157,10 @@ __device__ __forceinline__ float rem_euclid_2b(float a, float b) {
 
 // atan2 for the descriptor's gradient angles, written for this engine:
 // octant reduction to a = min(|x|,|y|) / max(|x|,|y|) in [0, 1], then
-// atan(a) = a * P(a^2) with a degree-7 polynomial fitted by iteratively
-// reweighted least squares on [0, 1] (relative error 1e-7 in f64, under 3 ulp
-// evaluated in f32), then the octant fix-ups. atan2(0, 0) = 0. Used where the
+// atan(a) = a * P(a^2) with P of degree 7, minimax in relative error on
+// [0, 1] (Lawson's reweighted least squares; tests/golden/fit_atan2.py makes
+// the coefficients; 2.5e-7 relative error evaluated in f32), then the octant
+// fix-ups: within 4 ulp of atan2f (tests/test_atan2_gpu.py). atan2(0, 0) = 0. Used where the
 // angle is interpolated linearly (descriptor bins), and by the orientation
 // histogram, whose bins are a hard floor, only away from the bin edges.
 __device__ __forceinline__ float atan2_poly(float y, float x) {
@@ -167,12 +168,12 @@ __device__ __forceinline__ float atan2_poly(float y, float x) {
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
     const float a = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
     const float t = a * a;
-    float p = -0.004693260882049799f;
-    p = fmaf(p, t, 0.024252355098724365f);
-    p = fmaf(p, t, -0.05948633328080177f);
-    p = fmaf(p, t, 0.0991428941488266f);
-    p = fmaf(p, t, -0.14019480347633362f);
-    p = fmaf(p, t, 0.19969724118709564f);
+    float p = -0.004693340510129929f;
+    p = fmaf(p, t, 0.024252643808722496f);
+    p = fmaf(p, t, -0.0594867542386055f);
+    p = fmaf(p, t, 0.09914319962263107f);
+    p = fmaf(p, t, -0.14019492268562317f);
+    p = fmaf(p, t, 0.19969725608825684f);
     p = fmaf(p, t, -0.33331990242004395f);
     p = fmaf(p, t, 0.9999998807907104f);
     float r = p * a;
@@ -182,18 +183,18 @@ __device__ __forceinline__ float atan2_poly(float y, float x) {
 }
 
 // atan2(y, x) in units of 45-degree bins (pi/4 = 1), in [-4, 4]: a = min/max
-// of |x|, |y| and an odd degree-9 polynomial in a fitted here to
-// atan(a) * 4/pi on [0, 1] (least squares reweighted towards the minimax
-// error, max error 1.5e-5 bin), then the octant fix-ups. For sums that are
+// of |x|, |y| and an odd degree-9 polynomial a * P(a^2), minimax in absolute
+// error against atan(a) * 4/pi on [0, 1] (tests/golden/fit_atan2.py; max
+// error 1.5e-5 bin), then the octant fix-ups. For sums that are
 // interpolated linearly into bins (the descriptor), not for exact angles.
 __device__ __forceinline__ float atan2_bins(float y, float x) {
     const float ax = fabsf(x), ay = fabsf(y);
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
     const float a = mx > 0.0f ? __fdividef(mn, mx) : 0.0f;
     const float t = a * a;
-    float p = 0.02654077112674713f;
-    p = fmaf(p, t, -0.10842433571815491f);
-    p = fmaf(p, t, 0.2293858826160431f);
+    float p = 0.02654082328081131f;
+    p = fmaf(p, t, -0.10842443257570267f);
+    p = fmaf(p, t, 0.22938594222068787f);
     p = fmaf(p, t, -0.4205571115016937f);
     p = fmaf(p, t, 1.2730693817138672f);
     float r = p * a;

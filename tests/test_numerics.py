@@ -34,3 +34,23 @@ def test_div255_is_the_ieee_division():
         q = round_f32(v * r)
         e = round_f32(-q * 255 + v)
         assert round_f32(e * r + q) == round_f32(Fraction(v, 255)), v
+
+
+def test_arctangent_coefficients_are_the_fits():
+    """The coefficients in sift_internal.cuh are what tests/golden/fit_atan2.py
+    makes, and their f32 errors on [0, 1] are the ones the comments state."""
+    import re
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    sys.path.insert(0, str(root / "tests" / "golden"))
+    import fit_atan2
+    src = (root / "sift_wgpu_gb300" / "csrc" / "sift_internal.cuh").read_text()
+    c = fit_atan2.coefficients()
+    for name in ("atan2_poly", "atan2_bins"):
+        body = src[src.index(f"float {name}(float y, float x)"):]
+        body = body[:body.index("float r = p * a;")]
+        got = [float(v) for v in re.findall(r"(-?\d+\.\d+(?:e-?\d+)?)f", body.split("float p = ", 1)[1])]
+        assert got == c[name][::-1], name
+    e = fit_atan2.max_errors(c)
+    assert e["atan2_poly_rel"] < 3.0e-7 and e["atan2_bins_abs_bins"] < 1.5e-5, e
