@@ -249,10 +249,14 @@ int sift_cuda_match(SiftCudaEngine* engine, const float* query, uint32_t n_query
     if (sift::launch_match(e.d_mq.as<float>(), n_query, e.d_mt.as<float>(), n_train, e.d_mo.as<SiftCudaMatch>(),
                            e.d_ms.p, st))
         return sift::cuda_fail(cudaGetLastError(), "match");
+    uint32_t err = 0;
     if (cudaMemcpyAsync(out, e.d_mo.p, (size_t)n_query * sizeof(SiftCudaMatch), cudaMemcpyDeviceToHost, st) !=
             cudaSuccess ||
+        cudaMemcpyAsync(&err, sift::match_error_word(e.d_ms.p, n_query, n_train), sizeof(err), cudaMemcpyDeviceToHost,
+                        st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return sift::cuda_fail(cudaGetLastError(), "match results");
+    if (err) return sift::fail(SIFT_CUDA_ERR_CUDA, "matching: a tensor-core pipeline wait ran out (no results)");
     return 0;
 }
 

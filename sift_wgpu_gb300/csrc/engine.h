@@ -59,6 +59,7 @@ int launch_export(const Counters* ctr, const Keypoint* kps, Counters* hctr, Keyp
 int launch_draw_keypoints(const uint8_t* d_gray, int stride, const Keypoint* d_kps, uint32_t n, uint8_t* d_rgb,
                           int pitch, int W, int H, uint8_t r, uint8_t g, uint8_t b, cudaStream_t st);
 size_t match_scratch_bytes(uint32_t nq, uint32_t nt);
+const uint32_t* match_error_word(const void* scratch, uint32_t nq, uint32_t nt);
 int launch_match(const float* d_q, uint32_t nq, const float* d_t, uint32_t nt, SiftCudaMatch* d_out, void* scratch,
                  cudaStream_t st);
 int launch_to_luma(int format, const uint8_t* px, long long stride, int W, int H, uint8_t* out, long long out_pitch,

@@ -3,13 +3,15 @@
 // input of Lowe's ratio test. Not part of the reference crate; it consumes
 // the 128-float descriptors that detect_and_compute returns.
 //
-// Squared distances are |q|^2 + |t|^2 - 2 q.t. A 128-query tile stays in
-// shared memory while 64-descriptor train tiles stream through it; TF32
-// tensor-core products pick each query's 4 best candidates per train chunk,
-// which are re-ranked with exact f32 dot products. Work items are (query
-// tile, train chunk) pairs taken from an atomic queue by a grid of one wave of
-// CTAs; a second kernel folds the chunks. Ties go to the lower train index, so
-// the result does not depend on the chunking or the order items are taken in.
+// Squared distances are |q|^2 + |t|^2 - 2 q.t. The products q.t run on the
+// 5th-generation tensor cores (tcgen05, TF32 operands, f32 accumulators in
+// tensor memory) over TMA-staged 128-descriptor tiles; they only select each
+// query's 4 best candidates per train chunk, which are re-ranked with exact
+// f32 dot products. (query tile, train chunk) items are CTAs; a second kernel
+// folds the chunks. Ties go to the lower train index, so the result does not
+// depend on the chunking.
+#include <cuda.h>
+
 #include <algorithm>
 
 #include "sift_internal.cuh"
@@ -17,7 +19,6 @@
 namespace sift {
 namespace {
 
-constexpr int kMT = 64;  // train descriptors per tile (the chunk unit)
 constexpr int kD = kDescLen;
 
 struct Best2 {
@@ -59,9 +60,13 @@ __device__ __forceinline__ Best2 fold(const Best2& a, const Best2& b) {
 }
 
 // Squared norm of each descriptor row, summed in index order.
-__global__ void k_sq_norms(const float* __restrict__ x, uint32_t n, float* __restrict__ out) {
+__global__ void k_sq_norms(const float* __restrict__ x, uint32_t n, float* __restrict__ out, uint32_t n_out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n_out) return;
+    if (i >= n) {  // padding: never a candidate
+        out[i] = INFINITY;
+        return;
+    }
     const float4* r = reinterpret_cast<const float4*>(x + (size_t)i * kD);
     float s = 0.0f;
 #pragma unroll 8
@@ -75,233 +80,317 @@ __global__ void k_sq_norms(const float* __restrict__ x, uint32_t n, float* __res
     out[i] = s;
 }
 
-// The dot products of a 128-query x 64-train tile come from
-// TF32 mma.sync (m16n8k8, f32 accumulate; 8 warps of 32 x 32): approximate
-// squared distances that only select each query's 4 best candidates of the
-// chunk (a running list per row behind a threshold test). The candidates are
-// then re-ranked with exact f32 distances computed as in the f32 kernel (the
-// dot product as an FMA chain in index order), so the returned best two are
-// the f32 result unless the TF32 error (relative ~1e-3 on a dot product)
-// pushes a true best-two outside the 4 candidates.
-constexpr int kTQ = 128, kTT = 64;  // CTA tile: queries x train
-constexpr int kTS = kD + 4;         // shared row stride (floats): fragment loads in 32 banks
-constexpr int kTThreads = 256;      // warps 4 (queries) x 2 (train), 32 x 32 each
-constexpr int kTCtasPerSm = 2;      // 101 KB of shared memory per CTA
 constexpr int kCand = 4;
 
-struct Cand4 {
-    float d[kCand];
-    int i[kCand];
-};
+// ---------------------------------------------------------------------------
+// 5th-generation tensor cores (tcgen05) with TMA-staged operands.
+//
+// One CTA per (query tile, train chunk) item. The query tile (128 rows x 128
+// floats, 64 KB) and the train tiles (128 rows, double-buffered) are loaded
+// by TMA (cp.async.bulk.tensor, 128-byte swizzle: four 32-float boxes per
+// tile) into the K-major layout the MMA reads. One thread issues
+// tcgen05.mma.kind::tf32 (M = 128 queries, N = 128 train, K = 8 per
+// instruction, 16 per tile) into one of two 128-column f32 accumulators in
+// tensor memory, so the epilogue of one tile overlaps the products of the
+// next. The epilogue warps own the accumulator's lanes: a thread reads one
+// query row's products of half the tile with tcgen05.ld, ranks the columns by
+// |t|^2 - 2 q.t and keeps the row's 4 best candidates of the chunk; the two
+// halves' lists are merged and re-ranked with exact f32 dot products.
+//
+// Roles: warps 0-7 epilogue (warp w: tensor-memory lanes 32 (w % 4) .., half
+// w / 4 of each tile's columns), warp 8 TMA producer, warp 9 MMA issuer and
+// tensor-memory owner. Every mbarrier
+// wait is bounded; a wait that runs out sets the error word and the CTA
+// leaves through the same exit (tensor memory is always freed).
+constexpr int kUM = 128, kUN = 128;                   // MMA M (queries) and N (train rows per tile)
+constexpr int kUThreads = 320;  // warps 0-7 epilogue, 8 TMA, 9 MMA
+constexpr uint32_t kUAtom = kUM * 128;                // one 32-float K slice of a 128-row tile: 16 KB
+constexpr uint32_t kUTile = 4 * kUAtom;               // 64 KB
+constexpr uint32_t kUSmem = 3 * kUTile + 8192 + 1024;  // query tile, two train stages, barriers and
+                                                       // epilogue buffers, alignment
+constexpr uint32_t kUTmemCols = 2 * kUN;
+constexpr uint32_t kUSpin = 1u << 26;                 // bounded waits (~seconds)
 
-__device__ __forceinline__ void cand_init(Cand4& c) {
-#pragma unroll
-    for (int k = 0; k < kCand; ++k) {
-        c.d[k] = INFINITY;
-        c.i[k] = -1;
-    }
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
 }
-
-// sorted insertion (ties to the lower index); the caller tests d < c.d[3]
-__device__ __forceinline__ void cand_push(Cand4& c, float d, int i) {
-#pragma unroll
-    for (int k = kCand - 1; k >= 0; --k) {
-        const bool above = k > 0 && before(d, i, c.d[k - 1], c.i[k - 1]);
-        if (before(d, i, c.d[k], c.i[k])) {
-            c.d[k] = above ? c.d[k - 1] : d;
-            c.i[k] = above ? c.i[k - 1] : i;
-        }
-    }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
 }
-
-__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// true once the barrier's phase with this parity has completed; false after
+// kUSpin polls (the caller records the timeout)
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
+    const uint32_t a = smem_u32(b);
+    for (uint32_t i = 0; i < kUSpin; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
     asm volatile(
-        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+// Shared-memory matrix descriptor of a K-major operand with 128-byte
+// swizzling: 8-row groups of 128-byte rows, 1024 bytes apart.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+// Instruction descriptor: D f32, A and B tf32, both K-major, N = 128, M = 128.
+constexpr uint32_t kUIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kUN >> 3) << 17) | ((uint32_t)(kUM >> 4) << 24);
+
+__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(
+            dtmem),
+        "l"(adesc), "l"(bdesc), "r"(kUIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// rows [row0, row0 + rows) of x into tile[r][k] (row stride kTS); past n: zeros
-__device__ __forceinline__ void stage_rows(const float* __restrict__ x, uint32_t n, uint32_t row0, int rows,
-                                           float* tile) {
-    for (int q = threadIdx.x; q < rows * (kD / 4); q += kTThreads) {
-        const int r = q / (kD / 4), k4 = q % (kD / 4);
-        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (row0 + r < n) v = reinterpret_cast<const float4*>(x + (size_t)(row0 + r) * kD)[k4];
-        *reinterpret_cast<float4*>(tile + r * kTS + 4 * k4) = v;
+__device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+__global__ void __launch_bounds__(kUThreads, 1)
+    k_match_umma(const __grid_constant__ CUtensorMap tmq, const __grid_constant__ CUtensorMap tmt,
+                 const float* __restrict__ q, const float* __restrict__ qn, uint32_t nq, const float* __restrict__ t,
+                 const float* __restrict__ tn, uint32_t nt, uint32_t chunk_tiles, uint32_t n_chunks,
+                 float4* __restrict__ part, uint32_t* __restrict__ err) {
+    extern __shared__ uint8_t usm_raw[];
+    uint8_t* usm = reinterpret_cast<uint8_t*>(((uintptr_t)usm_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t* qs = usm;                     // [4 K slices][128 rows][128 B], swizzled
+    uint8_t* ts = usm + kUTile;            // [2 stages] of the same
+    uint64_t* bars = reinterpret_cast<uint64_t*>(usm + 3 * kUTile);
+    uint64_t* q_full = bars;               // query tile landed
+    uint64_t* t_full = bars + 1;           // [2] train stage landed
+    uint64_t* t_empty = bars + 3;          // [2] train stage consumed by the MMAs
+    uint64_t* acc_full = bars + 5;         // [2] accumulator complete
+    uint64_t* acc_empty = bars + 7;        // [2] accumulator read by the epilogue
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
+    uint32_t* bad = tmem_slot + 1;         // a wait of this CTA ran out
+    float* tnb = reinterpret_cast<float*>(usm + 3 * kUTile + 1024);  // [2][kUN] train norms of a tile
+    float* mrg_d = tnb + 2 * kUN;                                     // [kUM][4] candidates of the second half
+    int* mrg_i = reinterpret_cast<int*>(mrg_d + kUM * 4);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t n_tiles_all = (nt + kUN - 1) / kUN;
+    const uint32_t qt = blockIdx.x / n_chunks, chunk = blockIdx.x - qt * n_chunks;
+    const uint32_t q0 = qt * kUM;
+    const uint32_t tile_lo = chunk * chunk_tiles;
+    const uint32_t tile_hi = min(tile_lo + chunk_tiles, n_tiles_all);
+    const int ntile = tile_hi > tile_lo ? (int)(tile_hi - tile_lo) : 0;
+    if (tid == 0) {
+        mbar_init(q_full, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(t_full + i, 1);
+            mbar_init(t_empty + i, 1);
+            mbar_init(acc_full + i, 1);
+            mbar_init(acc_empty + i, 256);
+        }
+        *bad = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-}
+    if (warp == 9) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kUTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
 
-__global__ void __launch_bounds__(kTThreads) k_match_tc(const float* __restrict__ q, const float* __restrict__ qn,
-                                                        uint32_t nq, const float* __restrict__ t,
-                                                        const float* __restrict__ tn, uint32_t nt,
-                                                        uint32_t chunk_tiles, uint32_t n_chunks,
-                                                        uint32_t* __restrict__ next, float4* __restrict__ part) {
-    extern __shared__ __align__(16) float sm[];
-    float* qs = sm;                                              // [kTQ][kTS]
-    float* ts = sm + kTQ * kTS;                                  // [kTT][kTS]
-    float* xd = ts + kTT * kTS;                                  // [2][kTQ][kCand] candidate exchange
-    int* xi = reinterpret_cast<int*>(xd + 2 * kTQ * kCand);      // [2][kTQ][kCand]
-    __shared__ uint32_t item_s;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, tq = lane & 3;  // mma fragment row group, thread in group
-    const int wq = warp & 3, wt = warp >> 2;
-    const uint32_t n_tiles = (nt + kTT - 1) / kTT;
-    const uint32_t items = ((nq + kTQ - 1) / kTQ) * n_chunks;
-    uint32_t staged = 0xffffffffu;
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) item_s = atomicAdd(next, 1u);
-        __syncthreads();
-        const uint32_t item = item_s;
-        if (item >= items) break;
-        const uint32_t qt = item / n_chunks, chunk = item - qt * n_chunks;
-        const uint32_t q0 = qt * kTQ;
-        if (qt != staged) {
-            stage_rows(q, nq, q0, kTQ, qs);
-            staged = qt;
-        }
-        // this thread's 4 rows: mi in {0, 1} x {g, g + 8}
-        float qnr[4];
-        Cand4 cand[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const uint32_t row = q0 + wq * 32 + (r >> 1) * 16 + g + (r & 1) * 8;
-            qnr[r] = row < nq ? qn[row] : 0.0f;
-            cand_init(cand[r]);
-        }
-        const uint32_t tile_lo = chunk * chunk_tiles, tile_hi = min(tile_lo + chunk_tiles, n_tiles);
-        for (uint32_t tt = tile_lo; tt < tile_hi; ++tt) {
-            const uint32_t t0 = tt * kTT;
-            __syncthreads();
-            stage_rows(t, nt, t0, kTT, ts);
-            __syncthreads();
-            float acc[2][4][4];
-#pragma unroll
-            for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-                for (int ni = 0; ni < 4; ++ni)
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) acc[mi][ni][e] = 0.0f;
-            const float* qa = qs + (wq * 32 + g) * kTS + tq;
-            const float* tb = ts + (wt * 32 + g) * kTS + tq;
-#pragma unroll 4
-            for (int kk = 0; kk < kD; kk += 8) {
-                uint32_t a[2][4], b[4][2];
-#pragma unroll
-                for (int mi = 0; mi < 2; ++mi) {
-                    const float* p = qa + mi * 16 * kTS + kk;
-                    a[mi][0] = __float_as_uint(p[0]);
-                    a[mi][1] = __float_as_uint(p[8 * kTS]);
-                    a[mi][2] = __float_as_uint(p[4]);
-                    a[mi][3] = __float_as_uint(p[8 * kTS + 4]);
+    if (warp == 8) {
+        if (lane == 0) {
+            // query tile, then the chunk's train tiles through two stages
+            mbar_expect_tx(q_full, kUTile);
+            for (int a = 0; a < 4; ++a) tma_load_2d(qs + a * kUAtom, &tmq, 32 * a, (int)q0, q_full);
+            int issued = 0;
+            for (int j = 0; j < ntile; ++j) {
+                const int st = j & 1;
+                if (j >= 2 && !mbar_wait(t_empty + st, ((j >> 1) - 1) & 1)) {
+                    atomicOr(bad, 1u);
+                    break;
                 }
-#pragma unroll
-                for (int ni = 0; ni < 4; ++ni) {
-                    const float* p = tb + ni * 8 * kTS + kk;
-                    b[ni][0] = __float_as_uint(p[0]);
-                    b[ni][1] = __float_as_uint(p[4]);
-                }
-#pragma unroll
-                for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-                    for (int ni = 0; ni < 4; ++ni) mma_tf32(acc[mi][ni], a[mi], b[ni]);
+                const int t0 = (int)(tile_lo + j) * kUN;
+                mbar_expect_tx(t_full + st, kUTile);
+                for (int a = 0; a < 4; ++a) tma_load_2d(ts + st * kUTile + a * kUAtom, &tmt, 32 * a, t0, t_full + st);
+                issued = j + 1;
             }
-            // accumulator (mi, ni, e): row wq*32 + mi*16 + g + 8*(e >> 1), column wt*32 + ni*8 + 2*tq + (e & 1)
+            // no copy of this CTA may still be landing when it exits (on the
+            // normal path these phases completed long ago)
+            bool landed = mbar_wait(q_full, 0);
+            for (int j = issued - 2 < 0 ? 0 : issued - 2; j < issued; ++j)
+                landed = mbar_wait(t_full + (j & 1), (j >> 1) & 1) && landed;
+            if (!landed) atomicOr(bad, 1u);
+        }
+    } else if (warp == 9) {
+        if (lane == 0) {
+            bool ok = mbar_wait(q_full, 0);
+            for (int j = 0; ok && j < ntile; ++j) {
+                const int st = j & 1, b = j & 1;
+                ok = mbar_wait(t_full + st, (j >> 1) & 1);
+                if (ok && j >= 2) ok = mbar_wait(acc_empty + b, ((j >> 1) - 1) & 1);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t qa = smem_u32(qs), ta = smem_u32(ts + st * kUTile);
 #pragma unroll
-            for (int ni = 0; ni < 4; ++ni)
-#pragma unroll
+                for (int k = 0; k < kD / 8; ++k) {
+                    // K slice k / 4, 32-byte step k % 4 inside the swizzled 128-byte rows
+                    const uint32_t off = (uint32_t)(k >> 2) * kUAtom + (uint32_t)(k & 3) * 32u;
+                    umma_tf32(tmem + (uint32_t)(b * kUN), umma_desc(qa + off), umma_desc(ta + off), k > 0 ? 1u : 0u);
+                }
+                umma_commit(t_empty + st);
+                umma_commit(acc_full + b);
+            }
+            if (!ok) atomicOr(bad, 1u);
+        }
+    } else {
+        // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. (query
+        // rows) and columns 64 (w / 4) .. of each tile; its candidates are
+        // ranked by |t|^2 - 2 q.t (the row's |q|^2 is common to all)
+        const int quarter = warp & 3, half = warp >> 2, etid = warp * 32 + lane;
+        const int r = quarter * 32 + lane;
+        const uint32_t row = q0 + (uint32_t)r;
+        float c0 = INFINITY, c1 = INFINITY, c2 = INFINITY, c3 = INFINITY;
+        int k0 = -1, k1 = -1, k2 = -1, k3 = -1;
+        bool ok = true;
+        for (int j = 0; j < ntile; ++j) {
+            const int b = j & 1;
+            const uint32_t col0 = (tile_lo + j) * kUN;
+            // the tile's train norms (padded with +inf past the end); the
+            // buffer of tile j was last read two tiles ago, before the barrier
+            // of the tile in between
+            if (etid < kUN) tnb[b * kUN + etid] = tn[col0 + etid];
+            if (ok) ok = mbar_wait(acc_full + b, (j >> 1) & 1);
+            epi_barrier();
+            if (ok) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const float* tb = tnb + b * kUN + half * 64;
+#pragma unroll 1
                 for (int c = 0; c < 2; ++c) {
-                    const uint32_t col = t0 + wt * 32 + ni * 8 + 2 * tq + c;
-                    if (col >= nt) continue;
-                    const float tnc = tn[col];
+                    float v[32];
+                    tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * kUN + half * 64 + 32 * c), v);
 #pragma unroll
-                    for (int r = 0; r < 4; ++r) {
-                        const float d = fmaf(-2.0f, acc[r >> 1][ni][2 * (r & 1) + c], qnr[r] + tnc);
-                        if (d < cand[r].d[kCand - 1] || (d == cand[r].d[kCand - 1] && (int)col < cand[r].i[kCand - 1]))
-                            cand_push(cand[r], d, (int)col);
+                    for (int i = 0; i < 32; ++i) {
+                        const float d = fmaf(-2.0f, v[i], tb[32 * c + i]);
+                        // columns rise, so a tie never goes before an earlier one
+                        if (d < c3) {
+                            const int col = (int)col0 + half * 64 + 32 * c + i;
+                            const bool b0 = d < c0, b1 = d < c1, b2 = d < c2;
+                            c3 = b2 ? c2 : d;
+                            k3 = b2 ? k2 : col;
+                            c2 = b1 ? c1 : (b2 ? d : c2);
+                            k2 = b1 ? k1 : (b2 ? col : k2);
+                            c1 = b0 ? c0 : (b1 ? d : c1);
+                            k1 = b0 ? k0 : (b1 ? col : k1);
+                            c0 = b0 ? d : c0;
+                            k0 = b0 ? col : k0;
+                        }
                     }
                 }
-        }
-        // merge the 4 lanes of a row group (tq), then the two column warps
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-#pragma unroll
-            for (int m = 1; m <= 2; m <<= 1) {
-                Cand4 o;
-#pragma unroll
-                for (int k = 0; k < kCand; ++k) {
-                    o.d[k] = __shfl_xor_sync(0xffffffffu, cand[r].d[k], m);
-                    o.i[k] = __shfl_xor_sync(0xffffffffu, cand[r].i[k], m);
-                }
-#pragma unroll
-                for (int k = 0; k < kCand; ++k)
-                    if (before(o.d[k], o.i[k], cand[r].d[kCand - 1], cand[r].i[kCand - 1])) cand_push(cand[r], o.d[k], o.i[k]);
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            } else {
+                atomicOr(bad, 1u);
             }
-            const int row = wq * 32 + (r >> 1) * 16 + g + (r & 1) * 8;
-            if (tq == 0)
-#pragma unroll
-                for (int k = 0; k < kCand; ++k) {
-                    xd[(wt * kTQ + row) * kCand + k] = cand[r].d[k];
-                    xi[(wt * kTQ + row) * kCand + k] = cand[r].i[k];
-                }
+            mbar_arrive(acc_empty + b);
         }
-        __syncthreads();
-        // exact re-ranking: thread pair (2 row, 2 row + 1) per query row, two
-        // candidates each out of the union of both column warps' lists
-        {
-            const int row = threadIdx.x >> 1, half = threadIdx.x & 1;
-            Cand4 u;
-            cand_init(u);
-#pragma unroll
-            for (int w = 0; w < 2; ++w)
+        // the second half's candidates to the first, then the exact
+        // re-ranking of the union (the dot product as an FMA chain in index
+        // order; ties to the lower train index)
+        if (half == 1) {
+            mrg_d[r * 4 + 0] = c0; mrg_i[r * 4 + 0] = k0;
+            mrg_d[r * 4 + 1] = c1; mrg_i[r * 4 + 1] = k1;
+            mrg_d[r * 4 + 2] = c2; mrg_i[r * 4 + 2] = k2;
+            mrg_d[r * 4 + 3] = c3; mrg_i[r * 4 + 3] = k3;
+        }
+        epi_barrier();
+        if (half == 0 && ok && row < nq) {
+            // the 4 best of the 8 by (d, index): two sorted lists of 4
+            int ci[kCand];
+            {
+                float da[8] = {c0, c1, c2, c3, mrg_d[r * 4], mrg_d[r * 4 + 1], mrg_d[r * 4 + 2], mrg_d[r * 4 + 3]};
+                int ia[8] = {k0, k1, k2, k3, mrg_i[r * 4], mrg_i[r * 4 + 1], mrg_i[r * 4 + 2], mrg_i[r * 4 + 3]};
+                int pa = 0, pb = 4;
 #pragma unroll
                 for (int k = 0; k < kCand; ++k) {
-                    const float d = xd[(w * kTQ + row) * kCand + k];
-                    const int i = xi[(w * kTQ + row) * kCand + k];
-                    if (i >= 0 && before(d, i, u.d[kCand - 1], u.i[kCand - 1])) cand_push(u, d, i);
+                    const bool takea = pb >= 8 || (pa < 4 && before(da[pa], ia[pa] < 0 ? 0x7fffffff : ia[pa], da[pb],
+                                                                     ia[pb] < 0 ? 0x7fffffff : ia[pb]));
+                    ci[k] = takea ? ia[pa] : ia[pb];
+                    pa += takea ? 1 : 0;
+                    pb += takea ? 0 : 1;
                 }
-            const uint32_t qi = q0 + row;
-            Best2 b{INFINITY, INFINITY, -1, -1};
-            if (qi < nq) {
-                const float qnq = qn[qi];
-                const float4* qv = reinterpret_cast<const float4*>(qs + row * kTS);
-#pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    const int ci = u.i[2 * half + k];
-                    if (ci < 0) continue;
-                    const float4* tv = reinterpret_cast<const float4*>(t + (size_t)ci * kD);
-                    float dot = 0.0f;
+            }
+            const float qnr = qn[row];
+            const float4* qv = reinterpret_cast<const float4*>(q + (size_t)row * kD);
+            Best2 bst{INFINITY, INFINITY, -1, -1};
+#pragma unroll 1
+            for (int k = 0; k < kCand; ++k) {
+                const int cj = ci[k];
+                if (cj < 0) continue;
+                const float4* tv = reinterpret_cast<const float4*>(t + (size_t)cj * kD);
+                float dot = 0.0f;
 #pragma unroll 8
-                    for (int k4 = 0; k4 < kD / 4; ++k4) {
-                        const float4 a = qv[k4], c = tv[k4];
-                        dot = fmaf(a.x, c.x, dot);
-                        dot = fmaf(a.y, c.y, dot);
-                        dot = fmaf(a.z, c.z, dot);
-                        dot = fmaf(a.w, c.w, dot);
-                    }
-                    push(b, fmaf(-2.0f, dot, qnq + tn[ci]), ci);
+                for (int k4 = 0; k4 < kD / 4; ++k4) {
+                    const float4 a4 = qv[k4], c4 = tv[k4];
+                    dot = fmaf(a4.x, c4.x, dot);
+                    dot = fmaf(a4.y, c4.y, dot);
+                    dot = fmaf(a4.z, c4.z, dot);
+                    dot = fmaf(a4.w, c4.w, dot);
                 }
+                push(bst, fmaf(-2.0f, dot, qnr + tn[cj]), cj);
             }
-            Best2 o;
-            o.d1 = __shfl_xor_sync(0xffffffffu, b.d1, 1);
-            o.d2 = __shfl_xor_sync(0xffffffffu, b.d2, 1);
-            o.i1 = __shfl_xor_sync(0xffffffffu, b.i1, 1);
-            o.i2 = __shfl_xor_sync(0xffffffffu, b.i2, 1);
-            b = fold(b, o);
-            if (half == 0 && qi < nq)
-                part[(size_t)chunk * nq + qi] = make_float4(b.d1, __int_as_float(b.i1), b.d2, __int_as_float(b.i2));
+            part[(size_t)chunk * nq + row] = make_float4(bst.d1, __int_as_float(bst.i1), bst.d2, __int_as_float(bst.i2));
         }
+    }
+    // every tensor-core operation of this CTA is complete before the barrier:
+    // the epilogue waited for the last accumulator (or the MMA thread stopped)
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (*bad && tid == 0) atomicOr(err, 1u);
+    if (warp == 9) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kUTmemCols) : "memory");
     }
 }
 
 // Fold the chunks of each query in chunk order and convert to distances.
 __global__ void k_match_fold(const float4* __restrict__ part, uint32_t nq, uint32_t splits,
-                             SiftCudaMatch* __restrict__ out) {
+                             SiftCudaMatch* __restrict__ out, const uint32_t* __restrict__ err) {
     const uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= nq) return;
     Best2 b{INFINITY, INFINITY, -1, -1};
-    for (uint32_t s = 0; s < splits; ++s) {
+    for (uint32_t s = 0; s < splits && !*err; ++s) {
         const float4 p = part[(size_t)s * nq + qi];
         b = fold(b, Best2{p.x, p.z, __float_as_int(p.y), __float_as_int(p.w)});
     }
@@ -313,46 +402,96 @@ __global__ void k_match_fold(const float4* __restrict__ part, uint32_t nq, uint3
     out[qi] = m;
 }
 
-// Train chunks of at least 16 tiles (1024 descriptors), at most 64 chunks.
-void match_chunks(uint32_t nt, uint32_t* chunk_tiles, uint32_t* n_chunks) {
-    const uint32_t tt = std::max<uint32_t>((nt + kMT - 1) / kMT, 1u);
-    *chunk_tiles = std::max<uint32_t>(16u, (tt + 63) / 64);
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+// train norms, padded to whole 128-descriptor tiles
+size_t tn_floats(uint32_t nt) { return ((size_t)nt + 127) / 128 * 128; }
+
+// Chunks of the train set for the tcgen05 kernel: enough (query tile, chunk)
+// items for two CTAs per multiprocessor, at most 64 chunks.
+void umma_chunks(uint32_t nq, uint32_t nt, uint32_t* chunk_tiles, uint32_t* n_chunks) {
+    const uint32_t tt = (nt + kUN - 1) / kUN, qt = std::max<uint32_t>((nq + kUM - 1) / kUM, 1u);
+    if (tt == 0) {
+        *chunk_tiles = 0;
+        *n_chunks = 0;
+        return;
+    }
+    uint32_t want = std::min<uint32_t>(std::min<uint32_t>((2u * 152u + qt - 1) / qt, tt), 64u);
+    *chunk_tiles = (tt + want - 1) / want;
     *n_chunks = (tt + *chunk_tiles - 1) / *chunk_tiles;
 }
 
-size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+// cuTensorMapEncodeTiled, from the driver the runtime already loaded.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(f);
+    }
+    return fn;
+}
+
+// Rows x 128 floats, boxes of 32 floats (128 bytes, the swizzle span) x 128
+// rows; rows past the end read as zeros.
+bool descriptor_map(CUtensorMap* m, const float* base, uint32_t rows) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)kD, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)kD * sizeof(float)};
+    const cuuint32_t box[2] = {32u, 128u};
+    const cuuint32_t estr[2] = {1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 }  // namespace
 
 size_t match_scratch_bytes(uint32_t nq, uint32_t nt) {
     uint32_t ct, nc;
-    match_chunks(nt, &ct, &nc);
-    return align256((size_t)nq * 4) + align256((size_t)nt * 4) + 256 + (size_t)nc * nq * sizeof(float4);
+    umma_chunks(nq, nt, &ct, &nc);
+    return align256((size_t)nq * 4) + align256(tn_floats(nt) * 4) + 256 + (size_t)std::max<uint32_t>(nc, 1) * nq * sizeof(float4);
 }
 
 int launch_match(const float* d_q, uint32_t nq, const float* d_t, uint32_t nt, SiftCudaMatch* d_out, void* scratch,
                  cudaStream_t st) {
     if (nq == 0) return 0;
     uint32_t chunk_tiles, n_chunks;
-    match_chunks(nt, &chunk_tiles, &n_chunks);
+    umma_chunks(nq, nt, &chunk_tiles, &n_chunks);
     char* p = static_cast<char*>(scratch);
     float* qn = reinterpret_cast<float*>(p);
     p += align256((size_t)nq * 4);
     float* tn = reinterpret_cast<float*>(p);
-    p += align256((size_t)nt * 4);
-    uint32_t* next = reinterpret_cast<uint32_t*>(p);
+    p += align256(tn_floats(nt) * 4);
+    uint32_t* err = reinterpret_cast<uint32_t*>(p);  // set by a tensor-core CTA whose wait ran out
     float4* part = reinterpret_cast<float4*>(p + 256);
-    k_sq_norms<<<(nq + 255) / 256, 256, 0, st>>>(d_q, nq, qn);
-    if (nt) k_sq_norms<<<(nt + 255) / 256, 256, 0, st>>>(d_t, nt, tn);
-    if (cudaMemsetAsync(next, 0, sizeof(uint32_t), st) != cudaSuccess) return -1;
-    const size_t smem = sizeof(float) * ((kTQ + kTT) * kTS + 2 * kTQ * kCand) + sizeof(int) * 2 * kTQ * kCand;
-    if (cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return -1;
-    const uint32_t items = ((nq + kTQ - 1) / kTQ) * n_chunks;
-    const uint32_t grid = std::min<uint32_t>(items, 152u * kTCtasPerSm);
-    k_match_tc<<<grid, kTThreads, smem, st>>>(d_q, qn, nq, d_t, tn, nt, chunk_tiles, n_chunks, next, part);
-    k_match_fold<<<(nq + 255) / 256, 256, 0, st>>>(part, nq, n_chunks, d_out);
+    if (cudaMemsetAsync(err, 0, sizeof(uint32_t), st) != cudaSuccess) return -1;
+    k_sq_norms<<<(nq + 255) / 256, 256, 0, st>>>(d_q, nq, qn, nq);
+    if (n_chunks) {
+        const uint32_t ntp = (uint32_t)tn_floats(nt);
+        k_sq_norms<<<(ntp + 255) / 256, 256, 0, st>>>(d_t, nt, tn, ntp);
+        CUtensorMap mq, mt;
+        if (!descriptor_map(&mq, d_q, nq) || !descriptor_map(&mt, d_t, nt)) return -1;
+        if (cudaFuncSetAttribute(k_match_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUSmem) != cudaSuccess)
+            return -1;
+        const uint32_t grid = ((nq + kUM - 1) / kUM) * n_chunks;
+        k_match_umma<<<grid, kUThreads, kUSmem, st>>>(mq, mt, d_q, qn, nq, d_t, tn, nt, chunk_tiles, n_chunks, part,
+                                                      err);
+    }
+    k_match_fold<<<(nq + 255) / 256, 256, 0, st>>>(part, nq, n_chunks, d_out, err);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+// The error word of the last launch_match on this scratch (after it ran).
+const uint32_t* match_error_word(const void* scratch, uint32_t nq, uint32_t nt) {
+    return reinterpret_cast<const uint32_t*>(static_cast<const char*>(scratch) + align256((size_t)nq * 4) +
+                                             align256(tn_floats(nt) * 4));
 }
 
 }  // namespace sift
