@@ -123,10 +123,9 @@ struct GaussPlane {
 };
 
 template <typename TG>
-__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const PyramidDev& pyr, int o, int layer,
+__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const OctaveDev& od, int S, int layer,
                                                     const float* lut) {
-    const int li = clampi(layer, 0, pyr.S + 2);
-    const OctaveDev& od = pyr.oct[o];
+    const int li = clampi(layer, 0, S + 2);
     return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H, lut};
 }
 
@@ -220,7 +219,7 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
 }
 
 template <typename TG>
-__global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __restrict__ arena, PyramidDev pyr,
+__global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __restrict__ arena, EntryTable tab,
                                                                 const float* __restrict__ lut255,
                                                                 const Keypoint* __restrict__ refined_at,
                                                                 const uint32_t* __restrict__ keep, uint32_t ncap,
@@ -250,10 +249,12 @@ __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __r
             continue;
         }
         const Keypoint kp = refined_at[i];
-        const int o = kp.octave;
+        const int e = kp.octave;  // entry
         uint32_t cnt = 0;
-        if (o >= 0 && o < pyr.num_octaves) {
-            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
+        if (e >= 0 && e < tab.n) {
+            const OctaveDev od = tab.ents[e];
+            const int o = od.octave;
+            const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer, lut);
             const float scale = __int_as_float((127 + o) << 23);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float so = __fdiv_rn(kp.size, scale);
@@ -399,7 +400,7 @@ constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad
 // Radii above the grid (not reachable with the default sigma) fall back to
 // per-sample bilinears from the level itself.
 template <typename TG>
-__global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __restrict__ arena, PyramidDev pyr,
+__global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __restrict__ arena, EntryTable tab,
                                                               const float* __restrict__ lut255,
                                                               const Keypoint* __restrict__ oriented,
                                                               OctCounters* __restrict__ oc,
@@ -435,15 +436,18 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
         if (next >= n) break;
         const uint32_t i = base + next;
         const Keypoint kp = oriented[i];
-        const int o = kp.octave;
+        const int e = kp.octave;  // entry
         for (int i = tid; i < kHistCopies * kHistStride; i += kDescThreads) hist[i] = 0u;
-        const bool valid_oct = o >= 0 && o < pyr.num_octaves;
+        const bool valid_oct = e >= 0 && e < tab.n;
+        OctaveDev od{};
+        if (valid_oct) od = tab.ents[e];
+        const int o = od.octave;
         const float scale = valid_oct ? __int_as_float((127 + o) << 23) : 1.0f;
         const float so = valid_oct ? __fdiv_rn(kp.size, scale) : 0.0f;
         const bool valid = valid_oct && so > 0.0f;
         float inv_fix = 0.0f;
         if (valid) {
-            const GaussPlane<TG> g = plane_for(arena, pyr, o, kp.layer, lut);
+            const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer, lut);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float ang = kp.angle;
             const float ca = cosf(ang), sa = sinf(ang);
@@ -686,10 +690,10 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
 }  // namespace
 
 template <typename TG>
-int launch_orientation(const TG* arena, const PyramidDev& pyr, const float* lut255, const Keypoint* refined_at,
+int launch_orientation(const TG* arena, const EntryTable& tab, const float* lut255, const Keypoint* refined_at,
                        const uint32_t* keep, uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count,
                        int grid, int persist_ctas, cudaStream_t st) {
-    if (launch_chained(k_orientation<TG>, grid, dim3(32, kOriWarps), 0, st, arena, pyr, lut255, refined_at, keep, ncap,
+    if (launch_chained(k_orientation<TG>, grid, dim3(32, kOriWarps), 0, st, arena, tab, lut255, refined_at, keep, ncap,
                        oc, ori_angle, ori_count, std::max(grid - persist_ctas, 0)) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
@@ -705,20 +709,20 @@ int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counter
 }
 
 template <typename TG>
-int launch_descriptor(const TG* arena, const PyramidDev& pyr, const float* lut255, const Keypoint* oriented,
+int launch_descriptor(const TG* arena, const EntryTable& tab, const float* lut255, const Keypoint* oriented,
                       OctCounters* oc, float* desc, uint32_t cap, float* hdesc, uint32_t hcap, int grid,
                       int persist_ctas, cudaStream_t st) {
     if (!hdesc) hcap = 0;
-    if (launch_chained(k_descriptor<TG>, grid, kDescThreads, 0, st, arena, pyr, lut255, oriented, oc, desc, cap, hdesc,
+    if (launch_chained(k_descriptor<TG>, grid, kDescThreads, 0, st, arena, tab, lut255, oriented, oc, desc, cap, hdesc,
                        hcap, std::max(grid - persist_ctas, 0)) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 #define SIFT_INST(TG)                                                                                              \
-    template int launch_orientation<TG>(const TG*, const PyramidDev&, const float*, const Keypoint*, const uint32_t*, \
+    template int launch_orientation<TG>(const TG*, const EntryTable&, const float*, const Keypoint*, const uint32_t*, \
                                         uint32_t, OctCounters*, float*, uint32_t*, int, int, cudaStream_t);        \
-    template int launch_descriptor<TG>(const TG*, const PyramidDev&, const float*, const Keypoint*, OctCounters*,  \
+    template int launch_descriptor<TG>(const TG*, const EntryTable&, const float*, const Keypoint*, OctCounters*,  \
                                        float*, uint32_t, float*, uint32_t, int, int, cudaStream_t);
 SIFT_INST(float)
 SIFT_INST(__half)

@@ -112,15 +112,11 @@ constexpr int kExSH = kExTY + 2;
 // unrolls, so the sliding window renames registers instead of moving them;
 // NL == 0: any S.
 template <int NL>
-__global__ void __launch_bounds__(256, 4) k_extrema_mask(const uint8_t* __restrict__ u8arena,
-                                                      const float* __restrict__ lut255, PyramidDev pyr, int o,
-                                                      int border, uint32_t* __restrict__ words) {
-    chain_wait();
-    extern __shared__ __align__(16) float tile[];  // [layers][kExSH][kExSW], then lut[256]
-    const OctaveDev& od = pyr.oct[o];
-    const int W = od.W, H = od.H, nw = od.nw, L = NL > 0 ? NL : pyr.S + 2;
+__device__ __forceinline__ void extrema_tile(const uint8_t* __restrict__ u8arena, const float* __restrict__ lut255,
+                                             const OctaveDev& od, int S, int border, uint32_t* __restrict__ words,
+                                             int x0, int y0, float* tile) {
+    const int W = od.W, H = od.H, nw = od.nw, L = NL > 0 ? NL : S + 2;
     const int tid = threadIdx.x, lane = tid & 31;
-    const int x0 = blockIdx.x * kExTX, y0 = blockIdx.y * kExTY;
     float* lut = tile + L * kExSH * kExSW;
     lut[tid] = lut255[tid];
     __syncthreads();
@@ -184,6 +180,39 @@ __global__ void __launch_bounds__(256, 4) k_extrema_mask(const uint8_t* __restri
     }
 }
 
+// The extrema mask of entry e (one octave of one image), a tile per CTA.
+template <int NL>
+__global__ void __launch_bounds__(256, 4) k_extrema_mask(const uint8_t* __restrict__ u8arena,
+                                                      const float* __restrict__ lut255, EntryTable tab, int e,
+                                                      int border, uint32_t* __restrict__ words) {
+    chain_wait();
+    extern __shared__ __align__(16) float tile[];  // [layers][kExSH][kExSW], then lut[256]
+    const OctaveDev od = tab.ents[e];
+    extrema_tile<NL>(u8arena, lut255, od, tab.S, border, words, blockIdx.x * kExTX, blockIdx.y * kExTY, tile);
+}
+
+// The extrema masks of entries e0 .. e0 + n_e - 1 in one launch: CTA b takes
+// tile b - tile_pref[k] of entry e0 + k, tile_pref[k] <= b < tile_pref[k + 1]
+// (row-major tiles of kExTX x kExTY).
+template <int NL>
+__global__ void __launch_bounds__(256, 4) k_extrema_mask_flat(const uint8_t* __restrict__ u8arena,
+                                                           const float* __restrict__ lut255, EntryTable tab, int e0,
+                                                           int n_e, const uint32_t* __restrict__ tile_pref,
+                                                           int border, uint32_t* __restrict__ words) {
+    chain_wait();
+    extern __shared__ __align__(16) float tile[];
+    const uint32_t b = blockIdx.x;
+    int lo = 0, hi = n_e;  // the last k with tile_pref[k] <= b
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (tile_pref[mid] <= b) lo = mid; else hi = mid;
+    }
+    const OctaveDev od = tab.ents[e0 + lo];
+    const int tx = (od.W + kExTX - 1) / kExTX;
+    const int t = (int)(b - tile_pref[lo]);
+    extrema_tile<NL>(u8arena, lut255, od, tab.S, border, words, (t % tx) * kExTX, (t / tx) * kExTY, tile);
+}
+
 // solve_linear_system (src/sift.rs:478-503), Cramer's rule in f32.
 __device__ __forceinline__ bool solve3(const float a[3][3], const float b[3], float x[3]) {
 #define M(p, q) __fmul_rn(p, q)
@@ -221,7 +250,8 @@ struct RefineParams {
 
 // One candidate through refine_and_filter_extrema (src/sift.rs:299-474).
 template <class Dog>
-__device__ bool refine_one(const Dog& dog, int o, int x, int y, int s, const RefineParams& rp, Keypoint* out) {
+__device__ bool refine_one(const Dog& dog, int o, int entry, int x, int y, int s, const RefineParams& rp,
+                           Keypoint* out) {
     int cx = x, cy = y, cl = s;
     const float scale = __int_as_float((127 + o) << 23);  // 2^o
     const int nl = rp.levels_dog;
@@ -274,7 +304,7 @@ __device__ bool refine_one(const Dog& dog, int o, int x, int y, int s, const Ref
             out->size = __fmul_rn(rp.sigma, p2);
             out->angle = 0.0f;
             out->response = val;
-            out->octave = o;
+            out->octave = entry;
             out->layer = rust_as_i32(roundf(lf));
             return true;
         }
@@ -286,28 +316,36 @@ __device__ bool refine_one(const Dog& dog, int o, int x, int y, int s, const Ref
     return false;
 }
 
-// One thread per mask word of octave o: the candidates of the word go to
-// their scanned slots in the octave's list, in x order within the word, i.e.
-// (layer, y, x) within the octave.
+// One thread per mask word of entries e0 .. e0 + n_e - 1 (their words are
+// consecutive; w counts from the first entry's first word): the candidates of
+// the word go to their scanned slots, in x order within the word, i.e.
+// (entry, layer, y, x) order. A candidate's octave field holds its entry.
 __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ u8arena, const float* __restrict__ lut255,
-                                              PyramidDev pyr, int o,
+                                              EntryTable tab, int e0, int n_e, long long n_words,
                                               const uint32_t* __restrict__ words,
                                               const uint32_t* __restrict__ cand_off,
                                               Keypoint* __restrict__ cands, uint32_t cap,
                                               Counters* __restrict__ ctr) {
     chain_wait();
-    const OctaveDev& od = pyr.oct[o];
-    const long long nwo = (long long)pyr.S * od.H * od.nw;
     const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= nwo) return;
+    if (w >= n_words) return;
     uint32_t word = words[w];
     if (word == 0u) return;
+    const long long base0 = tab.ents[e0].word_base;
+    int lo = 0, hi = n_e;  // the last entry whose first word is <= w
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (tab.ents[e0 + mid].word_base - base0 <= w) lo = mid; else hi = mid;
+    }
+    const int e = e0 + lo;
+    const OctaveDev od = tab.ents[e];
+    const long long we = w - (od.word_base - base0);
     const DogFromU8 dog{u8arena + od.u_off, lut255, od.plane, od.pitch, od.W, od.H};
-    const int c = (int)(w % od.nw);
-    const long long rowid = w / od.nw;
+    const int c = (int)(we % od.nw);
+    const long long rowid = we / od.nw;
     const int y = (int)(rowid % od.H);
     const int s = (int)(rowid / od.H) + 1;
-    const float scale = __int_as_float((127 + o) << 23);
+    const float scale = __int_as_float((127 + od.octave) << 23);
     uint32_t ci = cand_off[w];
     while (word) {
         const int b = __ffs(word) - 1;
@@ -323,16 +361,17 @@ __global__ void __launch_bounds__(256) k_emit(const uint8_t* __restrict__ u8aren
         k.size = 0.0f;
         k.angle = 0.0f;
         k.response = dog.at(s, x, y);
-        k.octave = o;
+        k.octave = e;
         k.layer = s;
         cands[ci++] = k;
     }
 }
 
-// One thread per candidate of octave o (persistent grid over its count); the
-// survivors are counted per warp into oc->n_ref (a count, order-free).
+// One thread per candidate (persistent grid over the count); a candidate's
+// entry (its octave field) gives its octave and DoG planes. The survivors are
+// counted per warp into oc->n_ref (a count, order-free).
 __global__ void __launch_bounds__(256) k_refine(const uint8_t* __restrict__ u8arena,
-                                                const float* __restrict__ lut255, PyramidDev pyr, int o,
+                                                const float* __restrict__ lut255, EntryTable tab,
                                                 RefineParams rp, const Keypoint* __restrict__ cands,
                                                 Keypoint* __restrict__ refined_at, uint32_t* __restrict__ keep,
                                                 uint32_t cap, OctCounters* __restrict__ oc) {
@@ -341,18 +380,18 @@ __global__ void __launch_bounds__(256) k_refine(const uint8_t* __restrict__ u8ar
     lut[threadIdx.x] = lut255[threadIdx.x];
     __syncthreads();
     const uint32_t n = min(oc->n_cand, cap);
-    const OctaveDev& od = pyr.oct[o];
-    const DogFromU8 dog{u8arena + od.u_off, lut, od.plane, od.pitch, od.W, od.H};
-    const float scale = __int_as_float((127 + o) << 23);
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
         const uint32_t i = i0 + threadIdx.x;
         bool ok = false;
         if (i < n) {
             const Keypoint k = cands[i];
+            const OctaveDev od = tab.ents[k.octave];
+            const DogFromU8 dog{u8arena + od.u_off, lut, od.plane, od.pitch, od.W, od.H};
+            const float scale = __int_as_float((127 + od.octave) << 23);
             const int x = rust_as_i32(__fdiv_rn(k.x, scale)), y = rust_as_i32(__fdiv_rn(k.y, scale));
             Keypoint r;
-            ok = refine_one(dog, o, x, y, k.layer, rp, &r);
+            ok = refine_one(dog, od.octave, k.octave, x, y, k.layer, rp, &r);
             if (ok) refined_at[i] = r;
             keep[i] = ok ? 1u : 0u;
         }
@@ -387,30 +426,51 @@ int launch_dog_dense(const uint8_t* u8arena, const float* lut255, const PyramidD
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
-                        uint32_t* words, cudaStream_t st) {
-    const OctaveDev& od = pyr.oct[o];
+static size_t extrema_smem(int S) { return sizeof(float) * ((size_t)(S + 2) * kExSH * kExSW + 256); }
+
+int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const EntryTable& tab, const OctaveDev& od,
+                        int e, int border, uint32_t* words, cudaStream_t st) {
     if (od.W <= 0 || od.H <= 0) return 0;
-    if (pyr.S + 2 > kExMaxLayers) return -1;
+    if (tab.S + 2 > kExMaxLayers) return -1;
     dim3 grid((od.W + kExTX - 1) / kExTX, (od.H + kExTY - 1) / kExTY);
-    const size_t smem = sizeof(float) * ((size_t)(pyr.S + 2) * kExSH * kExSW + 256);
-    void (*k)(const uint8_t*, const float*, PyramidDev, int, int, uint32_t*) =
-        pyr.S == 3 ? k_extrema_mask<5> : (pyr.S == 4 ? k_extrema_mask<6> : k_extrema_mask<0>);
+    const size_t smem = extrema_smem(tab.S);
+    void (*k)(const uint8_t*, const float*, EntryTable, int, int, uint32_t*) =
+        tab.S == 3 ? k_extrema_mask<5> : (tab.S == 4 ? k_extrema_mask<6> : k_extrema_mask<0>);
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return -1;
-    if (launch_chained(k, grid, 256, smem, st, u8arena, lut255, pyr, o, border, words) != cudaSuccess)
+    if (launch_chained(k, grid, 256, smem, st, u8arena, lut255, tab, e, border, words) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_emit(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, const uint32_t* words,
-                const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st) {
-    const OctaveDev& od = pyr.oct[o];
-    const long long nwo = (long long)pyr.S * od.H * od.nw;
-    if (nwo <= 0) return 0;
-    unsigned grid = (unsigned)((nwo + 255) / 256);
-    if (launch_chained(k_emit, grid, 256, 0, st, u8arena, lut255, pyr, o, words, cand_off, cands, cap,
+int extrema_tiles(int W, int H) {
+    return W > 0 && H > 0 ? ((W + kExTX - 1) / kExTX) * ((H + kExTY - 1) / kExTY) : 0;
+}
+
+int launch_extrema_mask_flat(const uint8_t* u8arena, const float* lut255, const EntryTable& tab, int e0, int n_e,
+                             const uint32_t* tile_pref, uint32_t n_tiles, int border, uint32_t* words,
+                             cudaStream_t st) {
+    if (n_tiles == 0) return 0;
+    if (tab.S + 2 > kExMaxLayers) return -1;
+    const size_t smem = extrema_smem(tab.S);
+    void (*k)(const uint8_t*, const float*, EntryTable, int, int, const uint32_t*, int, uint32_t*) =
+        tab.S == 3 ? k_extrema_mask_flat<5> : (tab.S == 4 ? k_extrema_mask_flat<6> : k_extrema_mask_flat<0>);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return -1;
+    if (launch_chained(k, n_tiles, 256, smem, st, u8arena, lut255, tab, e0, n_e, tile_pref, border, words) !=
+        cudaSuccess)
+        return -1;
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_emit(const uint8_t* u8arena, const float* lut255, const EntryTable& tab, int e0, int n_e,
+                long long n_words, const uint32_t* words, const uint32_t* cand_off, Keypoint* cands, uint32_t cap,
+                Counters* ctr, cudaStream_t st) {
+    if (n_words <= 0) return 0;
+    unsigned grid = (unsigned)((n_words + 255) / 256);
+    if (launch_chained(k_emit, grid, 256, 0, st, u8arena, lut255, tab, e0, n_e, n_words, words, cand_off, cands, cap,
                        ctr) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
@@ -418,13 +478,13 @@ int launch_emit(const uint8_t* u8arena, const float* lut255, const PyramidDev& p
 
 // Refinement is a chain of dependent scattered reads per candidate: up to
 // 5 CTAs of 8 warps per SM keep enough of them in flight.
-int launch_refine(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, float sigma,
-                  float contrast, float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep,
-                  uint32_t cap, OctCounters* oc, cudaStream_t st) {
-    RefineParams rp{sigma, contrast, edge, pyr.S, pyr.S + 2};
+int launch_refine(const uint8_t* u8arena, const float* lut255, const EntryTable& tab, float sigma, float contrast,
+                  float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
+                  OctCounters* oc, cudaStream_t st) {
+    RefineParams rp{sigma, contrast, edge, tab.S, tab.S + 2};
     const unsigned grid = (unsigned)std::min<size_t>(((size_t)cap + 255) / 256, 152 * 5);
-    if (launch_chained(k_refine, grid, 256, 0, st, u8arena, lut255, pyr, o, rp, cands, refined_at, keep, cap,
-                       oc) != cudaSuccess)
+    if (launch_chained(k_refine, grid, 256, 0, st, u8arena, lut255, tab, rp, cands, refined_at, keep, cap, oc) !=
+        cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }

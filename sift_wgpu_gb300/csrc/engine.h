@@ -64,24 +64,29 @@ int launch_match(const float* d_q, uint32_t nq, const float* d_t, uint32_t nt, S
                  cudaStream_t st);
 int launch_to_luma(int format, const uint8_t* px, long long stride, int W, int H, uint8_t* out, long long out_pitch,
                    cudaStream_t st);
-int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int border,
-                        uint32_t* words, cudaStream_t st);
+int launch_extrema_mask(const uint8_t* u8arena, const float* lut255, const EntryTable& tab, const OctaveDev& od,
+                        int e, int border, uint32_t* words, cudaStream_t st);
+int extrema_tiles(int W, int H);
+int launch_extrema_mask_flat(const uint8_t* u8arena, const float* lut255, const EntryTable& tab, int e0, int n_e,
+                             const uint32_t* tile_pref, uint32_t n_tiles, int border, uint32_t* words,
+                             cudaStream_t st);
 int launch_dog_dense(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, int l, float* out,
                      cudaStream_t st);
-int launch_emit(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, const uint32_t* words,
-                const uint32_t* cand_off, Keypoint* cands, uint32_t cap, Counters* ctr, cudaStream_t st);
-int launch_refine(const uint8_t* u8arena, const float* lut255, const PyramidDev& pyr, int o, float sigma,
-                  float contrast, float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep,
-                  uint32_t cap, OctCounters* oc, cudaStream_t st);
+int launch_emit(const uint8_t* u8arena, const float* lut255, const EntryTable& tab, int e0, int n_e,
+                long long n_words, const uint32_t* words, const uint32_t* cand_off, Keypoint* cands, uint32_t cap,
+                Counters* ctr, cudaStream_t st);
+int launch_refine(const uint8_t* u8arena, const float* lut255, const EntryTable& tab, float sigma, float contrast,
+                  float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
+                  OctCounters* oc, cudaStream_t st);
 template <typename TG>
-int launch_orientation(const TG* arena, const PyramidDev& pyr, const float* lut255, const Keypoint* refined_at,
+int launch_orientation(const TG* arena, const EntryTable& tab, const float* lut255, const Keypoint* refined_at,
                        const uint32_t* keep, uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count,
                        int grid, int persist_ctas, cudaStream_t st);
 int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counters* ctr, const float* ori_angle,
                        const uint32_t* ori_count, const uint32_t* ori_off, Keypoint* oriented, uint32_t cap,
                        cudaStream_t st);
 template <typename TG>
-int launch_descriptor(const TG* arena, const PyramidDev& pyr, const float* lut255, const Keypoint* oriented,
+int launch_descriptor(const TG* arena, const EntryTable& tab, const float* lut255, const Keypoint* oriented,
                       OctCounters* oc, float* desc, uint32_t cap, float* hdesc, uint32_t hcap, int grid,
                       int persist_ctas, cudaStream_t st);
 // Error reporting (engine.cu): the calling thread's sift_cuda_last_error.
@@ -205,6 +210,8 @@ struct Engine {
     DevMem d_dg, d_dk, d_drgb;       // drawing: grey input, keypoints, RGB output
     DevMem d_img, d_G, d_U, d_tmp, d_tmpo, d_ltmp, d_wts, d_ltab, d_lw;
     DevMem d_words, d_cand_off, d_keep, d_scan;
+    DevMem d_ents;  // the entry table: pyr.oct[0 .. num_octaves) in device memory
+    EntryTable tab() const { return EntryTable{d_ents.as<OctaveDev>(), pyr.num_octaves, pyr.S}; }
     DevMem d_cands, d_refined_at, d_ori_angle, d_ori_count, d_ori_off, d_oriented, d_desc, d_ctr;
     HostPinned h_ctr, h_kps, h_desc;
     // Host calls: the run ends with an export kernel that writes counters,
@@ -399,6 +406,8 @@ struct Engine {
             od.g_off = (long long)goff;
             od.word_base = (long long)wbase;
             od.u_off = (long long)uoff;
+            od.octave = o;
+            od.image = 0;
             goff += (size_t)od.plane * (S + 3);
             uoff += (size_t)od.plane * (S + 3);
             wbase += (size_t)S * oh * od.nw;
@@ -482,6 +491,10 @@ struct Engine {
         CK(d_lw.ensure(std::max<size_t>(ftab.size(), 4) * sizeof(float)), "cudaMalloc(lw)");
         const size_t nwb = std::max<size_t>((size_t)n_words, 1) * sizeof(uint32_t);
         CK(d_words.ensure(nwb), "cudaMalloc(words)");
+        CK(d_ents.ensure(sizeof(OctaveDev) * (size_t)std::max(O, 1)), "cudaMalloc(entries)");
+        if (O > 0)
+            CK(cudaMemcpyAsync(d_ents.p, g.oct, sizeof(OctaveDev) * (size_t)O, cudaMemcpyHostToDevice, st),
+               "H2D entries");
         CK(d_cand_off.ensure(nwb), "cudaMalloc(cand_off)");
         if (!wts.empty())
             CK(cudaMemcpyAsync(d_wts.p, wts.data(), wts.size() * sizeof(float), cudaMemcpyHostToDevice, st), "H2D wts");
@@ -611,19 +624,19 @@ struct Engine {
             OctCounters* oc = &ctr->oct[o];
             unsigned long long* sstate = d_scan.as<unsigned long long>() + pb[o];
             const long long nwo = octave_words(o);
-            if (od.nw > 0 && ok(launch_extrema_mask(U, lut, pyr, o, (int)p.image_border_width, d_words.as<uint32_t>(),
-                                                    q)))
+            if (od.nw > 0 && ok(launch_extrema_mask(U, lut, tab(), od, o, (int)p.image_border_width,
+                                                    d_words.as<uint32_t>(), q)))
                 return cuda_fail(cudaGetLastError(), "extrema mask");
             if (scan_exclusive(d_words.as<uint32_t>() + od.word_base, SCAN_POPC,
                                d_cand_off.as<uint32_t>() + od.word_base, (size_t)nwo, nullptr, &oc->n_cand, sstate,
                                &ctr->overflow, q))
                 return cuda_fail(cudaGetLastError(), "scan candidates");
             launches += nwo > 0 ? 1 : 0;
-            if (ok(launch_emit(U, lut, pyr, o, d_words.as<uint32_t>() + od.word_base,
+            if (ok(launch_emit(U, lut, tab(), o, 1, nwo, d_words.as<uint32_t>() + od.word_base,
                                d_cand_off.as<uint32_t>() + od.word_base, d_cands.as<Keypoint>() + cb[o], cap_c[o], ctr,
                                q)))
                 return cuda_fail(cudaGetLastError(), "emit");
-            if (ok(launch_refine(U, lut, pyr, o, p.sigma, p.contrast_threshold, p.edge_threshold,
+            if (ok(launch_refine(U, lut, tab(), p.sigma, p.contrast_threshold, p.edge_threshold,
                                  d_cands.as<Keypoint>() + cb[o], d_refined_at.as<Keypoint>() + cb[o],
                                  d_keep.as<uint32_t>() + cb[o], cap_c[o], oc, q)))
                 return cuda_fail(cudaGetLastError(), "refine");
@@ -635,7 +648,7 @@ struct Engine {
             // one warp-item per 8 candidate slots, 4 per warp; the last
             // 152 x ori_ctas_per_sm CTAs drain whatever is left
             const int grid = (int)std::max<uint32_t>(cap_c[o] / 64, 32);
-            if (ok(launch_orientation<TG>(G, pyr, lut, d_refined_at.as<Keypoint>() + cb[o], d_keep.as<uint32_t>() + cb[o],
+            if (ok(launch_orientation<TG>(G, tab(), lut, d_refined_at.as<Keypoint>() + cb[o], d_keep.as<uint32_t>() + cb[o],
                                           cap_c[o], oc, d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
                                           d_ori_count.as<uint32_t>() + cb[o], grid, 152 * tune.ori_ctas_per_sm, q)))
                 return cuda_fail(cudaGetLastError(), "orientation");
@@ -663,7 +676,7 @@ struct Engine {
             const int grid = (int)std::max<uint32_t>(cap_c[o] / 16, 64);
             // host calls: descriptors below cap_x go straight into the mapped
             // export buffer while the stage runs, the rest to d_desc
-            if (ok(launch_descriptor<TG>(G, pyr, lut, d_oriented.as<Keypoint>(), &ctr->oct[o], d_desc.as<float>(), cap_ori,
+            if (ok(launch_descriptor<TG>(G, tab(), lut, d_oriented.as<Keypoint>(), &ctr->oct[o], d_desc.as<float>(), cap_ori,
                                          exp ? hx_ddesc : nullptr, exp ? cap_x : 0u, grid,
                                          152 * tune.desc_ctas_per_sm, q)))
                 return cuda_fail(cudaGetLastError(), "descriptor");

@@ -68,16 +68,12 @@ constexpr int kRowThreads = 128;
 
 // One row per CTA. Shared layout: weights[taps] (padded to a multiple of 4),
 // then the row with r clamp-to-edge pixels on each side and 8 floats of slack.
-__global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __restrict__ in, int in_pitch,
-                                                           uint8_t* __restrict__ out, int out_pitch, int W, int r,
-                                                           const float* __restrict__ wts) {
-    chain_wait();
-    extern __shared__ __align__(16) float sm[];
+__device__ __forceinline__ void blur_row(const uint8_t* __restrict__ in, int in_pitch, uint8_t* __restrict__ out,
+                                         int out_pitch, int W, int r, const float* __restrict__ wts, int y, float* sm) {
     const int taps = 2 * r + 1;
     const int wpad = (taps + 3) & ~3;
     float* kw = sm;
     float* row = sm + wpad;
-    const int y = blockIdx.x;
     const uint8_t* src = in + (long long)y * in_pitch;
     for (int i = threadIdx.x; i < wpad; i += blockDim.x) kw[i] = i < taps ? wts[i] : 0.0f;
     const int padded = W + 2 * r;
@@ -148,6 +144,14 @@ __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __rest
     }
 }
 
+__global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __restrict__ in, int in_pitch,
+                                                           uint8_t* __restrict__ out, int out_pitch, int W, int r,
+                                                           const float* __restrict__ wts) {
+    chain_wait();
+    extern __shared__ __align__(16) float sm[];
+    blur_row(in, in_pitch, out, out_pitch, W, r, wts, blockIdx.x, sm);
+}
+
 constexpr int kColTX = 32;                 // output columns per CTA
 constexpr int kColRows = 64;               // output rows per CTA
 constexpr int kColThreads = 256;           // 8 column groups of 4 x 32 row groups of 2
@@ -167,21 +171,16 @@ template <typename TG>
 __device__ __forceinline__ void store_level4(TG* p, const int v[4], const float* lut);
 
 template <typename TG>
-__global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __restrict__ tmp, int tmp_pitch,
-                                                          TG* __restrict__ out, uint8_t* __restrict__ out_u8,
-                                                          int pitch, int W, int H, int r,
-                                                          const float* __restrict__ wts,
-                                                          const float* __restrict__ lut255) {
-    chain_wait();
-    extern __shared__ __align__(16) float sm[];
+__device__ __forceinline__ void blur_cols_tile(const uint8_t* __restrict__ tmp, int tmp_pitch, TG* __restrict__ out,
+                                               uint8_t* __restrict__ out_u8, int pitch, int W, int H, int r,
+                                               const float* __restrict__ wts, const float* __restrict__ lut255,
+                                               int x0, int y0, float* sm) {
     const int taps = 2 * r + 1;
     const int tp = taps8(r);
     float* kw = sm;
     float* lut = sm + tp;
     float* tile = lut + 256;
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * kColTX;
-    const int y0 = blockIdx.y * kColRows;
     for (int i = tid; i < tp; i += kColThreads) kw[i] = i < taps ? wts[i] : 0.0f;
     for (int i = tid; i < 256; i += kColThreads) lut[i] = lut255[i];
     const int rows = kColRows + tp - 1;
@@ -252,6 +251,18 @@ __global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __rest
     }
 }
 
+template <typename TG>
+__global__ void __launch_bounds__(kColThreads) k_blur_cols(const uint8_t* __restrict__ tmp, int tmp_pitch,
+                                                          TG* __restrict__ out, uint8_t* __restrict__ out_u8,
+                                                          int pitch, int W, int H, int r,
+                                                          const float* __restrict__ wts,
+                                                          const float* __restrict__ lut255) {
+    chain_wait();
+    extern __shared__ __align__(16) float sm[];
+    blur_cols_tile<TG>(tmp, tmp_pitch, out, out_u8, pitch, W, H, r, wts, lut255, blockIdx.x * kColTX,
+                       blockIdx.y * kColRows, sm);
+}
+
 // ---------------------------------------------------------------------------
 // Packed pairs of f32: mul.rn.f32x2 rounds each of the two products like a
 // scalar multiply. The products are added to scalar accumulators: a packed
@@ -320,14 +331,11 @@ __device__ __forceinline__ void store_level4<__half>(__half* p, const int v[4], 
 }
 
 template <typename TG, int R>
-__global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restrict__ in, int in_pitch,
-                                                          TG* __restrict__ out, uint8_t* __restrict__ out_u8,
-                                                          int pitch, int W, int H,
-                                                          const float* __restrict__ wts,
-                                                          const float* __restrict__ lut255) {
-    chain_wait();
+__device__ __forceinline__ void blur_level_tile(const uint8_t* __restrict__ in, int in_pitch, TG* __restrict__ out,
+                                                uint8_t* __restrict__ out_u8, int pitch, int W, int H,
+                                                const float* __restrict__ wts, const float* __restrict__ lut255,
+                                                int x0, int y0, float* sm) {
     static_assert(R >= 1 && R <= kFMaxR, "fused radius");
-    extern __shared__ __align__(16) float sm[];
     constexpr int taps = 2 * R + 1;
     constexpr int wpad = (taps + 3) & ~3;
     constexpr int RH = kFTY + 2 * R;
@@ -338,7 +346,6 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
     float* src = lut + 256;              // [RH][kFSW] staged input (u8 values)
     float* hb = src + (size_t)RH * kFSW;  // [RH][kFTX] horizontal pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int x0 = blockIdx.x * kFTX, y0 = blockIdx.y * kFTY;
     for (int i = tid; i < wpad; i += kFThreads) {
         const float k = i < taps ? wts[i] : 0.0f;
         kw2[i] = pack2(k, k);
@@ -456,6 +463,18 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
     }
 }
 
+template <typename TG, int R>
+__global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restrict__ in, int in_pitch,
+                                                          TG* __restrict__ out, uint8_t* __restrict__ out_u8,
+                                                          int pitch, int W, int H,
+                                                          const float* __restrict__ wts,
+                                                          const float* __restrict__ lut255) {
+    chain_wait();
+    extern __shared__ __align__(16) float sm[];
+    blur_level_tile<TG, R>(in, in_pitch, out, out_u8, pitch, W, H, wts, lut255, blockIdx.x * kFTX, blockIdx.y * kFTY,
+                           sm);
+}
+
 // A level whose blur increment is below 1e-4 is a copy of the previous one
 // (src/sift.rs:152-154).
 template <typename TG>
@@ -496,12 +515,11 @@ __global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride,
 constexpr int kLzT = 32, kLzSpan = 80, kLzMid = 81;  // odd mid stride: lanes on rows hit 32 banks
 
 template <typename TG>
-__global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict__ src, int src_pitch,
-                                                       TG* __restrict__ dst, uint8_t* __restrict__ dst_u8,
-                                                       int dst_pitch, int nW, int nH, const int* __restrict__ vtab,
-                                                       const float* __restrict__ vw, const int* __restrict__ htab,
-                                                       const float* __restrict__ hw, const LanczosUniform uni) {
-    chain_wait();
+__device__ __forceinline__ void lanczos_tile(const uint8_t* __restrict__ src, int src_pitch, TG* __restrict__ dst,
+                                             uint8_t* __restrict__ dst_u8, int dst_pitch, int nW, int nH,
+                                             const int* __restrict__ vtab, const float* __restrict__ vw,
+                                             const int* __restrict__ htab, const float* __restrict__ hw,
+                                             const LanczosUniform& uni, int ox0, int oy0) {
     __shared__ float in[kLzSpan][kLzSpan];
     __shared__ float mid[kLzT][kLzMid];
     const int* vleft = vtab;
@@ -511,7 +529,6 @@ __global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict
     const int* hcount = htab + nW;
     const int* hoff = htab + 2 * nW;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int ox0 = blockIdx.x * kLzT, oy0 = blockIdx.y * kLzT;
     const int ox1 = min(ox0 + kLzT, nW), oy1 = min(oy0 + kLzT, nH);
     const int x_lo = hleft[ox0], x_hi = hleft[ox1 - 1] + hcount[ox1 - 1];
     const int y_lo = vleft[oy0], y_hi = vleft[oy1 - 1] + vcount[oy1 - 1];
@@ -593,6 +610,17 @@ __global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict
         store_level(dst + od, v, norm255(v));
         dst_u8[od] = (uint8_t)v;
     }
+}
+
+template <typename TG>
+__global__ void __launch_bounds__(256) k_lanczos_fused(const uint8_t* __restrict__ src, int src_pitch,
+                                                       TG* __restrict__ dst, uint8_t* __restrict__ dst_u8,
+                                                       int dst_pitch, int nW, int nH, const int* __restrict__ vtab,
+                                                       const float* __restrict__ vw, const int* __restrict__ htab,
+                                                       const float* __restrict__ hw, const LanczosUniform uni) {
+    chain_wait();
+    lanczos_tile<TG>(src, src_pitch, dst, dst_u8, dst_pitch, nW, nH, vtab, vw, htab, hw, uni, blockIdx.x * kLzT,
+                     blockIdx.y * kLzT);
 }
 
 // Lanczos3 vertical pass (image 0.25.6 vertical_sample): tmp[oy][x] =

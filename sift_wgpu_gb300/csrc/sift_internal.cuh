@@ -47,7 +47,7 @@ struct Counters {
     OctCounters oct[kMaxOctaves];
 };
 
-// Geometry of one octave in the device arena.
+// Geometry of one octave of one image in the device arena.
 struct OctaveDev {
     int W, H, pitch;          // pitch in elements (G and u8 planes)
     int nw;                   // 32-pixel words per row of the extrema mask
@@ -55,6 +55,19 @@ struct OctaveDev {
     long long plane;          // elements per plane (pitch * H)
     long long word_base;      // first word of this octave in the mask arena
     long long u_off;          // byte offset of level 0 in the u8 level arena
+    int octave;               // the octave (keypoint scale 2^octave)
+    int image;                // the image of a batch (0 for one image)
+};
+
+// The (image, octave) entries of a run in device memory, image-major
+// (entry = image * num_octaves + octave). The detection, orientation and
+// descriptor kernels read a keypoint's geometry through its entry: inside a
+// run, a keypoint's `octave` field holds its entry index, which equals the
+// octave for a single image (a batch's export writes back the octave).
+struct EntryTable {
+    const OctaveDev* ents;
+    int n;  // entries
+    int S;  // num_intervals
 };
 
 struct PyramidDev {
