@@ -319,6 +319,43 @@ int sift_cuda_replay(SiftCudaServer* server, const SiftCudaParams* params, const
                      const SiftCudaReplayImage* images, uint32_t n_images, const SiftCudaReplayRequest* reqs,
                      uint32_t n_reqs, SiftCudaReplayResult* results, double* wall_s);
 
+/* ---- batched form: one run over many images ------------------------------ */
+
+/* detect_and_compute_with_backend (src/sift.rs:1244-1355) on a batch of 8-bit
+ * grayscale images of any sizes in one run (no counterpart in the reference,
+ * whose GPU arms take one image per call). Each stage of the hot path is one
+ * launch over the flattened work of every image: the pyramid one launch per
+ * (octave, level) over the tiles of that octave of all images, then
+ * extrema, candidate scan, emission, refinement, orientation, oriented
+ * keypoints and descriptors one launch each over all (image, octave)
+ * entries; the run is captured once per batch geometry as a CUDA graph. Every
+ * image's keypoints and descriptors are those of sift_cuda_detect_and_compute
+ * on it, bit for bit, in the same order. The batch keeps its levels as u8
+ * planes (opts->storage must be SIFT_CUDA_STORAGE_U8). */
+typedef struct {
+    const uint8_t* data;
+    uint32_t width, height, stride, reserved;
+} SiftCudaImage;
+
+typedef struct {
+    uint32_t n_images, total;
+    const uint32_t* offsets;     /* n_images + 1: image i's keypoints are [offsets[i], offsets[i + 1]) */
+    const SiftCudaKeypoint* kps; /* total keypoints, image after image */
+    const float* desc;           /* total x 128 */
+    uint32_t launches;           /* kernel launches of the run */
+    float device_ms;             /* device time of the run (images already on the device) */
+} SiftCudaBatchResult;
+
+typedef struct SiftCudaBatch SiftCudaBatch;
+
+int sift_cuda_batch_create(const SiftCudaParams* params, const SiftCudaOptions* opts, SiftCudaBatch** out);
+void sift_cuda_batch_destroy(SiftCudaBatch* batch);
+/* Runs the batch and synchronises. The result's arrays are mapped pinned host
+ * buffers owned by the batch object (the run writes them from the device),
+ * valid until its next call or destroy. */
+int sift_cuda_batch_detect_and_compute(SiftCudaBatch* batch, const SiftCudaImage* images, uint32_t n,
+                                       SiftCudaBatchResult* out);
+
 /* ---- descriptor matching ------------------------------------------------ */
 
 /* The nearest and second-nearest train descriptor of each query descriptor

@@ -116,6 +116,16 @@ class ReplayImage(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
+class BatchImage(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("stride", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("n_images", C.c_uint32), ("total", C.c_uint32), ("offsets", C.POINTER(C.c_uint32)),
+                ("kps", C.c_void_p), ("desc", C.c_void_p), ("launches", C.c_uint32), ("device_ms", C.c_float)]
+
+
 class ReplayRequest(C.Structure):
     _fields_ = [("arrival_s", C.c_double), ("image", C.c_uint32), ("reserved", C.c_uint32)]
 
@@ -178,6 +188,9 @@ def lib() -> C.CDLL:
                                                C.c_uint8, C.c_uint8, C.c_void_p, u32]),
         "sift_cuda_match": (C.c_int, [C.c_void_p, C.c_void_p, u32, C.c_void_p, u32, C.c_void_p]),
         "sift_cuda_match_scratch_bytes": (C.c_size_t, [u32, u32]),
+        "sift_cuda_batch_create": (C.c_int, [P(Params), P(Options), P(C.c_void_p)]),
+        "sift_cuda_batch_destroy": (None, [C.c_void_p]),
+        "sift_cuda_batch_detect_and_compute": (C.c_int, [C.c_void_p, P(BatchImage), u32, P(BatchResult)]),
         "sift_cuda_match_device": (C.c_int, [C.c_void_p, u32, C.c_void_p, u32, C.c_void_p, C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
@@ -202,7 +215,8 @@ def exported_symbols() -> list[str]:
         "sift_cuda_server_warm", "sift_cuda_server_stats", "sift_cuda_server_tuning", "sift_cuda_footprint_bytes",
         "sift_cuda_replay", "sift_cuda_gaussian_blur_u8_noalloc", "sift_cuda_draw_keypoints", "sift_cuda_match",
         "sift_cuda_match_scratch_bytes",
-        "sift_cuda_match_device",
+        "sift_cuda_match_device", "sift_cuda_batch_create", "sift_cuda_batch_destroy",
+        "sift_cuda_batch_detect_and_compute",
     ]
 
 

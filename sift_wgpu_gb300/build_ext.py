@@ -22,7 +22,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsiftcuda.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["scan.cu", "pyramid.cu", "detect.cu", "describe.cu", "engine.cu", "server.cu", "convert.cu", "export.cu", "noalloc.cu", "match.cu", "draw.cu"]
+CU_SOURCES = ["scan.cu", "pyramid.cu", "detect.cu", "describe.cu", "engine.cu", "server.cu", "convert.cu", "export.cu", "noalloc.cu", "match.cu", "draw.cu", "batch.cu"]
 CPP_SOURCES = ["tables.cpp"]
 HEADERS = ["sift_internal.cuh", "tables.h", "engine.h"]
 

@@ -23,6 +23,7 @@
 //   k_blur_rows    horizontal pass for larger radii, one row per CTA. u8 out.
 //   k_blur_cols    vertical pass for larger radii on a 32 x 64 tile.
 //   k_lanczos_fused  the 2x Lanczos3 resize between octaves, both passes.
+#include <cstring>
 #include <type_traits>
 
 #include "sift_internal.cuh"
@@ -662,6 +663,98 @@ __global__ void k_lanczos_h(const float* __restrict__ src, int src_pitch, TG* __
     dst_u8[od] = (uint8_t)v;
 }
 
+// ---------------------------------------------------------------------------
+// Flattened batch launches. The entries of a batch are image-major (entry =
+// image * O + octave); one launch covers octave o of every image. CTA b
+// serves the image k with pref[k] <= b < pref[k + 1], where pref is the
+// launch's prefix over the images' tile (or row) counts, and tile b - pref[k]
+// of that image; the tile bodies are the single-image kernels' own.
+__device__ __forceinline__ int find_image(const uint32_t* __restrict__ pref, int n, uint32_t b) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (pref[mid] <= b) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// level s of octave o from level s - 1 (from the input image when s == 0)
+__device__ __forceinline__ const uint8_t* level_src(const BatchPyr& bp, const OctaveDev& od, int k, int s,
+                                                    int* pitch) {
+    if (s == 0) {
+        *pitch = bp.img_pitch[k];
+        return bp.img + bp.img_off[k];
+    }
+    *pitch = od.pitch;
+    return bp.U + od.u_off + (long long)(s - 1) * od.plane;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kFThreads) kb_blur_level(BatchPyr bp, int o, int s, int n_img,
+                                                           const uint32_t* __restrict__ pref,
+                                                           const float* __restrict__ wts,
+                                                           const float* __restrict__ lut255) {
+    chain_wait();
+    extern __shared__ __align__(16) float sm[];
+    const int k = find_image(pref, n_img, blockIdx.x);
+    const OctaveDev od = bp.ents[k * bp.O + o];
+    const int t = (int)(blockIdx.x - pref[k]), tx = (od.W + kFTX - 1) / kFTX;
+    int in_pitch = 0;
+    const uint8_t* in = level_src(bp, od, k, s, &in_pitch);
+    uint8_t* out = bp.U + od.u_off + (long long)s * od.plane;
+    blur_level_tile<uint8_t, R>(in, in_pitch, out, out, od.pitch, od.W, od.H, wts, lut255, (t % tx) * kFTX,
+                                (t / tx) * kFTY, sm);
+}
+
+__global__ void __launch_bounds__(kRowThreads) kb_blur_rows(BatchPyr bp, uint8_t* __restrict__ tmp, int o, int s,
+                                                            int r, int n_img, const uint32_t* __restrict__ pref,
+                                                            const float* __restrict__ wts) {
+    chain_wait();
+    extern __shared__ __align__(16) float sm[];
+    const int k = find_image(pref, n_img, blockIdx.x);
+    const OctaveDev od = bp.ents[k * bp.O + o];
+    int in_pitch = 0;
+    const uint8_t* in = level_src(bp, od, k, s, &in_pitch);
+    blur_row(in, in_pitch, tmp + od.t_off, od.pitch, od.W, r, wts, (int)(blockIdx.x - pref[k]), sm);
+}
+
+__global__ void __launch_bounds__(kColThreads) kb_blur_cols(BatchPyr bp, const uint8_t* __restrict__ tmp, int o,
+                                                            int s, int r, int n_img,
+                                                            const uint32_t* __restrict__ pref,
+                                                            const float* __restrict__ wts,
+                                                            const float* __restrict__ lut255) {
+    chain_wait();
+    extern __shared__ __align__(16) float sm[];
+    const int k = find_image(pref, n_img, blockIdx.x);
+    const OctaveDev od = bp.ents[k * bp.O + o];
+    const int t = (int)(blockIdx.x - pref[k]), tx = (od.W + kColTX - 1) / kColTX;
+    uint8_t* out = bp.U + od.u_off + (long long)s * od.plane;
+    blur_cols_tile<uint8_t>(tmp + od.t_off, od.pitch, out, out, od.pitch, od.W, od.H, r, wts, lut255,
+                            (t % tx) * kColTX, (t / tx) * kColRows, sm);
+}
+
+// Lanczos tables of one image's resize from octave o to o + 1 (offsets into
+// the batch's integer and weight tables).
+struct BatchLz {
+    int vtab, vw, htab, hw;
+    LanczosUniform uni;
+};
+
+__global__ void __launch_bounds__(256) kb_lanczos(BatchPyr bp, int o, int n_img, const uint32_t* __restrict__ pref,
+                                                  const BatchLz* __restrict__ lz, const int* __restrict__ itab,
+                                                  const float* __restrict__ ftab) {
+    chain_wait();
+    const int k = find_image(pref, n_img, blockIdx.x);
+    const int e = k * bp.O + o;
+    const OctaveDev od = bp.ents[e], nx = bp.ents[e + 1];
+    const BatchLz& z = lz[e];
+    const int t = (int)(blockIdx.x - pref[k]), tx = (nx.W + kLzT - 1) / kLzT;
+    uint8_t* dst = bp.U + nx.u_off;
+    lanczos_tile<uint8_t>(bp.U + od.u_off + (long long)bp.S * od.plane, od.pitch, dst, dst, nx.pitch, nx.W, nx.H,
+                          itab + z.vtab, ftab + z.vw, itab + z.htab, ftab + z.hw, z.uni, (t % tx) * kLzT,
+                          (t / tx) * kLzT);
+}
+
 }  // namespace
 
 // ---- launchers ----------------------------------------------------------------
@@ -763,6 +856,72 @@ int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, 
 }
 
 int lanczos_fused_span() { return kLzSpan; }
+
+// ---- flattened batch launchers ------------------------------------------------
+
+int blur_level_tiles(int W, int H) { return W > 0 && H > 0 ? ((W + kFTX - 1) / kFTX) * ((H + kFTY - 1) / kFTY) : 0; }
+int blur_col_tiles(int W, int H) {
+    return W > 0 && H > 0 ? ((W + kColTX - 1) / kColTX) * ((H + kColRows - 1) / kColRows) : 0;
+}
+int lanczos_tiles(int nW, int nH) { return nW > 0 && nH > 0 ? ((nW + kLzT - 1) / kLzT) * ((nH + kLzT - 1) / kLzT) : 0; }
+size_t batch_lz_bytes() { return sizeof(BatchLz); }
+void batch_lz_fill(void* out, int vtab, int vw, int htab, int hw, const LanczosUniform& uni) {
+    BatchLz z{vtab, vw, htab, hw, uni};
+    std::memcpy(out, &z, sizeof z);
+}
+
+// Level s of octave o of every image of a batch: the fused kernel (r <= 8,
+// tiles prefixed by fused_pref) or the two passes (rows prefixed by
+// rows_pref, column tiles by cols_pref; tmp holds each entry's
+// horizontal-pass plane at its t_off).
+int launch_blur_level_flat(const BatchPyr& bp, uint8_t* tmp, int o, int s, int r, int n_img,
+                           const uint32_t* fused_pref, uint32_t n_fused, const uint32_t* rows_pref, uint32_t n_rows,
+                           int max_w, const uint32_t* cols_pref, uint32_t n_cols, const float* wts,
+                           const float* lut255, cudaStream_t st, int* launches, int fused_max_radius) {
+    if (r <= kFMaxR && r <= fused_max_radius) {
+        if (n_fused == 0) return 0;
+        void (*kern)(BatchPyr, int, int, int, const uint32_t*, const float*, const float*);
+        switch (r) {
+            case 1: kern = kb_blur_level<1>; break;
+            case 2: kern = kb_blur_level<2>; break;
+            case 3: kern = kb_blur_level<3>; break;
+            case 4: kern = kb_blur_level<4>; break;
+            case 5: kern = kb_blur_level<5>; break;
+            case 6: kern = kb_blur_level<6>; break;
+            case 7: kern = kb_blur_level<7>; break;
+            default: kern = kb_blur_level<8>; break;
+        }
+        const size_t smem = blur_fused_smem(r);
+        if (set_smem((const void*)kern, smem)) return -1;
+        if (launch_chained(kern, n_fused, kFThreads, smem, st, bp, o, s, n_img, fused_pref, wts, lut255) !=
+            cudaSuccess)
+            return -1;
+        *launches += 1;
+        return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+    }
+    if (n_rows == 0) return 0;
+    const size_t rs = blur_rows_smem(max_w, r), cs = blur_cols_smem(r);
+    if (set_smem((const void*)kb_blur_rows, rs) || set_smem((const void*)kb_blur_cols, cs)) return -1;
+    if (launch_chained(kb_blur_rows, n_rows, kRowThreads, rs, st, bp, tmp, o, s, r, n_img, rows_pref, wts) !=
+        cudaSuccess)
+        return -1;
+    if (launch_chained(kb_blur_cols, n_cols, kColThreads, cs, st, bp, (const uint8_t*)tmp, o, s, r, n_img, cols_pref,
+                       wts, lut255) != cudaSuccess)
+        return -1;
+    *launches += 2;
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+// The 2x Lanczos3 resize of octave o to o + 1 of every image (every resize
+// fits the fused kernel; the caller checks).
+int launch_lanczos_flat(const BatchPyr& bp, int o, int n_img, const uint32_t* pref, uint32_t n_tiles,
+                        const void* lz, const int* itab, const float* ftab, cudaStream_t st) {
+    if (n_tiles == 0) return 0;
+    if (launch_chained(kb_lanczos, n_tiles, 256, 0, st, bp, o, n_img, pref, (const BatchLz*)lz, itab, ftab) !=
+        cudaSuccess)
+        return -1;
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
 int lanczos_fused_tile() { return kLzT; }
 
 #define SIFT_INST(TG)                                                                                              \

@@ -57,6 +57,19 @@ struct OctaveDev {
     long long u_off;          // byte offset of level 0 in the u8 level arena
     int octave;               // the octave (keypoint scale 2^octave)
     int image;                // the image of a batch (0 for one image)
+    long long t_off;          // byte offset of the entry's horizontal-pass plane (batch runs)
+};
+
+// A batch's pyramid in device memory (u8 storage): the entries of the batch
+// (image-major), the u8 level arena, the horizontal-pass planes, and the
+// input images packed at per-image offsets.
+struct BatchPyr {
+    uint8_t* U;
+    const OctaveDev* ents;
+    int O, S;
+    const uint8_t* img;
+    const long long* img_off;
+    const int* img_pitch;
 };
 
 // The (image, octave) entries of a run in device memory, image-major

@@ -400,3 +400,83 @@ def draw_keypoints_to_image(img, keypoints, color=(255, 0, 0)) -> np.ndarray:
     the GPU by the default engine."""
     with Sift._lock:
         return Sift.default()._engine().draw_keypoints(img, keypoints, color)
+
+
+class Batch:
+    """The batched form (sift_cuda_batch_*): one run over many grayscale
+    images of any sizes, each stage one launch over the flattened work of all
+    of them, captured as one CUDA graph per batch geometry. Every image's
+    result is detect_and_compute's on it, bit for bit. Levels are kept as u8
+    planes."""
+
+    def __init__(self, params: "Sift | _capi.Params | None" = None, device: int = 0):
+        L = _capi.lib()
+        if params is None:
+            params = Sift.default()
+        p = params.to_c() if isinstance(params, Sift) else params
+        opts = _capi.Options()
+        L.sift_cuda_options_default(C.byref(opts))
+        opts.device = device
+        opts.storage = _capi.STORAGE_U8
+        h = C.c_void_p()
+        _capi.check(L.sift_cuda_batch_create(C.byref(p), C.byref(opts), C.byref(h)))
+        self._h = h
+        self.last_launch_count = 0
+        self.last_device_ms = 0.0
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _capi.lib().sift_cuda_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def detect_and_compute(self, images, copy: bool = True) -> list[tuple[np.ndarray, np.ndarray]]:
+        """(keypoints, descriptors) per image, in input order. copy=False
+        returns views of the batch's host buffers, valid until its next call."""
+        if not self._h:
+            raise SiftError("batch is closed")
+        imgs = []
+        for img in images:
+            g = _as_gray(img)
+            if g.strides[1] != 1:
+                g = np.ascontiguousarray(g)
+            imgs.append(g)
+        n = len(imgs)
+        arr = (_capi.BatchImage * max(n, 1))()
+        for i, g in enumerate(imgs):
+            arr[i].data = g.ctypes.data if g.size else None
+            arr[i].width = g.shape[1]
+            arr[i].height = g.shape[0]
+            arr[i].stride = g.strides[0] if g.size else g.shape[1]
+        res = _capi.BatchResult()
+        _capi.check(_capi.lib().sift_cuda_batch_detect_and_compute(self._h, arr, n, C.byref(res)))
+        self.last_launch_count = res.launches
+        self.last_device_ms = float(res.device_ms)
+        if n == 0:
+            return []
+        off = np.ctypeslib.as_array(res.offsets, shape=(n + 1,)).copy()
+        total = int(res.total)
+        if total:
+            kbuf = (C.c_char * (total * KEYPOINT_DTYPE.itemsize)).from_address(res.kps)
+            dbuf = (C.c_char * (total * DESC_LEN * 4)).from_address(res.desc)
+            kall = np.frombuffer(kbuf, dtype=KEYPOINT_DTYPE, count=total)
+            dall = np.frombuffer(dbuf, dtype=np.float32, count=total * DESC_LEN).reshape(total, DESC_LEN)
+        else:
+            kall = np.empty(0, KEYPOINT_DTYPE)
+            dall = np.empty((0, DESC_LEN), np.float32)
+        out = []
+        for i in range(n):
+            k, d = kall[off[i]:off[i + 1]], dall[off[i]:off[i + 1]]
+            out.append((k.copy(), d.copy()) if copy else (k, d))
+        return out
