@@ -1,10 +1,13 @@
-"""Precision statement: both storage modes against the FP64 ideal model (GPU).
+"""Precision statement: the three storage modes against the FP64 ideal model
+(GPU).
 
-F32 storage keeps Gaussian levels as f32 (v/255), F16 storage as f16 (v);
-both form every DoG value in f32 from the u8 level planes. Both hold the reference's u8-quantised levels exactly, so their
-outputs are bit-identical and their errors against the FP64 model (no u8
-rounding; oracle/ideal64.py) are the reference CPU path's own. The test
-prints the statement and checks that both modes give the same numbers.
+F32 storage keeps Gaussian levels as f32 (v/255), F16 storage as f16 (v), U8
+storage keeps only the u8 level planes; all three form every DoG value in
+f32 from the u8 level planes. All hold the reference's u8-quantised levels
+exactly, so their outputs are bit-identical and their errors against the
+FP64 model (no u8 rounding; oracle/ideal64.py) are the reference CPU path's
+own. The test prints the statement and checks that the modes give the same
+numbers.
 """
 import json
 
@@ -25,28 +28,18 @@ def test_precision_statement(built_lib, oracle_mod):
     dims = [(lv[0].shape[1], lv[0].shape[0]) for lv in pyr64]
     report = {"image": "512x512 synthetic, seed 0, Sift::default()"}
     outs = {}
-    for storage in ("f32", "f16"):
+    for storage in ("f32", "f16", "u8"):
         with sg.Engine(sg.Sift.default(), storage=storage) as eng:
             kps, desc = eng.detect_and_compute(img)
-            if storage == "f32":
-                dog = eng.debug_stage(sg.STAGE_DOG)
-            else:
-                # DoG as the f16 mode forms it: f32 differences of the stored levels / 255
-                pyr = eng.debug_stage(sg.STAGE_PYRAMID).astype(np.float32) / np.float32(255.0)
-                parts, off = [], 0
-                for (w, h) in dims:
-                    n = w * h
-                    lv = [pyr[off + s * n: off + (s + 1) * n] for s in range(6)]
-                    parts += [lv[s + 1] - lv[s] for s in range(5)]
-                    off += 6 * n
-                dog = np.concatenate(parts)
+            dog = eng.debug_stage(sg.STAGE_DOG)
         outs[storage] = (kps, desc, dog)
         report[storage] = {"dog": dog_errors(dog, dims, dog64), "keypoints": keypoint_errors(kps, desc, k64, d64)}
     print(json.dumps(report, indent=1))
     k32, dsc32, dog32 = outs["f32"]
-    k16, dsc16, dog16 = outs["f16"]
-    assert k16.tobytes() == k32.tobytes() and dsc16.tobytes() == dsc32.tobytes()
-    assert np.array_equal(dog16, dog32)
+    for storage in ("f16", "u8"):
+        k, dsc, dog = outs[storage]
+        assert k.tobytes() == k32.tobytes() and dsc.tobytes() == dsc32.tobytes(), storage
+        assert np.array_equal(dog, dog32), storage
     # the u8 truncation of every blur pass makes the levels darker, the DoG
     # biased negative by about 1/255 per level
     for row in report["f32"]["dog"]:
