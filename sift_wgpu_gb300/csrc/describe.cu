@@ -53,17 +53,17 @@ constexpr int kDescBudget = 2;  // keypoints per CTA
 // (div255 is the IEEE quotient for every u8 value), so every storage mode
 // reads the same values.
 template <typename T>
-__device__ __forceinline__ float gnorm(const T* p, const float* lut);
+__device__ __forceinline__ float gnorm(const T* p);
 template <>
-__device__ __forceinline__ float gnorm<float>(const float* p, const float*) {
+__device__ __forceinline__ float gnorm<float>(const float* p) {
     return *p;
 }
 template <>
-__device__ __forceinline__ float gnorm<__half>(const __half* p, const float*) {
+__device__ __forceinline__ float gnorm<__half>(const __half* p) {
     return div255(__half2float(*p));
 }
 template <>
-__device__ __forceinline__ float gnorm<uint8_t>(const uint8_t* p, const float*) {
+__device__ __forceinline__ float gnorm<uint8_t>(const uint8_t* p) {
     return div255(float_of_u8(*p));
 }
 
@@ -90,8 +90,7 @@ template <typename TG>
 struct GaussPlane {
     const TG* base;
     int pitch, W, H;
-    const float* lut;  // v / 255 (read by the u8 storage mode only)
-    __device__ __forceinline__ float at(const TG* p) const { return gnorm(p, lut); }
+    __device__ __forceinline__ float at(const TG* p) const { return gnorm(p); }
     // get_gauss_pixel_value (src/sift.rs:218-223)
     __device__ __forceinline__ float px(int x, int y) const {
         x = clampi(x, 0, W - 1);
@@ -123,10 +122,9 @@ struct GaussPlane {
 };
 
 template <typename TG>
-__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const OctaveDev& od, int S, int layer,
-                                                    const float* lut) {
+__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const OctaveDev& od, int S, int layer) {
     const int li = clampi(layer, 0, S + 2);
-    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H, lut};
+    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H};
 }
 
 
@@ -220,7 +218,6 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
 
 template <typename TG>
 __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __restrict__ arena, EntryTable tab,
-                                                                const float* __restrict__ lut255,
                                                                 const Keypoint* __restrict__ refined_at,
                                                                 const uint32_t* __restrict__ keep, uint32_t ncap,
                                                                 OctCounters* __restrict__ oc,
@@ -230,10 +227,7 @@ __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __r
     chain_wait();
     __shared__ float hist[kOriWarps][kOriBins][32];
     __shared__ float hs[kOriWarps][kOriBins];
-    __shared__ float lut[256];
     const int lane = threadIdx.x, wid = threadIdx.y;
-    for (int v = threadIdx.y * 32 + lane; v < 256; v += 32 * kOriWarps) lut[v] = lut255[v];
-    __syncthreads();
     const uint32_t n = min(oc->n_cand, ncap);  // candidate slots; rejected ones get 0 peaks
     const float two_pi = 2.0f * kPi;
     const float bin_w = 2.0f * kPi / (float)kOriBins;
@@ -254,7 +248,7 @@ __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __r
         if (e >= 0 && e < tab.n) {
             const OctaveDev od = tab.ents[e];
             const int o = od.octave;
-            const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer, lut);
+            const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer);
             const float scale = __int_as_float((127 + o) << 23);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float so = __fdiv_rn(kp.size, scale);
@@ -392,16 +386,17 @@ constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad
 //  1. The bilinear samples the gradients need, bilinear(xo + i, yo + j) for
 //     integer offsets i, j in [-(rad+1), rad+1], go to a shared grid once
 //     (the reference re-evaluates four bilinears per window sample).
-//  2. Each thread takes window samples in the reference's f32 order; the
-//     eight trilinear contributions are added to 128 shared bins as u32 fixed
-//     point (2^-f units, f chosen so no bin can overflow): integer addition is
-//     associative, so the descriptor is the same on every run.
+//  2. Each thread takes pairs of neighbouring window samples and evaluates
+//     both at once with Blackwell's packed f32x2 multiply/add/FMA (the kernel
+//     is bound by instruction issue); the eight trilinear contributions of
+//     each are added to 128 shared bins as u32 fixed point (2^-f units, f
+//     chosen so no bin can overflow): integer addition is associative, so the
+//     descriptor is the same on every run.
 //  3. Warp 0 normalises, clips at 0.2, renormalises.
 // Radii above the grid (not reachable with the default sigma) fall back to
 // per-sample bilinears from the level itself.
 template <typename TG>
 __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __restrict__ arena, EntryTable tab,
-                                                              const float* __restrict__ lut255,
                                                               const Keypoint* __restrict__ oriented,
                                                               OctCounters* __restrict__ oc,
                                                               float* __restrict__ desc, uint32_t cap,
@@ -417,11 +412,9 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     // banks apart; picking the copy by l >> 2 instead (4 neighbours per
     // copy) costs 13 % more time. The copies are summed in a fixed order;
     // integer sums make the order irrelevant.
-    __shared__ unsigned int hist[kHistCopies * kHistStride];
+    __shared__ __align__(16) unsigned int hist[kHistCopies * kHistStride];
     __shared__ float red_lo[kDescThreads / 32], red_hi[kDescThreads / 32];
-    __shared__ float lut[256];
     const int tid = threadIdx.x;
-    for (int v = tid; v < 256; v += kDescThreads) lut[v] = lut255[v];
     const uint32_t base = oc->out_base;
     uint32_t n = oc->n_ori;
     if (base >= cap) n = 0;
@@ -437,7 +430,8 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
         const uint32_t i = base + next;
         const Keypoint kp = oriented[i];
         const int e = kp.octave;  // entry
-        for (int i = tid; i < kHistCopies * kHistStride; i += kDescThreads) hist[i] = 0u;
+        for (int i = tid; i < kHistCopies * kHistStride / 4; i += kDescThreads)
+            reinterpret_cast<uint4*>(hist)[i] = make_uint4(0u, 0u, 0u, 0u);
         const bool valid_oct = e >= 0 && e < tab.n;
         OctaveDev od{};
         if (valid_oct) od = tab.ents[e];
@@ -447,7 +441,7 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
         const bool valid = valid_oct && so > 0.0f;
         float inv_fix = 0.0f;
         if (valid) {
-            const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer, lut);
+            const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer);
             const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
             const float ang = kp.angle;
             const float ca = cosf(ang), sa = sinf(ang);
@@ -550,13 +544,13 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
             const float to_fix = __int_as_float((127 + fbits) << 23);
             inv_fix = __int_as_float((127 - fbits) << 23);
             // Descriptor samples are interpolated linearly into their bins, so
-            // this loop is written for speed within the descriptor tolerance:
-            // fused multiply-adds, reciprocal products instead of divisions,
-            // the hardware's approximate square root and exp2 (scale folded
-            // in), an arctangent polynomial in units of angle bins (error
-            // 1.5e-5 bin) from which the relative angle is binned directly
-            // (floor and & 7 give the rem_euclid bins), and the fixed-point
-            // rounding fused into the weight product. Each changes a
+            // the sample loops are written for speed within the descriptor
+            // tolerance: fused multiply-adds, reciprocal products instead of
+            // divisions, the hardware's approximate square root and exp2
+            // (scale folded in), an arctangent polynomial in units of angle
+            // bins (error 1.5e-5 bin) from which the relative angle is binned
+            // directly (floor and & 7 give the rem_euclid bins), and the
+            // fixed-point rounding fused into the weight product. Each changes a
             // descriptor value by ~1e-5 or less.
             const float inv_bw = 1.0f / bw;
             const float angb = ang * (4.0f / kPi);  // keypoint angle in 45-degree bins
@@ -570,73 +564,149 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
             // windows that stay inside the level need no per-sample border test
             const bool edge = !(__fadd_rn(xo, -rad_f) >= 0.0f && __fadd_rn(xo, rad_f) < wm1 &&
                                 __fadd_rn(yo, -rad_f) >= 0.0f && __fadd_rn(yo, rad_f) < hm1);
-            // Sample k of the window (row-major) is (px, py) = (k % side - rad,
-            // k / side - rad), grid index c = (py + rad + 1) * gs + px + rad + 1.
-            // A thread steps k by the block size: px, py (exact small integers
-            // in f32) and c advance by fixed amounts, with one wrap per step.
-            const int q0 = tid / side, dq = kDescThreads / side;
-            const float dr_f = (float)(kDescThreads - dq * side), dq_f = (float)dq;
-            const int dc = dq * gs + (kDescThreads - dq * side);
-            auto samples = [&](auto edge_tag) {
-                constexpr bool kEdge = decltype(edge_tag)::value;
-                float px = (float)(tid - q0 * side) - rad_f, py = (float)q0 - rad_f;
-                int c = (q0 + 1) * gs + (tid - q0 * side) + 1;
-                for (;; px += dr_f, py += dq_f, c += dc) {
-                    // the wrap to the next row as selects: a branch here would
-                    // split the warp for the rest of the step
-                    const bool wrap = px > rad_f;
-                    px = wrap ? px - side_f : px;
-                    py = wrap ? py + 1.0f : py;
-                    c = wrap ? c + 2 : c;
-                    if (py > rad_f) break;
-                    const float rx = fmaf(ca, px, sa * py);
-                    const float ry = fmaf(-sa, px, ca * py);
-                    bool in = fabsf(rx) < lim && fabsf(ry) < lim;
-                    if constexpr (kEdge) {
-                        const float xs = xo + px, ys = yo + py;
-                        in = in && !(xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1);
-                    }
-                    // warps whose 32 samples all fall outside skip the rest
-                    if (!__any_sync(__activemask(), in)) continue;
-                    float gx, gy;
-                    if (use_grid) {
-                        gx = grid[c + 1] - grid[c - 1];
-                        gy = grid[c + gs] - grid[c - gs];
-                    } else {
-                        const float xs = xo + px, ys = yo + py;
-                        gx = __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
-                        gy = __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
-                    }
-                    if (in) {
-                        const float mag = sqrt_approx(fmaf(gx, gx, gy * gy));
-                        const float wm = mag * ex2_approx(fmaf(px, px, py * py) * wexp);
-                        const float ab = atan2_bins(gy, gx) - angb;  // in [-12, 4]
-                        const float xb = fmaf(rx, inv_bw, 1.5f), yb = fmaf(ry, inv_bw, 1.5f);
-                        int xbi, ybi, abi;
-                        const float xbf = floor_fi(xb, &xbi), ybf = floor_fi(yb, &ybi), abf = floor_fi(ab, &abi);
-                        const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
-                        const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
-                        // cells (xbi + i, ybi + j), i, j in {0, 1}: xbi, ybi in
-                        // -1..3, so all four lie in the padded 6 x 6 grid; the
-                        // eight adds are unconditional (a zero share adds 0)
-                        const float wx0 = 1.0f - fx, wx1 = fx;
-                        const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
-                        unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
+            if (use_grid) {
+                // Sample pairs: a thread takes window samples k and k + 1 (k
+                // even, row-major; (px, py) = (k % side - rad, k / side - rad))
+                // and evaluates both with packed f32x2 arithmetic, the same
+                // operations per element as one sample alone. Pair m = tid +
+                // 256 j: px, py (exact small integers in f32) and the grid
+                // index c of element 0 advance by fixed amounts with one wrap
+                // per step; element 1 is the next position of the row, or the
+                // first of the next row.
+                const int k0 = 2 * tid;
+                const int q0 = floor_i(((float)k0 + 0.5f) * (1.0f / side_f));
+                const int dq = (2 * kDescThreads) / side;
+                const float dr_f = (float)(2 * kDescThreads - dq * side), dq_f = (float)dq;
+                const int dc = dq * gs + (2 * kDescThreads - dq * side);
+                // the fixed-point scale rides in the exponent: exp2(d2 * wexp +
+                // fbits) = 2^fbits exp(-d2 / wd)
+                const float fb = (float)fbits;
+                const float2 ca2 = make_float2(ca, ca), sa2 = make_float2(sa, sa), nsa2 = make_float2(-sa, -sa);
+                const float2 ib2 = make_float2(inv_bw, inv_bw), half3 = make_float2(1.5f, 1.5f);
+                const float2 wexp2 = make_float2(wexp, wexp), fb2 = make_float2(fb, fb);
+                const float2 m15 = make_float2(kMagic15, kMagic15), nm15 = make_float2(-kMagic15, -kMagic15);
+                const float2 neg1 = make_float2(-1.0f, -1.0f), one2 = make_float2(1.0f, 1.0f);
+                const float2 mag2c = make_float2(kMagic, kMagic), angb2 = make_float2(angb, angb);
+                auto pairs = [&](auto edge_tag) {
+                    constexpr bool kEdge = decltype(edge_tag)::value;
+                    float px = (float)(k0 - q0 * side) - rad_f, py = (float)q0 - rad_f;
+                    int c = (q0 + 1) * gs + (k0 - q0 * side) + 1;
+                    for (;; px += dr_f, py += dq_f, c += dc) {
+                        const bool wrap = px > rad_f;
+                        px = wrap ? px - side_f : px;
+                        py = wrap ? py + 1.0f : py;
+                        c = wrap ? c + 2 : c;
+                        if (py > rad_f) break;
+                        // element 1: the row's next position or the next row's
+                        // first (grid index + 3); past the last row it is a
+                        // phantom that reads element 0's grid values
+                        const bool w1 = px >= rad_f;
+                        const float px1 = w1 ? -rad_f : px + 1.0f, py1 = w1 ? py + 1.0f : py;
+                        const bool v1 = py1 <= rad_f;
+                        const int c1 = v1 ? (w1 ? c + 3 : c + 1) : c;
+                        const float2 P = make_float2(px, px1), Q = make_float2(py, py1);
+                        const float2 rx = __ffma2_rn(P, ca2, __fmul2_rn(Q, sa2));
+                        const float2 ry = __ffma2_rn(P, nsa2, __fmul2_rn(Q, ca2));
+                        bool in0 = fabsf(rx.x) < lim && fabsf(ry.x) < lim;
+                        bool in1 = v1 && fabsf(rx.y) < lim && fabsf(ry.y) < lim;
+                        if constexpr (kEdge) {
+                            const float xs0 = xo + px, ys0 = yo + py, xs1 = xo + px1, ys1 = yo + py1;
+                            in0 = in0 && !(xs0 < 0.0f || xs0 >= wm1 || ys0 < 0.0f || ys0 >= hm1);
+                            in1 = in1 && !(xs1 < 0.0f || xs1 >= wm1 || ys1 < 0.0f || ys1 >= hm1);
+                        }
+                        // warps whose 64 samples all fall outside skip the rest
+                        if (!__any_sync(__activemask(), in0 || in1)) continue;
+                        if (!(in0 || in1)) continue;
+                        const float2 gx = __ffma2_rn(make_float2(grid[c - 1], grid[c1 - 1]), neg1,
+                                                     make_float2(grid[c + 1], grid[c1 + 1]));
+                        const float2 gy = __ffma2_rn(make_float2(grid[c - gs], grid[c1 - gs]), neg1,
+                                                     make_float2(grid[c + gs], grid[c1 + gs]));
+                        const float2 m2 = __ffma2_rn(gx, gx, __fmul2_rn(gy, gy));
+                        const float2 ea = __ffma2_rn(__ffma2_rn(P, P, __fmul2_rn(Q, Q)), wexp2, fb2);
+                        float2 wm = __fmul2_rn(make_float2(sqrt_approx(m2.x), sqrt_approx(m2.y)),
+                                               make_float2(ex2_approx(ea.x), ex2_approx(ea.y)));
+                        // an element outside the window adds zero shares to
+                        // cell (-1, -1) of its copy
+                        wm.x = in0 ? wm.x : 0.0f;
+                        wm.y = in1 ? wm.y : 0.0f;
+                        const float2 ab = __fadd2_rn(atan2_bins2(gy, gx), make_float2(-angb, -angb));
+                        const float2 xb = __ffma2_rn(rx, ib2, half3), yb = __ffma2_rn(ry, ib2, half3);
+                        // floors by the 1.5 * 2^23 rounding-down add: the low
+                        // bits of tx, ty, ta are the integers
+                        const float2 tx = __fadd2_rd(xb, m15), ty = __fadd2_rd(yb, m15), ta = __fadd2_rd(ab, m15);
+                        const float2 fx = __ffma2_rn(__fadd2_rn(tx, nm15), neg1, xb);
+                        const float2 fy = __ffma2_rn(__fadd2_rn(ty, nm15), neg1, yb);
+                        const float2 fa = __ffma2_rn(__fadd2_rn(ta, nm15), neg1, ab);
+                        // histogram word of cell (xbi, ybi), bin abi & 7:
+                        // ((ybi + 1) * 6 + xbi + 1) * 9 + (abi & 7), from the
+                        // float bits (the 0x4B400000 offsets cancel mod 2^32,
+                        // 0x4B400000 & 7 == 0)
+                        constexpr uint32_t kCellOff = 63u - 63u * 0x4B400000u;
+                        uint32_t at0 = __float_as_uint(ty.x) * (uint32_t)(kHistSide * kHistRow) +
+                                       __float_as_uint(tx.x) * (uint32_t)kHistRow + kCellOff +
+                                       (__float_as_uint(ta.x) & 7u);
+                        uint32_t at1 = __float_as_uint(ty.y) * (uint32_t)(kHistSide * kHistRow) +
+                                       __float_as_uint(tx.y) * (uint32_t)kHistRow + kCellOff +
+                                       (__float_as_uint(ta.y) & 7u);
+                        at0 = in0 ? at0 : 0u;
+                        at1 = in1 ? at1 : 0u;
+                        const float2 wy0 = __fmul2_rn(wm, __ffma2_rn(fy, neg1, one2)), wy1 = __fmul2_rn(wm, fy);
+                        const float2 wx0 = __ffma2_rn(fx, neg1, one2);
+                        const float2 wa0 = __ffma2_rn(fa, neg1, one2);
+                        unsigned int* h0 = hcopy + at0;
+                        unsigned int* h1 = hcopy + at1;
 #pragma unroll
                         for (int cc = 0; cc < 4; ++cc) {
-                            const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
-                            unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
-                            // the product rounded to the nearest integer (< 2^23 by the scale choice)
-                            atomicAdd(hc, __float_as_uint(__fmaf_rn(wxy, wa0, kMagic)) - 0x4B000000u);
-                            atomicAdd(hc + 1, __float_as_uint(__fmaf_rn(wxy, wa1, kMagic)) - 0x4B000000u);
+                            const float2 wxy = __fmul2_rn((cc & 1) ? fx : wx0, (cc & 2) ? wy1 : wy0);
+                            const int off = ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
+                            // the products rounded to the nearest integer (< 2^23 by the scale choice)
+                            const float2 n0 = __ffma2_rn(wxy, wa0, mag2c), n1 = __ffma2_rn(wxy, fa, mag2c);
+                            atomicAdd(h0 + off, __float_as_uint(n0.x) - 0x4B000000u);
+                            atomicAdd(h0 + off + 1, __float_as_uint(n1.x) - 0x4B000000u);
+                            atomicAdd(h1 + off, __float_as_uint(n0.y) - 0x4B000000u);
+                            atomicAdd(h1 + off + 1, __float_as_uint(n1.y) - 0x4B000000u);
                         }
                     }
+                };
+                if (edge)
+                    pairs(std::true_type{});
+                else
+                    pairs(std::false_type{});
+            } else {
+                // Radii above the grid: one sample per thread, four bilinears
+                // from the level per sample (the reference's own evaluation).
+                for (int k = tid; k < total; k += kDescThreads) {
+                    const int qy = k / side;
+                    const float px = (float)(k - qy * side) - rad_f, py = (float)qy - rad_f;
+                    const float rx = fmaf(ca, px, sa * py);
+                    const float ry = fmaf(-sa, px, ca * py);
+                    if (!(fabsf(rx) < lim && fabsf(ry) < lim)) continue;
+                    const float xs = xo + px, ys = yo + py;
+                    if (xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1) continue;
+                    const float gx =
+                        __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
+                    const float gy =
+                        __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
+                    const float mag = sqrt_approx(fmaf(gx, gx, gy * gy));
+                    const float wm = mag * ex2_approx(fmaf(px, px, py * py) * wexp);
+                    const float ab = atan2_bins(gy, gx) - angb;  // in [-12, 4]
+                    const float xb = fmaf(rx, inv_bw, 1.5f), yb = fmaf(ry, inv_bw, 1.5f);
+                    int xbi, ybi, abi;
+                    const float xbf = floor_fi(xb, &xbi), ybf = floor_fi(yb, &ybi), abf = floor_fi(ab, &abi);
+                    const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
+                    const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
+                    const float wx0 = 1.0f - fx, wx1 = fx;
+                    const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
+                    unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
+                        unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
+                        atomicAdd(hc, __float_as_uint(__fmaf_rn(wxy, wa0, kMagic)) - 0x4B000000u);
+                        atomicAdd(hc + 1, __float_as_uint(__fmaf_rn(wxy, wa1, kMagic)) - 0x4B000000u);
+                    }
                 }
-            };
-            if (edge)
-                samples(std::true_type{});
-            else
-                samples(std::false_type{});
+            }
         }
         __syncthreads();
         // normalize_and_clip_descriptor (src/sift.rs:889-913)
@@ -690,10 +760,10 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
 }  // namespace
 
 template <typename TG>
-int launch_orientation(const TG* arena, const EntryTable& tab, const float* lut255, const Keypoint* refined_at,
+int launch_orientation(const TG* arena, const EntryTable& tab, const Keypoint* refined_at,
                        const uint32_t* keep, uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count,
                        int grid, int persist_ctas, cudaStream_t st) {
-    if (launch_chained(k_orientation<TG>, grid, dim3(32, kOriWarps), 0, st, arena, tab, lut255, refined_at, keep, ncap,
+    if (launch_chained(k_orientation<TG>, grid, dim3(32, kOriWarps), 0, st, arena, tab, refined_at, keep, ncap,
                        oc, ori_angle, ori_count, std::max(grid - persist_ctas, 0)) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
@@ -709,20 +779,20 @@ int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counter
 }
 
 template <typename TG>
-int launch_descriptor(const TG* arena, const EntryTable& tab, const float* lut255, const Keypoint* oriented,
+int launch_descriptor(const TG* arena, const EntryTable& tab, const Keypoint* oriented,
                       OctCounters* oc, float* desc, uint32_t cap, float* hdesc, uint32_t hcap, int grid,
                       int persist_ctas, cudaStream_t st) {
     if (!hdesc) hcap = 0;
-    if (launch_chained(k_descriptor<TG>, grid, kDescThreads, 0, st, arena, tab, lut255, oriented, oc, desc, cap, hdesc,
+    if (launch_chained(k_descriptor<TG>, grid, kDescThreads, 0, st, arena, tab, oriented, oc, desc, cap, hdesc,
                        hcap, std::max(grid - persist_ctas, 0)) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 #define SIFT_INST(TG)                                                                                              \
-    template int launch_orientation<TG>(const TG*, const EntryTable&, const float*, const Keypoint*, const uint32_t*, \
+    template int launch_orientation<TG>(const TG*, const EntryTable&, const Keypoint*, const uint32_t*,           \
                                         uint32_t, OctCounters*, float*, uint32_t*, int, int, cudaStream_t);        \
-    template int launch_descriptor<TG>(const TG*, const EntryTable&, const float*, const Keypoint*, OctCounters*,  \
+    template int launch_descriptor<TG>(const TG*, const EntryTable&, const Keypoint*, OctCounters*,                \
                                        float*, uint32_t, float*, uint32_t, int, int, cudaStream_t);
 SIFT_INST(float)
 SIFT_INST(__half)

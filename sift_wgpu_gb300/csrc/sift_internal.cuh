@@ -229,6 +229,39 @@ __device__ __forceinline__ float atan2_bins(float y, float x) {
     return copysignf(r, y);
 }
 
+// atan2_bins of two gradients at once: the same polynomial and octant
+// fix-ups evaluated on f32x2 pairs (each element rounds as the scalar
+// operations do), with a = min * rcp(max) by the hardware reciprocal, so the
+// same error bound (tests/test_atan2_gpu.py).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float2 atan2_bins2(float2 y, float2 x) {
+    const float ax0 = fabsf(x.x), ay0 = fabsf(y.x), ax1 = fabsf(x.y), ay1 = fabsf(y.y);
+    const float2 mx = make_float2(fmaxf(ax0, ay0), fmaxf(ax1, ay1));
+    const float2 mn = make_float2(fminf(ax0, ay0), fminf(ax1, ay1));
+    // max(mx, 1e-30): atan2(0, 0) = 0 * 1e30 = 0
+    const float2 a =
+        __fmul2_rn(mn, make_float2(rcp_approx(fmaxf(mx.x, 1e-30f)), rcp_approx(fmaxf(mx.y, 1e-30f))));
+    const float2 t = __fmul2_rn(a, a);
+    float2 p = __ffma2_rn(make_float2(0.02654082328081131f, 0.02654082328081131f), t,
+                          make_float2(-0.10842443257570267f, -0.10842443257570267f));
+    p = __ffma2_rn(p, t, make_float2(0.22938594222068787f, 0.22938594222068787f));
+    p = __ffma2_rn(p, t, make_float2(-0.4205571115016937f, -0.4205571115016937f));
+    p = __ffma2_rn(p, t, make_float2(1.2730693817138672f, 1.2730693817138672f));
+    float2 r = __fmul2_rn(p, a);
+    const float2 neg1 = make_float2(-1.0f, -1.0f);
+    const float2 r2 = __ffma2_rn(r, neg1, make_float2(2.0f, 2.0f));
+    r.x = ay0 > ax0 ? r2.x : r.x;
+    r.y = ay1 > ax1 ? r2.y : r.y;
+    const float2 r4 = __ffma2_rn(r, neg1, make_float2(4.0f, 4.0f));
+    r.x = x.x < 0.0f ? r4.x : r.x;
+    r.y = x.y < 0.0f ? r4.y : r.y;
+    return make_float2(copysignf(r.x, y.x), copysignf(r.y, y.y));
+}
+
 // The hardware's approximate square root and base-2 exponential (one
 // instruction each; subnormal inputs and results flush to zero).
 __device__ __forceinline__ float sqrt_approx(float x) {

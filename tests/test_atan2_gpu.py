@@ -1,8 +1,9 @@
 """The engine's arctangent polynomials against CUDA's atan2f (GPU).
 
 atan2_poly decides orientation bins away from bin edges (within 1e-4 bin of
-an edge the exact atan2f path decides), atan2_bins places descriptor samples
-in their 45-degree bins (linearly interpolated). Both are evaluated on the
+an edge the exact atan2f path decides), atan2_bins and its f32x2 pair form
+atan2_bins2 place descriptor samples in their 45-degree bins (linearly
+interpolated). Both are evaluated on the
 device by tests/atan2_probe.cu over a dense grid of directions and
 magnitudes, the exact axes, the 36 orientation-bin edges and the 8
 descriptor-bin edges, and quantised gradients (differences of v / 255)."""
@@ -28,7 +29,7 @@ def probe(tmp_path_factory):
                     "-I", str(HERE.parent / "include"), "-Xcompiler", "-fPIC", "-shared", "-o", str(out),
                     str(HERE / "atan2_probe.cu")], check=True)
     L = C.CDLL(str(out))
-    L.atan2_probe.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.atan2_probe.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     return L
 
 
@@ -54,8 +55,9 @@ def inputs():
 def test_polynomials_against_atan2f(probe):
     y, x = inputs()
     n = len(y)
-    poly, bins, ref = (np.empty(n, np.float32) for _ in range(3))
-    assert probe.atan2_probe(y.ctypes.data, x.ctypes.data, n, poly.ctypes.data, bins.ctypes.data, ref.ctypes.data) == 0
+    poly, bins, bins2, ref = (np.empty(n, np.float32) for _ in range(4))
+    assert probe.atan2_probe(y.ctypes.data, x.ctypes.data, n, poly.ctypes.data, bins.ctypes.data, bins2.ctypes.data,
+                             ref.ctypes.data) == 0
     ref64 = ref.astype(np.float64)
     # atan2_poly: within 4 ulp of atan2f's angle (or 1e-12 rad near 0)
     err = np.abs(poly.astype(np.float64) - ref64)
@@ -68,6 +70,10 @@ def test_polynomials_against_atan2f(probe):
     # atan2_bins: within 1.5e-5 of atan2f * 4 / pi, in bins
     eb = np.abs(bins.astype(np.float64) - ref64 * 4 / math.pi)
     assert float(eb.max()) < 1.5e-5 + 1e-6, float(eb.max())
+    # the pair form (hardware reciprocal instead of the fast division): the
+    # same bound
+    eb2 = np.abs(bins2.astype(np.float64) - ref64 * 4 / math.pi)
+    assert float(eb2.max()) < 1.5e-5 + 1e-6, float(eb2.max())
     # exact axes and the origin
     for (yy, xx, want) in [(0.0, 0.0, 0.0), (0.0, 1.0, 0.0), (1.0, 0.0, 2.0), (-1.0, 0.0, -2.0)]:
         k = np.nonzero((y == yy) & (x == xx))[0][0]
