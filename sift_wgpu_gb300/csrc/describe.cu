@@ -374,6 +374,7 @@ __global__ void k_orient_emit(const Keypoint* __restrict__ refined_at, uint32_t 
 }
 
 constexpr int kDescThreads = 128;
+static_assert(kDescThreads == kDescLen && kDescThreads == 128, "one descriptor bin per thread, four warps");
 constexpr int kHistRow = 9;      // 8 angle bins + slot 8, the share of bin 0 that wrapped from bin 7
 constexpr int kHistSide = 6;     // cells -1..4 per axis: the 4 x 4 window and a border that takes the
                                  // trilinear spill, so no sample needs a clamp or a validity test
@@ -420,31 +421,41 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     if (base >= cap) n = 0;
     else if (n > cap - base) n = cap - base;
     const float sqrt2 = __fsqrt_rn(2.0f);
-    __shared__ uint32_t next;
+    // Keypoints differ ~4x in window area: they come from a queue. Thread 0
+    // claims the next item while the CTA works on the current one (slot
+    // next[p ^ 1]), unless the CTA retires after the current one.
+    __shared__ uint32_t next[2];
     const bool persist = (int)blockIdx.x >= persist_from;
-    for (int taken = 0; persist || taken < kDescBudget; ++taken) {
-        // keypoints differ ~4x in window area: take them from a queue
-        if (tid == 0) next = atomicAdd(&oc->next_desc, 1u);
-        __syncthreads();
-        if (next >= n) break;
-        const uint32_t i = base + next;
+    if (tid == 0) next[0] = atomicAdd(&oc->next_desc, 1u);
+    for (int taken = 0, p = 0;; ++taken, p ^= 1) {
+        __syncthreads();  // next[p] is visible, the grid and histogram are free
+        const uint32_t cur = next[p];
+        if (cur >= n) break;
+        const bool more = persist || taken + 1 < kDescBudget;
+        uint32_t claim = n;
+        if (tid == 0 && more) claim = atomicAdd(&oc->next_desc, 1u);
+        const uint32_t i = base + cur;
         const Keypoint kp = oriented[i];
         const int e = kp.octave;  // entry
-        for (int i = tid; i < kHistCopies * kHistStride / 4; i += kDescThreads)
-            reinterpret_cast<uint4*>(hist)[i] = make_uint4(0u, 0u, 0u, 0u);
+        for (int w = tid; w < kHistCopies * kHistStride / 4; w += kDescThreads)
+            reinterpret_cast<uint4*>(hist)[w] = make_uint4(0u, 0u, 0u, 0u);
         const bool valid_oct = e >= 0 && e < tab.n;
         OctaveDev od{};
         if (valid_oct) od = tab.ents[e];
         const int o = od.octave;
-        const float scale = valid_oct ? __int_as_float((127 + o) << 23) : 1.0f;
-        const float so = valid_oct ? __fdiv_rn(kp.size, scale) : 0.0f;
+        // division by 2^o is the multiplication by 2^-o, exactly
+        const float inv_scale = valid_oct ? __int_as_float((127 - o) << 23) : 1.0f;
+        const float so = valid_oct ? __fmul_rn(kp.size, inv_scale) : 0.0f;
         const bool valid = valid_oct && so > 0.0f;
         float inv_fix = 0.0f;
         if (valid) {
             const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer);
-            const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
+            const float xo = __fmul_rn(kp.x, inv_scale), yo = __fmul_rn(kp.y, inv_scale);
             const float ang = kp.angle;
-            const float ca = cosf(ang), sa = sinf(ang);
+            // the hardware sine and cosine (|ang| <= pi; absolute error ~4e-7,
+            // a shift of ~1e-5 px at the window's edge)
+            float sa, ca;
+            __sincosf(ang, &sa, &ca);
             const float bw = __fmul_rn(3.0f, so);
             const float ww = __fmul_rn(bw, 4.0f);
             const float wsig = __fmul_rn(0.5f, ww);
@@ -708,52 +719,42 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                 }
             }
         }
-        __syncthreads();
-        // normalize_and_clip_descriptor (src/sift.rs:889-913)
-        if (tid < 32) {
-            float d[4];
+        __syncthreads();  // the histogram is complete
+        // normalize_and_clip_descriptor (src/sift.rs:889-913), one bin per
+        // thread; the sums of squares over the four warps in a fixed order
+        {
+            const int bin = tid;  // (iy * 4 + ix) * 8 + ia
+            const int cell = bin >> 3, ia = bin & 7;
+            const int at = (((cell >> 2) + 1) * kHistSide + (cell & 3) + 1) * kHistRow + ia;
+            unsigned v = 0u;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int bin = tid + 32 * q;  // (iy * 4 + ix) * 8 + ia
-                const int cell = bin >> 3, ia = bin & 7;
-                const int at = (((cell >> 2) + 1) * kHistSide + (cell & 3) + 1) * kHistRow + ia;
-                unsigned v = 0u;
+            for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at];
+            if (ia == 0)
 #pragma unroll
-                for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at];
-                if (ia == 0)
-#pragma unroll
-                    for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at + 8];
-                d[q] = __fmul_rn((float)v, inv_fix);
-            }
-            float ss = 0.0f;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) ss = __fadd_rn(ss, __fmul_rn(d[q], d[q]));
+                for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at + 8];
+            float d = __fmul_rn((float)v, inv_fix);
+            float ss = __fmul_rn(d, d);
 #pragma unroll
             for (int m = 16; m > 0; m >>= 1) ss = __fadd_rn(ss, __shfl_xor_sync(0xffffffffu, ss, m));
-            const float norm = __fsqrt_rn(ss);
-            if (!(norm < 1e-8f)) {
-                const float inv = __fdiv_rn(1.0f, norm);
-                float s2 = 0.0f;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    d[q] = fminf(__fmul_rn(d[q], inv), 0.2f);
-                    s2 = __fadd_rn(s2, __fmul_rn(d[q], d[q]));
-                }
+            if ((tid & 31) == 0) red_lo[tid >> 5] = ss;
+            __syncthreads();
+            const float norm = __fsqrt_rn(__fadd_rn(__fadd_rn(red_lo[0], red_lo[1]), __fadd_rn(red_lo[2], red_lo[3])));
+            if (!(norm < 1e-8f)) {  // the same for every thread
+                d = fminf(__fmul_rn(d, __fdiv_rn(1.0f, norm)), 0.2f);
+                float s2 = __fmul_rn(d, d);
 #pragma unroll
                 for (int m = 16; m > 0; m >>= 1) s2 = __fadd_rn(s2, __shfl_xor_sync(0xffffffffu, s2, m));
-                const float n2 = __fsqrt_rn(s2);
-                if (!(n2 < 1e-8f)) {
-                    const float inv2 = __fdiv_rn(1.0f, n2);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) d[q] = __fmul_rn(d[q], inv2);
-                }
+                if ((tid & 31) == 0) red_hi[tid >> 5] = s2;
+                __syncthreads();
+                const float n2 =
+                    __fsqrt_rn(__fadd_rn(__fadd_rn(red_hi[0], red_hi[1]), __fadd_rn(red_hi[2], red_hi[3])));
+                if (!(n2 < 1e-8f)) d = __fmul_rn(d, __fdiv_rn(1.0f, n2));
             }
             // keypoints below hcap straight into the host call's mapped buffer
             float* dst = (i < hcap ? hdesc : desc) + (size_t)i * kDescLen;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) dst[tid + 32 * q] = d[q];
+            dst[bin] = d;
         }
-        __syncthreads();
+        if (tid == 0) next[p ^ 1] = claim;
     }
 }
 
