@@ -480,32 +480,43 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                 const bool inner = px0 >= 0 && py0 >= 0 && px0 + gs < g.W && py0 + gs < g.H;
                 const float inv_gs = 1.0f / (float)gs;
                 if (inner) {
-                    // A thread makes a column strip of 4 grid points from 5
-                    // pixel rows: each row's horizontal lerp serves two points
-                    // (10 loads for 4 points); consecutive lanes take
-                    // consecutive columns. The same two lerps per point as
-                    // below, so the same values.
-                    const int strips = (gs + 3) >> 2;
+                    // A thread makes a strip of 4 x 2 grid points from 5 x 3
+                    // pixels: each row's horizontal lerps serve the points
+                    // above and below it, both columns at once on f32x2
+                    // pairs (15 loads for 8 points); consecutive lanes take
+                    // consecutive column pairs. The same two lerps per point
+                    // as below, so the same values.
+                    const int strips = (gs + 3) >> 2, cps = (gs + 1) >> 1;
+                    const float inv_cps = 1.0f / (float)cps;
                     const TG* org = g.base + py0 * g.pitch + px0;
+                    const float2 fdx2 = make_float2(fdx, fdx), fdy2 = make_float2(fdy, fdy);
+                    const float2 neg1 = make_float2(-1.0f, -1.0f);
                     float tf = (float)tid;
-                    for (int t = tid; t < strips * gs; t += kDescThreads, tf += (float)kDescThreads) {
-                        const int sy = floor_i((tf + 0.5f) * inv_gs);
-                        const int qx = t - sy * gs, qy0 = 4 * sy;
+                    for (int t = tid; t < strips * cps; t += kDescThreads, tf += (float)kDescThreads) {
+                        const int sy = floor_i((tf + 0.5f) * inv_cps);
+                        const int qx = 2 * (t - sy * cps), qy0 = 4 * sy;
                         const int nr = min(4, gs - qy0);
+                        // an odd-width grid's last pair has a phantom second
+                        // column: its third pixel repeats the second (in
+                        // bounds) and nothing is stored for it
+                        const bool two = qx + 1 < gs;
+                        const int o2 = two ? 2 : 1;
                         const TG* pp = org + qy0 * g.pitch + qx;
-                        float a0 = graw(pp), a1 = graw(pp + 1);
-                        float rp = fmaf(fdx, a1 - a0, a0);
+                        float2 A = make_float2(graw(pp), graw(pp + 1));
+                        float2 rp = __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(A.y, graw(pp + o2))), A);
+                        float* gp = grid + qy0 * gs + qx;
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             if (j < nr) {
                                 pp += g.pitch;
-                                a0 = graw(pp);
-                                a1 = graw(pp + 1);
-                                const float rn = fmaf(fdx, a1 - a0, a0);
-                                const float b = fmaf(fdy, rn - rp, rp);
-                                grid[(qy0 + j) * gs + qx] = b;
-                                lo = fminf(lo, b);
-                                hi = fmaxf(hi, b);
+                                A = make_float2(graw(pp), graw(pp + 1));
+                                const float2 rn =
+                                    __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(A.y, graw(pp + o2))), A);
+                                const float2 b = __ffma2_rn(fdy2, __ffma2_rn(rp, neg1, rn), rp);
+                                gp[j * gs] = b.x;
+                                if (two) gp[j * gs + 1] = b.y;
+                                lo = fminf(lo, fminf(b.x, b.y));
+                                hi = fmaxf(hi, fmaxf(b.x, b.y));
                                 rp = rn;
                             }
                         }
@@ -550,8 +561,9 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
             // and every single contribution (<= sqrt(2) * range) below 2^23,
             // where the rounding add below converts it exactly
             const float per = 1.4143f * range;
-            const int fbits = max(0, min(40, min(floor_i(log2f(4.0e9f / (per * (float)total))),
-                                                 floor_i(log2f(8.0e6f / per)))));
+            // floor(log2 q) of a positive normal float is its exponent field
+            const int fbits = max(0, min(40, min((__float_as_int(4.0e9f / (per * (float)total)) >> 23) - 127,
+                                                 (__float_as_int(8.0e6f / per) >> 23) - 127)));
             const float to_fix = __int_as_float((127 + fbits) << 23);
             inv_fix = __int_as_float((127 - fbits) << 23);
             // Descriptor samples are interpolated linearly into their bins, so
@@ -571,24 +583,24 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
             // of the window edge, whose shares there are ~0, are left out)
             const float lim = __fmul_rn(2.5f, bw) * 0.99999905f;
             unsigned int* hcopy = hist + (tid & 7) * kHistStride;
-            const float side_f = (float)side, rad_f = (float)rad;
+            const float rad_f = (float)rad;
             // windows that stay inside the level need no per-sample border test
             const bool edge = !(__fadd_rn(xo, -rad_f) >= 0.0f && __fadd_rn(xo, rad_f) < wm1 &&
                                 __fadd_rn(yo, -rad_f) >= 0.0f && __fadd_rn(yo, rad_f) < hm1);
             if (use_grid) {
-                // Sample pairs: a thread takes window samples k and k + 1 (k
-                // even, row-major; (px, py) = (k % side - rad, k / side - rad))
-                // and evaluates both with packed f32x2 arithmetic, the same
-                // operations per element as one sample alone. Pair m = tid +
-                // 256 j: px, py (exact small integers in f32) and the grid
-                // index c of element 0 advance by fixed amounts with one wrap
-                // per step; element 1 is the next position of the row, or the
-                // first of the next row.
-                const int k0 = 2 * tid;
-                const int q0 = floor_i(((float)k0 + 0.5f) * (1.0f / side_f));
-                const int dq = (2 * kDescThreads) / side;
-                const float dr_f = (float)(2 * kDescThreads - dq * side), dq_f = (float)dq;
-                const int dc = dq * gs + (2 * kDescThreads - dq * side);
+                // Sample pairs: a thread takes the window samples (px, py) and
+                // (px + 1, py), px = -rad, -rad + 2, .., rad (the last pair of a
+                // row has a phantom second element, px = rad + 1, outside the
+                // window), and evaluates both with packed f32x2 arithmetic,
+                // the same operations per element as one sample alone. Pair m
+                // = tid + 128 j of the rad + 1 pairs per row: px, py (exact
+                // small integers in f32) and the grid index c of element 0
+                // advance by fixed amounts with one row wrap per step.
+                const int hp = rad + 1;
+                const int q0 = tid / hp, dq = kDescThreads / hp;
+                const float dr_f = (float)(2 * (kDescThreads - dq * hp)), dq_f = (float)dq;
+                const int dc = dq * gs + 2 * (kDescThreads - dq * hp);
+                const float wrap_f = (float)(2 * hp);
                 // the fixed-point scale rides in the exponent: exp2(d2 * wexp +
                 // fbits) = 2^fbits exp(-d2 / wd)
                 const float fb = (float)fbits;
@@ -600,30 +612,30 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                 const float2 mag2c = make_float2(kMagic, kMagic), angb2 = make_float2(angb, angb);
                 auto pairs = [&](auto edge_tag) {
                     constexpr bool kEdge = decltype(edge_tag)::value;
-                    float px = (float)(k0 - q0 * side) - rad_f, py = (float)q0 - rad_f;
-                    int c = (q0 + 1) * gs + (k0 - q0 * side) + 1;
+                    float px = (float)(2 * (tid - q0 * hp)) - rad_f, py = (float)q0 - rad_f;
+                    int c = (q0 + 1) * gs + 2 * (tid - q0 * hp) + 1;
                     for (;; px += dr_f, py += dq_f, c += dc) {
+                        // the wrap to the next row as selects: a branch here
+                        // would split the warp for the rest of the step
                         const bool wrap = px > rad_f;
-                        px = wrap ? px - side_f : px;
+                        px = wrap ? px - wrap_f : px;
                         py = wrap ? py + 1.0f : py;
-                        c = wrap ? c + 2 : c;
+                        c = wrap ? c + 1 : c;
                         if (py > rad_f) break;
-                        // element 1: the row's next position or the next row's
-                        // first (grid index + 3); past the last row it is a
-                        // phantom that reads element 0's grid values
-                        const bool w1 = px >= rad_f;
-                        const float px1 = w1 ? -rad_f : px + 1.0f, py1 = w1 ? py + 1.0f : py;
-                        const bool v1 = py1 <= rad_f;
-                        const int c1 = v1 ? (w1 ? c + 3 : c + 1) : c;
-                        const float2 P = make_float2(px, px1), Q = make_float2(py, py1);
+                        // element 1 at grid index c + 1 (the phantom's reads
+                        // stay inside the grid)
+                        const bool v1 = px < rad_f;
+                        const int c1 = c + 1;
+                        const float2 P = make_float2(px, px + 1.0f), Q = make_float2(py, py);
                         const float2 rx = __ffma2_rn(P, ca2, __fmul2_rn(Q, sa2));
                         const float2 ry = __ffma2_rn(P, nsa2, __fmul2_rn(Q, ca2));
                         bool in0 = fabsf(rx.x) < lim && fabsf(ry.x) < lim;
                         bool in1 = v1 && fabsf(rx.y) < lim && fabsf(ry.y) < lim;
                         if constexpr (kEdge) {
-                            const float xs0 = xo + px, ys0 = yo + py, xs1 = xo + px1, ys1 = yo + py1;
-                            in0 = in0 && !(xs0 < 0.0f || xs0 >= wm1 || ys0 < 0.0f || ys0 >= hm1);
-                            in1 = in1 && !(xs1 < 0.0f || xs1 >= wm1 || ys1 < 0.0f || ys1 >= hm1);
+                            const float xs0 = xo + px, ys0 = yo + py, xs1 = xo + P.y;
+                            const bool rowin = !(ys0 < 0.0f || ys0 >= hm1);
+                            in0 = in0 && rowin && !(xs0 < 0.0f || xs0 >= wm1);
+                            in1 = in1 && rowin && !(xs1 < 0.0f || xs1 >= wm1);
                         }
                         // warps whose 64 samples all fall outside skip the rest
                         if (!__any_sync(__activemask(), in0 || in1)) continue;
