@@ -501,24 +501,33 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                         // bounds) and nothing is stored for it
                         const bool two = qx + 1 < gs;
                         const int o2 = two ? 2 : 1;
+                        // all 15 loads first (rows past the strip's last
+                        // repeat it), then the lerps
                         const TG* pp = org + qy0 * g.pitch + qx;
-                        float2 A = make_float2(graw(pp), graw(pp + 1));
-                        float2 rp = __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(A.y, graw(pp + o2))), A);
+                        float a[5][3];
+#pragma unroll
+                        for (int j = 0; j < 5; ++j) {
+                            const TG* pr = pp + min(j, nr) * g.pitch;
+                            a[j][0] = graw(pr);
+                            a[j][1] = graw(pr + 1);
+                            a[j][2] = graw(pr + o2);
+                        }
+                        float2 A = make_float2(a[0][0], a[0][1]);
+                        float2 rp = __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(a[0][1], a[0][2])), A);
                         float* gp = grid + qy0 * gs + qx;
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
+                            A = make_float2(a[j + 1][0], a[j + 1][1]);
+                            const float2 rn =
+                                __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(a[j + 1][1], a[j + 1][2])), A);
+                            const float2 b = __ffma2_rn(fdy2, __ffma2_rn(rp, neg1, rn), rp);
                             if (j < nr) {
-                                pp += g.pitch;
-                                A = make_float2(graw(pp), graw(pp + 1));
-                                const float2 rn =
-                                    __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(A.y, graw(pp + o2))), A);
-                                const float2 b = __ffma2_rn(fdy2, __ffma2_rn(rp, neg1, rn), rp);
                                 gp[j * gs] = b.x;
                                 if (two) gp[j * gs + 1] = b.y;
                                 lo = fminf(lo, fminf(b.x, b.y));
                                 hi = fmaxf(hi, fmaxf(b.x, b.y));
-                                rp = rn;
                             }
+                            rp = rn;
                         }
                     }
                 } else {
