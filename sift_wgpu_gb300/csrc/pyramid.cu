@@ -31,8 +31,9 @@
 namespace sift {
 namespace {
 
-// v / 255 in f32 (IEEE division, as the reference computes it).
-__device__ __forceinline__ float norm255(int v) { return __fdiv_rn((float)v, 255.0f); }
+// v / 255 in f32, the IEEE quotient the reference computes (div255: a
+// multiply and one fused correction, exact for every u8 value).
+__device__ __forceinline__ float norm255(int v) { return div255((float)v); }
 
 // Level storage: f32 holds v/255 (the reference's convert_u8_to_f32_gray
 // value, src/sift.rs:92-101), f16 holds v (v/255 is not exact in f16), u8
@@ -514,6 +515,7 @@ __global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride,
 // shared loads, the tap loops unrolled; the sums are the same, in the same
 // order.
 constexpr int kLzT = 32, kLzSpan = 80, kLzMid = 81;  // odd mid stride: lanes on rows hit 32 banks
+constexpr int kLzIn = 96;  // staged row: 16-byte aligned x from x_lo & ~15, x_lo - (x_lo & ~15) + span <= 95
 
 template <typename TG>
 __device__ __forceinline__ void lanczos_tile(const uint8_t* __restrict__ src, int src_pitch, TG* __restrict__ dst,
@@ -521,7 +523,7 @@ __device__ __forceinline__ void lanczos_tile(const uint8_t* __restrict__ src, in
                                              const int* __restrict__ vtab, const float* __restrict__ vw,
                                              const int* __restrict__ htab, const float* __restrict__ hw,
                                              const LanczosUniform& uni, int ox0, int oy0) {
-    __shared__ float in[kLzSpan][kLzSpan];
+    __shared__ __align__(16) float in_rows[kLzSpan][kLzIn];
     __shared__ float mid[kLzT][kLzMid];
     const int* vleft = vtab;
     const int* vcount = vtab + nH;
@@ -534,20 +536,29 @@ __device__ __forceinline__ void lanczos_tile(const uint8_t* __restrict__ src, in
     const int x_lo = hleft[ox0], x_hi = hleft[ox1 - 1] + hcount[ox1 - 1];
     const int y_lo = vleft[oy0], y_hi = vleft[oy1 - 1] + vcount[oy1 - 1];
     const int sw = x_hi - x_lo, sh = y_hi - y_lo;
-    // stage: aligned 4-byte words covering [x_lo, x_hi) of each source row
-    const int xa = x_lo & ~3;
-    const int nq = (x_hi - xa + 3) >> 2;
-    for (int q = tid; q < sh * nq; q += 256) {
-        const int yy = q / nq, k = q - yy * nq;
-        const uint8_t* p = src + (long long)(y_lo + yy) * src_pitch + xa + 4 * k;
-        const unsigned b = *reinterpret_cast<const unsigned*>(p);
+    // stage: 16-byte words from xa = x_lo & ~15 (staged column c holds x =
+    // xa + c; the words end at align16(x_hi) <= the row pitch, a multiple of
+    // 32), each byte to a float by one byte permute and one subtraction
+    const int xa = x_lo & ~15, xo = x_lo - xa;
+    const int nq = (x_hi - xa + 15) >> 4;
+    if ((src_pitch & 15) == 0) {
+        for (int q = tid; q < sh * nq; q += 256) {
+            const int yy = q / nq, k = q - yy * nq;
+            float v[16];
+            unpack16(*reinterpret_cast<const uint4*>(src + (long long)(y_lo + yy) * src_pitch + xa + 16 * k), v);
+            float4* d = reinterpret_cast<float4*>(&in_rows[yy][16 * k]);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int xx = xa + 4 * k + e - x_lo;
-            if (xx >= 0 && xx < sw) in[yy][xx] = float_of_u8((b >> (8 * e)) & 0xffu);
+            for (int e = 0; e < 4; ++e) d[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+        }
+    } else {
+        for (int q = tid; q < sh * sw; q += 256) {
+            const int yy = q / sw, xx = q - yy * sw;
+            in_rows[yy][xo + xx] = float_of_u8(src[(long long)(y_lo + yy) * src_pitch + x_lo + xx]);
         }
     }
     __syncthreads();
+    // in[y][x]: source (y_lo + y, x_lo + x)
+    auto in = [&](int y, int x) -> float { return in_rows[y][xo + x]; };
     if (ox0 >= uni.x0 && ox0 + kLzT <= uni.x1 && oy0 >= uni.y0 && oy0 + kLzT <= uni.y1) {
         // vertical pass: warp w makes mid rows 4w .. 4w+3 from source rows
         // 8w .. 8w+17 (output row r reads from 2r, tap i at j = 2r + i)
@@ -555,7 +566,7 @@ __device__ __forceinline__ void lanczos_tile(const uint8_t* __restrict__ src, in
             float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
             for (int j = 0; j < 18; ++j) {
-                const float v = in[8 * warp + j][xx];
+                const float v = in(8 * warp + j, xx);
 #pragma unroll
                 for (int r = 0; r < 4; ++r)
                     if (j - 2 * r >= 0 && j - 2 * r < kLz2xTaps) a[r] = __fadd_rn(a[r], __fmul_rn(v, uni.wv[j - 2 * r]));
@@ -592,7 +603,7 @@ __device__ __forceinline__ void lanczos_tile(const uint8_t* __restrict__ src, in
         const int l = vleft[oy] - y_lo, c = vcount[oy], o = voff[oy];
         for (int xx = lane; xx < sw; xx += 32) {
             float t = 0.0f;
-            for (int i = 0; i < c; ++i) t = __fadd_rn(t, __fmul_rn(in[l + i][xx], vw[o + i]));
+            for (int i = 0; i < c; ++i) t = __fadd_rn(t, __fmul_rn(in(l + i, xx), vw[o + i]));
             mid[oyl][xx] = t;
         }
     }
