@@ -216,6 +216,108 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
     }
 }
 
+// The orientation peaks of one refined keypoint (src/sift.rs:605-726),
+// computed by one warp: the window into the warp's bin-major histogram
+// hist[36][32], the column sums and the two smoothing passes in hs[36], the
+// peaks in bin order written to angles[0 .. count). Returns the count (the
+// same in every lane).
+template <typename TG>
+__device__ __forceinline__ uint32_t orient_one(const TG* __restrict__ arena, const EntryTable& tab, const Keypoint& kp,
+                                               float* hist, float* hs, int lane, const AxisBins& ab,
+                                               float* __restrict__ angles) {
+    const float two_pi = 2.0f * kPi;
+    const float bin_w = 2.0f * kPi / (float)kOriBins;
+    const int e = kp.octave;  // entry
+    if (!(e >= 0 && e < tab.n)) return 0;
+    const OctaveDev od = tab.ents[e];
+    const int o = od.octave;
+    const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer);
+    const float scale = __int_as_float((127 + o) << 23);
+    const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
+    const float so = __fdiv_rn(kp.size, scale);
+    if (!(so > 0.0f)) return 0;
+    const int r = rust_as_i32(roundf(__fmul_rn(4.5f, so)));
+    const float ws = __fmul_rn(1.5f, so);
+    const float wd = __fmul_rn(__fmul_rn(2.0f, ws), ws);
+#pragma unroll
+    for (int b = 0; b < kOriBins; ++b) hist[b * 32 + lane] = 0.0f;
+
+    // Windows entirely inside the level (most keypoints) take the loop
+    // without bounds checks; the others add +0.0 for samples outside, which
+    // leaves a bin bit-identical.
+    const bool interior = xo - (float)r >= 2.5f && xo + (float)r <= (float)(g.W - 3) - 0.5f &&
+                          yo - (float)r >= 2.5f && yo + (float)r <= (float)(g.H - 3) - 0.5f;
+    if (interior)
+        ori_window<TG, false>(g, xo, yo, r, wd, hist, lane, ab);
+    else
+        ori_window<TG, true>(g, xo, yo, r, wd, hist, lane, ab);
+    __syncwarp();
+    // Column sums: bin `lane` in four interleaved partial sums (the column
+    // index rotated by the bin keeps the 32 lanes in 32 banks), bins 32..35
+    // by eight lanes each and a shuffle tree.
+    {
+        const float* hb = hist + lane * 32;
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll
+        for (int l = 0; l < 32; l += 4) {
+            s0 = __fadd_rn(s0, hb[(l + lane) & 31]);
+            s1 = __fadd_rn(s1, hb[(l + 1 + lane) & 31]);
+            s2 = __fadd_rn(s2, hb[(l + 2 + lane) & 31]);
+            s3 = __fadd_rn(s3, hb[(l + 3 + lane) & 31]);
+        }
+        hs[lane] = __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
+        const int bb = 32 + (lane >> 3), c0 = (lane & 7) * 4;
+        const float* ht = hist + bb * 32;
+        float t = __fadd_rn(__fadd_rn(ht[(c0 + bb) & 31], ht[(c0 + 1 + bb) & 31]),
+                            __fadd_rn(ht[(c0 + 2 + bb) & 31], ht[(c0 + 3 + bb) & 31]));
+        t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 1));
+        t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 2));
+        t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 4));
+        if ((lane & 7) == 0) hs[bb] = t;
+    }
+    __syncwarp();
+    for (int it = 0; it < 2; ++it) {
+        float nv0 = 0.0f, nv1 = 0.0f;
+        for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) {
+            const float v = __fdiv_rn(
+                __fadd_rn(__fadd_rn(hs[(b + kOriBins - 1) % kOriBins], hs[b]), hs[(b + 1) % kOriBins]), 3.0f);
+            if (q == 0) nv0 = v; else nv1 = v;
+        }
+        __syncwarp();
+        for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) hs[b] = q == 0 ? nv0 : nv1;
+        __syncwarp();
+    }
+    float mx = fmaxf(hs[lane], lane + 32 < kOriBins ? hs[lane + 32] : 0.0f);
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, m));
+    const float thr = __fmul_rn(mx, 0.8f);
+    bool pk[2] = {false, false};
+    float pa[2] = {0.0f, 0.0f};
+    for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) {
+        const float cv = hs[b];
+        if (!(cv >= thr)) continue;
+        const float pv = hs[(b + kOriBins - 1) % kOriBins];
+        const float nv = hs[(b + 1) % kOriBins];
+        if (cv > pv && cv > nv) {
+            const float den = __fadd_rn(__fsub_rn(pv, __fmul_rn(2.0f, cv)), nv);
+            const float off = fabsf(den) > 1e-5f ? __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(pv, nv)), den) : 0.0f;
+            const float center = __fmul_rn(__fadd_rn((float)b, 0.5f), bin_w);
+            const float a = __fadd_rn(center, __fmul_rn(off, bin_w));
+            float fa = rem_euclid_2b(a, two_pi);  // a in (0, 2 pi + pi/36)
+            if (fa > kPi) fa = __fsub_rn(fa, two_pi);
+            pk[q] = true;
+            pa[q] = fa;
+        }
+    }
+    const uint32_t m0 = __ballot_sync(0xffffffffu, pk[0]);
+    const uint32_t m1 = __ballot_sync(0xffffffffu, pk[1]);
+    const uint32_t lt = (1u << lane) - 1u;
+    if (pk[0]) angles[__popc(m0 & lt)] = pa[0];
+    if (pk[1]) angles[__popc(m0) + __popc(m1 & lt)] = pa[1];
+    __syncwarp();
+    return (uint32_t)(__popc(m0) + __popc(m1));
+}
+
 template <typename TG>
 __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __restrict__ arena, EntryTable tab,
                                                                 const Keypoint* __restrict__ refined_at,
@@ -229,8 +331,6 @@ __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __r
     __shared__ float hs[kOriWarps][kOriBins];
     const int lane = threadIdx.x, wid = threadIdx.y;
     const uint32_t n = min(oc->n_cand, ncap);  // candidate slots; rejected ones get 0 peaks
-    const float two_pi = 2.0f * kPi;
-    const float bin_w = 2.0f * kPi / (float)kOriBins;
     const AxisBins ab = axis_bins();
     const bool persist = (int)blockIdx.x >= persist_from;
     for (int taken = 0; persist || taken < kOriBudget; ++taken) {
@@ -238,106 +338,10 @@ __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __r
         if (lane == 0) i = atomicAdd(&oc->next_ori, 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= n) break;
-        if (!keep[i]) {
-            if (lane == 0) ori_count[i] = 0;
-            continue;
-        }
-        const Keypoint kp = refined_at[i];
-        const int e = kp.octave;  // entry
         uint32_t cnt = 0;
-        if (e >= 0 && e < tab.n) {
-            const OctaveDev od = tab.ents[e];
-            const int o = od.octave;
-            const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer);
-            const float scale = __int_as_float((127 + o) << 23);
-            const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
-            const float so = __fdiv_rn(kp.size, scale);
-            if (so > 0.0f) {
-                const int r = rust_as_i32(roundf(__fmul_rn(4.5f, so)));
-                const float ws = __fmul_rn(1.5f, so);
-                const float wd = __fmul_rn(__fmul_rn(2.0f, ws), ws);
-#pragma unroll
-                for (int b = 0; b < kOriBins; ++b) hist[wid][b][lane] = 0.0f;
-
-                // Windows entirely inside the level (most keypoints) take the
-                // loop without bounds checks; the others add +0.0 for samples
-                // outside, which leaves a bin bit-identical.
-                const bool interior = xo - (float)r >= 2.5f && xo + (float)r <= (float)(g.W - 3) - 0.5f &&
-                                      yo - (float)r >= 2.5f && yo + (float)r <= (float)(g.H - 3) - 0.5f;
-                if (interior)
-                    ori_window<TG, false>(g, xo, yo, r, wd, &hist[wid][0][0], lane, ab);
-                else
-                    ori_window<TG, true>(g, xo, yo, r, wd, &hist[wid][0][0], lane, ab);
-                __syncwarp();
-                // Column sums: bin `lane` in four interleaved partial sums (the
-                // column index rotated by the bin keeps the 32 lanes in 32
-                // banks), bins 32..35 by eight lanes each and a shuffle tree.
-                {
-                    const float* hb = &hist[wid][lane][0];
-                    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-#pragma unroll
-                    for (int l = 0; l < 32; l += 4) {
-                        s0 = __fadd_rn(s0, hb[(l + lane) & 31]);
-                        s1 = __fadd_rn(s1, hb[(l + 1 + lane) & 31]);
-                        s2 = __fadd_rn(s2, hb[(l + 2 + lane) & 31]);
-                        s3 = __fadd_rn(s3, hb[(l + 3 + lane) & 31]);
-                    }
-                    hs[wid][lane] = __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
-                    const int bb = 32 + (lane >> 3), c0 = (lane & 7) * 4;
-                    const float* ht = &hist[wid][bb][0];
-                    float t = __fadd_rn(__fadd_rn(ht[(c0 + bb) & 31], ht[(c0 + 1 + bb) & 31]),
-                                        __fadd_rn(ht[(c0 + 2 + bb) & 31], ht[(c0 + 3 + bb) & 31]));
-                    t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 1));
-                    t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 2));
-                    t = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 4));
-                    if ((lane & 7) == 0) hs[wid][bb] = t;
-                }
-                __syncwarp();
-                for (int it = 0; it < 2; ++it) {
-                    float nv0 = 0.0f, nv1 = 0.0f;
-                    for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) {
-                        const float v = __fdiv_rn(
-                            __fadd_rn(__fadd_rn(hs[wid][(b + kOriBins - 1) % kOriBins], hs[wid][b]),
-                                      hs[wid][(b + 1) % kOriBins]),
-                            3.0f);
-                        if (q == 0) nv0 = v; else nv1 = v;
-                    }
-                    __syncwarp();
-                    for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) hs[wid][b] = q == 0 ? nv0 : nv1;
-                    __syncwarp();
-                }
-                float mx = fmaxf(hs[wid][lane], lane + 32 < kOriBins ? hs[wid][lane + 32] : 0.0f);
-#pragma unroll
-                for (int m = 16; m > 0; m >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, m));
-                const float thr = __fmul_rn(mx, 0.8f);
-                bool pk[2] = {false, false};
-                float pa[2] = {0.0f, 0.0f};
-                for (int b = lane, q = 0; b < kOriBins; b += 32, ++q) {
-                    const float cv = hs[wid][b];
-                    if (!(cv >= thr)) continue;
-                    const float pv = hs[wid][(b + kOriBins - 1) % kOriBins];
-                    const float nv = hs[wid][(b + 1) % kOriBins];
-                    if (cv > pv && cv > nv) {
-                        const float den = __fadd_rn(__fsub_rn(pv, __fmul_rn(2.0f, cv)), nv);
-                        const float off =
-                            fabsf(den) > 1e-5f ? __fdiv_rn(__fmul_rn(0.5f, __fsub_rn(pv, nv)), den) : 0.0f;
-                        const float center = __fmul_rn(__fadd_rn((float)b, 0.5f), bin_w);
-                        const float a = __fadd_rn(center, __fmul_rn(off, bin_w));
-                        float fa = rem_euclid_2b(a, two_pi);  // a in (0, 2 pi + pi/36)
-                        if (fa > kPi) fa = __fsub_rn(fa, two_pi);
-                        pk[q] = true;
-                        pa[q] = fa;
-                    }
-                }
-                const uint32_t m0 = __ballot_sync(0xffffffffu, pk[0]);
-                const uint32_t m1 = __ballot_sync(0xffffffffu, pk[1]);
-                const uint32_t lt = (1u << lane) - 1u;
-                if (pk[0]) ori_angle[(size_t)i * kOriMaxPeaks + __popc(m0 & lt)] = pa[0];
-                if (pk[1]) ori_angle[(size_t)i * kOriMaxPeaks + __popc(m0) + __popc(m1 & lt)] = pa[1];
-                cnt = (uint32_t)(__popc(m0) + __popc(m1));
-                __syncwarp();
-            }
-        }
+        if (keep[i])
+            cnt = orient_one<TG>(arena, tab, refined_at[i], &hist[wid][0][0], &hs[wid][0], lane, ab,
+                                 ori_angle + (size_t)i * kOriMaxPeaks);
         if (lane == 0) ori_count[i] = cnt;
     }
 }
@@ -383,7 +387,9 @@ constexpr int kHistStride = 324; // 36 * kHistRow; 324 % 32 = 4 puts a bin's 8 c
 constexpr int kDescRadGrid = 31;                      // largest radius served from the grid
 constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad+1
 
-// One CTA per oriented keypoint (persistent over the list).
+// The descriptor of one oriented keypoint (src/sift.rs:917-1060 and
+// normalize_and_clip_descriptor, src/sift.rs:889-913), computed by the whole
+// CTA (kDescThreads threads; it synchronises the CTA) into dst[0 .. 128):
 //  1. The bilinear samples the gradients need, bilinear(xo + i, yo + j) for
 //     integer offsets i, j in [-(rad+1), rad+1], go to a shared grid once
 //     (the reference re-evaluates four bilinears per window sample).
@@ -393,9 +399,363 @@ constexpr int kDescGridSide = 2 * kDescRadGrid + 3;   // offsets -(rad+1) .. rad
 //     each are added to 128 shared bins as u32 fixed point (2^-f units, f
 //     chosen so no bin can overflow): integer addition is associative, so the
 //     descriptor is the same on every run.
-//  3. Warp 0 normalises, clips at 0.2, renormalises.
+//  3. The four warps normalise, clip at 0.2, renormalise.
 // Radii above the grid (not reachable with the default sigma) fall back to
 // per-sample bilinears from the level itself.
+template <typename TG>
+__device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const EntryTable& tab, const Keypoint& kp,
+                                             float* grid, unsigned int* hist, float* red_lo, float* red_hi,
+                                             float* __restrict__ dst) {
+    const int tid = threadIdx.x;
+    const float sqrt2 = __fsqrt_rn(2.0f);
+    const int e = kp.octave;  // entry
+    for (int w = tid; w < kHistCopies * kHistStride / 4; w += kDescThreads)
+        reinterpret_cast<uint4*>(hist)[w] = make_uint4(0u, 0u, 0u, 0u);
+    const bool valid_oct = e >= 0 && e < tab.n;
+    OctaveDev od{};
+    if (valid_oct) od = tab.ents[e];
+    const int o = od.octave;
+    // division by 2^o is the multiplication by 2^-o, exactly
+    const float inv_scale = valid_oct ? __int_as_float((127 - o) << 23) : 1.0f;
+    const float so = valid_oct ? __fmul_rn(kp.size, inv_scale) : 0.0f;
+    const bool valid = valid_oct && so > 0.0f;
+    float inv_fix = 0.0f;
+    if (valid) {
+        const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer);
+        const float xo = __fmul_rn(kp.x, inv_scale), yo = __fmul_rn(kp.y, inv_scale);
+        const float ang = kp.angle;
+        // the hardware sine and cosine (|ang| <= pi; absolute error ~4e-7,
+        // a shift of ~1e-5 px at the window's edge)
+        float sa, ca;
+        __sincosf(ang, &sa, &ca);
+        const float bw = __fmul_rn(3.0f, so);
+        const float ww = __fmul_rn(bw, 4.0f);
+        const float wsig = __fmul_rn(0.5f, ww);
+        const float wd = __fmul_rn(__fmul_rn(2.0f, wsig), wsig);
+        const int rad = rust_as_i32(ceilf(__fmul_rn(__fmul_rn(ww, sqrt2), 0.5f)));
+        const float wm1 = (float)(g.W - 1), hm1 = (float)(g.H - 1);
+        const int side = 2 * rad + 1;
+        const int total = side * side;
+        const bool use_grid = rad <= kDescRadGrid;
+        const int gs = side + 2;
+        float lo = 3.0e38f, hi = 0.0f;
+        if (use_grid) {
+            // Bilinear samples at the window's integer offsets, in v units
+            // (graw), straight from the level (the patch stays in L1). All
+            // of them share the
+            // fraction of (xo, yo): the reference's sample positions xo + i
+            // differ from it only by the rounding of that sum. Clamped
+            // reads (get_gauss_pixel_value) only for windows at the border.
+            const float xf = floorf(xo), yf = floorf(yo);
+            const float fdx = xo - xf, fdy = yo - yf;
+            const int px0 = (int)xf - (rad + 1), py0 = (int)yf - (rad + 1);
+            const bool inner = px0 >= 0 && py0 >= 0 && px0 + gs < g.W && py0 + gs < g.H;
+            const float inv_gs = 1.0f / (float)gs;
+            if (inner) {
+                // A thread makes a strip of 4 x 2 grid points from 5 x 3
+                // pixels: each row's horizontal lerps serve the points
+                // above and below it, both columns at once on f32x2
+                // pairs (15 loads for 8 points); consecutive lanes take
+                // consecutive column pairs. The same two lerps per point
+                // as below, so the same values.
+                const int strips = (gs + 3) >> 2, cps = (gs + 1) >> 1;
+                const float inv_cps = 1.0f / (float)cps;
+                const TG* org = g.base + py0 * g.pitch + px0;
+                const float2 fdx2 = make_float2(fdx, fdx), fdy2 = make_float2(fdy, fdy);
+                const float2 neg1 = make_float2(-1.0f, -1.0f);
+                float tf = (float)tid;
+                for (int t = tid; t < strips * cps; t += kDescThreads, tf += (float)kDescThreads) {
+                    const int sy = floor_i((tf + 0.5f) * inv_cps);
+                    const int qx = 2 * (t - sy * cps), qy0 = 4 * sy;
+                    const int nr = min(4, gs - qy0);
+                    // an odd-width grid's last pair has a phantom second
+                    // column: its third pixel repeats the second (in
+                    // bounds) and nothing is stored for it
+                    const bool two = qx + 1 < gs;
+                    const int o2 = two ? 2 : 1;
+                    // all 15 loads first (rows past the strip's last
+                    // repeat it), then the lerps
+                    const TG* pp = org + qy0 * g.pitch + qx;
+                    float a[5][3];
+#pragma unroll
+                    for (int j = 0; j < 5; ++j) {
+                        const TG* pr = pp + min(j, nr) * g.pitch;
+                        a[j][0] = graw(pr);
+                        a[j][1] = graw(pr + 1);
+                        a[j][2] = graw(pr + o2);
+                    }
+                    float2 A = make_float2(a[0][0], a[0][1]);
+                    float2 rp = __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(a[0][1], a[0][2])), A);
+                    float* gp = grid + qy0 * gs + qx;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        A = make_float2(a[j + 1][0], a[j + 1][1]);
+                        const float2 rn =
+                            __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(a[j + 1][1], a[j + 1][2])), A);
+                        const float2 b = __ffma2_rn(fdy2, __ffma2_rn(rp, neg1, rn), rp);
+                        if (j < nr) {
+                            gp[j * gs] = b.x;
+                            if (two) gp[j * gs + 1] = b.y;
+                            lo = fminf(lo, fminf(b.x, b.y));
+                            hi = fmaxf(hi, fmaxf(b.x, b.y));
+                        }
+                        rp = rn;
+                    }
+                }
+            } else {
+                float qf = (float)tid;
+                for (int q = tid; q < gs * gs; q += kDescThreads, qf += (float)kDescThreads) {
+                    const int qy = floor_i((qf + 0.5f) * inv_gs);
+                    const int qx = q - qy * gs;
+                    const float q11 = g.px_raw(px0 + qx, py0 + qy), q21 = g.px_raw(px0 + qx + 1, py0 + qy);
+                    const float q12 = g.px_raw(px0 + qx, py0 + qy + 1), q22 = g.px_raw(px0 + qx + 1, py0 + qy + 1);
+                    // the reference's bilinear blend as two lerps (within the
+                    // descriptor tolerance)
+                    const float r0 = fmaf(fdx, q21 - q11, q11), r1 = fmaf(fdx, q22 - q12, q12);
+                    const float b = fmaf(fdy, r1 - r0, r0);
+                    grid[q] = b;
+                    lo = fminf(lo, b);
+                    hi = fmaxf(hi, b);
+                }
+            }
+        } else {
+            lo = 0.0f;
+            hi = 1.0f;
+        }
+        // Fixed point: |gx|, |gy| <= range of the sampled values, so every
+        // bin is below sqrt(2) * range * total (Gaussian and trilinear
+        // weights <= 1 with unit sum); the scale is the largest power of
+        // two that keeps that bound under 2^32.
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, m));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, m));
+        }
+        if ((tid & 31) == 0) {
+            red_lo[tid >> 5] = lo;
+            red_hi[tid >> 5] = hi;
+        }
+        __syncthreads();
+        lo = fminf(fminf(red_lo[0], red_lo[1]), fminf(red_lo[2], red_lo[3]));
+        hi = fmaxf(fmaxf(red_hi[0], red_hi[1]), fmaxf(red_hi[2], red_hi[3]));
+        const float range = fmaxf(hi - lo, 1.0f / 65536.0f);
+        // and every single contribution (<= sqrt(2) * range) below 2^23,
+        // where the rounding add below converts it exactly
+        const float per = 1.4143f * range;
+        // floor(log2 q) of a positive normal float is its exponent field
+        const int fbits = max(0, min(40, min((__float_as_int(4.0e9f / (per * (float)total)) >> 23) - 127,
+                                             (__float_as_int(8.0e6f / per) >> 23) - 127)));
+        const float to_fix = __int_as_float((127 + fbits) << 23);
+        inv_fix = __int_as_float((127 - fbits) << 23);
+        // Descriptor samples are interpolated linearly into their bins, so
+        // the sample loops are written for speed within the descriptor
+        // tolerance: fused multiply-adds, reciprocal products instead of
+        // divisions, the hardware's approximate square root and exp2
+        // (scale folded in), an arctangent polynomial in units of angle
+        // bins (error 1.5e-5 bin) from which the relative angle is binned
+        // directly (floor and & 7 give the rem_euclid bins), and the
+        // fixed-point rounding fused into the weight product. Each changes a
+        // descriptor value by ~1e-5 or less.
+        const float inv_bw = 1.0f / bw;
+        const float angb = ang * (4.0f / kPi);  // keypoint angle in 45-degree bins
+        const float wexp = -1.4426950408889634f / wd;  // exp(-d2/wd) = exp2(d2 * wexp)
+        // |rx|, |ry| below lim keep xb, yb inside (-1, 4) after rounding, so
+        // every cell index lies in the padded grid (samples within 1e-6
+        // of the window edge, whose shares there are ~0, are left out)
+        const float lim = __fmul_rn(2.5f, bw) * 0.99999905f;
+        unsigned int* hcopy = hist + (tid & 7) * kHistStride;
+        const float rad_f = (float)rad;
+        // windows that stay inside the level need no per-sample border test
+        const bool edge = !(__fadd_rn(xo, -rad_f) >= 0.0f && __fadd_rn(xo, rad_f) < wm1 &&
+                            __fadd_rn(yo, -rad_f) >= 0.0f && __fadd_rn(yo, rad_f) < hm1);
+        if (use_grid) {
+            // Sample pairs: a thread takes the window samples (px, py) and
+            // (px + 1, py), px = -rad, -rad + 2, .., rad (the last pair of a
+            // row has a phantom second element, px = rad + 1, outside the
+            // window), and evaluates both with packed f32x2 arithmetic,
+            // the same operations per element as one sample alone. Pair m
+            // = tid + 128 j of the rad + 1 pairs per row: px, py (exact
+            // small integers in f32) and the grid index c of element 0
+            // advance by fixed amounts with one row wrap per step.
+            const int hp = rad + 1;
+            const int q0 = tid / hp, dq = kDescThreads / hp;
+            const float dr_f = (float)(2 * (kDescThreads - dq * hp)), dq_f = (float)dq;
+            const int dc = dq * gs + 2 * (kDescThreads - dq * hp);
+            const float wrap_f = (float)(2 * hp);
+            // the fixed-point scale rides in the exponent: exp2(d2 * wexp +
+            // fbits) = 2^fbits exp(-d2 / wd)
+            const float fb = (float)fbits;
+            const float2 ca2 = make_float2(ca, ca), sa2 = make_float2(sa, sa), nsa2 = make_float2(-sa, -sa);
+            const float2 ib2 = make_float2(inv_bw, inv_bw), half3 = make_float2(1.5f, 1.5f);
+            const float2 wexp2 = make_float2(wexp, wexp), fb2 = make_float2(fb, fb);
+            const float2 m15 = make_float2(kMagic15, kMagic15), nm15 = make_float2(-kMagic15, -kMagic15);
+            const float2 neg1 = make_float2(-1.0f, -1.0f), one2 = make_float2(1.0f, 1.0f);
+            const float2 mag2c = make_float2(kMagic, kMagic), angb2 = make_float2(angb, angb);
+            auto pairs = [&](auto edge_tag) {
+                constexpr bool kEdge = decltype(edge_tag)::value;
+                float px = (float)(2 * (tid - q0 * hp)) - rad_f, py = (float)q0 - rad_f;
+                int c = (q0 + 1) * gs + 2 * (tid - q0 * hp) + 1;
+                for (;; px += dr_f, py += dq_f, c += dc) {
+                    // the wrap to the next row as selects: a branch here
+                    // would split the warp for the rest of the step
+                    const bool wrap = px > rad_f;
+                    px = wrap ? px - wrap_f : px;
+                    py = wrap ? py + 1.0f : py;
+                    c = wrap ? c + 1 : c;
+                    if (py > rad_f) break;
+                    // element 1 at grid index c + 1 (the phantom's reads
+                    // stay inside the grid)
+                    const bool v1 = px < rad_f;
+                    const int c1 = c + 1;
+                    const float2 P = make_float2(px, px + 1.0f), Q = make_float2(py, py);
+                    const float2 rx = __ffma2_rn(P, ca2, __fmul2_rn(Q, sa2));
+                    const float2 ry = __ffma2_rn(P, nsa2, __fmul2_rn(Q, ca2));
+                    bool in0 = fabsf(rx.x) < lim && fabsf(ry.x) < lim;
+                    bool in1 = v1 && fabsf(rx.y) < lim && fabsf(ry.y) < lim;
+                    if constexpr (kEdge) {
+                        const float xs0 = xo + px, ys0 = yo + py, xs1 = xo + P.y;
+                        const bool rowin = !(ys0 < 0.0f || ys0 >= hm1);
+                        in0 = in0 && rowin && !(xs0 < 0.0f || xs0 >= wm1);
+                        in1 = in1 && rowin && !(xs1 < 0.0f || xs1 >= wm1);
+                    }
+                    // warps whose 64 samples all fall outside skip the rest
+                    if (!__any_sync(__activemask(), in0 || in1)) continue;
+                    if (!(in0 || in1)) continue;
+                    const float2 gx = __ffma2_rn(make_float2(grid[c - 1], grid[c1 - 1]), neg1,
+                                                 make_float2(grid[c + 1], grid[c1 + 1]));
+                    const float2 gy = __ffma2_rn(make_float2(grid[c - gs], grid[c1 - gs]), neg1,
+                                                 make_float2(grid[c + gs], grid[c1 + gs]));
+                    const float2 m2 = __ffma2_rn(gx, gx, __fmul2_rn(gy, gy));
+                    const float2 ea = __ffma2_rn(__ffma2_rn(P, P, __fmul2_rn(Q, Q)), wexp2, fb2);
+                    float2 wm = __fmul2_rn(make_float2(sqrt_approx(m2.x), sqrt_approx(m2.y)),
+                                           make_float2(ex2_approx(ea.x), ex2_approx(ea.y)));
+                    // an element outside the window adds zero shares to
+                    // cell (-1, -1) of its copy
+                    wm.x = in0 ? wm.x : 0.0f;
+                    wm.y = in1 ? wm.y : 0.0f;
+                    const float2 ab = __fadd2_rn(atan2_bins2(gy, gx), make_float2(-angb, -angb));
+                    const float2 xb = __ffma2_rn(rx, ib2, half3), yb = __ffma2_rn(ry, ib2, half3);
+                    // floors by the 1.5 * 2^23 rounding-down add: the low
+                    // bits of tx, ty, ta are the integers
+                    const float2 tx = __fadd2_rd(xb, m15), ty = __fadd2_rd(yb, m15), ta = __fadd2_rd(ab, m15);
+                    const float2 fx = __ffma2_rn(__fadd2_rn(tx, nm15), neg1, xb);
+                    const float2 fy = __ffma2_rn(__fadd2_rn(ty, nm15), neg1, yb);
+                    const float2 fa = __ffma2_rn(__fadd2_rn(ta, nm15), neg1, ab);
+                    // histogram word of cell (xbi, ybi), bin abi & 7:
+                    // ((ybi + 1) * 6 + xbi + 1) * 9 + (abi & 7), from the
+                    // float bits (the 0x4B400000 offsets cancel mod 2^32,
+                    // 0x4B400000 & 7 == 0)
+                    constexpr uint32_t kCellOff = 63u - 63u * 0x4B400000u;
+                    uint32_t at0 = __float_as_uint(ty.x) * (uint32_t)(kHistSide * kHistRow) +
+                                   __float_as_uint(tx.x) * (uint32_t)kHistRow + kCellOff +
+                                   (__float_as_uint(ta.x) & 7u);
+                    uint32_t at1 = __float_as_uint(ty.y) * (uint32_t)(kHistSide * kHistRow) +
+                                   __float_as_uint(tx.y) * (uint32_t)kHistRow + kCellOff +
+                                   (__float_as_uint(ta.y) & 7u);
+                    at0 = in0 ? at0 : 0u;
+                    at1 = in1 ? at1 : 0u;
+                    const float2 wy0 = __fmul2_rn(wm, __ffma2_rn(fy, neg1, one2)), wy1 = __fmul2_rn(wm, fy);
+                    const float2 wx0 = __ffma2_rn(fx, neg1, one2);
+                    const float2 wa0 = __ffma2_rn(fa, neg1, one2);
+                    unsigned int* h0 = hcopy + at0;
+                    unsigned int* h1 = hcopy + at1;
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const float2 wxy = __fmul2_rn((cc & 1) ? fx : wx0, (cc & 2) ? wy1 : wy0);
+                        const int off = ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
+                        // the products rounded to the nearest integer (< 2^23 by the scale choice)
+                        const float2 n0 = __ffma2_rn(wxy, wa0, mag2c), n1 = __ffma2_rn(wxy, fa, mag2c);
+                        atomicAdd(h0 + off, __float_as_uint(n0.x) - 0x4B000000u);
+                        atomicAdd(h0 + off + 1, __float_as_uint(n1.x) - 0x4B000000u);
+                        atomicAdd(h1 + off, __float_as_uint(n0.y) - 0x4B000000u);
+                        atomicAdd(h1 + off + 1, __float_as_uint(n1.y) - 0x4B000000u);
+                    }
+                }
+            };
+            if (edge)
+                pairs(std::true_type{});
+            else
+                pairs(std::false_type{});
+        } else {
+            // Radii above the grid: one sample per thread, four bilinears
+            // from the level per sample (the reference's own evaluation).
+            for (int k = tid; k < total; k += kDescThreads) {
+                const int qy = k / side;
+                const float px = (float)(k - qy * side) - rad_f, py = (float)qy - rad_f;
+                const float rx = fmaf(ca, px, sa * py);
+                const float ry = fmaf(-sa, px, ca * py);
+                if (!(fabsf(rx) < lim && fabsf(ry) < lim)) continue;
+                const float xs = xo + px, ys = yo + py;
+                if (xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1) continue;
+                const float gx =
+                    __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
+                const float gy =
+                    __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
+                const float mag = sqrt_approx(fmaf(gx, gx, gy * gy));
+                const float wm = mag * ex2_approx(fmaf(px, px, py * py) * wexp);
+                const float ab = atan2_bins(gy, gx) - angb;  // in [-12, 4]
+                const float xb = fmaf(rx, inv_bw, 1.5f), yb = fmaf(ry, inv_bw, 1.5f);
+                int xbi, ybi, abi;
+                const float xbf = floor_fi(xb, &xbi), ybf = floor_fi(yb, &ybi), abf = floor_fi(ab, &abi);
+                const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
+                const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
+                const float wx0 = 1.0f - fx, wx1 = fx;
+                const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
+                unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) {
+                    const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
+                    unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
+                    atomicAdd(hc, __float_as_uint(__fmaf_rn(wxy, wa0, kMagic)) - 0x4B000000u);
+                    atomicAdd(hc + 1, __float_as_uint(__fmaf_rn(wxy, wa1, kMagic)) - 0x4B000000u);
+                }
+            }
+        }
+    }
+    __syncthreads();  // the histogram is complete
+    // normalize_and_clip_descriptor (src/sift.rs:889-913), one bin per
+    // thread; the sums of squares over the four warps in a fixed order
+    {
+        const int bin = tid;  // (iy * 4 + ix) * 8 + ia
+        const int cell = bin >> 3, ia = bin & 7;
+        const int at = (((cell >> 2) + 1) * kHistSide + (cell & 3) + 1) * kHistRow + ia;
+        unsigned v = 0u;
+#pragma unroll
+        for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at];
+        if (ia == 0)
+#pragma unroll
+            for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at + 8];
+        float d = __fmul_rn((float)v, inv_fix);
+        float ss = __fmul_rn(d, d);
+#pragma unroll
+        for (int m = 16; m > 0; m >>= 1) ss = __fadd_rn(ss, __shfl_xor_sync(0xffffffffu, ss, m));
+        if ((tid & 31) == 0) red_lo[tid >> 5] = ss;
+        __syncthreads();
+        const float norm = __fsqrt_rn(__fadd_rn(__fadd_rn(red_lo[0], red_lo[1]), __fadd_rn(red_lo[2], red_lo[3])));
+        if (!(norm < 1e-8f)) {  // the same for every thread
+            d = fminf(__fmul_rn(d, __fdiv_rn(1.0f, norm)), 0.2f);
+            float s2 = __fmul_rn(d, d);
+#pragma unroll
+            for (int m = 16; m > 0; m >>= 1) s2 = __fadd_rn(s2, __shfl_xor_sync(0xffffffffu, s2, m));
+            if ((tid & 31) == 0) red_hi[tid >> 5] = s2;
+            __syncthreads();
+            const float n2 =
+                __fsqrt_rn(__fadd_rn(__fadd_rn(red_hi[0], red_hi[1]), __fadd_rn(red_hi[2], red_hi[3])));
+            if (!(n2 < 1e-8f)) d = __fmul_rn(d, __fdiv_rn(1.0f, n2));
+        }
+            dst[bin] = d;
+    }
+}
+
+// One CTA per oriented keypoint (persistent over the list), describe_one on
+// each. Neighbouring samples land in the same bins, so the lanes of a warp
+// add into kHistCopies copies of the histogram: adds to one address
+// serialise, adds to distinct copies do not. Lane l uses copy l & 7, so the
+// lanes sharing a copy hold samples 16 apart (mostly different cells) and
+// neighbouring lanes, which often hit the same bin, use copies 4 banks apart;
+// picking the copy by l >> 2 instead (4 neighbours per copy) costs 13 % more
+// time. The copies are summed in a fixed order; integer sums make the order
+// irrelevant.
 template <typename TG>
 __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __restrict__ arena, EntryTable tab,
                                                               const Keypoint* __restrict__ oriented,
@@ -405,14 +765,6 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                                                               int persist_from) {
     chain_wait();
     __shared__ float grid[kDescGridSide * kDescGridSide];
-    // Neighbouring samples land in the same bins, so the lanes of a warp add
-    // into kHistCopies copies of the histogram: adds to one address
-    // serialise, adds to distinct copies do not. Lane l uses copy l & 7, so
-    // the lanes sharing a copy hold samples 8 apart (mostly different cells)
-    // and neighbouring lanes, which often hit the same bin, use copies 4
-    // banks apart; picking the copy by l >> 2 instead (4 neighbours per
-    // copy) costs 13 % more time. The copies are summed in a fixed order;
-    // integer sums make the order irrelevant.
     __shared__ __align__(16) unsigned int hist[kHistCopies * kHistStride];
     __shared__ float red_lo[kDescThreads / 32], red_hi[kDescThreads / 32];
     const int tid = threadIdx.x;
@@ -420,7 +772,6 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
     uint32_t n = oc->n_ori;
     if (base >= cap) n = 0;
     else if (n > cap - base) n = cap - base;
-    const float sqrt2 = __fsqrt_rn(2.0f);
     // Keypoints differ ~4x in window area: they come from a queue. Thread 0
     // claims the next item while the CTA works on the current one (slot
     // next[p ^ 1]), unless the CTA retires after the current one.
@@ -436,348 +787,12 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
         if (tid == 0 && more) claim = atomicAdd(&oc->next_desc, 1u);
         const uint32_t i = base + cur;
         const Keypoint kp = oriented[i];
-        const int e = kp.octave;  // entry
-        for (int w = tid; w < kHistCopies * kHistStride / 4; w += kDescThreads)
-            reinterpret_cast<uint4*>(hist)[w] = make_uint4(0u, 0u, 0u, 0u);
-        const bool valid_oct = e >= 0 && e < tab.n;
-        OctaveDev od{};
-        if (valid_oct) od = tab.ents[e];
-        const int o = od.octave;
-        // division by 2^o is the multiplication by 2^-o, exactly
-        const float inv_scale = valid_oct ? __int_as_float((127 - o) << 23) : 1.0f;
-        const float so = valid_oct ? __fmul_rn(kp.size, inv_scale) : 0.0f;
-        const bool valid = valid_oct && so > 0.0f;
-        float inv_fix = 0.0f;
-        if (valid) {
-            const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer);
-            const float xo = __fmul_rn(kp.x, inv_scale), yo = __fmul_rn(kp.y, inv_scale);
-            const float ang = kp.angle;
-            // the hardware sine and cosine (|ang| <= pi; absolute error ~4e-7,
-            // a shift of ~1e-5 px at the window's edge)
-            float sa, ca;
-            __sincosf(ang, &sa, &ca);
-            const float bw = __fmul_rn(3.0f, so);
-            const float ww = __fmul_rn(bw, 4.0f);
-            const float wsig = __fmul_rn(0.5f, ww);
-            const float wd = __fmul_rn(__fmul_rn(2.0f, wsig), wsig);
-            const int rad = rust_as_i32(ceilf(__fmul_rn(__fmul_rn(ww, sqrt2), 0.5f)));
-            const float wm1 = (float)(g.W - 1), hm1 = (float)(g.H - 1);
-            const int side = 2 * rad + 1;
-            const int total = side * side;
-            const bool use_grid = rad <= kDescRadGrid;
-            const int gs = side + 2;
-            float lo = 3.0e38f, hi = 0.0f;
-            if (use_grid) {
-                // Bilinear samples at the window's integer offsets, in v units
-                // (graw), straight from the level (the patch stays in L1). All
-                // of them share the
-                // fraction of (xo, yo): the reference's sample positions xo + i
-                // differ from it only by the rounding of that sum. Clamped
-                // reads (get_gauss_pixel_value) only for windows at the border.
-                const float xf = floorf(xo), yf = floorf(yo);
-                const float fdx = xo - xf, fdy = yo - yf;
-                const int px0 = (int)xf - (rad + 1), py0 = (int)yf - (rad + 1);
-                const bool inner = px0 >= 0 && py0 >= 0 && px0 + gs < g.W && py0 + gs < g.H;
-                const float inv_gs = 1.0f / (float)gs;
-                if (inner) {
-                    // A thread makes a strip of 4 x 2 grid points from 5 x 3
-                    // pixels: each row's horizontal lerps serve the points
-                    // above and below it, both columns at once on f32x2
-                    // pairs (15 loads for 8 points); consecutive lanes take
-                    // consecutive column pairs. The same two lerps per point
-                    // as below, so the same values.
-                    const int strips = (gs + 3) >> 2, cps = (gs + 1) >> 1;
-                    const float inv_cps = 1.0f / (float)cps;
-                    const TG* org = g.base + py0 * g.pitch + px0;
-                    const float2 fdx2 = make_float2(fdx, fdx), fdy2 = make_float2(fdy, fdy);
-                    const float2 neg1 = make_float2(-1.0f, -1.0f);
-                    float tf = (float)tid;
-                    for (int t = tid; t < strips * cps; t += kDescThreads, tf += (float)kDescThreads) {
-                        const int sy = floor_i((tf + 0.5f) * inv_cps);
-                        const int qx = 2 * (t - sy * cps), qy0 = 4 * sy;
-                        const int nr = min(4, gs - qy0);
-                        // an odd-width grid's last pair has a phantom second
-                        // column: its third pixel repeats the second (in
-                        // bounds) and nothing is stored for it
-                        const bool two = qx + 1 < gs;
-                        const int o2 = two ? 2 : 1;
-                        // all 15 loads first (rows past the strip's last
-                        // repeat it), then the lerps
-                        const TG* pp = org + qy0 * g.pitch + qx;
-                        float a[5][3];
-#pragma unroll
-                        for (int j = 0; j < 5; ++j) {
-                            const TG* pr = pp + min(j, nr) * g.pitch;
-                            a[j][0] = graw(pr);
-                            a[j][1] = graw(pr + 1);
-                            a[j][2] = graw(pr + o2);
-                        }
-                        float2 A = make_float2(a[0][0], a[0][1]);
-                        float2 rp = __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(a[0][1], a[0][2])), A);
-                        float* gp = grid + qy0 * gs + qx;
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            A = make_float2(a[j + 1][0], a[j + 1][1]);
-                            const float2 rn =
-                                __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(a[j + 1][1], a[j + 1][2])), A);
-                            const float2 b = __ffma2_rn(fdy2, __ffma2_rn(rp, neg1, rn), rp);
-                            if (j < nr) {
-                                gp[j * gs] = b.x;
-                                if (two) gp[j * gs + 1] = b.y;
-                                lo = fminf(lo, fminf(b.x, b.y));
-                                hi = fmaxf(hi, fmaxf(b.x, b.y));
-                            }
-                            rp = rn;
-                        }
-                    }
-                } else {
-                    float qf = (float)tid;
-                    for (int q = tid; q < gs * gs; q += kDescThreads, qf += (float)kDescThreads) {
-                        const int qy = floor_i((qf + 0.5f) * inv_gs);
-                        const int qx = q - qy * gs;
-                        const float q11 = g.px_raw(px0 + qx, py0 + qy), q21 = g.px_raw(px0 + qx + 1, py0 + qy);
-                        const float q12 = g.px_raw(px0 + qx, py0 + qy + 1), q22 = g.px_raw(px0 + qx + 1, py0 + qy + 1);
-                        // the reference's bilinear blend as two lerps (within the
-                        // descriptor tolerance)
-                        const float r0 = fmaf(fdx, q21 - q11, q11), r1 = fmaf(fdx, q22 - q12, q12);
-                        const float b = fmaf(fdy, r1 - r0, r0);
-                        grid[q] = b;
-                        lo = fminf(lo, b);
-                        hi = fmaxf(hi, b);
-                    }
-                }
-            } else {
-                lo = 0.0f;
-                hi = 1.0f;
-            }
-            // Fixed point: |gx|, |gy| <= range of the sampled values, so every
-            // bin is below sqrt(2) * range * total (Gaussian and trilinear
-            // weights <= 1 with unit sum); the scale is the largest power of
-            // two that keeps that bound under 2^32.
-#pragma unroll
-            for (int m = 16; m > 0; m >>= 1) {
-                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, m));
-                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, m));
-            }
-            if ((tid & 31) == 0) {
-                red_lo[tid >> 5] = lo;
-                red_hi[tid >> 5] = hi;
-            }
-            __syncthreads();
-            lo = fminf(fminf(red_lo[0], red_lo[1]), fminf(red_lo[2], red_lo[3]));
-            hi = fmaxf(fmaxf(red_hi[0], red_hi[1]), fmaxf(red_hi[2], red_hi[3]));
-            const float range = fmaxf(hi - lo, 1.0f / 65536.0f);
-            // and every single contribution (<= sqrt(2) * range) below 2^23,
-            // where the rounding add below converts it exactly
-            const float per = 1.4143f * range;
-            // floor(log2 q) of a positive normal float is its exponent field
-            const int fbits = max(0, min(40, min((__float_as_int(4.0e9f / (per * (float)total)) >> 23) - 127,
-                                                 (__float_as_int(8.0e6f / per) >> 23) - 127)));
-            const float to_fix = __int_as_float((127 + fbits) << 23);
-            inv_fix = __int_as_float((127 - fbits) << 23);
-            // Descriptor samples are interpolated linearly into their bins, so
-            // the sample loops are written for speed within the descriptor
-            // tolerance: fused multiply-adds, reciprocal products instead of
-            // divisions, the hardware's approximate square root and exp2
-            // (scale folded in), an arctangent polynomial in units of angle
-            // bins (error 1.5e-5 bin) from which the relative angle is binned
-            // directly (floor and & 7 give the rem_euclid bins), and the
-            // fixed-point rounding fused into the weight product. Each changes a
-            // descriptor value by ~1e-5 or less.
-            const float inv_bw = 1.0f / bw;
-            const float angb = ang * (4.0f / kPi);  // keypoint angle in 45-degree bins
-            const float wexp = -1.4426950408889634f / wd;  // exp(-d2/wd) = exp2(d2 * wexp)
-            // |rx|, |ry| below lim keep xb, yb inside (-1, 4) after rounding, so
-            // every cell index lies in the padded grid (samples within 1e-6
-            // of the window edge, whose shares there are ~0, are left out)
-            const float lim = __fmul_rn(2.5f, bw) * 0.99999905f;
-            unsigned int* hcopy = hist + (tid & 7) * kHistStride;
-            const float rad_f = (float)rad;
-            // windows that stay inside the level need no per-sample border test
-            const bool edge = !(__fadd_rn(xo, -rad_f) >= 0.0f && __fadd_rn(xo, rad_f) < wm1 &&
-                                __fadd_rn(yo, -rad_f) >= 0.0f && __fadd_rn(yo, rad_f) < hm1);
-            if (use_grid) {
-                // Sample pairs: a thread takes the window samples (px, py) and
-                // (px + 1, py), px = -rad, -rad + 2, .., rad (the last pair of a
-                // row has a phantom second element, px = rad + 1, outside the
-                // window), and evaluates both with packed f32x2 arithmetic,
-                // the same operations per element as one sample alone. Pair m
-                // = tid + 128 j of the rad + 1 pairs per row: px, py (exact
-                // small integers in f32) and the grid index c of element 0
-                // advance by fixed amounts with one row wrap per step.
-                const int hp = rad + 1;
-                const int q0 = tid / hp, dq = kDescThreads / hp;
-                const float dr_f = (float)(2 * (kDescThreads - dq * hp)), dq_f = (float)dq;
-                const int dc = dq * gs + 2 * (kDescThreads - dq * hp);
-                const float wrap_f = (float)(2 * hp);
-                // the fixed-point scale rides in the exponent: exp2(d2 * wexp +
-                // fbits) = 2^fbits exp(-d2 / wd)
-                const float fb = (float)fbits;
-                const float2 ca2 = make_float2(ca, ca), sa2 = make_float2(sa, sa), nsa2 = make_float2(-sa, -sa);
-                const float2 ib2 = make_float2(inv_bw, inv_bw), half3 = make_float2(1.5f, 1.5f);
-                const float2 wexp2 = make_float2(wexp, wexp), fb2 = make_float2(fb, fb);
-                const float2 m15 = make_float2(kMagic15, kMagic15), nm15 = make_float2(-kMagic15, -kMagic15);
-                const float2 neg1 = make_float2(-1.0f, -1.0f), one2 = make_float2(1.0f, 1.0f);
-                const float2 mag2c = make_float2(kMagic, kMagic), angb2 = make_float2(angb, angb);
-                auto pairs = [&](auto edge_tag) {
-                    constexpr bool kEdge = decltype(edge_tag)::value;
-                    float px = (float)(2 * (tid - q0 * hp)) - rad_f, py = (float)q0 - rad_f;
-                    int c = (q0 + 1) * gs + 2 * (tid - q0 * hp) + 1;
-                    for (;; px += dr_f, py += dq_f, c += dc) {
-                        // the wrap to the next row as selects: a branch here
-                        // would split the warp for the rest of the step
-                        const bool wrap = px > rad_f;
-                        px = wrap ? px - wrap_f : px;
-                        py = wrap ? py + 1.0f : py;
-                        c = wrap ? c + 1 : c;
-                        if (py > rad_f) break;
-                        // element 1 at grid index c + 1 (the phantom's reads
-                        // stay inside the grid)
-                        const bool v1 = px < rad_f;
-                        const int c1 = c + 1;
-                        const float2 P = make_float2(px, px + 1.0f), Q = make_float2(py, py);
-                        const float2 rx = __ffma2_rn(P, ca2, __fmul2_rn(Q, sa2));
-                        const float2 ry = __ffma2_rn(P, nsa2, __fmul2_rn(Q, ca2));
-                        bool in0 = fabsf(rx.x) < lim && fabsf(ry.x) < lim;
-                        bool in1 = v1 && fabsf(rx.y) < lim && fabsf(ry.y) < lim;
-                        if constexpr (kEdge) {
-                            const float xs0 = xo + px, ys0 = yo + py, xs1 = xo + P.y;
-                            const bool rowin = !(ys0 < 0.0f || ys0 >= hm1);
-                            in0 = in0 && rowin && !(xs0 < 0.0f || xs0 >= wm1);
-                            in1 = in1 && rowin && !(xs1 < 0.0f || xs1 >= wm1);
-                        }
-                        // warps whose 64 samples all fall outside skip the rest
-                        if (!__any_sync(__activemask(), in0 || in1)) continue;
-                        if (!(in0 || in1)) continue;
-                        const float2 gx = __ffma2_rn(make_float2(grid[c - 1], grid[c1 - 1]), neg1,
-                                                     make_float2(grid[c + 1], grid[c1 + 1]));
-                        const float2 gy = __ffma2_rn(make_float2(grid[c - gs], grid[c1 - gs]), neg1,
-                                                     make_float2(grid[c + gs], grid[c1 + gs]));
-                        const float2 m2 = __ffma2_rn(gx, gx, __fmul2_rn(gy, gy));
-                        const float2 ea = __ffma2_rn(__ffma2_rn(P, P, __fmul2_rn(Q, Q)), wexp2, fb2);
-                        float2 wm = __fmul2_rn(make_float2(sqrt_approx(m2.x), sqrt_approx(m2.y)),
-                                               make_float2(ex2_approx(ea.x), ex2_approx(ea.y)));
-                        // an element outside the window adds zero shares to
-                        // cell (-1, -1) of its copy
-                        wm.x = in0 ? wm.x : 0.0f;
-                        wm.y = in1 ? wm.y : 0.0f;
-                        const float2 ab = __fadd2_rn(atan2_bins2(gy, gx), make_float2(-angb, -angb));
-                        const float2 xb = __ffma2_rn(rx, ib2, half3), yb = __ffma2_rn(ry, ib2, half3);
-                        // floors by the 1.5 * 2^23 rounding-down add: the low
-                        // bits of tx, ty, ta are the integers
-                        const float2 tx = __fadd2_rd(xb, m15), ty = __fadd2_rd(yb, m15), ta = __fadd2_rd(ab, m15);
-                        const float2 fx = __ffma2_rn(__fadd2_rn(tx, nm15), neg1, xb);
-                        const float2 fy = __ffma2_rn(__fadd2_rn(ty, nm15), neg1, yb);
-                        const float2 fa = __ffma2_rn(__fadd2_rn(ta, nm15), neg1, ab);
-                        // histogram word of cell (xbi, ybi), bin abi & 7:
-                        // ((ybi + 1) * 6 + xbi + 1) * 9 + (abi & 7), from the
-                        // float bits (the 0x4B400000 offsets cancel mod 2^32,
-                        // 0x4B400000 & 7 == 0)
-                        constexpr uint32_t kCellOff = 63u - 63u * 0x4B400000u;
-                        uint32_t at0 = __float_as_uint(ty.x) * (uint32_t)(kHistSide * kHistRow) +
-                                       __float_as_uint(tx.x) * (uint32_t)kHistRow + kCellOff +
-                                       (__float_as_uint(ta.x) & 7u);
-                        uint32_t at1 = __float_as_uint(ty.y) * (uint32_t)(kHistSide * kHistRow) +
-                                       __float_as_uint(tx.y) * (uint32_t)kHistRow + kCellOff +
-                                       (__float_as_uint(ta.y) & 7u);
-                        at0 = in0 ? at0 : 0u;
-                        at1 = in1 ? at1 : 0u;
-                        const float2 wy0 = __fmul2_rn(wm, __ffma2_rn(fy, neg1, one2)), wy1 = __fmul2_rn(wm, fy);
-                        const float2 wx0 = __ffma2_rn(fx, neg1, one2);
-                        const float2 wa0 = __ffma2_rn(fa, neg1, one2);
-                        unsigned int* h0 = hcopy + at0;
-                        unsigned int* h1 = hcopy + at1;
-#pragma unroll
-                        for (int cc = 0; cc < 4; ++cc) {
-                            const float2 wxy = __fmul2_rn((cc & 1) ? fx : wx0, (cc & 2) ? wy1 : wy0);
-                            const int off = ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
-                            // the products rounded to the nearest integer (< 2^23 by the scale choice)
-                            const float2 n0 = __ffma2_rn(wxy, wa0, mag2c), n1 = __ffma2_rn(wxy, fa, mag2c);
-                            atomicAdd(h0 + off, __float_as_uint(n0.x) - 0x4B000000u);
-                            atomicAdd(h0 + off + 1, __float_as_uint(n1.x) - 0x4B000000u);
-                            atomicAdd(h1 + off, __float_as_uint(n0.y) - 0x4B000000u);
-                            atomicAdd(h1 + off + 1, __float_as_uint(n1.y) - 0x4B000000u);
-                        }
-                    }
-                };
-                if (edge)
-                    pairs(std::true_type{});
-                else
-                    pairs(std::false_type{});
-            } else {
-                // Radii above the grid: one sample per thread, four bilinears
-                // from the level per sample (the reference's own evaluation).
-                for (int k = tid; k < total; k += kDescThreads) {
-                    const int qy = k / side;
-                    const float px = (float)(k - qy * side) - rad_f, py = (float)qy - rad_f;
-                    const float rx = fmaf(ca, px, sa * py);
-                    const float ry = fmaf(-sa, px, ca * py);
-                    if (!(fabsf(rx) < lim && fabsf(ry) < lim)) continue;
-                    const float xs = xo + px, ys = yo + py;
-                    if (xs < 0.0f || xs >= wm1 || ys < 0.0f || ys >= hm1) continue;
-                    const float gx =
-                        __fsub_rn(g.bilinear(__fadd_rn(xs, 1.0f), ys), g.bilinear(__fsub_rn(xs, 1.0f), ys));
-                    const float gy =
-                        __fsub_rn(g.bilinear(xs, __fadd_rn(ys, 1.0f)), g.bilinear(xs, __fsub_rn(ys, 1.0f)));
-                    const float mag = sqrt_approx(fmaf(gx, gx, gy * gy));
-                    const float wm = mag * ex2_approx(fmaf(px, px, py * py) * wexp);
-                    const float ab = atan2_bins(gy, gx) - angb;  // in [-12, 4]
-                    const float xb = fmaf(rx, inv_bw, 1.5f), yb = fmaf(ry, inv_bw, 1.5f);
-                    int xbi, ybi, abi;
-                    const float xbf = floor_fi(xb, &xbi), ybf = floor_fi(yb, &ybi), abf = floor_fi(ab, &abi);
-                    const float fx = xb - xbf, fy = yb - ybf, fa = ab - abf;
-                    const float wa1 = fa * to_fix, wa0 = to_fix - wa1;
-                    const float wx0 = 1.0f - fx, wx1 = fx;
-                    const float wy0 = wm * (1.0f - fy), wy1 = wm * fy;
-                    unsigned int* h0 = hcopy + ((ybi + 1) * kHistSide + (xbi + 1)) * kHistRow + (abi & 7);
-#pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) {
-                        const float wxy = ((cc & 1) ? wx1 : wx0) * ((cc & 2) ? wy1 : wy0);
-                        unsigned int* hc = h0 + ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
-                        atomicAdd(hc, __float_as_uint(__fmaf_rn(wxy, wa0, kMagic)) - 0x4B000000u);
-                        atomicAdd(hc + 1, __float_as_uint(__fmaf_rn(wxy, wa1, kMagic)) - 0x4B000000u);
-                    }
-                }
-            }
-        }
-        __syncthreads();  // the histogram is complete
-        // normalize_and_clip_descriptor (src/sift.rs:889-913), one bin per
-        // thread; the sums of squares over the four warps in a fixed order
-        {
-            const int bin = tid;  // (iy * 4 + ix) * 8 + ia
-            const int cell = bin >> 3, ia = bin & 7;
-            const int at = (((cell >> 2) + 1) * kHistSide + (cell & 3) + 1) * kHistRow + ia;
-            unsigned v = 0u;
-#pragma unroll
-            for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at];
-            if (ia == 0)
-#pragma unroll
-                for (int c = 0; c < kHistCopies; ++c) v += hist[c * kHistStride + at + 8];
-            float d = __fmul_rn((float)v, inv_fix);
-            float ss = __fmul_rn(d, d);
-#pragma unroll
-            for (int m = 16; m > 0; m >>= 1) ss = __fadd_rn(ss, __shfl_xor_sync(0xffffffffu, ss, m));
-            if ((tid & 31) == 0) red_lo[tid >> 5] = ss;
-            __syncthreads();
-            const float norm = __fsqrt_rn(__fadd_rn(__fadd_rn(red_lo[0], red_lo[1]), __fadd_rn(red_lo[2], red_lo[3])));
-            if (!(norm < 1e-8f)) {  // the same for every thread
-                d = fminf(__fmul_rn(d, __fdiv_rn(1.0f, norm)), 0.2f);
-                float s2 = __fmul_rn(d, d);
-#pragma unroll
-                for (int m = 16; m > 0; m >>= 1) s2 = __fadd_rn(s2, __shfl_xor_sync(0xffffffffu, s2, m));
-                if ((tid & 31) == 0) red_hi[tid >> 5] = s2;
-                __syncthreads();
-                const float n2 =
-                    __fsqrt_rn(__fadd_rn(__fadd_rn(red_hi[0], red_hi[1]), __fadd_rn(red_hi[2], red_hi[3])));
-                if (!(n2 < 1e-8f)) d = __fmul_rn(d, __fdiv_rn(1.0f, n2));
-            }
-            // keypoints below hcap straight into the host call's mapped buffer
-            float* dst = (i < hcap ? hdesc : desc) + (size_t)i * kDescLen;
-            dst[bin] = d;
-        }
+        // keypoints below hcap straight into the host call's mapped buffer
+        describe_one<TG>(arena, tab, kp, grid, hist, red_lo, red_hi, (i < hcap ? hdesc : desc) + (size_t)i * kDescLen);
         if (tid == 0) next[p ^ 1] = claim;
     }
 }
+
 
 }  // namespace
 
