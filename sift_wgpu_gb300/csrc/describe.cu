@@ -338,6 +338,7 @@ __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __r
         if (lane == 0) i = atomicAdd(&oc->next_ori, 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= n) break;
+        i = n - 1 - i;  // from the last slot: the largest windows first
         uint32_t cnt = 0;
         if (keep[i])
             cnt = orient_one<TG>(arena, tab, refined_at[i], &hist[wid][0][0], &hs[wid][0], lane, ab,
@@ -785,7 +786,10 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
         const bool more = persist || taken + 1 < kDescBudget;
         uint32_t claim = n;
         if (tid == 0 && more) claim = atomicAdd(&oc->next_desc, 1u);
-        const uint32_t i = base + cur;
+        // the queue runs from the last keypoint: an octave's list is in layer
+        // order, so the largest windows go first and the smallest make the
+        // tail of the stage
+        const uint32_t i = base + (n - 1 - cur);
         const Keypoint kp = oriented[i];
         // keypoints below hcap straight into the host call's mapped buffer
         describe_one<TG>(arena, tab, kp, grid, hist, red_lo, red_hi, (i < hcap ? hdesc : desc) + (size_t)i * kDescLen);
