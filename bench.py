@@ -185,14 +185,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def traffic_from_profiles(workload: str, stage: str):
+def traffic_from_profiles(workload: str, stage: str, kind: str = "dram_bytes"):
+    """A per-run figure of one stage from profiles/traffic.json (scoped ncu
+    captures): kind "dram_bytes" (DRAM read + write bytes) or "inst" (warp
+    instructions); None where nothing was captured."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
     try:
-        return json.loads(p.read_text()).get(workload, {}).get(stage)
-    except (ValueError, OSError):
+        return json.loads(p.read_text()).get(kind, {}).get(workload, {}).get(stage)
+    except (ValueError, OSError, AttributeError):
         return None
+
+
+def issue_roofline(inst, ms: float, sm_mhz):
+    """Instruction issue as the roofline of an issue-bound stage: warp
+    instructions per run (ncu) over the stage time, against 152 SMs x 4
+    schedulers x one warp instruction per clock at the sampled SM clock."""
+    if not inst or not ms or not sm_mhz:
+        return None
+    peak = 152 * 4 * float(sm_mhz) * 1e6 / 1e9
+    achieved = inst / (ms / 1e3) / 1e9
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "G warp instructions/s",
+            "frac": achieved / peak, "inst_per_run": inst, "peak_kind": "152 SMs x 4 schedulers x sampled SM clock"}
 
 
 def measured_peaks() -> tuple[float, str]:
@@ -677,9 +692,11 @@ def run_cuda(args, world, rank, local):
         roof = {"stage": dominant, "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
                 "frac": gbs / peak, "traffic": traffic_from_profiles(args.workload, dominant),
                 "algorithmic_bytes": alg, "ms": per_run[dominant], "peak_kind": peak_kind,
-                "note": ("issue-bound gather stage (ncu: k_descriptor 86 % issue-active, k_orientation "
-                         "latency-bound, profiles/); its DRAM bytes are small, so the HBM fraction is low by "
-                         "nature; roofline_pyramid_dog is the HBM roofline of the pyramid stage")}
+                "issue_slots": issue_roofline(traffic_from_profiles(args.workload, dominant, "inst"),
+                                              per_run[dominant], clocks.get("sm_mhz")),
+                "note": ("issue-bound gather stage: its DRAM bytes are small, so the HBM fraction is low by "
+                         "nature; issue_slots is the roofline that binds it (warp instructions from a scoped ncu "
+                         "capture, profiles/); roofline_pyramid_dog is the HBM roofline of the pyramid stage")}
 
     out = None
     if rank == 0:

@@ -112,9 +112,19 @@ def test_measured_peaks_come_from_the_measured_file():
 
 def test_traffic_figures_exist_for_the_bench_workloads():
     # figures come from scoped ncu captures; a stage that was not captured
-    # reports null, the dominant stage of the headline workload must be there
-    for wl in ("1080p", "4096"):
-        for stage in ("pyramid_dog", "extrema_refine", "orientation", "descriptor"):
-            t = bench.traffic_from_profiles(wl, stage)
-            assert t is None or (isinstance(t, int) and t > 0), (wl, stage)
+    # reports null, the dominant stage of both workloads must be there
+    for kind in ("dram_bytes", "inst"):
+        for wl in ("1080p", "4096"):
+            for stage in ("pyramid_dog", "extrema_refine", "orientation", "descriptor"):
+                t = bench.traffic_from_profiles(wl, stage, kind)
+                assert t is None or (isinstance(t, int) and t > 0), (kind, wl, stage)
     assert bench.traffic_from_profiles("1080p", "descriptor") > 0
+    assert bench.traffic_from_profiles("1080p", "descriptor", "inst") > 0
+    assert bench.traffic_from_profiles("4096", "descriptor", "inst") > 0
+
+
+def test_issue_roofline():
+    r = bench.issue_roofline(1.258e9, 2.0, 2070.0)  # 1.258 G warp instructions in 2 ms
+    assert r["bound"] == "issue" and r["peak"] == pytest.approx(152 * 4 * 2.07)
+    assert r["achieved"] == pytest.approx(629.0) and r["frac"] == pytest.approx(629.0 / (152 * 4 * 2.07))
+    assert bench.issue_roofline(None, 2.0, 2070.0) is None and bench.issue_roofline(1e9, 2.0, None) is None
