@@ -343,7 +343,10 @@ typedef struct {
     const SiftCudaKeypoint* kps; /* total keypoints, image after image */
     const float* desc;           /* total x 128 */
     uint32_t launches;           /* kernel launches of the run */
-    float device_ms;             /* device time of the run (images already on the device) */
+    float device_ms;             /* device time of the run (from its first kernel) */
+    uint32_t images_in_place;    /* 1: the run read the images from the caller's buffers (a device
+                                    that reads pageable host memory, every image 16-byte aligned
+                                    with a stride a multiple of 16); 0: from a device copy */
 } SiftCudaBatchResult;
 
 typedef struct SiftCudaBatch SiftCudaBatch;

@@ -123,7 +123,8 @@ class BatchImage(C.Structure):
 
 class BatchResult(C.Structure):
     _fields_ = [("n_images", C.c_uint32), ("total", C.c_uint32), ("offsets", C.POINTER(C.c_uint32)),
-                ("kps", C.c_void_p), ("desc", C.c_void_p), ("launches", C.c_uint32), ("device_ms", C.c_float)]
+                ("kps", C.c_void_p), ("desc", C.c_void_p), ("launches", C.c_uint32), ("device_ms", C.c_float),
+                ("images_in_place", C.c_uint32)]
 
 
 class ReplayRequest(C.Structure):

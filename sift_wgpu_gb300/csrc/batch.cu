@@ -96,7 +96,12 @@ struct BatchEngine {
     std::vector<std::vector<LevelBlur>> lv;
     size_t lut_off = 0;
 
-    DevMem d_img, d_U, d_tmp, d_tmp2, d_ents, d_pref, d_imgoff, d_imgpitch, d_wts, d_ltab, d_lw, d_lz;
+    DevMem d_img, d_U, d_tmp, d_tmp2, d_ents, d_pref, d_imgaddr, d_imgpitch, d_wts, d_ltab, d_lw, d_lz;
+    // the device reads pageable host memory coherently (Grace's address
+    // translation): the base level then reads the caller's images in place
+    bool host_reads = false;
+    std::vector<unsigned long long> h_addr;
+    std::vector<int> h_pitch;
     DevMem d_words, d_cand_off, d_scan, d_cands, d_refined, d_keep, d_ori_angle, d_ori_count, d_ori_off, d_oriented,
         d_desc, d_ctr;
     HostPinned h_ctr;
@@ -117,6 +122,7 @@ struct BatchEngine {
     uint32_t cap_cand = 0, cap_ori = 0;
     size_t scan_words = 0, scan_b = 0;  // scan state: words scan at 0, orientation-count scan at scan_b
     uint32_t n_out = 0;
+    bool images_in_place = false;  // the last run read the caller's images in place
 
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -140,7 +146,7 @@ struct BatchEngine {
     }
     EntryTable tab() const { return EntryTable{d_ents.as<OctaveDev>(), N * O, S}; }
     BatchPyr bpyr() const {
-        return BatchPyr{d_U.as<uint8_t>(), d_ents.as<OctaveDev>(), O, S, d_img.as<uint8_t>(), d_imgoff.as<long long>(),
+        return BatchPyr{d_U.as<uint8_t>(), d_ents.as<OctaveDev>(), O, S, d_imgaddr.as<unsigned long long>(),
                         d_imgpitch.as<int>()};
     }
     const uint32_t* pref(size_t off) const { return d_pref.as<uint32_t>() + off; }
@@ -156,6 +162,9 @@ struct BatchEngine {
         CK(cudaEventCreate(&ev_t1), "cudaEventCreate");
         CK(d_ctr.ensure(sizeof(Counters)), "cudaMalloc(counters)");
         CK(h_ctr.ensure(sizeof(Counters)), "cudaHostAlloc(counters)");
+        int pageable = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, opt.device) != cudaSuccess) pageable = 0;
+        host_reads = pageable == 1;
         return 0;
     }
 
@@ -300,7 +309,7 @@ struct BatchEngine {
         CK(d_tmp2.ensure(std::max<size_t>(toff, 16)), "cudaMalloc(tmp)");
         CK(d_ents.ensure(sizeof(OctaveDev) * std::max<size_t>(ents.size(), 1)), "cudaMalloc(entries)");
         CK(d_pref.ensure(sizeof(uint32_t) * pr.size()), "cudaMalloc(prefixes)");
-        CK(d_imgoff.ensure(sizeof(long long) * std::max(N, 1)), "cudaMalloc(image table)");
+        CK(d_imgaddr.ensure(sizeof(unsigned long long) * std::max(N, 1)), "cudaMalloc(image table)");
         CK(d_imgpitch.ensure(sizeof(int) * std::max(N, 1)), "cudaMalloc(image table)");
         CK(d_wts.ensure(sizeof(float) * wts.size()), "cudaMalloc(wts)");
         CK(d_ltab.ensure(sizeof(int) * std::max<size_t>(itab.size(), 4)), "cudaMalloc(ltab)");
@@ -313,10 +322,6 @@ struct BatchEngine {
             CK(cudaMemcpyAsync(d_ents.p, ents.data(), sizeof(OctaveDev) * ents.size(), cudaMemcpyHostToDevice, st),
                "H2D entries");
         CK(cudaMemcpyAsync(d_pref.p, pr.data(), sizeof(uint32_t) * pr.size(), cudaMemcpyHostToDevice, st), "H2D pref");
-        if (N) {
-            CK(cudaMemcpyAsync(d_imgoff.p, img_off.data(), sizeof(long long) * N, cudaMemcpyHostToDevice, st), "H2D");
-            CK(cudaMemcpyAsync(d_imgpitch.p, img_pitch.data(), sizeof(int) * N, cudaMemcpyHostToDevice, st), "H2D");
-        }
         CK(cudaMemcpyAsync(d_wts.p, wts.data(), sizeof(float) * wts.size(), cudaMemcpyHostToDevice, st), "H2D wts");
         if (!itab.empty())
             CK(cudaMemcpyAsync(d_ltab.p, itab.data(), sizeof(int) * itab.size(), cudaMemcpyHostToDevice, st), "H2D");
@@ -507,11 +512,36 @@ struct BatchEngine {
         const bool changed = ents.empty() || d != dims;
         if (int rc = ensure_geometry(d)) return rc;
         if (int rc = ensure_export(n_out, changed)) return rc;
-        for (uint32_t i = 0; i < n; ++i)
-            if (imgs[i].width && imgs[i].height)
-                CK(cudaMemcpy2DAsync(d_img.as<uint8_t>() + img_off[i], img_pitch[i], imgs[i].data, imgs[i].stride,
-                                     imgs[i].width, imgs[i].height, cudaMemcpyHostToDevice, st),
-                   "copy image");
+        // The base level reads each image where it is: the caller's buffer on
+        // a device that reads pageable host memory coherently, when every
+        // image starts and strides on 16 bytes (the level kernel's staging
+        // loads) and the base level is a blur (a copied base level is a copy
+        // node that reads the device copy); else the batch's device copy.
+        bool direct = host_reads && base.sigma > 0.0f;
+        for (uint32_t i = 0; i < n && direct; ++i)
+            if (imgs[i].width && imgs[i].height &&
+                (((uintptr_t)imgs[i].data & 15) != 0 || (imgs[i].stride & 15) != 0 || imgs[i].stride > (1u << 30)))
+                direct = false;
+        h_addr.assign(n, 0);
+        h_pitch.assign(n, 0);
+        for (uint32_t i = 0; i < n; ++i) {
+            if (direct) {
+                h_addr[i] = (unsigned long long)(uintptr_t)imgs[i].data;
+                h_pitch[i] = (int)imgs[i].stride;
+            } else {
+                h_addr[i] = (unsigned long long)(uintptr_t)(d_img.as<uint8_t>() + img_off[i]);
+                h_pitch[i] = img_pitch[i];
+                if (imgs[i].width && imgs[i].height)
+                    CK(cudaMemcpy2DAsync(d_img.as<uint8_t>() + img_off[i], img_pitch[i], imgs[i].data,
+                                         imgs[i].stride, imgs[i].width, imgs[i].height, cudaMemcpyHostToDevice, st),
+                       "copy image");
+            }
+        }
+        CK(cudaMemcpyAsync(d_imgaddr.p, h_addr.data(), sizeof(unsigned long long) * n, cudaMemcpyHostToDevice, st),
+           "H2D image table");
+        CK(cudaMemcpyAsync(d_imgpitch.p, h_pitch.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st),
+           "H2D image table");
+        images_in_place = direct;
         for (int attempt = 0; attempt < 8; ++attempt) {
             if (int rc = run()) return rc;
             CK(cudaStreamSynchronize(st), "batch run");
@@ -601,5 +631,6 @@ extern "C" int sift_cuda_batch_detect_and_compute(SiftCudaBatch* batch, const Si
     out->desc = reinterpret_cast<const float*>(b.hx.as<char>() + b.hx_desc_off());
     out->launches = b.launches;
     out->device_ms = b.device_ms;
+    out->images_in_place = b.images_in_place ? 1u : 0u;
     return 0;
 }

@@ -694,7 +694,7 @@ __device__ __forceinline__ const uint8_t* level_src(const BatchPyr& bp, const Oc
                                                     int* pitch) {
     if (s == 0) {
         *pitch = bp.img_pitch[k];
-        return bp.img + bp.img_off[k];
+        return reinterpret_cast<const uint8_t*>(bp.img_addr[k]);
     }
     *pitch = od.pitch;
     return bp.U + od.u_off + (long long)(s - 1) * od.plane;

@@ -67,8 +67,10 @@ struct BatchPyr {
     uint8_t* U;
     const OctaveDev* ents;
     int O, S;
-    const uint8_t* img;
-    const long long* img_off;
+    // image k: address of its first byte (the batch's device copy, or the
+    // caller's host buffer on a device that reads pageable host memory) and
+    // its row pitch in bytes
+    const unsigned long long* img_addr;
     const int* img_pitch;
 };
 

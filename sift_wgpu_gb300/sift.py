@@ -423,6 +423,7 @@ class Batch:
         self._h = h
         self.last_launch_count = 0
         self.last_device_ms = 0.0
+        self.last_images_in_place = False
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -463,6 +464,7 @@ class Batch:
         _capi.check(_capi.lib().sift_cuda_batch_detect_and_compute(self._h, arr, n, C.byref(res)))
         self.last_launch_count = res.launches
         self.last_device_ms = float(res.device_ms)
+        self.last_images_in_place = bool(res.images_in_place)
         if n == 0:
             return []
         off = np.ctypeslib.as_array(res.offsets, shape=(n + 1,)).copy()

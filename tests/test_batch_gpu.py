@@ -51,6 +51,30 @@ def test_batch_equals_single_engine(sgb):
         assert b.detect_and_compute([]) == []
 
 
+def test_images_in_place_and_copied_agree(sgb):
+    """Images that start and stride on 16 bytes are read where they are on a
+    device that reads pageable host memory (a GB300 with its Grace host); the
+    same images with a 1-byte wider stride go through the device copy. Both
+    runs give the same results."""
+    import torch
+    imgs = [synth_image(700 + i, w, h) for i, (w, h) in enumerate([(640, 480), (1280, 720), (512, 1024)])]
+    padded = []
+    for im in imgs:
+        h, w = im.shape
+        buf = np.zeros((h, w + 1), np.uint8)
+        buf[:, :w] = im
+        padded.append(buf[:, :w])  # stride w + 1
+    with sgb.Batch(sgb.Sift.default()) as b:
+        a = b.detect_and_compute(imgs)
+        in_place = b.last_images_in_place
+        c = b.detect_and_compute(padded)
+        assert not b.last_images_in_place
+    assert all(same(x, y) for x, y in zip(a, c))
+    assert sum(len(k) for k, _ in a) > 100
+    if "GB300" in torch.cuda.get_device_name(0):  # Grace host: pageable memory is device-readable
+        assert in_place
+
+
 def test_batch64_sample_with_six_octaves(sgb):
     """Twelve images of the uneven 64-image batch (the smallest, the largest,
     the most elongated and nine more) under Sift::new(1.6, 6, 3, 0.5, 0.04,
