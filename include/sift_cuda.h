@@ -221,6 +221,12 @@ int sift_cuda_debug_stage(SiftCudaEngine* engine, int stage, void* out, uint64_t
 /* Device-side kernel launches of the last run (for launch accounting). */
 uint32_t sift_cuda_last_launch_count(SiftCudaEngine* engine);
 
+/* 1 if the last host call's run read the image where the caller keeps it (a
+ * pageable host image, 16-byte aligned with a stride a multiple of 16, on a
+ * device that reads pageable host memory coherently, e.g. a GB300 with its
+ * Grace host), 0 if it read the engine's device copy. */
+uint32_t sift_cuda_last_image_in_place(SiftCudaEngine* engine);
+
 /* Per-stage device time accounting, the CUDA-event counterpart of the
  * reference's SIFT_PROFILE stage timers (src/gpu_sift_v2.rs:795-855). While
  * enabled, every run records events on the engine's stream at the stage

@@ -169,6 +169,7 @@ def lib() -> C.CDLL:
         "sift_cuda_stream": (C.c_void_p, [C.c_void_p]),
         "sift_cuda_debug_stage": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, u64, P(u64)]),
         "sift_cuda_last_launch_count": (u32, [C.c_void_p]),
+        "sift_cuda_last_image_in_place": (u32, [C.c_void_p]),
         "sift_cuda_profile_enable": (C.c_int, [C.c_void_p, C.c_int]),
         "sift_cuda_profile_read": (C.c_int, [C.c_void_p, P(f32), u32, P(u32)]),
         "sift_cuda_gaussian_blur_u8_noalloc": (C.c_int, [C.c_void_p, u32, u32, u32, C.c_void_p, u32, f32,
@@ -210,7 +211,7 @@ def exported_symbols() -> list[str]:
         "sift_cuda_detect_and_compute_view", "sift_cuda_detect_and_compute_pixels", "sift_cuda_to_luma",
         "sift_cuda_result_free", "sift_cuda_last_error", "sift_cuda_run_device",
         "sift_cuda_device_outputs", "sift_cuda_synchronize", "sift_cuda_stream",
-        "sift_cuda_debug_stage", "sift_cuda_last_launch_count", "sift_cuda_profile_enable",
+        "sift_cuda_debug_stage", "sift_cuda_last_launch_count", "sift_cuda_last_image_in_place", "sift_cuda_profile_enable",
         "sift_cuda_profile_read", "sift_cuda_server_options_default", "sift_cuda_server_create",
         "sift_cuda_server_destroy", "sift_cuda_server_submit", "sift_cuda_server_poll", "sift_cuda_server_release",
         "sift_cuda_server_warm", "sift_cuda_server_stats", "sift_cuda_server_tuning", "sift_cuda_footprint_bytes",

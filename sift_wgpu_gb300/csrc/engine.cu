@@ -301,6 +301,10 @@ void* sift_cuda_stream(SiftCudaEngine* engine) { return engine ? (void*)engine->
 
 uint32_t sift_cuda_last_launch_count(SiftCudaEngine* engine) { return engine ? engine->e.launches : 0; }
 
+uint32_t sift_cuda_last_image_in_place(SiftCudaEngine* engine) {
+    return engine && engine->e.image_in_place ? 1u : 0u;
+}
+
 int sift_cuda_profile_enable(SiftCudaEngine* engine, int enable) {
     if (!engine) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "engine is NULL");
     engine->e.prof = enable != 0;

@@ -40,13 +40,13 @@ namespace sift {
 template <typename TG>
 int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, int r, const float* wts, const float* lut255, cudaStream_t st, int* launches,
-                      int fused_max_radius);
+                      int fused_max_radius, const ImgRef* ref = nullptr);
 template <typename TG>
 int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, cudaStream_t st);
 template <typename TG>
 int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, uint8_t* out_u8, int pitch, int W, int H,
-                       cudaStream_t st);
+                       cudaStream_t st, const ImgRef* ref = nullptr);
 template <typename TG>
 int launch_lanczos(const uint8_t* src, int src_pitch, int W, int H, float* tmp, int tmp_pitch, TG* dst,
                    uint8_t* dst_u8, int dst_pitch, int nW, int nH, const int* vtab, const float* vw, const int* htab,
@@ -231,6 +231,15 @@ struct Engine {
         return (float*)(hx.as<char>() + align_up(sizeof(Counters), 256) + align_up((size_t)cap_x * sizeof(Keypoint), 256));
     }
     size_t img_pitch = 0;
+    // The image cell the base level reads (ImgRef): set by every upload.
+    // Pageable caller images are read where they are when the device reads
+    // pageable host memory coherently (a GB300's Grace host), saving the
+    // staged copy; pinned and device images are copied to d_img (a DMA copy
+    // is faster than the base level's staging reads over the host link).
+    DevMem d_ref;
+    HostPinned h_ref;
+    int pageable_reads = -1;  // device attribute, read once
+    bool image_in_place = false, ref_valid = false;
     uint32_t launches = 0;
     bool last_desc = true;
 
@@ -690,11 +699,12 @@ struct Engine {
                 int nl = 0;
                 if (launch_blur_level<TG>(img, (int)stride, d_tmp.as<uint8_t>(), G + o0.g_off, U + o0.u_off,
                                           o0.pitch, o0.W, o0.H, base.radius, wts + base.woff, lut, st,
-                                          &nl, tune.fused_max_radius))
+                                          &nl, tune.fused_max_radius, d_ref.as<ImgRef>()))
                     return cuda_fail(cudaGetLastError(), "blur (base)");
                 launches += nl;
             } else {
-                if (ok(launch_u8_to_level<TG>(img, stride, G + o0.g_off, U + o0.u_off, o0.pitch, o0.W, o0.H, st)))
+                if (ok(launch_u8_to_level<TG>(img, stride, G + o0.g_off, U + o0.u_off, o0.pitch, o0.W, o0.H, st,
+                                              d_ref.as<ImgRef>())))
                     return cuda_fail(cudaGetLastError(), "base copy");
             }
         }
@@ -887,7 +897,37 @@ struct Engine {
         if (pitch != img_pitch || !d_img.p || d_img.bytes < pitch * std::max<uint32_t>(h, 1)) drop_graph();
         img_pitch = pitch;
         CK(d_img.ensure(img_pitch * std::max<uint32_t>(h, 1)), "cudaMalloc(image)");
-        if (w && h && img) CK(cudaMemcpy2DAsync(d_img.p, img_pitch, img, stride, w, h, kind, st), "copy image");
+        if (!d_ref.p) {
+            CK(d_ref.ensure(sizeof(ImgRef)), "cudaMalloc(image cell)");
+            CK(h_ref.ensure(sizeof(ImgRef)), "cudaHostAlloc(image cell)");
+        }
+        if (pageable_reads < 0) {
+            int v = 0;
+            if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, opt.device) != cudaSuccess) v = 0;
+            pageable_reads = v == 1 ? 1 : 0;
+        }
+        // in place: a pageable host image starting and striding on 16 bytes
+        // (the level kernel's staging loads), a blurred base level
+        bool in_place = false;
+        if (pageable_reads && kind == cudaMemcpyHostToDevice && img && w && h && base.sigma > 0.0f &&
+            ((uintptr_t)img & 15) == 0 && (stride & 15) == 0 && stride <= (1u << 30)) {
+            cudaPointerAttributes a{};
+            if (cudaPointerGetAttributes(&a, img) == cudaSuccess) in_place = a.type == cudaMemoryTypeUnregistered;
+            else cudaGetLastError();
+        }
+        image_in_place = in_place;
+        const ImgRef cell = in_place ? ImgRef{img, (long long)stride} : ImgRef{d_img.as<uint8_t>(), (long long)img_pitch};
+        if (!in_place && w && h && img)
+            CK(cudaMemcpy2DAsync(d_img.p, img_pitch, img, stride, w, h, kind, st), "copy image");
+        // The cell is rewritten only when it changes: a run that reads it is
+        // ordered after the copy on the stream, and a changed cell comes from
+        // a host call, which has waited for the previous run to end.
+        ImgRef* r = h_ref.as<ImgRef>();
+        if (!ref_valid || r->ptr != cell.ptr || r->pitch != cell.pitch) {
+            *r = cell;
+            CK(cudaMemcpyAsync(d_ref.p, h_ref.p, sizeof(ImgRef), cudaMemcpyHostToDevice, st), "H2D image cell");
+            ref_valid = true;
+        }
         return 0;
     }
 

@@ -148,8 +148,13 @@ __device__ __forceinline__ void blur_row(const uint8_t* __restrict__ in, int in_
 
 __global__ void __launch_bounds__(kRowThreads) k_blur_rows(const uint8_t* __restrict__ in, int in_pitch,
                                                            uint8_t* __restrict__ out, int out_pitch, int W, int r,
-                                                           const float* __restrict__ wts) {
+                                                           const float* __restrict__ wts,
+                                                           const ImgRef* __restrict__ ref) {
     chain_wait();
+    if (ref) {  // a host call's base level: the image is wherever the cell says
+        in = ref->ptr;
+        in_pitch = (int)ref->pitch;
+    }
     extern __shared__ __align__(16) float sm[];
     blur_row(in, in_pitch, out, out_pitch, W, r, wts, blockIdx.x, sm);
 }
@@ -470,8 +475,13 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
                                                           TG* __restrict__ out, uint8_t* __restrict__ out_u8,
                                                           int pitch, int W, int H,
                                                           const float* __restrict__ wts,
-                                                          const float* __restrict__ lut255) {
+                                                          const float* __restrict__ lut255,
+                                                          const ImgRef* __restrict__ ref) {
     chain_wait();
+    if (ref) {  // a host call's base level: the image is wherever the cell says
+        in = ref->ptr;
+        in_pitch = (int)ref->pitch;
+    }
     extern __shared__ __align__(16) float sm[];
     blur_level_tile<TG, R>(in, in_pitch, out, out_u8, pitch, W, H, wts, lut255, blockIdx.x * kFTX, blockIdx.y * kFTY,
                            sm);
@@ -494,8 +504,12 @@ __global__ void k_copy_level(const TG* __restrict__ prev, const uint8_t* __restr
 // Base level without a blur (sigma <= assumed_blur, src/sift.rs:1204-1214).
 template <typename TG>
 __global__ void k_u8_to_level(const uint8_t* __restrict__ img, long long stride, TG* __restrict__ out,
-                              uint8_t* __restrict__ out_u8, int pitch, int W, int H) {
+                              uint8_t* __restrict__ out_u8, int pitch, int W, int H, const ImgRef* __restrict__ ref) {
     chain_wait();
+    if (ref) {
+        img = ref->ptr;
+        stride = ref->pitch;
+    }
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y;
     if (x >= W) return;
@@ -789,10 +803,10 @@ static int set_smem(const void* k, size_t smem) {
 template <typename TG>
 int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, int r, const float* wts, const float* lut255, cudaStream_t st, int* launches,
-                      int fused_max_radius) {
+                      int fused_max_radius, const ImgRef* ref) {
     const size_t smem = blur_fused_smem(r);
     if (r <= kFMaxR && r <= fused_max_radius) {
-        void (*kern)(const uint8_t*, int, TG*, uint8_t*, int, int, int, const float*, const float*);
+        void (*kern)(const uint8_t*, int, TG*, uint8_t*, int, int, int, const float*, const float*, const ImgRef*);
         switch (r) {
             case 1: kern = k_blur_level<TG, 1>; break;
             case 2: kern = k_blur_level<TG, 2>; break;
@@ -805,15 +819,16 @@ int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, ui
         }
         if (set_smem((const void*)kern, smem)) return -1;
         dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
-        if (launch_chained(kern, grid, kFThreads, smem, st, in, in_pitch, out, out_u8, pitch, W, H, wts,
-                           lut255) != cudaSuccess)
+        if (launch_chained(kern, grid, kFThreads, smem, st, in, in_pitch, out, out_u8, pitch, W, H, wts, lut255,
+                           ref) != cudaSuccess)
             return -1;
         *launches += 1;
         return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     }
     const size_t rs = blur_rows_smem(W, r), cs = blur_cols_smem(r);
     if (set_smem((const void*)k_blur_rows, rs) || set_smem((const void*)k_blur_cols<TG>, cs)) return -1;
-    if (launch_chained(k_blur_rows, H, kRowThreads, rs, st, in, in_pitch, tmp, pitch, W, r, wts) != cudaSuccess)
+    if (launch_chained(k_blur_rows, H, kRowThreads, rs, st, in, in_pitch, tmp, pitch, W, r, wts, ref) !=
+        cudaSuccess)
         return -1;
     dim3 grid((W + kColTX - 1) / kColTX, (H + kColRows - 1) / kColRows);
     if (launch_chained(k_blur_cols<TG>, grid, kColThreads, cs, st, tmp, pitch, out, out_u8, pitch, W, H, r, wts,
@@ -834,9 +849,10 @@ int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* 
 
 template <typename TG>
 int launch_u8_to_level(const uint8_t* img, long long stride, TG* out, uint8_t* out_u8, int pitch, int W, int H,
-                       cudaStream_t st) {
+                       cudaStream_t st, const ImgRef* ref) {
     dim3 grid((W + 255) / 256, H);
-    if (launch_chained(k_u8_to_level<TG>, grid, 256, 0, st, img, stride, out, out_u8, pitch, W, H) != cudaSuccess)
+    if (launch_chained(k_u8_to_level<TG>, grid, 256, 0, st, img, stride, out, out_u8, pitch, W, H, ref) !=
+        cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -937,10 +953,11 @@ int lanczos_fused_tile() { return kLzT; }
 
 #define SIFT_INST(TG)                                                                                              \
     template int launch_blur_level<TG>(const uint8_t*, int, uint8_t*, TG*, uint8_t*, int, int, int, int,           \
-                                       const float*, const float*, cudaStream_t, int*, int);                       \
+                                       const float*, const float*, cudaStream_t, int*, int, const ImgRef*);        \
     template int launch_copy_level<TG>(const TG*, const uint8_t*, TG*, uint8_t*, int, int, int,                    \
                                        cudaStream_t);                                                              \
-    template int launch_u8_to_level<TG>(const uint8_t*, long long, TG*, uint8_t*, int, int, int, cudaStream_t);    \
+    template int launch_u8_to_level<TG>(const uint8_t*, long long, TG*, uint8_t*, int, int, int, cudaStream_t,     \
+                                        const ImgRef*);                                                            \
     template int launch_lanczos<TG>(const uint8_t*, int, int, int, float*, int, TG*, uint8_t*, int, int, int,      \
                                     const int*, const float*, const int*, const float*, const LanczosUniform&,      \
                                     cudaStream_t, bool, int*);

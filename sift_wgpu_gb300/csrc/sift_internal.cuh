@@ -63,6 +63,14 @@ struct OctaveDev {
 // A batch's pyramid in device memory (u8 storage): the entries of the batch
 // (image-major), the u8 level arena, the horizontal-pass planes, and the
 // input images packed at per-image offsets.
+// Where a host call's image is read from, set before each run: the
+// engine's device copy, or the caller's pageable buffer on a device that
+// reads pageable host memory coherently (the captured graph reads the cell).
+struct ImgRef {
+    const uint8_t* ptr;
+    long long pitch;
+};
+
 struct BatchPyr {
     uint8_t* U;
     const OctaveDev* ents;

@@ -283,6 +283,11 @@ class Engine:
     def last_launch_count(self) -> int:
         return int(_capi.lib().sift_cuda_last_launch_count(self.handle))
 
+    @property
+    def last_image_in_place(self) -> bool:
+        """Whether the last host call read the image where the caller keeps it."""
+        return bool(_capi.lib().sift_cuda_last_image_in_place(self.handle))
+
     STAGE_NAMES = ("pyramid_dog", "extrema_refine", "orientation", "descriptor")
 
     def profile(self, enable: bool) -> None:

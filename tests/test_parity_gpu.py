@@ -157,6 +157,33 @@ def test_strided_input_and_determinism(sgb):
     assert d1.tobytes() == d2.tobytes() == d3.tobytes()
 
 
+def test_image_in_place_and_copied_agree(sgb):
+    """A pageable image that starts and strides on 16 bytes is read where it
+    is on a GB300 (its Grace host memory is device-readable); a pinned image
+    and one with a 1-byte wider stride are copied to the device first. All
+    give the same keypoints and descriptors, pyramid included."""
+    import torch
+    img = image(sgb, 1280, 720, 33)
+    eng = engine_for(sgb, (1.6, 4, 3, 0.5, 0.04, 10.0))
+    k1, d1 = eng.detect_and_compute(img)
+    in_place = eng.last_image_in_place
+    p1 = eng.debug_stage(sgb.STAGE_PYRAMID)
+    pinned = torch.from_numpy(img).pin_memory().numpy()
+    k2, d2 = eng.detect_and_compute(pinned)
+    assert not eng.last_image_in_place
+    buf = np.zeros((720, 1281), np.uint8)
+    buf[:, :1280] = img
+    k3, d3 = eng.detect_and_compute(buf[:, :1280])
+    assert not eng.last_image_in_place
+    assert k1.tobytes() == k2.tobytes() == k3.tobytes()
+    assert d1.tobytes() == d2.tobytes() == d3.tobytes()
+    assert np.array_equal(eng.debug_stage(sgb.STAGE_PYRAMID), p1)
+    k4, d4 = eng.detect_and_compute(img)  # back in place (the cell is rewritten)
+    assert k4.tobytes() == k1.tobytes() and d4.tobytes() == d1.tobytes()
+    if "GB300" in torch.cuda.get_device_name(0):
+        assert in_place and eng.last_image_in_place
+
+
 @pytest.mark.parametrize("storage", ["f16", "u8"])
 def test_other_storage_modes_are_exact(sgb, storage):
     """u8-valued levels are exact in f16 and in u8 (read as v / 255 through
