@@ -152,9 +152,9 @@ __device__ __forceinline__ AxisBins axis_bins() {
 // bin-major histogram hist[bin][32]: the gradient (gx, gy) at window offset
 // (fdx, fdy), added as +0.0 when the sample lies outside the level (`in`
 // false), which leaves a bin bit-identical.
+// bf: the polynomial bin position of the gradient (ori_bin_pos2).
 __device__ __forceinline__ void ori_add(float gx, float gy, float fdx, float fdy, float inv_wd, bool in,
-                                        float* hist, int lane, const AxisBins& ab) {
-    const float two_pi = 2.0f * kPi;
+                                        float* hist, int lane, const AxisBins& ab, float bf) {
     // the hardware square root (within an ulp; the bins are sums whose
     // order differs from the reference's anyway)
     const float mag = sqrt_approx(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
@@ -168,9 +168,6 @@ __device__ __forceinline__ void ori_add(float gx, float gy, float fdx, float fdy
     // takes atan2f and the IEEE division, the exact sequence (rare: the
     // branch no longer splits warps on every flat patch). Away from the
     // edges all three floor to the same bin.
-    const float pa = atan2_poly(gy, gx);
-    const float pn = pa < 0.0f ? __fadd_rn(pa, two_pi) : pa;
-    float bf = __fmul_rn(pn, (float)kOriBins / two_pi);
     const bool axis = gx == 0.0f || gy == 0.0f;  // (0, 0): atan2 0, angle 0
     const float bax = gy == 0.0f ? (gx < 0.0f ? ab.left : ab.right) : (gy > 0.0f ? ab.up : ab.down);
     bf = axis ? bax : bf;
@@ -182,9 +179,23 @@ __device__ __forceinline__ void ori_add(float gx, float gy, float fdx, float fdy
     *h = __fadd_rn(*h, in ? v : 0.0f);
 }
 
+// The polynomial bin positions of two gradients: atan2_poly to [0, 2 pi),
+// times 36 / (2 pi) (src/sift.rs:652-656), on f32x2 pairs.
+__device__ __forceinline__ float2 ori_bin_pos2(float2 gy, float2 gx) {
+    const float two_pi = 2.0f * kPi;
+    const float2 pa = atan2_poly2(gy, gx);
+    const float2 pw = __fadd2_rn(pa, make_float2(two_pi, two_pi));
+    const float2 pn = make_float2(pa.x < 0.0f ? pw.x : pa.x, pa.y < 0.0f ? pw.y : pa.y);
+    const float k = (float)kOriBins / two_pi;
+    return __fmul2_rn(pn, make_float2(k, k));
+}
+
 // The orientation window of one keypoint (src/sift.rs:640-662), lane-strided:
 // sample k = lane + 32 j of the (2r+1)^2 window, read from the level (the
-// reads mostly hit L1). Windows at the level's border take the CHECK form.
+// reads mostly hit L1). A lane takes its samples two at a time (k and
+// k + 32: their loads in flight together, the two arctangents on f32x2
+// pairs) and adds them to its histogram column in window order, as one at a
+// time would. Windows at the level's border take the CHECK form.
 template <typename TG, bool CHECK>
 __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, float yo, int r, float wd, float* hist,
                                            int lane, const AxisBins& ab) {
@@ -196,23 +207,40 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
     // by fixed amounts per step, with one row wrap (as selects) at most.
     const int q0 = lane / side, dq = 32 / side;
     const float dr_f = (float)(32 - dq * side), dq_f = (float)dq;
-    float fdx = (float)(lane - q0 * side) - r_f, fdy = (float)q0 - r_f;
-    for (;; fdx += dr_f, fdy += dq_f) {
-        const bool wrap = fdx > r_f;
-        fdx = wrap ? fdx - side_f : fdx;
-        fdy = wrap ? fdy + 1.0f : fdy;
-        if (fdy > r_f) break;
+    auto wrap = [&](float& x, float& y) {
+        const bool w = x > r_f;
+        x = w ? x - side_f : x;
+        y = w ? y + 1.0f : y;
+    };
+    // the gradient at a window offset (src/sift.rs:640-651)
+    auto grad = [&](float fdx, float fdy, float& gx, float& gy, bool& in) {
         int xi = round_away_i(__fadd_rn(xo, fdx));
         int yi = round_away_i(__fadd_rn(yo, fdy));
-        bool in = true;
+        in = true;
         if (CHECK) {
             in = !(xi < 1 || xi >= g.W - 1 || yi < 1 || yi >= g.H - 1);
             xi = clampi(xi, 1, g.W - 2);
             yi = clampi(yi, 1, g.H - 2);
         }
-        const float gx = __fsub_rn(g.px_in(xi + 1, yi), g.px_in(xi - 1, yi));
-        const float gy = __fsub_rn(g.px_in(xi, yi + 1), g.px_in(xi, yi - 1));
-        ori_add(gx, gy, fdx, fdy, inv_wd, in, hist, lane, ab);
+        gx = __fsub_rn(g.px_in(xi + 1, yi), g.px_in(xi - 1, yi));
+        gy = __fsub_rn(g.px_in(xi, yi + 1), g.px_in(xi, yi - 1));
+    };
+    float fdx = (float)(lane - q0 * side) - r_f, fdy = (float)q0 - r_f;
+    for (;;) {
+        wrap(fdx, fdy);
+        if (fdy > r_f) break;
+        float fdx1 = fdx + dr_f, fdy1 = fdy + dq_f;
+        wrap(fdx1, fdy1);
+        const bool has1 = fdy1 <= r_f;  // else the second reads the first's offset and is not added
+        float gx0, gy0, gx1, gy1;
+        bool in0, in1;
+        grad(fdx, fdy, gx0, gy0, in0);
+        grad(has1 ? fdx1 : fdx, has1 ? fdy1 : fdy, gx1, gy1, in1);
+        const float2 bf = ori_bin_pos2(make_float2(gy0, gy1), make_float2(gx0, gx1));
+        ori_add(gx0, gy0, fdx, fdy, inv_wd, in0, hist, lane, ab, bf.x);
+        if (has1) ori_add(gx1, gy1, fdx1, fdy1, inv_wd, in1, hist, lane, ab, bf.y);
+        fdx = fdx1 + dr_f;
+        fdy = fdy1 + dq_f;
     }
 }
 

@@ -218,6 +218,43 @@ __device__ __forceinline__ float atan2_poly(float y, float x) {
     return copysignf(r, y);
 }
 
+// atan2_poly of two gradients at once: the same operations on f32x2 pairs
+// (each element rounds as the scalar ones do); a = min * rcp(max) by the
+// hardware reciprocal, the form __fdividef takes for these arguments, so the
+// results equal atan2_poly's (tests/test_atan2_gpu.py).
+// the hardware's approximate reciprocal (one instruction)
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float2 atan2_poly2(float2 y, float2 x) {
+    const float ax0 = fabsf(x.x), ay0 = fabsf(y.x), ax1 = fabsf(x.y), ay1 = fabsf(y.y);
+    const float mx0 = fmaxf(ax0, ay0), mx1 = fmaxf(ax1, ay1);
+    const float2 mn = make_float2(fminf(ax0, ay0), fminf(ax1, ay1));
+    float2 a = __fmul2_rn(mn, make_float2(rcp_approx(mx0), rcp_approx(mx1)));
+    a.x = mx0 > 0.0f ? a.x : 0.0f;
+    a.y = mx1 > 0.0f ? a.y : 0.0f;
+    const float2 t = __fmul2_rn(a, a);
+    float2 p = __ffma2_rn(make_float2(-0.004693340510129929f, -0.004693340510129929f), t,
+                          make_float2(0.024252643808722496f, 0.024252643808722496f));
+    p = __ffma2_rn(p, t, make_float2(-0.0594867542386055f, -0.0594867542386055f));
+    p = __ffma2_rn(p, t, make_float2(0.09914319962263107f, 0.09914319962263107f));
+    p = __ffma2_rn(p, t, make_float2(-0.14019492268562317f, -0.14019492268562317f));
+    p = __ffma2_rn(p, t, make_float2(0.19969725608825684f, 0.19969725608825684f));
+    p = __ffma2_rn(p, t, make_float2(-0.33331990242004395f, -0.33331990242004395f));
+    p = __ffma2_rn(p, t, make_float2(0.9999998807907104f, 0.9999998807907104f));
+    float2 r = __fmul2_rn(p, a);
+    const float2 neg1 = make_float2(-1.0f, -1.0f);
+    const float2 r2 = __ffma2_rn(r, neg1, make_float2(1.5707963705062866f, 1.5707963705062866f));
+    r.x = ay0 > ax0 ? r2.x : r.x;
+    r.y = ay1 > ax1 ? r2.y : r.y;
+    const float2 r4 = __ffma2_rn(r, neg1, make_float2(3.1415927410125732f, 3.1415927410125732f));
+    r.x = x.x < 0.0f ? r4.x : r.x;
+    r.y = x.y < 0.0f ? r4.y : r.y;
+    return make_float2(copysignf(r.x, y.x), copysignf(r.y, y.y));
+}
+
 // atan2(y, x) in units of 45-degree bins (pi/4 = 1), in [-4, 4]: a = min/max
 // of |x|, |y| and an odd degree-9 polynomial a * P(a^2), minimax in absolute
 // error against atan(a) * 4/pi on [0, 1] (tests/golden/fit_atan2.py; max
@@ -243,11 +280,6 @@ __device__ __forceinline__ float atan2_bins(float y, float x) {
 // fix-ups evaluated on f32x2 pairs (each element rounds as the scalar
 // operations do), with a = min * rcp(max) by the hardware reciprocal, so the
 // same error bound (tests/test_atan2_gpu.py).
-__device__ __forceinline__ float rcp_approx(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
 __device__ __forceinline__ float2 atan2_bins2(float2 y, float2 x) {
     const float ax0 = fabsf(x.x), ay0 = fabsf(y.x), ax1 = fabsf(x.y), ay1 = fabsf(y.y);
     const float2 mx = make_float2(fmaxf(ax0, ay0), fmaxf(ax1, ay1));

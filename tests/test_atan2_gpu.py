@@ -1,7 +1,8 @@
 """The engine's arctangent polynomials against CUDA's atan2f (GPU).
 
-atan2_poly decides orientation bins away from bin edges (within 1e-4 bin of
-an edge the exact atan2f path decides), atan2_bins and its f32x2 pair form
+atan2_poly (and its f32x2 pair form atan2_poly2, which must give the same
+values) decides orientation bins away from bin edges (within 1e-4 bin of an
+edge the exact atan2f path decides), atan2_bins and its pair form
 atan2_bins2 place descriptor samples in their 45-degree bins (linearly
 interpolated). Both are evaluated on the
 device by tests/atan2_probe.cu over a dense grid of directions and
@@ -29,7 +30,7 @@ def probe(tmp_path_factory):
                     "-I", str(HERE.parent / "include"), "-Xcompiler", "-fPIC", "-shared", "-o", str(out),
                     str(HERE / "atan2_probe.cu")], check=True)
     L = C.CDLL(str(out))
-    L.atan2_probe.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.atan2_probe.argtypes = [C.c_void_p, C.c_void_p, C.c_int] + [C.c_void_p] * 5
     return L
 
 
@@ -55,9 +56,11 @@ def inputs():
 def test_polynomials_against_atan2f(probe):
     y, x = inputs()
     n = len(y)
-    poly, bins, bins2, ref = (np.empty(n, np.float32) for _ in range(4))
+    poly, bins, bins2, poly2, ref = (np.empty(n, np.float32) for _ in range(5))
     assert probe.atan2_probe(y.ctypes.data, x.ctypes.data, n, poly.ctypes.data, bins.ctypes.data, bins2.ctypes.data,
-                             ref.ctypes.data) == 0
+                             poly2.ctypes.data, ref.ctypes.data) == 0
+    # the orientation's pair form gives atan2_poly's values bit for bit
+    assert poly2.tobytes() == poly.tobytes()
     ref64 = ref.astype(np.float64)
     # atan2_poly: within 4 ulp of atan2f's angle (or 1e-12 rad near 0)
     err = np.abs(poly.astype(np.float64) - ref64)
