@@ -745,7 +745,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64", "serve", "match"], default="1080p")
-    ap.add_argument("--storage", choices=["f32", "f16", "u8"], default="f32")
+    ap.add_argument("--storage", choices=["f32", "f16", "u8"], default="u8")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain section")

@@ -80,7 +80,9 @@ typedef struct {
  * it reads it (no DoG plane is stored). U8 stores nothing else: orientation
  * and descriptors read v / 255 from the u8 planes through the IEEE quotient
  * table. F32 and F16 also store every level in that type (4 and 2 more bytes
- * per pixel), which orientation and descriptors then read. */
+ * per pixel), which orientation and descriptors then read. U8 is the default
+ * (sift_cuda_options_default): the smallest footprint and, measured on a
+ * GB300, the fastest of the three; all three give the same output. */
 typedef enum {
     SIFT_CUDA_STORAGE_F32 = 0, /* u8 planes + levels stored as f32 (v / 255) */
     SIFT_CUDA_STORAGE_F16 = 1, /* u8 planes + levels stored as f16 (v) */
@@ -89,7 +91,7 @@ typedef enum {
 
 typedef struct {
     int32_t device;   /* CUDA device ordinal */
-    int32_t storage;  /* SiftCudaStorage */
+    int32_t storage;  /* SiftCudaStorage (default SIFT_CUDA_STORAGE_U8) */
     uint32_t reserved[6];
 } SiftCudaOptions;
 

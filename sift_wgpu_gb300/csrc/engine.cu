@@ -78,7 +78,7 @@ void sift_cuda_options_default(SiftCudaOptions* out) {
     if (!out) return;
     std::memset(out, 0, sizeof(*out));
     out->device = 0;
-    out->storage = SIFT_CUDA_STORAGE_F32;
+    out->storage = SIFT_CUDA_STORAGE_U8;
 }
 
 const char* sift_cuda_last_error(void) { return sift::g_last_error.c_str(); }

@@ -492,7 +492,7 @@ void sift_cuda_server_options_default(SiftCudaServerOptions* o) {
     if (!o) return;
     std::memset(o, 0, sizeof(*o));
     o->device = 0;
-    o->storage = SIFT_CUDA_STORAGE_F32;
+    o->storage = SIFT_CUDA_STORAGE_U8;
     o->arena_bytes = 40ull << 30;
     o->max_inflight = 8;
     o->autotune = 0;

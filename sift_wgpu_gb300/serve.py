@@ -41,7 +41,7 @@ class Served:
         return self.done_s - self.submit_s
 
 
-def footprint_bytes(sift: Sift, width: int, height: int, storage: str = "f32") -> int:
+def footprint_bytes(sift: Sift, width: int, height: int, storage: str = "u8") -> int:
     """Device bytes of one slot for a width x height image (admission estimate)."""
     p = sift.to_c()
     return int(_capi.lib().sift_cuda_footprint_bytes(C.byref(p), _STORAGE[storage], width, height))
@@ -64,7 +64,7 @@ def _c_image(img: np.ndarray):
 class Server:
     """A continuous-batching SIFT server on one GPU."""
 
-    def __init__(self, sift: Sift | None = None, device: int = 0, storage: str = "f32",
+    def __init__(self, sift: Sift | None = None, device: int = 0, storage: str = "u8",
                  arena_bytes: int = 40 << 30, max_inflight: int = 8, autotune: bool = False):
         L = _capi.lib()
         self.sift = sift or Sift.default()
@@ -229,7 +229,7 @@ class Server:
 
 
 def replay(images: list, arrivals_s, image_index, server: Server | None = None, sift: Sift | None = None,
-           storage: str = "f32", device: int = 0) -> tuple[np.ndarray, np.ndarray, float]:
+           storage: str = "u8", device: int = 0) -> tuple[np.ndarray, np.ndarray, float]:
     """Open-loop replay. Request i (image images[image_index[i]]) is due at
     arrivals_s[i] after the start; returns (latency_s per request, keypoint
     count per request, wall seconds). server=None replays the plain path:

@@ -107,7 +107,7 @@ def _keypoint_array(keypoints) -> np.ndarray:
 class Engine:
     """One libsiftcuda engine: a CUDA stream plus resident device arenas."""
 
-    def __init__(self, params: "Sift | _capi.Params | None" = None, device: int = 0, storage: str = "f32"):
+    def __init__(self, params: "Sift | _capi.Params | None" = None, device: int = 0, storage: str = "u8"):
         L = _capi.lib()
         if params is None:
             params = Sift.default()

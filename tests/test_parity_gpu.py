@@ -35,7 +35,7 @@ def sgb(built_lib):
 _engines = {}
 
 
-def engine_for(sgb, args, storage="f32"):
+def engine_for(sgb, args, storage="u8"):
     key = (args, storage)
     if key not in _engines:
         _engines[key] = sgb.Engine(sgb.Sift.new(*args), storage=storage)
@@ -184,22 +184,22 @@ def test_image_in_place_and_copied_agree(sgb):
         assert in_place and eng.last_image_in_place
 
 
-@pytest.mark.parametrize("storage", ["f16", "u8"])
+@pytest.mark.parametrize("storage", ["f32", "f16"])
 def test_other_storage_modes_are_exact(sgb, storage):
-    """u8-valued levels are exact in f16 and in u8 (read as v / 255 through
-    the IEEE quotient table), and every mode forms DoG from the same u8
-    planes, so f16 and u8 storage give the f32 mode's output bit for bit,
-    pyramid included."""
+    """u8-valued levels are exact in f32 (as v / 255) and in f16 (as v), the
+    u8 default reads v / 255 through the IEEE quotient, and every mode forms
+    DoG from the same u8 planes, so f32 and f16 storage give the u8 mode's
+    output bit for bit, pyramid included."""
     args = (1.6, 4, 3, 0.5, 0.04, 10.0)
     img = image(sgb, 1920, 1080, 1)
-    e32 = engine_for(sgb, args)
-    k32, d32 = e32.detect_and_compute(img)
-    p32 = e32.debug_stage(sgb.STAGE_PYRAMID)
+    e8 = engine_for(sgb, args, "u8")
+    k8, d8 = e8.detect_and_compute(img)
+    p8 = e8.debug_stage(sgb.STAGE_PYRAMID)
     e = engine_for(sgb, args, storage)
     k, d = e.detect_and_compute(img)
-    assert k.tobytes() == k32.tobytes()
-    assert d.tobytes() == d32.tobytes()
-    assert np.array_equal(e.debug_stage(sgb.STAGE_PYRAMID), p32)
+    assert k.tobytes() == k8.tobytes()
+    assert d.tobytes() == d8.tobytes()
+    assert np.array_equal(e.debug_stage(sgb.STAGE_PYRAMID), p8)
 
 
 def test_high_contrast_threshold(sgb):
@@ -244,7 +244,7 @@ def test_large_6_octave_properties(sgb):
     n = np.linalg.norm(d1, axis=1)
     assert np.all((np.abs(n - 1) < 1e-4) | (n == 0))
     assert np.all((k1["x"] >= -1) & (k1["x"] <= 4097) & (k1["y"] >= -1) & (k1["y"] <= 4097))
-    for storage in ("f16", "u8"):
+    for storage in ("f16", "f32"):
         ks, ds = engine_for(sgb, args, storage).detect_and_compute(img)
         assert ks.tobytes() == k1.tobytes() and ds.tobytes() == d1.tobytes(), storage
 
