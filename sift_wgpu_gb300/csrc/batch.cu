@@ -452,7 +452,7 @@ struct BatchEngine {
                           "batch refine"))
             return rc;
         const int ogrid = (int)std::max<uint32_t>(cap_cand / 64, 32);
-        if (int rc = bump(launch_orientation<uint8_t>(U, tb, d_refined.as<Keypoint>(), d_keep.as<uint32_t>(),
+        if (int rc = bump(launch_orientation<uint8_t>(U, tb, lut, d_refined.as<Keypoint>(), d_keep.as<uint32_t>(),
                                                       cap_cand, oc, d_ori_angle.as<float>(), d_ori_count.as<uint32_t>(),
                                                       ogrid, 152 * 4, st),
                           "batch orientation"))

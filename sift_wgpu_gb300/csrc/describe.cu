@@ -90,7 +90,15 @@ template <typename TG>
 struct GaussPlane {
     const TG* base;
     int pitch, W, H;
-    __device__ __forceinline__ float at(const TG* p) const { return gnorm(p); }
+    // u8 levels: v / 255 from this table (shared memory) when given, else
+    // by div255; both are the IEEE quotient
+    const float* lut;
+    __device__ __forceinline__ float at(const TG* p) const {
+        if constexpr (std::is_same<TG, uint8_t>::value) {
+            if (lut) return lut[*p];
+        }
+        return gnorm(p);
+    }
     // get_gauss_pixel_value (src/sift.rs:218-223)
     __device__ __forceinline__ float px(int x, int y) const {
         x = clampi(x, 0, W - 1);
@@ -122,9 +130,10 @@ struct GaussPlane {
 };
 
 template <typename TG>
-__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const OctaveDev& od, int S, int layer) {
+__device__ __forceinline__ GaussPlane<TG> plane_for(const TG* arena, const OctaveDev& od, int S, int layer,
+                                                    const float* lut = nullptr) {
     const int li = clampi(layer, 0, S + 2);
-    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H};
+    return GaussPlane<TG>{arena + od.g_off + (long long)li * od.plane, od.pitch, od.W, od.H, lut};
 }
 
 
@@ -252,14 +261,14 @@ __device__ __forceinline__ void ori_window(const GaussPlane<TG>& g, float xo, fl
 template <typename TG>
 __device__ __forceinline__ uint32_t orient_one(const TG* __restrict__ arena, const EntryTable& tab, const Keypoint& kp,
                                                float* hist, float* hs, int lane, const AxisBins& ab,
-                                               float* __restrict__ angles) {
+                                               float* __restrict__ angles, const float* lut) {
     const float two_pi = 2.0f * kPi;
     const float bin_w = 2.0f * kPi / (float)kOriBins;
     const int e = kp.octave;  // entry
     if (!(e >= 0 && e < tab.n)) return 0;
     const OctaveDev od = tab.ents[e];
     const int o = od.octave;
-    const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer);
+    const GaussPlane<TG> g = plane_for(arena, od, tab.S, kp.layer, lut);
     const float scale = __int_as_float((127 + o) << 23);
     const float xo = __fdiv_rn(kp.x, scale), yo = __fdiv_rn(kp.y, scale);
     const float so = __fdiv_rn(kp.size, scale);
@@ -348,6 +357,7 @@ __device__ __forceinline__ uint32_t orient_one(const TG* __restrict__ arena, con
 
 template <typename TG>
 __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __restrict__ arena, EntryTable tab,
+                                                                const float* __restrict__ lut255,
                                                                 const Keypoint* __restrict__ refined_at,
                                                                 const uint32_t* __restrict__ keep, uint32_t ncap,
                                                                 OctCounters* __restrict__ oc,
@@ -357,7 +367,15 @@ __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __r
     chain_wait();
     __shared__ float hist[kOriWarps][kOriBins][32];
     __shared__ float hs[kOriWarps][kOriBins];
+    // u8 levels: v / 255 from a shared copy of the table (one load per
+    // pixel instead of a conversion and the three-instruction quotient)
+    __shared__ float slut[256];
     const int lane = threadIdx.x, wid = threadIdx.y;
+    constexpr bool kU8 = std::is_same<TG, uint8_t>::value;
+    if (kU8) {
+        for (int v = wid * 32 + lane; v < 256; v += 32 * kOriWarps) slut[v] = lut255[v];
+        __syncthreads();
+    }
     const uint32_t n = min(oc->n_cand, ncap);  // candidate slots; rejected ones get 0 peaks
     const AxisBins ab = axis_bins();
     const bool persist = (int)blockIdx.x >= persist_from;
@@ -370,7 +388,7 @@ __global__ void __launch_bounds__(32 * kOriWarps, 5) k_orientation(const TG* __r
         uint32_t cnt = 0;
         if (keep[i])
             cnt = orient_one<TG>(arena, tab, refined_at[i], &hist[wid][0][0], &hs[wid][0], lane, ab,
-                                 ori_angle + (size_t)i * kOriMaxPeaks);
+                                 ori_angle + (size_t)i * kOriMaxPeaks, kU8 ? slut : nullptr);
         if (lane == 0) ori_count[i] = cnt;
     }
 }
@@ -829,10 +847,10 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
 }  // namespace
 
 template <typename TG>
-int launch_orientation(const TG* arena, const EntryTable& tab, const Keypoint* refined_at,
+int launch_orientation(const TG* arena, const EntryTable& tab, const float* lut255, const Keypoint* refined_at,
                        const uint32_t* keep, uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count,
                        int grid, int persist_ctas, cudaStream_t st) {
-    if (launch_chained(k_orientation<TG>, grid, dim3(32, kOriWarps), 0, st, arena, tab, refined_at, keep, ncap,
+    if (launch_chained(k_orientation<TG>, grid, dim3(32, kOriWarps), 0, st, arena, tab, lut255, refined_at, keep, ncap,
                        oc, ori_angle, ori_count, std::max(grid - persist_ctas, 0)) != cudaSuccess)
         return -1;
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
@@ -859,7 +877,8 @@ int launch_descriptor(const TG* arena, const EntryTable& tab, const Keypoint* or
 }
 
 #define SIFT_INST(TG)                                                                                              \
-    template int launch_orientation<TG>(const TG*, const EntryTable&, const Keypoint*, const uint32_t*,           \
+    template int launch_orientation<TG>(const TG*, const EntryTable&, const float*, const Keypoint*,               \
+                                        const uint32_t*,                                                           \
                                         uint32_t, OctCounters*, float*, uint32_t*, int, int, cudaStream_t);        \
     template int launch_descriptor<TG>(const TG*, const EntryTable&, const Keypoint*, OctCounters*,                \
                                        float*, uint32_t, float*, uint32_t, int, int, cudaStream_t);

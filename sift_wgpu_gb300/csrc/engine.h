@@ -79,7 +79,7 @@ int launch_refine(const uint8_t* u8arena, const float* lut255, const EntryTable&
                   float edge, const Keypoint* cands, Keypoint* refined_at, uint32_t* keep, uint32_t cap,
                   OctCounters* oc, cudaStream_t st);
 template <typename TG>
-int launch_orientation(const TG* arena, const EntryTable& tab, const Keypoint* refined_at,
+int launch_orientation(const TG* arena, const EntryTable& tab, const float* lut255, const Keypoint* refined_at,
                        const uint32_t* keep, uint32_t ncap, OctCounters* oc, float* ori_angle, uint32_t* ori_count,
                        int grid, int persist_ctas, cudaStream_t st);
 int launch_orient_emit(const Keypoint* refined_at, uint32_t ncap, int o, Counters* ctr, const float* ori_angle,
@@ -657,7 +657,7 @@ struct Engine {
             // one warp-item per 8 candidate slots, 4 per warp; the last
             // 152 x ori_ctas_per_sm CTAs drain whatever is left
             const int grid = (int)std::max<uint32_t>(cap_c[o] / 64, 32);
-            if (ok(launch_orientation<TG>(G, tab(), d_refined_at.as<Keypoint>() + cb[o], d_keep.as<uint32_t>() + cb[o],
+            if (ok(launch_orientation<TG>(G, tab(), lut, d_refined_at.as<Keypoint>() + cb[o], d_keep.as<uint32_t>() + cb[o],
                                           cap_c[o], oc, d_ori_angle.as<float>() + (size_t)cb[o] * kOriMaxPeaks,
                                           d_ori_count.as<uint32_t>() + cb[o], grid, 152 * tune.ori_ctas_per_sm, q)))
                 return cuda_fail(cudaGetLastError(), "orientation");
