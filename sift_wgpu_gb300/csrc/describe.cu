@@ -4,9 +4,10 @@
 // (src/sift.rs:605-726) and compute (src/sift.rs:917-1060) with
 // normalize_and_clip_descriptor (src/sift.rs:889-913).
 //
-//   k_orientation   one warp per refined keypoint: the (2r+1)^2 window is
-//                   split over the lanes, each lane adds into its own column of
-//                   a bin-major shared histogram (conflict-free, no atomics),
+//   k_orientation   one warp per refined keypoint (orient_one): the (2r+1)^2
+//                   window is split over the lanes, each lane takes its samples
+//                   two at a time and adds them into its own column of a
+//                   bin-major shared histogram (conflict-free, no atomics),
 //                   columns are summed in a fixed order, then the two [1,1,1]/3
 //                   smoothing passes and the peak test run one bin per lane;
 //                   peaks come out in bin order through a ballot.
@@ -14,19 +15,23 @@
 //                   it) writes its c_i oriented copies at the scanned offset,
 //                   so the output order is the reference's (keypoint, bin)
 //                   order.
-//   k_descriptor    one CTA per oriented keypoint: the bilinear samples of the
-//                   window are computed once into a shared grid, window samples
-//                   are split over the threads, trilinear contributions are
-//                   added into 128 shared bins as u32 fixed point (integer
-//                   addition is associative, so the result does not depend on
-//                   scheduling), then L2 normalise, clip at 0.2, renormalise.
+//   k_descriptor    one CTA per oriented keypoint (describe_one): the bilinear
+//                   samples of the window are computed once into a shared grid,
+//                   pairs of window samples are split over the threads and
+//                   evaluated on packed f32x2 arithmetic, trilinear
+//                   contributions are added into 128 shared bins as u32 fixed
+//                   point (integer addition is associative, so the result does
+//                   not depend on scheduling), then L2 normalise, clip at 0.2,
+//                   renormalise.
+// Both queues run from the last item of an octave's list (the largest
+// windows first).
 //
 // The orientation histogram follows the reference's f32 operation order
 // without FMA, except the Gaussian weight (hardware exponential of a
 // reciprocal product) and the angle (polynomial atan2 away from bin edges,
 // atan2f and the IEEE division next to them, so every bin index is exact);
 // its column sums are in a fixed order. The descriptor loop trades exactness
-// for speed within the descriptor tolerance (see k_descriptor). Orientations
+// for speed within the descriptor tolerance (see describe_one). Orientations
 // and descriptors therefore agree with the reference within rounding, not bit
 // for bit.
 #include <algorithm>

@@ -9,11 +9,12 @@
 // forms from them. Products and sums are rounded one by one
 // (__fmul_rn/__fadd_rn) in the reference's tap order.
 //
-// Every level is written two ways: the u8 plane (1 byte/pixel, what the next
-// level, the resize and the extrema and refinement stages read; DoG is formed
-// from it there, never stored) and the stored level in the storage type (f32
-// v/255 or f16 v, read by the orientation and descriptor stages). Nothing in
-// the chain re-reads a 4-byte plane.
+// Every level is written as its u8 plane (1 byte/pixel, what the next level,
+// the resize and every later stage read; DoG is formed from it where it is
+// read, never stored) and, in the f32 and f16 storage modes, also in that
+// type (f32 v/255 or f16 v, read by orientation and descriptors); the default
+// u8 storage writes the u8 plane alone. Nothing in the chain re-reads a
+// 4-byte plane.
 //
 // Kernels
 //   k_blur_level   both separable passes of a level for r <= 8 (the first two
@@ -23,6 +24,8 @@
 //   k_blur_rows    horizontal pass for larger radii, one row per CTA. u8 out.
 //   k_blur_cols    vertical pass for larger radii on a 32 x 64 tile.
 //   k_lanczos_fused  the 2x Lanczos3 resize between octaves, both passes.
+// The base level of a host call reads its image through an ImgRef cell (the
+// engine's device copy, or the caller's pageable buffer in place).
 #include <cstring>
 #include <type_traits>
 
