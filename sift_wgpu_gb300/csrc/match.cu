@@ -15,6 +15,7 @@
 #include <algorithm>
 
 #include "sift_internal.cuh"
+#include "tma.cuh"
 
 namespace sift {
 namespace {
@@ -111,39 +112,8 @@ constexpr uint32_t kUSmem = 3 * kUTile + 8192 + 1024;  // query tile, two train 
 constexpr uint32_t kUTmemCols = 2 * kUN;
 constexpr uint32_t kUSpin = 1u << 26;                 // bounded waits (~seconds)
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-// true once the barrier's phase with this parity has completed; false after
-// kUSpin polls (the caller records the timeout)
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
-    const uint32_t a = smem_u32(b);
-    for (uint32_t i = 0; i < kUSpin; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(dst)),
-        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
+// bounded mbarrier waits of this kernel
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) { return sift::mbar_wait(b, parity, kUSpin); }
 // Shared-memory matrix descriptor of a K-major operand with 128-byte
 // swizzling: 8-row groups of 128-byte rows, 1024 bytes apart.
 __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
@@ -217,7 +187,7 @@ __global__ void __launch_bounds__(kUThreads, 1)
             mbar_init(acc_empty + i, 256);
         }
         *bad = 0u;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init_fence();
     }
     if (warp == 9) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -418,23 +388,6 @@ void umma_chunks(uint32_t nq, uint32_t nt, uint32_t* chunk_tiles, uint32_t* n_ch
     uint32_t want = std::min<uint32_t>(std::min<uint32_t>((2u * 152u + qt - 1) / qt, tt), 64u);
     *chunk_tiles = (tt + want - 1) / want;
     *n_chunks = (tt + *chunk_tiles - 1) / *chunk_tiles;
-}
-
-// cuTensorMapEncodeTiled, from the driver the runtime already loaded.
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn encode_tiled() {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(f);
-    }
-    return fn;
 }
 
 // Rows x 128 floats, boxes of 32 floats (128 bytes, the swizzle span) x 128

@@ -340,51 +340,85 @@ __device__ __forceinline__ void store_level4<__half>(__half* p, const int v[4], 
     *reinterpret_cast<uint2*>(p) = u;
 }
 
-template <typename TG, int R>
-__device__ __forceinline__ void blur_level_tile(const uint8_t* __restrict__ in, int in_pitch, TG* __restrict__ out,
-                                                uint8_t* __restrict__ out_u8, int pitch, int W, int H,
-                                                const float* __restrict__ wts, const float* __restrict__ lut255,
-                                                int x0, int y0, float* sm) {
-    static_assert(R >= 1 && R <= kFMaxR, "fused radius");
-    constexpr int taps = 2 * R + 1;
-    constexpr int wpad = (taps + 3) & ~3;
-    constexpr int RH = kFTY + 2 * R;
-    constexpr int sh = R & 3;
-    f32x2* kw2 = reinterpret_cast<f32x2*>(sm);  // [wpad] (k, k), vertical pass
-    float* kw = sm + 2 * wpad;                  // [wpad] k, horizontal pass
-    float* lut = kw + wpad;
-    float* src = lut + 256;              // [RH][kFSW] staged input (u8 values)
-    float* hb = src + (size_t)RH * kFSW;  // [RH][kFTX] horizontal pass
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < wpad; i += kFThreads) {
-        const float k = i < taps ? wts[i] : 0.0f;
+// Shared layout of the fused level kernel (floats): kw2[wpad] (pairs),
+// kw[wpad], lut[256], src[RH][kFSW] (staged input as floats), hb[RH][kFTX].
+template <int R>
+struct FusedLayout {
+    static constexpr int taps = 2 * R + 1;
+    static constexpr int wpad = (taps + 3) & ~3;
+    static constexpr int RH = kFTY + 2 * R;
+    static constexpr int sh = R & 3;
+};
+
+// the tap weights (single and paired) and the v / 255 table into shared memory
+template <int R>
+__device__ __forceinline__ void blur_level_weights(const float* __restrict__ wts, const float* __restrict__ lut255,
+                                                   float* sm) {
+    using Lx = FusedLayout<R>;
+    f32x2* kw2 = reinterpret_cast<f32x2*>(sm);
+    float* kw = sm + 2 * Lx::wpad;
+    float* lut = kw + Lx::wpad;
+    for (int i = threadIdx.x; i < Lx::wpad; i += kFThreads) {
+        const float k = i < Lx::taps ? wts[i] : 0.0f;
         kw2[i] = pack2(k, k);
         kw[i] = k;
     }
-    for (int i = tid; i < 256; i += kFThreads) lut[i] = lut255[i];
-    const bool interior = x0 >= 16 && x0 + 80 <= W && y0 >= R && y0 + kFTY + R <= H && (in_pitch & 15) == 0;
-    if (interior) {
+    for (int i = threadIdx.x; i < 256; i += kFThreads) lut[i] = lut255[i];
+}
+
+template <int R>
+__device__ __forceinline__ bool blur_level_interior(int x0, int y0, int W, int H) {
+    return x0 >= 16 && x0 + 80 <= W && y0 >= R && y0 + kFTY + R <= H;
+}
+
+// Stages the tile's (64 + 2R)-row neighbourhood from the previous level's u8
+// plane (global memory) as floats: interior tiles with 16-byte loads of
+// [x0 - 16, x0 + 80), border tiles clamp-to-edge.
+template <int R>
+__device__ __forceinline__ void blur_level_stage_global(const uint8_t* __restrict__ in, int in_pitch, int W, int H,
+                                                        int x0, int y0, float* sm) {
+    using Lx = FusedLayout<R>;
+    float* src = sm + 3 * Lx::wpad + 256;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (blur_level_interior<R>(x0, y0, W, H) && (in_pitch & 15) == 0) {
         constexpr int Q = 6;
         const uint8_t* org = in + (long long)(y0 - R) * in_pitch + (x0 - 16);
 #pragma unroll 2
-        for (int q = tid; q < RH * Q; q += kFThreads) {
+        for (int q = tid; q < Lx::RH * Q; q += kFThreads) {
             const int yy = q / Q, k = q - yy * Q;
             float v[16];
             unpack16(*reinterpret_cast<const uint4*>(org + (long long)yy * in_pitch + 16 * k), v);
-            float* d = src + (size_t)yy * kFSW + sh + 16 * k;
+            float* d = src + (size_t)yy * kFSW + Lx::sh + 16 * k;
 #pragma unroll
             for (int e = 0; e < 16; ++e) d[e] = v[e];
         }
     } else {
         // clamp-to-edge, only the columns the passes read: 16 + sh - R .. sh + 80 + R
-        for (int yy = warp; yy < RH; yy += kFThreads / 32) {
+        for (int yy = warp; yy < Lx::RH; yy += kFThreads / 32) {
             const uint8_t* row = in + (long long)clampi(y0 - R + yy, 0, H - 1) * in_pitch;
             float* d = src + (size_t)yy * kFSW;
-            for (int c = 16 + sh - R + lane; c <= sh + 80 + R; c += 32)
-                d[c] = float_of_u8(row[clampi(x0 - 16 - sh + c, 0, W - 1)]);
+            for (int c = 16 + Lx::sh - R + lane; c <= Lx::sh + 80 + R; c += 32)
+                d[c] = float_of_u8(row[clampi(x0 - 16 - Lx::sh + c, 0, W - 1)]);
         }
     }
-    __syncthreads();
+}
+
+// Both passes from the staged floats (the caller synchronises the CTA
+// between staging and this): horizontal pass into hb, then the vertical pass,
+// writing the level and its u8 plane.
+template <typename TG, int R>
+__device__ __forceinline__ void blur_level_compute(TG* __restrict__ out, uint8_t* __restrict__ out_u8, int pitch,
+                                                   int W, int H, int x0, int y0, float* sm) {
+    using Lx = FusedLayout<R>;
+    constexpr int taps = Lx::taps;
+    constexpr int RH = Lx::RH;
+    constexpr int sh = Lx::sh;
+    const f32x2* kw2 = reinterpret_cast<const f32x2*>(sm);
+    const float* kw = sm + 2 * Lx::wpad;
+    const float* lut = kw + Lx::wpad;
+    const float* src = lut + 256;
+    float* hb = const_cast<float*>(src) + (size_t)RH * kFSW;
+    const int tid = threadIdx.x;
     // horizontal pass: 16 threads per row, 4 outputs each (float4 sliding window)
     {
         const int xq = (tid & 15) * 4;
@@ -471,6 +505,19 @@ __device__ __forceinline__ void blur_level_tile(const uint8_t* __restrict__ in, 
             }
         }
     }
+}
+
+
+template <typename TG, int R>
+__device__ __forceinline__ void blur_level_tile(const uint8_t* __restrict__ in, int in_pitch, TG* __restrict__ out,
+                                                uint8_t* __restrict__ out_u8, int pitch, int W, int H,
+                                                const float* __restrict__ wts, const float* __restrict__ lut255,
+                                                int x0, int y0, float* sm) {
+    static_assert(R >= 1 && R <= kFMaxR, "fused radius");
+    blur_level_weights<R>(wts, lut255, sm);
+    blur_level_stage_global<R>(in, in_pitch, W, H, x0, y0, sm);
+    __syncthreads();
+    blur_level_compute<TG, R>(out, out_u8, pitch, W, H, x0, y0, sm);
 }
 
 template <typename TG, int R>
