@@ -653,8 +653,8 @@ def run_cuda(args, world, rank, local):
     e2e_value = world * e2e_n / e2e_s
     d2h = 16 + nk * (28 + 512)
 
-    # the drop-in call as the documented Rust arm makes it: a pageable image,
-    # results copied out of the engine's buffers into arrays the caller owns
+    # the drop-in call: a pageable image, results in arrays the caller owns
+    # (sift_cuda_detect_and_compute copies them out of the engine's buffers)
     pageable = np.array(img, copy=True)
     for _ in range(max(1, args.warmup)):
         eng.detect_and_compute(pageable)
@@ -712,8 +712,8 @@ def run_cuda(args, world, rank, local):
                     "form": "sift_cuda_detect_and_compute_view, pinned host image, results read in place"},
             "e2e_dropin": {"value": dropin_value, "unit": "images/s", "h2d_bytes_per_step": w * h,
                            "d2h_bytes_per_step": d2h,
-                           "form": "pageable host image through sift_cuda_detect_and_compute_view, keypoints and "
-                                   "descriptors copied into caller-owned arrays (the Rust arm's copy)"},
+                           "form": "pageable host image through sift_cuda_detect_and_compute: the library copies "
+                                   "keypoints and descriptors into arrays the caller owns (and frees)"},
             "keypoints_per_s": {"device": value * int(nk), "e2e": e2e_value * int(nk)},
             "roofline": roof,
             "roofline_pyramid_dog": roof_pyr,

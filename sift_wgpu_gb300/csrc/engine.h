@@ -29,6 +29,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sift_internal.cuh"
@@ -988,9 +989,29 @@ struct Engine {
             return fail(SIFT_CUDA_ERR_OUT_OF_MEMORY, "host allocation of the result");
         }
         if (n == 0) return 0;
-        std::memcpy(out->kps, hx_kps(), sizeof(Keypoint) * n);
-        if (with_desc) std::memcpy(out->desc, hx_desc(), sizeof(float) * kDescLen * n);
+        copy_out(out->kps, hx_kps(), sizeof(Keypoint) * n);
+        if (with_desc) copy_out(out->desc, hx_desc(), sizeof(float) * kDescLen * n);
         return 0;
+    }
+
+    // A result copy of several MB over a few host threads: one thread moves
+    // a fraction of the host's memory bandwidth.
+    static void copy_out(void* dst, const void* src, size_t bytes) {
+        constexpr size_t kChunk = 2u << 20;
+        const size_t hw = std::max<size_t>(std::thread::hardware_concurrency(), 1);
+        const size_t nt = std::min<size_t>(std::min<size_t>(4, bytes / kChunk), hw);
+        if (nt <= 1) {
+            std::memcpy(dst, src, bytes);
+            return;
+        }
+        const size_t per = ((bytes + nt - 1) / nt + 4095) & ~(size_t)4095;
+        std::vector<std::thread> th;
+        for (size_t i = 1; i < nt && i * per < bytes; ++i) {
+            const size_t a = i * per, b = std::min(bytes, a + per);
+            th.emplace_back([=] { std::memcpy((char*)dst + a, (const char*)src + a, b - a); });
+        }
+        std::memcpy(dst, src, std::min(per, bytes));
+        for (auto& t : th) t.join();
     }
 };
 

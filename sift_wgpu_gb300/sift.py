@@ -104,6 +104,34 @@ def _keypoint_array(keypoints) -> np.ndarray:
     return a
 
 
+class _ResultOwner:
+    """Frees a SiftCudaResult's arrays when the numpy arrays over them are gone."""
+
+    def __init__(self, res):
+        self.res = res
+
+    def __del__(self):
+        try:
+            _capi.lib().sift_cuda_result_free(C.byref(self.res))
+        except Exception:
+            pass
+
+
+def _owned_result(res, with_desc: bool):
+    """(keypoints, descriptors) over the arrays a non-view entry allocated."""
+    n = res.n
+    owner = _ResultOwner(res)
+    kb = (C.c_char * (n * KEYPOINT_DTYPE.itemsize)).from_address(C.cast(res.kps, C.c_void_p).value)
+    kb._owner = owner
+    kps = np.frombuffer(kb, dtype=KEYPOINT_DTYPE)
+    desc = None
+    if with_desc:
+        db = (C.c_float * (n * DESC_LEN)).from_address(C.cast(res.desc, C.c_void_p).value)
+        db._owner = owner
+        desc = np.frombuffer(db, dtype=np.float32).reshape(n, DESC_LEN)
+    return kps, desc
+
+
 class Engine:
     """One libsiftcuda engine: a CUDA stream plus resident device arenas."""
 
@@ -146,8 +174,11 @@ class Engine:
         self.close()
 
     def _call(self, fn, img: np.ndarray, with_desc: bool, view: bool = False):
-        """Runs fn and copies its result into owned arrays. view=True: fn is
-        a view entry (results in the engine's host buffers, not freed)."""
+        """Runs fn and returns its result as arrays the caller owns. view=True:
+        fn is a view entry (results in the engine's host buffers), copied out;
+        otherwise fn returns arrays the library allocated for this call, which
+        the returned numpy arrays wrap without a copy and free with
+        sift_cuda_result_free when both are gone."""
         img = _as_gray(img)
         h, w = img.shape
         stride = img.strides[0]
@@ -156,8 +187,10 @@ class Engine:
             stride = w
         res = _capi.Result()
         _capi.check(fn(self.handle, img.ctypes.data if img.size else None, w, h, stride, C.byref(res)))
+        n = res.n
+        if not view and n:
+            return _owned_result(res, with_desc)
         try:
-            n = res.n
             kps = np.empty(n, dtype=KEYPOINT_DTYPE)
             if n:
                 C.memmove(kps.ctypes.data, res.kps, n * KEYPOINT_DTYPE.itemsize)
@@ -178,8 +211,10 @@ class Engine:
         a = np.asarray(img)
         if a.ndim == 3 and a.dtype == np.uint8 and a.shape[2] in (3, 4):
             return self.detect_and_compute_pixels(a, _capi.PIXELS_RGB8 if a.shape[2] == 3 else _capi.PIXELS_RGBA8)
-        # the view entry and one copy out of the buffers the GPU wrote
-        return self._call(_capi.lib().sift_cuda_detect_and_compute_view, img, True, view=True)
+        # the drop-in entry: the library copies the results out of the
+        # buffers the GPU wrote (over a few host threads) into arrays that
+        # are returned without another copy
+        return self._call(_capi.lib().sift_cuda_detect_and_compute, img, True)
 
     def detect_and_compute_pixels(self, img, fmt: int) -> tuple[np.ndarray, np.ndarray]:
         """A colour image (H x W x 3 for PIXELS_RGB8, H x W x 4 for PIXELS_RGBA8
