@@ -490,8 +490,17 @@ __device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const
         const int total = side * side;
         const bool use_grid = rad <= kDescRadGrid;
         const int gs = side + 2;
+        // Grid layout: row gr (0 .. gs - 1) at gr * gst + (gr & 1), row
+        // stride gst = gs + 1 (even), one spare slot per row (the last of
+        // an even row, the first of an odd row). With the pair loop's
+        // phase (the pairs of odd rows start one sample to the left), all
+        // four float pairs a pair of samples reads are 8-byte aligned.
+        const int gst = gs + 1;
         float lo = 3.0e38f, hi = 0.0f;
         if (use_grid) {
+            // the spare slots, read only for the phantom element of a
+            // row's end pair, hold 0
+            if (tid < gs) grid[tid * gst + ((tid & 1) ? 0 : gs)] = 0.0f;
             // Bilinear samples at the window's integer offsets, in v units
             // (graw), straight from the level (the patch stays in L1). All
             // of them share the
@@ -538,7 +547,7 @@ __device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const
                     }
                     float2 A = make_float2(a[0][0], a[0][1]);
                     float2 rp = __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(a[0][1], a[0][2])), A);
-                    float* gp = grid + qy0 * gs + qx;
+                    float* gp = grid + qy0 * gst + qx;  // qy0 even
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
                         A = make_float2(a[j + 1][0], a[j + 1][1]);
@@ -546,8 +555,8 @@ __device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const
                             __ffma2_rn(fdx2, __ffma2_rn(A, neg1, make_float2(a[j + 1][1], a[j + 1][2])), A);
                         const float2 b = __ffma2_rn(fdy2, __ffma2_rn(rp, neg1, rn), rp);
                         if (j < nr) {
-                            gp[j * gs] = b.x;
-                            if (two) gp[j * gs + 1] = b.y;
+                            gp[j * gst + (j & 1)] = b.x;
+                            if (two) gp[j * gst + (j & 1) + 1] = b.y;
                             lo = fminf(lo, fminf(b.x, b.y));
                             hi = fmaxf(hi, fmaxf(b.x, b.y));
                         }
@@ -565,7 +574,7 @@ __device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const
                     // descriptor tolerance)
                     const float r0 = fmaf(fdx, q21 - q11, q11), r1 = fmaf(fdx, q22 - q12, q12);
                     const float b = fmaf(fdy, r1 - r0, r0);
-                    grid[q] = b;
+                    grid[qy * gst + (qy & 1) + qx] = b;
                     lo = fminf(lo, b);
                     hi = fmaxf(hi, b);
                 }
@@ -592,7 +601,8 @@ __device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const
         hi = fmaxf(fmaxf(red_hi[0], red_hi[1]), fmaxf(red_hi[2], red_hi[3]));
         const float range = fmaxf(hi - lo, 1.0f / 65536.0f);
         // and every single contribution (<= sqrt(2) * range) below 2^23,
-        // where the rounding add below converts it exactly
+        // where its rounding to an integer is exact (the subnormal grid of
+        // the pair loop, the 2^23 rounding add of the per-sample loop)
         const float per = 1.4143f * range;
         // floor(log2 q) of a positive normal float is its exponent field
         const int fbits = max(0, min(40, min((__float_as_int(4.0e9f / (per * (float)total)) >> 23) - 127,
@@ -622,47 +632,64 @@ __device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const
                             __fadd_rn(yo, -rad_f) >= 0.0f && __fadd_rn(yo, rad_f) < hm1);
         if (use_grid) {
             // Sample pairs: a thread takes the window samples (px, py) and
-            // (px + 1, py), px = -rad, -rad + 2, .., rad (the last pair of a
-            // row has a phantom second element, px = rad + 1, outside the
-            // window), and evaluates both with packed f32x2 arithmetic,
-            // the same operations per element as one sample alone. Pair m
-            // = tid + 128 j of the rad + 1 pairs per row: px, py (exact
-            // small integers in f32) and the grid index c of element 0
+            // (px + 1, py) and evaluates both with packed f32x2 arithmetic,
+            // the same operations per element as one sample alone. A row
+            // has rad + 1 pairs: from px = -rad in rows of even grid index
+            // (the last pair's second element, px = rad + 1, is outside the
+            // window), from px = -rad - 1 in rows of odd grid index (the
+            // first pair's first element is outside), so the float pairs
+            // of the gradients' grid reads are 8-byte aligned (one 64-bit
+            // load each). Pair m = tid + 128 j: the base offset pxb (= px
+            // in even rows, px + 1 in odd ones), py (exact small integers
+            // in f32), the row parity p and the grid index c of element 0
             // advance by fixed amounts with one row wrap per step.
             const int hp = rad + 1;
             const int q0 = tid / hp, dq = kDescThreads / hp;
             const float dr_f = (float)(2 * (kDescThreads - dq * hp)), dq_f = (float)dq;
-            const int dc = dq * gs + 2 * (kDescThreads - dq * hp);
+            const int dc = dq * gst + 2 * (kDescThreads - dq * hp);
+            const int dqp = dq & 1;
             const float wrap_f = (float)(2 * hp);
-            // the fixed-point scale rides in the exponent: exp2(d2 * wexp +
-            // fbits) = 2^fbits exp(-d2 / wd)
-            const float fb = (float)fbits;
+            // Fixed point on the subnormal grid: a float below 2^-125 is
+            // k * 2^-149 and its bit pattern is k, so a contribution scaled
+            // by 2^(fbits - 149) and rounded once to the nearest float (the
+            // last multiply) has the fixed-point integer as its bits (k <
+            // 2^23 by the scale choice): no conversion and no offset to
+            // subtract before the atomic. The scale is split so every factor
+            // stays a normal float: 2^(fbits - 49) rides in the exponent,
+            // exp2(d2 * wexp + fbits - 49) = 2^(fbits - 49) exp(-d2 / wd),
+            // and 2^-100 in the two angle weights. (The library is built
+            // without flush-to-zero, and mul.rn.f32x2 keeps subnormals.)
+            const float fb = (float)(fbits - 49);
             const float2 ca2 = make_float2(ca, ca), sa2 = make_float2(sa, sa), nsa2 = make_float2(-sa, -sa);
             const float2 ib2 = make_float2(inv_bw, inv_bw), half3 = make_float2(1.5f, 1.5f);
             const float2 wexp2 = make_float2(wexp, wexp), fb2 = make_float2(fb, fb);
             const float2 m15 = make_float2(kMagic15, kMagic15), nm15 = make_float2(-kMagic15, -kMagic15);
             const float2 neg1 = make_float2(-1.0f, -1.0f), one2 = make_float2(1.0f, 1.0f);
-            const float2 mag2c = make_float2(kMagic, kMagic), angb2 = make_float2(angb, angb);
+            constexpr float kAngScale = 7.888609052210118e-31f;  // 2^-100
+            const float2 as2 = make_float2(kAngScale, kAngScale), nas2 = make_float2(-kAngScale, -kAngScale);
+            const float2 angb2 = make_float2(angb, angb);
             auto pairs = [&](auto edge_tag) {
                 constexpr bool kEdge = decltype(edge_tag)::value;
-                float px = (float)(2 * (tid - q0 * hp)) - rad_f, py = (float)q0 - rad_f;
-                int c = (q0 + 1) * gs + 2 * (tid - q0 * hp) + 1;
-                for (;; px += dr_f, py += dq_f, c += dc) {
+                float pxb = (float)(2 * (tid - q0 * hp)) - rad_f, py = (float)q0 - rad_f;
+                int c = (q0 + 1) * gst + 2 * (tid - q0 * hp) + 1;  // odd
+                int p = (q0 + 1) & 1;                               // parity of grid row q0 + 1
+                for (;; pxb += dr_f, py += dq_f, c += dc, p ^= dqp) {
                     // the wrap to the next row as selects: a branch here
                     // would split the warp for the rest of the step
-                    const bool wrap = px > rad_f;
-                    px = wrap ? px - wrap_f : px;
+                    const bool wrap = pxb > rad_f;
+                    pxb = wrap ? pxb - wrap_f : pxb;
                     py = wrap ? py + 1.0f : py;
-                    c = wrap ? c + 1 : c;
+                    c = wrap ? c + 2 : c;
+                    p = wrap ? p ^ 1 : p;
                     if (py > rad_f) break;
-                    // element 1 at grid index c + 1 (the phantom's reads
-                    // stay inside the grid)
-                    const bool v1 = px < rad_f;
-                    const int c1 = c + 1;
+                    const float px = p ? pxb - 1.0f : pxb;
+                    const bool v0 = px >= -rad_f, v1 = px < rad_f;
+                    // rows gr - 1 and gr + 1 sit one slot the other way
+                    const int cv = c + 1 - 2 * p;
                     const float2 P = make_float2(px, px + 1.0f), Q = make_float2(py, py);
                     const float2 rx = __ffma2_rn(P, ca2, __fmul2_rn(Q, sa2));
                     const float2 ry = __ffma2_rn(P, nsa2, __fmul2_rn(Q, ca2));
-                    bool in0 = fabsf(rx.x) < lim && fabsf(ry.x) < lim;
+                    bool in0 = v0 && fabsf(rx.x) < lim && fabsf(ry.x) < lim;
                     bool in1 = v1 && fabsf(rx.y) < lim && fabsf(ry.y) < lim;
                     if constexpr (kEdge) {
                         const float xs0 = xo + px, ys0 = yo + py, xs1 = xo + P.y;
@@ -673,10 +700,13 @@ __device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const
                     // warps whose 64 samples all fall outside skip the rest
                     if (!__any_sync(__activemask(), in0 || in1)) continue;
                     if (!(in0 || in1)) continue;
-                    const float2 gx = __ffma2_rn(make_float2(grid[c - 1], grid[c1 - 1]), neg1,
-                                                 make_float2(grid[c + 1], grid[c1 + 1]));
-                    const float2 gy = __ffma2_rn(make_float2(grid[c - gs], grid[c1 - gs]), neg1,
-                                                 make_float2(grid[c + gs], grid[c1 + gs]));
+                    // (left, right) and (above, below) of both elements
+                    const float2 gl = *reinterpret_cast<const float2*>(grid + c - 1);
+                    const float2 gr = *reinterpret_cast<const float2*>(grid + c + 1);
+                    const float2 gu = *reinterpret_cast<const float2*>(grid + cv - gst);
+                    const float2 gd = *reinterpret_cast<const float2*>(grid + cv + gst);
+                    const float2 gx = __ffma2_rn(gl, neg1, gr);
+                    const float2 gy = __ffma2_rn(gu, neg1, gd);
                     const float2 m2 = __ffma2_rn(gx, gx, __fmul2_rn(gy, gy));
                     const float2 ea = __ffma2_rn(__ffma2_rn(P, P, __fmul2_rn(Q, Q)), wexp2, fb2);
                     float2 wm = __fmul2_rn(make_float2(sqrt_approx(m2.x), sqrt_approx(m2.y)),
@@ -708,19 +738,21 @@ __device__ __forceinline__ void describe_one(const TG* __restrict__ arena, const
                     at1 = in1 ? at1 : 0u;
                     const float2 wy0 = __fmul2_rn(wm, __ffma2_rn(fy, neg1, one2)), wy1 = __fmul2_rn(wm, fy);
                     const float2 wx0 = __ffma2_rn(fx, neg1, one2);
-                    const float2 wa0 = __ffma2_rn(fa, neg1, one2);
+                    // (1 - fa) * 2^-100 and fa * 2^-100 (exact scalings)
+                    const float2 wa0 = __ffma2_rn(fa, nas2, as2), wa1 = __fmul2_rn(fa, as2);
                     unsigned int* h0 = hcopy + at0;
                     unsigned int* h1 = hcopy + at1;
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc) {
                         const float2 wxy = __fmul2_rn((cc & 1) ? fx : wx0, (cc & 2) ? wy1 : wy0);
                         const int off = ((cc & 2) ? kHistSide * kHistRow : 0) + ((cc & 1) ? kHistRow : 0);
-                        // the products rounded to the nearest integer (< 2^23 by the scale choice)
-                        const float2 n0 = __ffma2_rn(wxy, wa0, mag2c), n1 = __ffma2_rn(wxy, fa, mag2c);
-                        atomicAdd(h0 + off, __float_as_uint(n0.x) - 0x4B000000u);
-                        atomicAdd(h0 + off + 1, __float_as_uint(n1.x) - 0x4B000000u);
-                        atomicAdd(h1 + off, __float_as_uint(n0.y) - 0x4B000000u);
-                        atomicAdd(h1 + off + 1, __float_as_uint(n1.y) - 0x4B000000u);
+                        // the products, rounded to the nearest fixed-point
+                        // integer on the subnormal grid, are their own bits
+                        const float2 n0 = __fmul2_rn(wxy, wa0), n1 = __fmul2_rn(wxy, wa1);
+                        atomicAdd(h0 + off, __float_as_uint(n0.x));
+                        atomicAdd(h0 + off + 1, __float_as_uint(n1.x));
+                        atomicAdd(h1 + off, __float_as_uint(n0.y));
+                        atomicAdd(h1 + off + 1, __float_as_uint(n1.y));
                     }
                 }
             };
@@ -816,7 +848,7 @@ __global__ void __launch_bounds__(kDescThreads, 8) k_descriptor(const TG* __rest
                                                               float* __restrict__ hdesc, uint32_t hcap,
                                                               int persist_from) {
     chain_wait();
-    __shared__ float grid[kDescGridSide * kDescGridSide];
+    __shared__ __align__(16) float grid[kDescGridSide * (kDescGridSide + 1)];
     __shared__ __align__(16) unsigned int hist[kHistCopies * kHistStride];
     __shared__ float red_lo[kDescThreads / 32], red_hi[kDescThreads / 32];
     const int tid = threadIdx.x;
