@@ -583,7 +583,7 @@ def run_cuda(args, world, rank, local):
     torch.cuda.set_device(local)
     from synthetic import synth_image
     img = synth_image(seed, w, h)
-    eng = sg.Engine(sg.Sift.new(*sargs), device=local, storage=args.storage)
+    eng = sg.Engine(sg.Sift.new(*sargs), device=local, storage=args.storage, level_tile_rows=args.level_tile_rows)
     stream = torch.cuda.ExternalStream(eng.stream, device=torch.device("cuda", local))
     d_img = torch.from_numpy(img).to(f"cuda:{local}")
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
@@ -706,7 +706,8 @@ def run_cuda(args, world, rank, local):
             "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{w}x{h} u8 synthetic frame, seed {seed}, Sift::new{sargs}",
-                       "storage": args.storage, "parallelism": f"replicas x{world}",
+                       "storage": args.storage, "level_tile_rows": args.level_tile_rows or 64,
+                       "parallelism": f"replicas x{world}",
                        "l2": "256 MiB flush before every step", "keypoints": int(nk)},
             "e2e": {"value": e2e_value, "unit": "images/s", "h2d_bytes_per_step": w * h, "d2h_bytes_per_step": d2h,
                     "form": "sift_cuda_detect_and_compute_view, pinned host image, results read in place"},
@@ -746,6 +747,8 @@ def main():
     ap.add_argument("--impl", choices=["cuda", "reference"], default="cuda")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch64", "serve", "match"], default="1080p")
     ap.add_argument("--storage", choices=["f32", "f16", "u8"], default="u8")
+    ap.add_argument("--level-tile-rows", type=int, choices=[0, 32, 64], default=0,
+                    help="rows of the fused level kernel's tiles (0: the default, 64)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-serving", action="store_true", help="skip the served-vs-plain section")

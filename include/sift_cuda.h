@@ -90,9 +90,11 @@ typedef enum {
 } SiftCudaStorage;
 
 typedef struct {
-    int32_t device;   /* CUDA device ordinal */
-    int32_t storage;  /* SiftCudaStorage (default SIFT_CUDA_STORAGE_U8) */
-    uint32_t reserved[6];
+    int32_t device;          /* CUDA device ordinal */
+    int32_t storage;         /* SiftCudaStorage (default SIFT_CUDA_STORAGE_U8) */
+    int32_t level_tile_rows; /* rows of the fused level kernel's tiles: 0 (default: 64), 64 or 32;
+                                the output is the same (the batched form always uses 64) */
+    uint32_t reserved[5];
 } SiftCudaOptions;
 
 typedef struct SiftCudaEngine SiftCudaEngine;
@@ -300,6 +302,11 @@ int sift_cuda_server_stats(SiftCudaServer* server, SiftCudaServerStats* out);
 /* Launch shape chosen for a size by the autotuner: [fused blur radius limit,
  * orientation CTAs/SM, descriptor CTAs/SM]; returns 1 if tuned, 0 if default. */
 int sift_cuda_server_tuning(SiftCudaServer* server, uint32_t width, uint32_t height, int32_t* knobs3);
+/* The same with every knob: writes the first min(n_knobs, 4) of [fused blur
+ * radius limit, fused level tile rows (64 or 32), orientation CTAs/SM,
+ * descriptor CTAs/SM]; returns 1 if tuned, 0 if default. */
+int sift_cuda_server_tuning_knobs(SiftCudaServer* server, uint32_t width, uint32_t height, int32_t* knobs,
+                                  uint32_t n_knobs);
 /* Device bytes a slot for a width x height image holds (admission estimate). */
 uint64_t sift_cuda_footprint_bytes(const SiftCudaParams* params, int32_t storage, uint32_t width,
                                    uint32_t height);

@@ -54,7 +54,8 @@ class Params(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("device", C.c_int32), ("storage", C.c_int32), ("reserved", C.c_uint32 * 6)]
+    _fields_ = [("device", C.c_int32), ("storage", C.c_int32), ("level_tile_rows", C.c_int32),
+                ("reserved", C.c_uint32 * 5)]
 
 
 class Keypoint(C.Structure):
@@ -183,6 +184,7 @@ def lib() -> C.CDLL:
         "sift_cuda_server_warm": (C.c_int, [C.c_void_p, C.c_void_p, u32, u32, u32, u32]),
         "sift_cuda_server_stats": (C.c_int, [C.c_void_p, P(ServerStats)]),
         "sift_cuda_server_tuning": (C.c_int, [C.c_void_p, u32, u32, P(i32)]),
+        "sift_cuda_server_tuning_knobs": (C.c_int, [C.c_void_p, u32, u32, P(i32), u32]),
         "sift_cuda_footprint_bytes": (u64, [P(Params), i32, u32, u32]),
         "sift_cuda_replay": (C.c_int, [C.c_void_p, P(Params), P(Options), P(ReplayImage), u32, P(ReplayRequest),
                                        u32, P(ReplayResult), P(C.c_double)]),
@@ -214,7 +216,8 @@ def exported_symbols() -> list[str]:
         "sift_cuda_debug_stage", "sift_cuda_last_launch_count", "sift_cuda_last_image_in_place", "sift_cuda_profile_enable",
         "sift_cuda_profile_read", "sift_cuda_server_options_default", "sift_cuda_server_create",
         "sift_cuda_server_destroy", "sift_cuda_server_submit", "sift_cuda_server_poll", "sift_cuda_server_release",
-        "sift_cuda_server_warm", "sift_cuda_server_stats", "sift_cuda_server_tuning", "sift_cuda_footprint_bytes",
+        "sift_cuda_server_warm", "sift_cuda_server_stats", "sift_cuda_server_tuning",
+        "sift_cuda_server_tuning_knobs", "sift_cuda_footprint_bytes",
         "sift_cuda_replay", "sift_cuda_gaussian_blur_u8_noalloc", "sift_cuda_draw_keypoints", "sift_cuda_match",
         "sift_cuda_match_scratch_bytes",
         "sift_cuda_match_device", "sift_cuda_batch_create", "sift_cuda_batch_destroy",

@@ -94,6 +94,8 @@ int sift_cuda_create(const SiftCudaParams* params, const SiftCudaOptions* opts, 
     if (opts) o = *opts;
     if (o.storage != SIFT_CUDA_STORAGE_F32 && o.storage != SIFT_CUDA_STORAGE_F16 && o.storage != SIFT_CUDA_STORAGE_U8)
         return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "unknown storage mode");
+    if (o.level_tile_rows != 0 && o.level_tile_rows != 32 && o.level_tile_rows != 64)
+        return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "level_tile_rows must be 0, 32 or 64");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0)
@@ -103,6 +105,7 @@ int sift_cuda_create(const SiftCudaParams* params, const SiftCudaOptions* opts, 
     if (!eng) return sift::fail(SIFT_CUDA_ERR_OUT_OF_MEMORY, "engine allocation");
     eng->e.p = *params;
     eng->e.opt = o;
+    if (o.level_tile_rows) eng->e.tune.level_tile_rows = o.level_tile_rows;
     if (int rc = eng->e.init()) {
         delete eng;
         return rc;

@@ -41,7 +41,7 @@ namespace sift {
 template <typename TG>
 int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, int r, const float* wts, const float* lut255, cudaStream_t st, int* launches,
-                      int fused_max_radius, const ImgRef* ref = nullptr);
+                      int fused_max_radius, const ImgRef* ref = nullptr, int tile_rows = 64);
 template <typename TG>
 int launch_copy_level(const TG* prev, const uint8_t* prev_u8, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, cudaStream_t st);
@@ -246,15 +246,17 @@ struct Engine {
 
     // Launch-shape knobs (set by the batch autotuner; the defaults are the
     // tuned values for single 1080p..4096 images): the largest blur radius
-    // that runs as one fused kernel, and the persistent grids of the
-    // orientation and descriptor kernels in CTAs per SM.
+    // that runs as one fused kernel, the persistent grids of the
+    // orientation and descriptor kernels in CTAs per SM, and the height of
+    // the fused level kernel's tiles (64 or 32 rows).
     struct Tuning {
         int fused_max_radius = 8;
         int ori_ctas_per_sm = 4;
         int desc_ctas_per_sm = 8;
+        int level_tile_rows = 64;
         bool operator==(const Tuning& o) const {
             return fused_max_radius == o.fused_max_radius && ori_ctas_per_sm == o.ori_ctas_per_sm &&
-                   desc_ctas_per_sm == o.desc_ctas_per_sm;
+                   desc_ctas_per_sm == o.desc_ctas_per_sm && level_tile_rows == o.level_tile_rows;
         }
     } tune{};
 
@@ -609,7 +611,8 @@ struct Engine {
             }
             int nl = 0;
             if (launch_blur_level<TG>(prev_u8, od.pitch, tmp, out, out_u8, od.pitch, od.W, od.H, b.radius,
-                                      wts + b.woff, lut, q, &nl, tune.fused_max_radius))
+                                      wts + b.woff, lut, q, &nl, tune.fused_max_radius, nullptr,
+                                      tune.level_tile_rows))
                 return cuda_fail(cudaGetLastError(), "blur level");
             launches += nl;
             return 0;
@@ -700,7 +703,7 @@ struct Engine {
                 int nl = 0;
                 if (launch_blur_level<TG>(img, (int)stride, d_tmp.as<uint8_t>(), G + o0.g_off, U + o0.u_off,
                                           o0.pitch, o0.W, o0.H, base.radius, wts + base.woff, lut, st,
-                                          &nl, tune.fused_max_radius, d_ref.as<ImgRef>()))
+                                          &nl, tune.fused_max_radius, d_ref.as<ImgRef>(), tune.level_tile_rows))
                     return cuda_fail(cudaGetLastError(), "blur (base)");
                 launches += nl;
             } else {

@@ -316,9 +316,9 @@ constexpr int kFTX = 64, kFTY = 64, kFThreads = 256;
 constexpr int kFMaxR = 8;
 constexpr int kFSW = 100;  // staged row stride (floats): sh + 96 <= 99
 
-size_t blur_fused_smem(int r) {
+size_t blur_fused_smem(int r, int ty = kFTY) {
     const int taps = 2 * r + 1;
-    const size_t rows = (size_t)kFTY + 2 * r;
+    const size_t rows = (size_t)ty + 2 * r;
     return sizeof(float) * ((size_t)3 * ((taps + 3) & ~3) + 256 + rows * kFSW + rows * kFTX);
 }
 
@@ -342,49 +342,54 @@ __device__ __forceinline__ void store_level4<__half>(__half* p, const int v[4], 
 
 // Shared layout of the fused level kernel (floats): kw2[wpad] (pairs),
 // kw[wpad], lut[256], src[RH][kFSW] (staged input as floats), hb[RH][kFTX].
-template <int R>
+// A tile is 64 columns by TY rows (64, or 32 for more, smaller CTAs on small
+// planes), computed by 4 * TY threads: 16 per row in the horizontal pass,
+// 4 x 4 outputs each in the vertical pass.
+template <int R, int TY = kFTY>
 struct FusedLayout {
+    static_assert(TY == 32 || TY == 64, "fused tile height");
     static constexpr int taps = 2 * R + 1;
     static constexpr int wpad = (taps + 3) & ~3;
-    static constexpr int RH = kFTY + 2 * R;
+    static constexpr int RH = TY + 2 * R;
     static constexpr int sh = R & 3;
+    static constexpr int threads = 4 * TY;
 };
 
 // the tap weights (single and paired) and the v / 255 table into shared memory
-template <int R>
+template <int R, int TY = kFTY>
 __device__ __forceinline__ void blur_level_weights(const float* __restrict__ wts, const float* __restrict__ lut255,
                                                    float* sm) {
-    using Lx = FusedLayout<R>;
+    using Lx = FusedLayout<R, TY>;
     f32x2* kw2 = reinterpret_cast<f32x2*>(sm);
     float* kw = sm + 2 * Lx::wpad;
     float* lut = kw + Lx::wpad;
-    for (int i = threadIdx.x; i < Lx::wpad; i += kFThreads) {
+    for (int i = threadIdx.x; i < Lx::wpad; i += Lx::threads) {
         const float k = i < Lx::taps ? wts[i] : 0.0f;
         kw2[i] = pack2(k, k);
         kw[i] = k;
     }
-    for (int i = threadIdx.x; i < 256; i += kFThreads) lut[i] = lut255[i];
+    for (int i = threadIdx.x; i < 256; i += Lx::threads) lut[i] = lut255[i];
 }
 
-template <int R>
+template <int R, int TY = kFTY>
 __device__ __forceinline__ bool blur_level_interior(int x0, int y0, int W, int H) {
-    return x0 >= 16 && x0 + 80 <= W && y0 >= R && y0 + kFTY + R <= H;
+    return x0 >= 16 && x0 + 80 <= W && y0 >= R && y0 + TY + R <= H;
 }
 
-// Stages the tile's (64 + 2R)-row neighbourhood from the previous level's u8
+// Stages the tile's (TY + 2R)-row neighbourhood from the previous level's u8
 // plane (global memory) as floats: interior tiles with 16-byte loads of
 // [x0 - 16, x0 + 80), border tiles clamp-to-edge.
-template <int R>
+template <int R, int TY = kFTY>
 __device__ __forceinline__ void blur_level_stage_global(const uint8_t* __restrict__ in, int in_pitch, int W, int H,
                                                         int x0, int y0, float* sm) {
-    using Lx = FusedLayout<R>;
+    using Lx = FusedLayout<R, TY>;
     float* src = sm + 3 * Lx::wpad + 256;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (blur_level_interior<R>(x0, y0, W, H) && (in_pitch & 15) == 0) {
+    if (blur_level_interior<R, TY>(x0, y0, W, H) && (in_pitch & 15) == 0) {
         constexpr int Q = 6;
         const uint8_t* org = in + (long long)(y0 - R) * in_pitch + (x0 - 16);
 #pragma unroll 2
-        for (int q = tid; q < Lx::RH * Q; q += kFThreads) {
+        for (int q = tid; q < Lx::RH * Q; q += Lx::threads) {
             const int yy = q / Q, k = q - yy * Q;
             float v[16];
             unpack16(*reinterpret_cast<const uint4*>(org + (long long)yy * in_pitch + 16 * k), v);
@@ -394,7 +399,7 @@ __device__ __forceinline__ void blur_level_stage_global(const uint8_t* __restric
         }
     } else {
         // clamp-to-edge, only the columns the passes read: 16 + sh - R .. sh + 80 + R
-        for (int yy = warp; yy < Lx::RH; yy += kFThreads / 32) {
+        for (int yy = warp; yy < Lx::RH; yy += Lx::threads / 32) {
             const uint8_t* row = in + (long long)clampi(y0 - R + yy, 0, H - 1) * in_pitch;
             float* d = src + (size_t)yy * kFSW;
             for (int c = 16 + Lx::sh - R + lane; c <= Lx::sh + 80 + R; c += 32)
@@ -406,10 +411,10 @@ __device__ __forceinline__ void blur_level_stage_global(const uint8_t* __restric
 // Both passes from the staged floats (the caller synchronises the CTA
 // between staging and this): horizontal pass into hb, then the vertical pass,
 // writing the level and its u8 plane.
-template <typename TG, int R>
+template <typename TG, int R, int TY = kFTY>
 __device__ __forceinline__ void blur_level_compute(TG* __restrict__ out, uint8_t* __restrict__ out_u8, int pitch,
                                                    int W, int H, int x0, int y0, float* sm) {
-    using Lx = FusedLayout<R>;
+    using Lx = FusedLayout<R, TY>;
     constexpr int taps = Lx::taps;
     constexpr int RH = Lx::RH;
     constexpr int sh = Lx::sh;
@@ -422,7 +427,7 @@ __device__ __forceinline__ void blur_level_compute(TG* __restrict__ out, uint8_t
     // horizontal pass: 16 threads per row, 4 outputs each (float4 sliding window)
     {
         const int xq = (tid & 15) * 4;
-        for (int yy = tid >> 4; yy < RH; yy += kFThreads / 16) {
+        for (int yy = tid >> 4; yy < RH; yy += Lx::threads / 16) {
             const float* base = src + (size_t)yy * kFSW + (16 + sh - R) + xq;
             float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
             float4 A = *reinterpret_cast<const float4*>(base);
@@ -508,20 +513,20 @@ __device__ __forceinline__ void blur_level_compute(TG* __restrict__ out, uint8_t
 }
 
 
-template <typename TG, int R>
+template <typename TG, int R, int TY = kFTY>
 __device__ __forceinline__ void blur_level_tile(const uint8_t* __restrict__ in, int in_pitch, TG* __restrict__ out,
                                                 uint8_t* __restrict__ out_u8, int pitch, int W, int H,
                                                 const float* __restrict__ wts, const float* __restrict__ lut255,
                                                 int x0, int y0, float* sm) {
     static_assert(R >= 1 && R <= kFMaxR, "fused radius");
-    blur_level_weights<R>(wts, lut255, sm);
-    blur_level_stage_global<R>(in, in_pitch, W, H, x0, y0, sm);
+    blur_level_weights<R, TY>(wts, lut255, sm);
+    blur_level_stage_global<R, TY>(in, in_pitch, W, H, x0, y0, sm);
     __syncthreads();
-    blur_level_compute<TG, R>(out, out_u8, pitch, W, H, x0, y0, sm);
+    blur_level_compute<TG, R, TY>(out, out_u8, pitch, W, H, x0, y0, sm);
 }
 
-template <typename TG, int R>
-__global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restrict__ in, int in_pitch,
+template <typename TG, int R, int TY>
+__global__ void __launch_bounds__(4 * TY) k_blur_level(const uint8_t* __restrict__ in, int in_pitch,
                                                           TG* __restrict__ out, uint8_t* __restrict__ out_u8,
                                                           int pitch, int W, int H,
                                                           const float* __restrict__ wts,
@@ -533,8 +538,8 @@ __global__ void __launch_bounds__(kFThreads) k_blur_level(const uint8_t* __restr
         in_pitch = (int)ref->pitch;
     }
     extern __shared__ __align__(16) float sm[];
-    blur_level_tile<TG, R>(in, in_pitch, out, out_u8, pitch, W, H, wts, lut255, blockIdx.x * kFTX, blockIdx.y * kFTY,
-                           sm);
+    blur_level_tile<TG, R, TY>(in, in_pitch, out, out_u8, pitch, W, H, wts, lut255, blockIdx.x * kFTX,
+                               blockIdx.y * TY, sm);
 }
 
 // A level whose blur increment is below 1e-4 is a copy of the previous one
@@ -848,32 +853,52 @@ static int set_smem(const void* k, size_t smem) {
 }
 
 // One level from the previous level's u8 plane: fused when r <= 8 and r <=
-// fused_max_radius (the horizontal pass recomputes a 2r-row halo per 64-row
-// tile, which stops paying beyond r = 8), else the two separable passes.
+// fused_max_radius (the horizontal pass recomputes a 2r-row halo per tile,
+// which stops paying beyond r = 8), on tiles of tile_rows (64 or 32) rows,
+// else the two separable passes.
+template <typename TG, int TY>
+using BlurLevelKernel = void (*)(const uint8_t*, int, TG*, uint8_t*, int, int, int, const float*, const float*,
+                                 const ImgRef*);
+template <typename TG, int TY>
+BlurLevelKernel<TG, TY> blur_level_kernel(int r) {
+    switch (r) {
+        case 1: return k_blur_level<TG, 1, TY>;
+        case 2: return k_blur_level<TG, 2, TY>;
+        case 3: return k_blur_level<TG, 3, TY>;
+        case 4: return k_blur_level<TG, 4, TY>;
+        case 5: return k_blur_level<TG, 5, TY>;
+        case 6: return k_blur_level<TG, 6, TY>;
+        case 7: return k_blur_level<TG, 7, TY>;
+        default: return k_blur_level<TG, 8, TY>;
+    }
+}
+
+template <typename TG, int TY>
+int launch_blur_level_fused(const uint8_t* in, int in_pitch, TG* out, uint8_t* out_u8, int pitch, int W, int H,
+                            int r, const float* wts, const float* lut255, cudaStream_t st, const ImgRef* ref) {
+    const BlurLevelKernel<TG, TY> kern = blur_level_kernel<TG, TY>(r);
+    const size_t smem = blur_fused_smem(r, TY);
+    if (set_smem((const void*)kern, smem)) return -1;
+    dim3 grid((W + kFTX - 1) / kFTX, (H + TY - 1) / TY);
+    if (launch_chained(kern, grid, 4 * TY, smem, st, in, in_pitch, out, out_u8, pitch, W, H, wts, lut255, ref) !=
+        cudaSuccess)
+        return -1;
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
 template <typename TG>
 int launch_blur_level(const uint8_t* in, int in_pitch, uint8_t* tmp, TG* out, uint8_t* out_u8, int pitch, int W,
                       int H, int r, const float* wts, const float* lut255, cudaStream_t st, int* launches,
-                      int fused_max_radius, const ImgRef* ref) {
-    const size_t smem = blur_fused_smem(r);
+                      int fused_max_radius, const ImgRef* ref, int tile_rows) {
     if (r <= kFMaxR && r <= fused_max_radius) {
-        void (*kern)(const uint8_t*, int, TG*, uint8_t*, int, int, int, const float*, const float*, const ImgRef*);
-        switch (r) {
-            case 1: kern = k_blur_level<TG, 1>; break;
-            case 2: kern = k_blur_level<TG, 2>; break;
-            case 3: kern = k_blur_level<TG, 3>; break;
-            case 4: kern = k_blur_level<TG, 4>; break;
-            case 5: kern = k_blur_level<TG, 5>; break;
-            case 6: kern = k_blur_level<TG, 6>; break;
-            case 7: kern = k_blur_level<TG, 7>; break;
-            default: kern = k_blur_level<TG, 8>; break;
-        }
-        if (set_smem((const void*)kern, smem)) return -1;
-        dim3 grid((W + kFTX - 1) / kFTX, (H + kFTY - 1) / kFTY);
-        if (launch_chained(kern, grid, kFThreads, smem, st, in, in_pitch, out, out_u8, pitch, W, H, wts, lut255,
-                           ref) != cudaSuccess)
-            return -1;
+        const int rc = tile_rows == 32
+                           ? launch_blur_level_fused<TG, 32>(in, in_pitch, out, out_u8, pitch, W, H, r, wts, lut255,
+                                                             st, ref)
+                           : launch_blur_level_fused<TG, 64>(in, in_pitch, out, out_u8, pitch, W, H, r, wts, lut255,
+                                                             st, ref);
+        if (rc) return rc;
         *launches += 1;
-        return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+        return 0;
     }
     const size_t rs = blur_rows_smem(W, r), cs = blur_cols_smem(r);
     if (set_smem((const void*)k_blur_rows, rs) || set_smem((const void*)k_blur_cols<TG>, cs)) return -1;
@@ -1003,7 +1028,7 @@ int lanczos_fused_tile() { return kLzT; }
 
 #define SIFT_INST(TG)                                                                                              \
     template int launch_blur_level<TG>(const uint8_t*, int, uint8_t*, TG*, uint8_t*, int, int, int, int,           \
-                                       const float*, const float*, cudaStream_t, int*, int, const ImgRef*);        \
+                                       const float*, const float*, cudaStream_t, int*, int, const ImgRef*, int);   \
     template int launch_copy_level<TG>(const TG*, const uint8_t*, TG*, uint8_t*, int, int, int,                    \
                                        cudaStream_t);                                                              \
     template int launch_u8_to_level<TG>(const uint8_t*, long long, TG*, uint8_t*, int, int, int, cudaStream_t,     \

@@ -28,9 +28,9 @@
 //              that arrives while others run is launched at once if a slot is
 //              free — continuous batching, not a queue in front of one engine.
 //   autotune   Optionally, the first slot of each size times a few launch
-//              shapes (fused blur radius limit, orientation and descriptor
-//              grids) by coordinate descent and every slot of that size uses
-//              the fastest.
+//              shapes (fused blur radius limit, fused level tile height,
+//              orientation and descriptor grids) by coordinate descent and
+//              every slot of that size uses the fastest.
 //
 // sift_cuda_replay drives either this server or the plain one-call-per-image
 // path with an open-loop request trace and reports per-request latency.
@@ -233,7 +233,7 @@ struct Server {
     }
 
     // Times the slot's graph for a few launch shapes on the image already in
-    // its engine, coordinate descent over the three knobs (service thread).
+    // its engine, coordinate descent over the four knobs (service thread).
     int autotune(Slot* s) {
         Engine& e = *s->eng;
         cudaEvent_t a = nullptr, b = nullptr;
@@ -256,13 +256,17 @@ struct Server {
         Engine::Tuning best = e.tune;
         float best_ms = 0.0f;
         int rc = time_cfg(best, &best_ms);
-        const int radii[] = {8, 4, 0}, oris[] = {2, 4, 8}, descs[] = {4, 8, 16};
-        for (int knob = 0; knob < 3 && !rc; ++knob) {
-            for (int v = 0; v < 3 && !rc; ++v) {
+        // candidate values per knob: fused radius limit, level tile rows,
+        // orientation CTAs/SM, descriptor CTAs/SM
+        const int vals[4][3] = {{8, 4, 0}, {64, 32, 0}, {2, 4, 8}, {4, 8, 16}};
+        const int nvals[4] = {3, 2, 3, 3};
+        for (int knob = 0; knob < 4 && !rc; ++knob) {
+            for (int v = 0; v < nvals[knob] && !rc; ++v) {
                 Engine::Tuning t = best;
-                if (knob == 0) t.fused_max_radius = radii[v];
-                if (knob == 1) t.ori_ctas_per_sm = oris[v];
-                if (knob == 2) t.desc_ctas_per_sm = descs[v];
+                if (knob == 0) t.fused_max_radius = vals[0][v];
+                if (knob == 1) t.level_tile_rows = vals[1][v];
+                if (knob == 2) t.ori_ctas_per_sm = vals[2][v];
+                if (knob == 3) t.desc_ctas_per_sm = vals[3][v];
                 if (t == best) continue;
                 float ms = 0.0f;
                 rc = time_cfg(t, &ms);
@@ -680,6 +684,19 @@ int sift_cuda_server_tuning(SiftCudaServer* server, uint32_t width, uint32_t hei
     knobs3[0] = t.fused_max_radius;
     knobs3[1] = t.ori_ctas_per_sm;
     knobs3[2] = t.desc_ctas_per_sm;
+    return it != S.tuned.end() ? 1 : 0;
+}
+
+int sift_cuda_server_tuning_knobs(SiftCudaServer* server, uint32_t width, uint32_t height, int32_t* knobs,
+                                  uint32_t n_knobs) {
+    if (!server || (!knobs && n_knobs)) return sift::fail(SIFT_CUDA_ERR_INVALID_ARGUMENT, "server or knobs is NULL");
+    Server& S = server->s;
+    std::lock_guard<std::mutex> lk(S.mu);
+    auto it = S.tuned.find(sift::TuneKey{width, height});
+    sift::Engine::Tuning t{};
+    if (it != S.tuned.end()) t = it->second;
+    const int32_t all[4] = {t.fused_max_radius, t.level_tile_rows, t.ori_ctas_per_sm, t.desc_ctas_per_sm};
+    for (uint32_t i = 0; i < n_knobs && i < 4; ++i) knobs[i] = all[i];
     return it != S.tuned.end() ? 1 : 0;
 }
 

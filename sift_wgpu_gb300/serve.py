@@ -160,9 +160,10 @@ class Server:
         return {f: getattr(s, f) for f, _ in _capi.ServerStats._fields_ if f != "reserved"}
 
     def tuning(self, width: int, height: int) -> tuple[bool, dict]:
-        k = (C.c_int32 * 3)()
-        tuned = _capi.lib().sift_cuda_server_tuning(self._h, width, height, k) == 1
-        return tuned, {"fused_max_radius": k[0], "ori_ctas_per_sm": k[1], "desc_ctas_per_sm": k[2]}
+        k = (C.c_int32 * 4)()
+        tuned = _capi.lib().sift_cuda_server_tuning_knobs(self._h, width, height, k, 4) == 1
+        return tuned, {"fused_max_radius": k[0], "level_tile_rows": k[1], "ori_ctas_per_sm": k[2],
+                       "desc_ctas_per_sm": k[3]}
 
     def _copy_out(self, r: Served):
         kps, desc = r.keypoints.copy(), r.descriptors.copy()

@@ -135,7 +135,8 @@ def _owned_result(res, with_desc: bool):
 class Engine:
     """One libsiftcuda engine: a CUDA stream plus resident device arenas."""
 
-    def __init__(self, params: "Sift | _capi.Params | None" = None, device: int = 0, storage: str = "u8"):
+    def __init__(self, params: "Sift | _capi.Params | None" = None, device: int = 0, storage: str = "u8",
+                 level_tile_rows: int = 0):
         L = _capi.lib()
         if params is None:
             params = Sift.default()
@@ -144,6 +145,7 @@ class Engine:
         L.sift_cuda_options_default(C.byref(opts))
         opts.device = device
         opts.storage = {"f32": _capi.STORAGE_F32, "f16": _capi.STORAGE_F16, "u8": _capi.STORAGE_U8}[storage]
+        opts.level_tile_rows = level_tile_rows  # 0: the default (64-row tiles)
         h = C.c_void_p()
         _capi.check(L.sift_cuda_create(C.byref(p), C.byref(opts), C.byref(h)))
         self._h = h

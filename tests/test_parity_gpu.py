@@ -202,6 +202,30 @@ def test_other_storage_modes_are_exact(sgb, storage):
     assert np.array_equal(e.debug_stage(sgb.STAGE_PYRAMID), p8)
 
 
+@pytest.mark.parametrize("w,h,seed,args", [(1920, 1080, 1, (1.6, 4, 3, 0.5, 0.04, 10.0)),
+                                            (333, 217, 2, (1.6, 4, 3, 0.5, 0.04, 10.0)),
+                                            (1024, 1024, 5, (1.6, 6, 3, 0.5, 0.04, 10.0))])
+def test_level_tile_rows_32_is_exact(sgb, w, h, seed, args):
+    """The fused level kernel on 32-row tiles (an option and an autotuner
+    knob) computes every level pixel with the same operations as on 64-row
+    tiles: the pyramid, keypoints and descriptors are bit-identical, on a
+    size whose last tile row is partial and with six octaves."""
+    img = image(sgb, w, h, seed)
+    e64 = engine_for(sgb, args, "u8")
+    k64, d64 = e64.detect_and_compute(img)
+    p64 = e64.debug_stage(sgb.STAGE_PYRAMID)
+    with sgb.Engine(sgb.Sift.new(*args), level_tile_rows=32) as e32:
+        k32, d32 = e32.detect_and_compute(img)
+        assert np.array_equal(e32.debug_stage(sgb.STAGE_PYRAMID), p64)
+    assert k32.tobytes() == k64.tobytes()
+    assert d32.tobytes() == d64.tobytes()
+
+
+def test_level_tile_rows_rejects_other_values(sgb):
+    with pytest.raises(sgb.SiftCudaError):
+        sgb.Engine(sgb.Sift.default(), level_tile_rows=48)
+
+
 def test_high_contrast_threshold(sgb):
     """tests/integration_test.rs:228-281"""
     img = image(sgb, 512, 512, 0)

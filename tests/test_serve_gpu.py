@@ -117,7 +117,7 @@ def test_autotune_keeps_results(sgb, images, alone):
         assert same((r.keypoints, r.descriptors), alone[2])
         tuned, knobs = srv.tuning(1920, 1080)
         assert tuned
-        assert knobs["fused_max_radius"] in (0, 4, 8)
+        assert knobs["fused_max_radius"] in (0, 4, 8) and knobs["level_tile_rows"] in (32, 64)
         assert knobs["ori_ctas_per_sm"] in (2, 4, 8) and knobs["desc_ctas_per_sm"] in (4, 8, 16)
         srv.submit(images[2], tag=1)
         r = srv.poll(timeout_s=60)
