@@ -95,6 +95,25 @@ def test_engine_errors_are_reported(built_lib):
     assert rc == 1 and res.n == 0
 
 
+def test_option_and_tuning_query_arguments_are_checked(built_lib):
+    """Checked before any device call (no GPU needed): a fused level tile
+    height other than 0, 32 or 64, and a tuning query without a server."""
+    from sift_wgpu_gb300 import _capi
+    L = _capi.lib()
+    p = _capi.Params()
+    L.sift_cuda_params_default(C.byref(p))
+    o = _capi.Options()
+    L.sift_cuda_options_default(C.byref(o))
+    assert o.level_tile_rows == 0 and o.storage == _capi.STORAGE_U8
+    o.level_tile_rows = 48
+    h = C.c_void_p()
+    rc = L.sift_cuda_create(C.byref(p), C.byref(o), C.byref(h))
+    assert rc == 1 and b"level_tile_rows" in L.sift_cuda_last_error() and not h.value
+    knobs = (C.c_int32 * 4)()
+    assert L.sift_cuda_server_tuning_knobs(None, 1920, 1080, knobs, 4) == 1
+    assert L.sift_cuda_server_tuning(None, 1920, 1080, knobs) == 1
+
+
 def footprint_restated(S, O, w, h, es):
     """The admission estimate of a server slot, restated: the arena layout
     (pitch = width rounded to 32; S+3 Gaussian and S+3 u8 planes per octave,
